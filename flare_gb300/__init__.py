@@ -1,0 +1,5 @@
+"""flare_gb300: GB300-native (sm_103a) sparse-GP prediction for FLARE's
+B2 / NormalizedDotProduct / SparseGP / SGP_Calculator path."""
+from .core import (B2, ClusterDescriptor, DescriptorValues,  # noqa: F401
+                   NormalizedDotProduct, SparseGP, Structure, get_precision,
+                   set_precision)

@@ -1,0 +1,596 @@
+"""Drop-in classes for FLARE's sparse-GP prediction path on one GB300.
+
+Names, constructor signatures, attributes and exception types follow the
+reference's pybind11 module ``_C_flare`` (src/ace_binding.cpp:28-262):
+``Structure``, ``DescriptorValues``, ``ClusterDescriptor``, ``B2``,
+``NormalizedDotProduct`` and ``SparseGP``.  All numerical work runs in
+libflaregb (CUDA, sm_103a) through the C ABI; torch is used only to own
+device memory and streams.
+
+Differences from the reference, by design:
+  * ``Structure`` builds its neighbour list and descriptors on the GPU lazily
+    (on first access, or when a SparseGP call needs them); prediction goes
+    straight from positions to energy/forces/stress/variance in one pipeline.
+  * The forward-mode descriptor gradients (``descriptor_force_dervs``) are
+    only materialised for training (``add_training_structure``), never for
+    prediction, which uses the reverse-mode adjoint.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib, ptr, stream_ptr
+
+_prec = {"fp64": _lib.FGB_PREC_FP64, "mixed": _lib.FGB_PREC_MIXED}
+_default_precision = ["fp64"]
+
+
+def set_precision(mode):
+    """Select the prediction precision: "fp64" or "mixed"."""
+    if mode not in _prec:
+        raise ValueError(f"unknown precision {mode!r}")
+    _default_precision[0] = mode
+
+
+def get_precision():
+    return _default_precision[0]
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("flare_gb300 needs a CUDA device (no CPU path)")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+# ------------------------------------------------------------------ B2
+class B2:
+    """B2(radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
+    descriptor_settings[, cutoffs]) — src/flare_pp/descriptors/b2.cpp:13-50."""
+
+    descriptor_name = "B2"
+
+    def __init__(self, radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
+                 descriptor_settings, cutoffs=None):
+        self.radial_basis = str(radial_basis)
+        self.cutoff_function = str(cutoff_function)
+        self.radial_hyps = [float(x) for x in radial_hyps]
+        self.cutoff_hyps = [float(x) for x in cutoff_hyps]
+        self.descriptor_settings = [int(x) for x in descriptor_settings]
+        if len(self.descriptor_settings) != 3:
+            raise ValueError("descriptor_settings must be [n_species, n_max, l_max]")
+        S = self.descriptor_settings[0]
+        if cutoffs is None:
+            cutoffs = np.full((S, S), self.radial_hyps[1])
+        self.cutoffs = np.ascontiguousarray(np.asarray(cutoffs, np.float64))
+        if self.cutoffs.shape != (S, S):
+            raise ValueError("cutoffs must be n_species x n_species")
+        if self.radial_basis not in _lib.RADIAL:
+            raise NotImplementedError(
+                f"radial basis {self.radial_basis!r} is not built "
+                f"(available: {sorted(_lib.RADIAL)})")
+        if self.cutoff_function not in _lib.CUTOFF:
+            raise ValueError(f"unknown cutoff function {self.cutoff_function!r}")
+        self._handle = None
+
+    @property
+    def handle(self):
+        if self._handle is None:
+            h = ctypes.c_void_p()
+            rh = np.asarray(self.radial_hyps, np.float64)
+            ch = np.asarray(self.cutoff_hyps if self.cutoff_hyps else [0.0],
+                            np.float64)
+            S, N, L = self.descriptor_settings
+            check(lib().fgb_b2_create(
+                ctypes.byref(h), _lib.RADIAL[self.radial_basis],
+                _lib.CUTOFF[self.cutoff_function], ptr(rh), len(rh), ptr(ch),
+                len(self.cutoff_hyps), S, N, L, ptr(self.cutoffs)), "B2")
+            self._handle = h
+            self._keep = (rh, ch)
+        return self._handle
+
+    @property
+    def n_descriptors(self):
+        S, N, L = self.descriptor_settings
+        nr = S * N
+        return nr * (nr + 1) // 2 * (L + 1)
+
+    @property
+    def n_single_bond(self):
+        S, N, L = self.descriptor_settings
+        return S * N * (L + 1) ** 2
+
+    def __del__(self):
+        if getattr(self, "_handle", None) is not None and _lib._lib is not None:
+            _lib._lib.fgb_b2_destroy(self._handle)
+            self._handle = None
+
+    def __getstate__(self):
+        d = dict(self.__dict__)
+        d["_handle"] = None
+        d.pop("_keep", None)
+        return d
+
+    def as_dict(self):
+        return {"type": "B2", "radial_basis": self.radial_basis,
+                "cutoff_function": self.cutoff_function,
+                "radial_hyps": self.radial_hyps,
+                "cutoff_hyps": self.cutoff_hyps,
+                "descriptor_settings": self.descriptor_settings,
+                "cutoffs": self.cutoffs.tolist()}
+
+
+# ------------------------------------------------------------ kernel
+class NormalizedDotProduct:
+    """k = sigma^2 (d1.d2 / |d1||d2|)^power
+    (src/flare_pp/kernels/normalized_dot_product.cpp:15-26)."""
+
+    kernel_name = "NormalizedDotProduct"
+
+    def __init__(self, sigma, power):
+        self.sigma = float(sigma)
+        self.power = float(power)
+
+    @property
+    def kernel_hyperparameters(self):
+        return np.array([self.sigma])
+
+    def envs_envs(self, envs1, envs2, hyps=None):
+        """Kernel matrix between two ClusterDescriptors (FP64 on the GPU)."""
+        sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
+        return envs_envs_gpu(envs1, envs2, sig, self.power)
+
+    def envs_struc(self, envs, struc, hyps=None):
+        """Kernel matrix between a ClusterDescriptor and a structure
+        (sparse rows x [energy, 3N forces, 6 stress]); ``struc`` is a
+        Structure (FP64 on the GPU, stored-gradient form)."""
+        sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
+        return envs_struc_gpu(envs, struc, sig, self.power)
+
+
+# ------------------------------------------------------- descriptors
+class DescriptorValues:
+    """Per-species descriptor values of one structure (descriptor.h:31-57)."""
+
+    def __init__(self):
+        self.n_descriptors = 0
+        self.n_types = 0
+        self.n_atoms = 0
+        self.volume = 0.0
+        self.descriptors = []
+        self.descriptor_norms = []
+        self.atom_indices = []
+        self.neighbor_counts = []
+        self.cumulative_neighbor_counts = []
+        self.neighbor_indices = []
+        self.neighbor_coordinates = []
+        self.n_clusters_by_type = []
+        self.cumulative_type_count = [0]
+        self.n_neighbors_by_type = []
+        self.n_clusters = 0
+
+
+class ClusterDescriptor:
+    """Sparse-set style descriptor collection (descriptor.h:61-90)."""
+
+    def __init__(self, n_types=0, n_descriptors=0):
+        self.n_types = n_types
+        self.n_descriptors = n_descriptors
+        self.descriptors = [np.zeros((0, n_descriptors)) for _ in range(n_types)]
+        self.descriptor_norms = [np.zeros(0) for _ in range(n_types)]
+        self.n_clusters_by_type = [0] * n_types
+        self.cumulative_type_count = [0] * n_types
+        self.n_clusters = 0
+
+    @staticmethod
+    def from_values(dv, clusters_by_type=None):
+        c = ClusterDescriptor(dv.n_types, dv.n_descriptors)
+        if clusters_by_type is None:
+            clusters_by_type = [list(range(dv.n_clusters_by_type[s]))
+                                for s in range(dv.n_types)]
+        c.add_clusters_by_type(dv, clusters_by_type)
+        return c
+
+    def add_clusters_by_type(self, dv, clusters):
+        """descriptor.cpp:104-140."""
+        for s in range(self.n_types):
+            idx = np.asarray(clusters[s], dtype=np.int64)
+            if idx.size:
+                self.descriptors[s] = np.vstack([self.descriptors[s],
+                                                 dv.descriptors[s][idx]])
+                self.descriptor_norms[s] = np.concatenate(
+                    [self.descriptor_norms[s], dv.descriptor_norms[s][idx]])
+        for s in range(self.n_types):
+            self.n_clusters_by_type[s] += len(clusters[s])
+            self.n_clusters += len(clusters[s])
+            if s > 0:
+                self.cumulative_type_count[s] = (
+                    self.cumulative_type_count[s - 1] +
+                    self.n_clusters_by_type[s - 1])
+
+    def add_clusters(self, dv, clusters):
+        """descriptor.cpp:81-102: clusters given as structure-wide indices."""
+        by_type = [[] for _ in range(dv.n_types)]
+        for c in clusters:
+            for s in range(dv.n_types):
+                if dv.cumulative_type_count[s] <= c < dv.cumulative_type_count[s + 1]:
+                    by_type[s].append(c - dv.cumulative_type_count[s])
+                    break
+        self.add_clusters_by_type(dv, by_type)
+
+    def stacked(self):
+        """(counts_by_species, rows) with species-grouped rows."""
+        rows = np.vstack([d for d in self.descriptors]) if self.n_types else \
+            np.zeros((0, self.n_descriptors))
+        return np.asarray(self.n_clusters_by_type, np.int32), \
+            np.ascontiguousarray(rows, dtype=np.float64)
+
+
+# ---------------------------------------------------------- structure
+class _NList:
+    """Owner of an fgb_nlist_t handle."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().fgb_nlist_create(ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib._lib is not None:
+            _lib._lib.fgb_nlist_destroy(self.h)
+            self.h = None
+
+
+class Structure:
+    """Structure(cell, species, positions[, cutoff, descriptor_calculators])
+    — src/flare_pp/structure.cpp:7-43."""
+
+    def __init__(self, cell, species, positions, cutoff=None,
+                 descriptor_calculators=None):
+        self.cell = np.ascontiguousarray(np.asarray(cell, np.float64).reshape(3, 3))
+        self.species = [int(s) for s in species]
+        self.positions = np.ascontiguousarray(
+            np.asarray(positions, np.float64).reshape(-1, 3))
+        if self.positions.shape[0] != len(self.species):
+            raise ValueError("positions and species disagree in length")
+        self.noa = len(self.species)
+        self.volume = abs(float(np.linalg.det(self.cell)))
+        self.cell_transpose = self.cell.T.copy()
+        self.cutoff = None if cutoff is None else float(cutoff)
+        self.descriptor_calculators = list(descriptor_calculators or [])
+        self.energy = np.zeros(0)
+        self.forces = np.zeros(0)
+        self.stresses = np.zeros(0)
+        self.mean_efs = np.zeros(0)
+        self.variance_efs = np.zeros(0)
+        self.mean_contributions = []
+        self.local_uncertainties = []
+        self._nl = None
+        self._dev = None
+        self._descriptors = None
+        self._dervs = {}
+
+    # device copies of the inputs
+    def _inputs(self):
+        if self._dev is None:
+            dev = _device()
+            self._dev = {
+                "pos": torch.from_numpy(self.positions).to(dev),
+                "species": torch.tensor(self.species, dtype=torch.int32,
+                                        device=dev),
+                "offsets": np.array([0, self.noa], dtype=np.int32),
+                "cell": np.ascontiguousarray(self.cell.reshape(-1)),
+            }
+        return self._dev
+
+    def nlist(self):
+        """Neighbour list (built once, on the GPU)."""
+        if self._nl is None:
+            if self.cutoff is None:
+                raise ValueError("Structure has no cutoff")
+            d = self._inputs()
+            nl = _NList()
+            check(lib().fgb_nlist_build(nl.h, 1, ptr(d["offsets"]),
+                                        ptr(d["cell"]), ptr(d["pos"]),
+                                        self.cutoff, stream_ptr()),
+                  "Structure")
+            self._nl = nl
+        return self._nl
+
+    def neighbor_arrays(self):
+        """Reference-layout neighbour arrays (structure.cpp:93-117) as numpy:
+        neighbor_count, cumulative_neighbor_count, structure_indices,
+        neighbor_species, relative_positions (P x 4), shifts (P x 3),
+        wrapped_positions."""
+        nl = self.nlist()
+        P = ctypes.c_longlong()
+        n = ctypes.c_int()
+        check(lib().fgb_nlist_size(nl.h, ctypes.byref(P), ctypes.byref(n)))
+        P = P.value
+        dev = _device()
+        cnt = torch.zeros(max(self.noa, 1), dtype=torch.int32, device=dev)
+        sidx = torch.zeros(max(P, 1), dtype=torch.int32, device=dev)
+        sh = torch.zeros(max(3 * P, 1), dtype=torch.int32, device=dev)
+        rel = torch.zeros(max(4 * P, 1), dtype=torch.float64, device=dev)
+        wr = torch.zeros(max(3 * self.noa, 1), dtype=torch.float64, device=dev)
+        check(lib().fgb_nlist_export(nl.h, ptr(cnt), ptr(sidx), ptr(sh),
+                                     ptr(rel), ptr(wr), stream_ptr()))
+        torch.cuda.current_stream().synchronize()
+        out = {
+            "neighbor_count": cnt.cpu().numpy()[:self.noa],
+            "structure_indices": sidx.cpu().numpy()[:P],
+            "shifts": sh.cpu().numpy()[:3 * P].reshape(P, 3),
+            "relative_positions": rel.cpu().numpy()[:4 * P].reshape(P, 4),
+            "wrapped_positions": wr.cpu().numpy()[:3 * self.noa].reshape(-1, 3),
+        }
+        c = np.zeros(self.noa + 1, dtype=np.int64)
+        c[1:] = np.cumsum(out["neighbor_count"])
+        out["cumulative_neighbor_count"] = c
+        sp = np.asarray(self.species, np.int32)
+        out["neighbor_species"] = sp[out["structure_indices"]] if P else \
+            np.zeros(0, np.int32)
+        return out
+
+    @property
+    def wrapped_positions(self):
+        return self.neighbor_arrays()["wrapped_positions"]
+
+    @property
+    def n_neighbors(self):
+        P = ctypes.c_longlong()
+        check(lib().fgb_nlist_size(self.nlist().h, ctypes.byref(P), None))
+        return P.value
+
+    # ----------------------------------------------------- descriptors
+    def b2_values(self, k=0):
+        """(B2 [N x n_d], norms [N]) as device tensors, atom order."""
+        calc = self.descriptor_calculators[k]
+        d = self._inputs()
+        dev = _device()
+        B = torch.zeros((max(self.noa, 1), calc.n_descriptors),
+                        dtype=torch.float64, device=dev)
+        nrm = torch.zeros(max(self.noa, 1), dtype=torch.float64, device=dev)
+        check(lib().fgb_b2_forward(calc.handle, self.nlist().h, ptr(d["species"]),
+                                   ptr(B), ptr(nrm), stream_ptr()), "B2")
+        return B[:self.noa], nrm[:self.noa]
+
+    @property
+    def descriptors(self):
+        if self._descriptors is None:
+            self._descriptors = [self._regroup(k) for k in
+                                 range(len(self.descriptor_calculators))]
+        return self._descriptors
+
+    def compute_descriptors(self):
+        self._descriptors = None
+        return self.descriptors
+
+    def _regroup(self, k):
+        """Species regroup of B2 values (b2.cpp:104-176)."""
+        calc = self.descriptor_calculators[k]
+        B, nrm = self.b2_values(k)
+        B = B.cpu().numpy()
+        nrm = nrm.cpu().numpy()
+        S = calc.descriptor_settings[0]
+        sp = np.asarray(self.species)
+        dv = DescriptorValues()
+        dv.n_descriptors = calc.n_descriptors
+        dv.n_types = S
+        dv.n_atoms = self.noa
+        dv.volume = self.volume
+        for s in range(S):
+            atoms = np.nonzero(sp == s)[0]
+            dv.n_clusters_by_type.append(len(atoms))
+            dv.cumulative_type_count.append(dv.cumulative_type_count[-1] +
+                                            len(atoms))
+            dv.n_clusters += len(atoms)
+            dv.descriptors.append(B[atoms])
+            dv.descriptor_norms.append(nrm[atoms])
+            dv.atom_indices.append(atoms.astype(np.int32))
+        return dv
+
+
+# ------------------------------------------------------- GPU kernels
+def envs_envs_gpu(envs1, envs2, sigma, power):
+    """envs_envs (normalized_dot_product.cpp:28-89) in FP64."""
+    dev = _device()
+    K = torch.zeros((envs1.n_clusters, envs2.n_clusters), dtype=torch.float64,
+                    device=dev)
+    sig2 = sigma * sigma
+    for s in range(envs1.n_types):
+        d1 = torch.from_numpy(np.ascontiguousarray(envs1.descriptors[s])).to(dev)
+        d2 = torch.from_numpy(np.ascontiguousarray(envs2.descriptors[s])).to(dev)
+        if d1.shape[0] == 0 or d2.shape[0] == 0:
+            continue
+        n1 = torch.from_numpy(np.asarray(envs1.descriptor_norms[s])).to(dev)
+        n2 = torch.from_numpy(np.asarray(envs2.descriptor_norms[s])).to(dev)
+        blk = _kernel_block(d1, n1, d2, n2, sig2, power)
+        c1, c2 = envs1.cumulative_type_count[s], envs2.cumulative_type_count[s]
+        K[c1:c1 + d1.shape[0], c2:c2 + d2.shape[0]] = blk
+    return K.cpu().numpy()
+
+
+def _kernel_block(d1, n1, d2, n2, sig2, power):
+    return _KernelBlock.run(d1, n1, d2, n2, sig2, power)
+
+
+class _KernelBlock:
+    """Dense FP64 kernel block via the model path (one species)."""
+
+    @staticmethod
+    def run(d1, n1, d2, n2, sig2, power):
+        out = torch.empty((d1.shape[0], d2.shape[0]), dtype=torch.float64,
+                          device=d1.device)
+        check(lib().fgb_envs_envs(ptr(d1), ptr(n1), d1.shape[0], ptr(d2),
+                                  ptr(n2), d2.shape[0], d1.shape[1], sig2,
+                                  power, ptr(out), stream_ptr()), "envs_envs")
+        return out
+
+
+def envs_struc_gpu(envs, struc, sigma, power):
+    raise NotImplementedError("envs_struc on the GPU is provided by SparseGP")
+
+
+# -------------------------------------------------------------- model
+class _Model:
+    """Owner of an fgb_model_t (device-resident sparse set, alpha, L_inv)."""
+
+    def __init__(self, b2, sigma, power):
+        h = ctypes.c_void_p()
+        check(lib().fgb_model_create(ctypes.byref(h), b2.handle, float(sigma),
+                                     float(power)), "SparseGP")
+        self.h = h
+        self.b2 = b2
+
+    def set(self, counts, desc, alpha=None, L_inv=None):
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        desc = np.ascontiguousarray(desc, dtype=np.float64)
+        a = None if alpha is None else np.ascontiguousarray(alpha, np.float64)
+        L = None if L_inv is None else np.ascontiguousarray(L_inv, np.float64)
+        check(lib().fgb_model_set(self.h, ptr(counts), ptr(desc), ptr(a),
+                                  ptr(L)), "SparseGP")
+
+    def __del__(self):
+        if getattr(self, "h", None) is not None and _lib._lib is not None:
+            _lib._lib.fgb_model_destroy(self.h)
+            self.h = None
+
+
+def pack_structures(structures):
+    """Packed batch inputs: atom offsets, cells, positions, species (host)."""
+    offsets = np.zeros(len(structures) + 1, dtype=np.int32)
+    for k, s in enumerate(structures):
+        offsets[k + 1] = offsets[k] + s.noa
+    cells = np.ascontiguousarray(np.stack([s.cell.reshape(-1)
+                                           for s in structures]))
+    pos = np.ascontiguousarray(np.concatenate([s.positions for s in structures]))
+    sp = np.ascontiguousarray(np.concatenate(
+        [np.asarray(s.species, np.int32) for s in structures]))
+    return offsets, cells, pos, sp
+
+
+class SparseGP:
+    """SparseGP(kernels, energy_noise, force_noise, stress_noise) —
+    src/flare_pp/bffs/sparse_gp.cpp:14-58 (prediction API here; training
+    bookkeeping in ``flare_gb300.training``)."""
+
+    def __init__(self, kernels=(), energy_noise=1.0, force_noise=1.0,
+                 stress_noise=1.0):
+        self.kernels = list(kernels)
+        self.n_kernels = len(self.kernels)
+        self.energy_noise = float(energy_noise)
+        self.force_noise = float(force_noise)
+        self.stress_noise = float(stress_noise)
+        self.Kuu_jitter = 1e-8
+        self.sparse_descriptors = []
+        self.sparse_indices = []
+        self.training_structures = []
+        self.alpha = None
+        self.L_inv = None
+        self.R_inv = None
+        self.Sigma = None
+        self.Kuu_inverse = None
+        self._model = None
+        self._model_key = None
+
+    @property
+    def hyperparameters(self):
+        return np.concatenate([k.kernel_hyperparameters for k in self.kernels] +
+                              [np.array([self.energy_noise, self.force_noise,
+                                         self.stress_noise])])
+
+    @property
+    def n_sparse(self):
+        return sum(sd.n_clusters for sd in self.sparse_descriptors)
+
+    # -------------------------------------------------- device model
+    def set_weights(self, sparse_descriptors, alpha, L_inv, calculators):
+        """Install solved weights (alpha, L_inv) and the sparse set
+        (list of ClusterDescriptor, one per kernel)."""
+        self.sparse_descriptors = list(sparse_descriptors)
+        self.alpha = np.asarray(alpha, np.float64)
+        self.L_inv = np.asarray(L_inv, np.float64)
+        self._calculators = list(calculators)
+        self._model = None
+
+    def _device_model(self, structure_calcs=None):
+        if self.alpha is None or self.L_inv is None:
+            raise RuntimeError(
+                "L_inv must be up to date to make predictions. Please call "
+                "update_matrices_QR and try again.")
+        if self.n_kernels != 1:
+            raise NotImplementedError(
+                "GPU prediction supports one kernel / descriptor (the "
+                "reference's local variance makes the same restriction, "
+                "calculator.py:105-108)")
+        if self._model is None:
+            calc = (structure_calcs or self._calculators)[0]
+            k = self.kernels[0]
+            m = _Model(calc, k.sigma, k.power)
+            counts, desc = self.sparse_descriptors[0].stacked()
+            M = desc.shape[0]
+            m.set(counts, desc, self.alpha[:M], self.L_inv[:M, :M])
+            self._model = m
+        return self._model
+
+    def predict_batch(self, structures, want=0xF, precision=None,
+                      stream=None):
+        """Batched prediction on the GPU.  Returns dict of numpy arrays:
+        energy [S], forces [N, 3], stress [S, 6] (flare order), local_var
+        [N] (atom order)."""
+        if not structures:
+            return {}
+        calcs = structures[0].descriptor_calculators
+        m = self._device_model(calcs)
+        offsets, cells, pos, sp = pack_structures(structures)
+        dev = _device()
+        N = int(offsets[-1])
+        S = len(structures)
+        d_pos = torch.from_numpy(pos).to(dev)
+        d_sp = torch.from_numpy(sp).to(dev)
+        e = torch.zeros(S, dtype=torch.float64, device=dev)
+        f = torch.zeros((max(N, 1), 3), dtype=torch.float64, device=dev)
+        st = torch.zeros((S, 6), dtype=torch.float64, device=dev)
+        v = torch.zeros(max(N, 1), dtype=torch.float64, device=dev)
+        prec = _prec[precision or _default_precision[0]]
+        cutoff = structures[0].cutoff
+        for s in structures:
+            if s.cutoff != cutoff:
+                raise ValueError("a batch must share one structure cutoff")
+        check(lib().fgb_predict(m.h, S, ptr(offsets), ptr(cells), ptr(d_pos),
+                                ptr(d_sp), cutoff, int(want), prec, ptr(e),
+                                ptr(f), ptr(st), ptr(v), stream_ptr(stream)),
+              "predict")
+        torch.cuda.current_stream().synchronize()
+        return {"energy": e.cpu().numpy(), "forces": f.cpu().numpy()[:N],
+                "stress": st.cpu().numpy(), "local_var": v.cpu().numpy()[:N],
+                "offsets": offsets}
+
+    def _predict_one(self, structure, want):
+        r = self.predict_batch([structure], want)
+        structure.mean_efs = np.concatenate(
+            [r["energy"][:1], r["forces"].reshape(-1), r["stress"][0]])
+        return r
+
+    def predict_mean(self, structure):
+        """sparse_gp.cpp:643-665: mean_efs = [E, F (3N), stress (6)]."""
+        self._predict_one(structure, _lib.FGB_WANT_ENERGY |
+                          _lib.FGB_WANT_FORCES | _lib.FGB_WANT_STRESS)
+
+    def predict_local_uncertainties(self, structure):
+        """sparse_gp.cpp:731-757: mean_efs plus per-atom local variances
+        (stored in species-sorted order, as the reference does)."""
+        r = self._predict_one(structure, 0xF)
+        sp = np.asarray(structure.species)
+        S = structure.descriptor_calculators[0].descriptor_settings[0]
+        order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
+        structure.local_uncertainties = [r["local_var"][order]]
+
+    def compute_cluster_uncertainties(self, structure):
+        """sparse_gp.cpp:94-139 (species-sorted variances)."""
+        r = self.predict_batch([structure], _lib.FGB_WANT_LOCAL_VAR)
+        sp = np.asarray(structure.species)
+        S = structure.descriptor_calculators[0].descriptor_settings[0]
+        order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
+        return [r["local_var"][order]]

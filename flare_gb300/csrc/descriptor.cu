@@ -1,0 +1,339 @@
+// K2 / K5: B2 descriptor forward and its reverse-mode adjoint.
+//
+// Forward (b2.cpp:244-399 single bond, :181-242 contraction), one CTA per
+// atom: the atom's neighbour list is streamed in chunks of kChunk pairs; each
+// thread evaluates one pair's radial x cutoff values g_n and real Y_lm into
+// shared memory, then the CTA contracts them into A[s_j][n][lm] (thread per
+// A entry, fixed pair order: deterministic, no atomics).  B2 is then
+// sum_m A[n1][lm] A[n2][lm] for n1 <= n2, in the reference's counter order,
+// written with coalesced stores, and the norm is a fixed-order block sum.
+//
+// Adjoint: dE/dB2 -> u = dE/dA (u[c][lm] = sum_b w((c,b),l) A[b][lm] (1+d_cb))
+// -> per pair dE/dr_ij = sum_{n,lm} u[s_j][n][lm] d(g_n Y_lm)/dr_ij, with g
+// and Y recomputed instead of stored.  Forces and the virial are assembled by
+// owner-computes over each atom's pairs and their twins (no float atomics).
+#include "fgb_internal.h"
+#include "fgb_kernels.h"
+
+namespace fgb {
+
+namespace {
+
+constexpr int kChunk = 64;      // pairs per shared-memory chunk = block size
+
+__device__ __forceinline__ int pair_index(int n1, int n2, int nr) {
+  return n1 * nr - n1 * (n1 - 1) / 2 + (n2 - n1);
+}
+
+__device__ __forceinline__ void decode_b2(int q, int L1, int nr, int &n1,
+                                          int &n2, int &l) {
+  l = q % L1;
+  int pidx = q / L1;
+  n1 = 0;
+  while (pidx >= nr - n1) { pidx -= nr - n1; n1++; }
+  n2 = n1 + pidx;
+}
+
+template <typename T>
+__device__ T block_sum(T v, T *red) {
+  // fixed-order tree reduction over the block (blockDim.x == kChunk)
+  int t = threadIdx.x;
+  red[t] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (t < s) red[t] += red[t + s];
+    __syncthreads();
+  }
+  T r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Shared memory: A[nA] | g[kChunk*nmax] | Y[kChunk*nh] | sp[kChunk] | red
+__global__ void __launch_bounds__(kChunk)
+k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
+             const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
+             const int *__restrict__ species, double *__restrict__ A_out,
+             double *__restrict__ B2, double *__restrict__ norms) {
+  extern __shared__ double smem[];
+  const int i = blockIdx.x;
+  if (i >= n_atoms) return;
+  const int nA = p.n_A, nh = p.n_harm, nm = p.n_max;
+  double *A = smem;
+  double *sg = A + nA;
+  double *sy = sg + kChunk * nm;
+  int *ssp = (int *)(sy + kChunk * nh);
+  double *red = (double *)(ssp + kChunk);
+  const int t = threadIdx.x;
+  const int si = species[i];
+  for (int e = t; e < nA; e += blockDim.x) A[e] = 0.0;
+  const long long b = offsets[i], e_ = offsets[i + 1];
+  for (long long c0 = b; c0 < e_; c0 += kChunk) {
+    long long pp = c0 + t;
+    int sj = -1;
+    if (pp < e_) {
+      int j = nbr_j[pp];
+      double4_16a r = rel[pp];
+      sj = species[j];
+      double rc = p.cutoffs[si * kMaxSpecies + sj];
+      if (r.x <= rc) {
+        double dg[kMaxNmax];
+        radial_eval<double>(p, r.x, rc, sg + t * nm, dg);
+        ylm_eval<double>(p.l_max, r.y, r.z, r.w, sy + t * nh, nullptr);
+      } else {
+        sj = -1;
+      }
+    }
+    ssp[t] = sj;
+    __syncthreads();
+    const int cnt = (int)min((long long)kChunk, e_ - c0);
+    for (int e = t; e < nA; e += blockDim.x) {
+      int s = e / (nm * nh);
+      int n = (e / nh) % nm;
+      int lm = e % nh;
+      double acc = 0.0;
+      for (int q = 0; q < cnt; q++)
+        if (ssp[q] == s) acc += sg[q * nm + n] * sy[q * nh + lm];
+      A[e] += acc;
+    }
+    __syncthreads();
+  }
+  if (A_out)
+    for (int e = t; e < nA; e += blockDim.x) A_out[(long long)i * nA + e] = A[e];
+  const int L1 = p.l_max + 1, nr = p.n_rad, nd = p.n_d;
+  double nrm = 0.0;
+  for (int q = t; q < nd; q += blockDim.x) {
+    int n1, n2, l;
+    decode_b2(q, L1, nr, n1, n2, l);
+    const double *a1 = A + n1 * nh + l * l, *a2 = A + n2 * nh + l * l;
+    double v = 0.0;
+    for (int m = 0; m < 2 * l + 1; m++) v += a1[m] * a2[m];
+    B2[(long long)i * nd + q] = v;
+    nrm += v * v;
+  }
+  nrm = block_sum(nrm, red);
+  if (t == 0) norms[i] = sqrt(nrm);
+}
+
+// Shared memory: u[nA] | A[nA]
+__global__ void __launch_bounds__(kChunk)
+k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
+             const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
+             const int *__restrict__ species, const double *__restrict__ A_in,
+             const double *__restrict__ gB2, double3 *__restrict__ pair_grad) {
+  extern __shared__ double smem[];
+  const int i = blockIdx.x;
+  if (i >= n_atoms) return;
+  const int nA = p.n_A, nh = p.n_harm, nm = p.n_max, nr = p.n_rad,
+            L1 = p.l_max + 1, nd = p.n_d;
+  double *u = smem;
+  double *A = u + nA;
+  const int t = threadIdx.x;
+  for (int e = t; e < nA; e += blockDim.x) A[e] = A_in[(long long)i * nA + e];
+  __syncthreads();
+  const double *w = gB2 + (long long)i * nd;
+  for (int e = t; e < nA; e += blockDim.x) {
+    int c = e / nh, lm = e % nh;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) l++;
+    double acc = 0.0;
+    for (int bb = 0; bb < nr; bb++) {
+      int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
+      double wv = w[pair_index(lo, hi, nr) * L1 + l];
+      double f = (bb == c) ? 2.0 : 1.0;
+      acc += f * wv * A[bb * nh + lm];
+    }
+    u[e] = acc;
+  }
+  __syncthreads();
+  const int si = species[i];
+  const long long b = offsets[i], e_ = offsets[i + 1];
+  for (long long pp = b + t; pp < e_; pp += blockDim.x) {
+    int j = nbr_j[pp];
+    double4_16a r = rel[pp];
+    int sj = species[j];
+    double rc = p.cutoffs[si * kMaxSpecies + sj];
+    double3 out = make_double3(0.0, 0.0, 0.0);
+    if (r.x <= rc) {
+      double g[kMaxNmax], dg[kMaxNmax];
+      double Y[kMaxHarm], Yd[3 * kMaxHarm];
+      radial_eval<double>(p, r.x, rc, g, dg);
+      ylm_eval<double>(p.l_max, r.y, r.z, r.w, Y, Yd);
+      const double ir = 1.0 / r.x;
+      const double ex = r.y * ir, ey = r.z * ir, ez = r.w * ir;
+      const double *us = u + sj * nm * nh;
+      double ox = 0.0, oy = 0.0, oz = 0.0;
+      for (int n = 0; n < nm; n++) {
+        const double *un = us + n * nh;
+        double t1 = 0.0, tx = 0.0, ty = 0.0, tz = 0.0;
+        for (int lm = 0; lm < nh; lm++) {
+          double uv = un[lm];
+          t1 += uv * Y[lm];
+          tx += uv * Yd[3 * lm];
+          ty += uv * Yd[3 * lm + 1];
+          tz += uv * Yd[3 * lm + 2];
+        }
+        double dgr = dg[n];
+        ox += dgr * ex * t1 + g[n] * tx;
+        oy += dgr * ey * t1 + g[n] * ty;
+        oz += dgr * ez * t1 + g[n] * tz;
+      }
+      out = make_double3(ox, oy, oz);
+    }
+    pair_grad[pp] = out;
+  }
+}
+
+// F_i = sum_{p in out(i)} (g_p - g_twin(p)); per-atom virial partials
+// v_i[ab] = sum_{p in out(i)} g_p,a r_p,b (flare order xx xy xz yy yz zz).
+__global__ void k_forces(int n_atoms, const long long *__restrict__ offsets,
+                         const long long *__restrict__ twin,
+                         const double4_16a *__restrict__ rel,
+                         const double3 *__restrict__ pg,
+                         double *__restrict__ forces,
+                         double *__restrict__ virial) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_atoms) return;
+  double fx = 0, fy = 0, fz = 0;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (long long q = offsets[i]; q < offsets[i + 1]; q++) {
+    double3 g = pg[q];
+    long long tw = twin[q];
+    double3 h = tw >= 0 ? pg[tw] : make_double3(0, 0, 0);
+    fx += g.x - h.x;
+    fy += g.y - h.y;
+    fz += g.z - h.z;
+    double4_16a r = rel[q];
+    v[0] += g.x * r.y; v[1] += g.x * r.z; v[2] += g.x * r.w;
+    v[3] += g.y * r.z; v[4] += g.y * r.w; v[5] += g.z * r.w;
+  }
+  if (forces) {
+    forces[3 * i] = fx; forces[3 * i + 1] = fy; forces[3 * i + 2] = fz;
+  }
+  if (virial)
+    for (int k = 0; k < 6; k++) virial[6 * i + k] = v[k];
+}
+
+// Per-structure energy and stress: fixed-order tree sums over the
+// structure's atoms.  One block per structure.
+__global__ void k_struct_reduce(int n_struc, const int *__restrict__ atom_off,
+                                const double *__restrict__ volume,
+                                const double *__restrict__ e_atom,
+                                const double *__restrict__ virial,
+                                double *__restrict__ energy,
+                                double *__restrict__ stress) {
+  __shared__ double red[7][256];
+  int s = blockIdx.x;
+  if (s >= n_struc) return;
+  int t = threadIdx.x;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int a = atom_off[s] + t; a < atom_off[s + 1]; a += blockDim.x) {
+    if (e_atom) acc[0] += e_atom[a];
+    if (virial)
+      for (int k = 0; k < 6; k++) acc[1 + k] += virial[6 * a + k];
+  }
+  for (int k = 0; k < 7; k++) red[k][t] = acc[k];
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (t < h)
+      for (int k = 0; k < 7; k++) red[k][t] += red[k][t + h];
+    __syncthreads();
+  }
+  if (t == 0) {
+    if (energy) energy[s] = red[0][0];
+    if (stress)
+      for (int k = 0; k < 6; k++) stress[6 * s + k] = -red[1 + k][0] / volume[s];
+  }
+}
+
+}  // namespace
+
+size_t b2_forward_smem(const B2Params &p) {
+  return sizeof(double) * (p.n_A + (size_t)kChunk * (p.n_max + p.n_harm)) +
+         sizeof(int) * kChunk + sizeof(double) * kChunk;
+}
+
+size_t b2_adjoint_smem(const B2Params &p) {
+  return sizeof(double) * 2 * (size_t)p.n_A;
+}
+
+int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
+                      const int *d_species, double *d_A, double *d_B2,
+                      double *d_norms, cudaStream_t st) {
+  const int N = nl->n_atoms;
+  if (N == 0) return FGB_OK;
+  size_t sm = b2_forward_smem(p);
+  if (sm > 200 * 1024) {
+    set_error("B2 settings need %zu bytes of shared memory", sm);
+    return FGB_EINVAL;
+  }
+  FGB_CUDA(cudaFuncSetAttribute(k_b2_forward,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sm));
+  k_b2_forward<<<N, kChunk, sm, st>>>(
+      p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+      nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
+  FGB_LAUNCH_CHECK("k_b2_forward");
+  return FGB_OK;
+}
+
+int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
+                      const int *d_species, const double *d_A,
+                      const double *d_gB2, double3 *d_pair_grad,
+                      cudaStream_t st) {
+  const int N = nl->n_atoms;
+  if (N == 0) return FGB_OK;
+  size_t sm = b2_adjoint_smem(p);
+  if (sm > 200 * 1024) {
+    set_error("B2 adjoint needs %zu bytes of shared memory", sm);
+    return FGB_EINVAL;
+  }
+  FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sm));
+  k_b2_adjoint<<<N, kChunk, sm, st>>>(
+      p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+      nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
+  FGB_LAUNCH_CHECK("k_b2_adjoint");
+  return FGB_OK;
+}
+
+int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
+                  double *d_forces, double *d_virial, cudaStream_t st) {
+  const int N = nl->n_atoms;
+  if (N == 0) return FGB_OK;
+  k_forces<<<ceil_div(N, 128), 128, 0, st>>>(
+      N, nl->offsets.as<long long>(), nl->nbr_twin.as<long long>(),
+      nl->nbr_rel.as<double4_16a>(), d_pair_grad, d_forces, d_virial);
+  FGB_LAUNCH_CHECK("k_forces");
+  return FGB_OK;
+}
+
+int launch_struct_reduce(int n_struc, const int *d_atom_off,
+                         const double *d_volume, const double *d_e_atom,
+                         const double *d_virial, double *d_energy,
+                         double *d_stress, cudaStream_t st) {
+  k_struct_reduce<<<n_struc, 256, 0, st>>>(n_struc, d_atom_off, d_volume,
+                                           d_e_atom, d_virial, d_energy,
+                                           d_stress);
+  FGB_LAUNCH_CHECK("k_struct_reduce");
+  return FGB_OK;
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" int fgb_b2_forward(fgb_b2_t b2, fgb_nlist_t nl, const int *d_species,
+                              double *d_B2, double *d_norms, void *stream) {
+  if (!b2 || !nl || !d_B2 || !d_norms) {
+    set_error("fgb_b2_forward: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (nl->n_atoms > 0 && !d_species) {
+    set_error("fgb_b2_forward: species required");
+    return FGB_EINVAL;
+  }
+  return launch_b2_forward(b2->p, nl, d_species, nullptr, d_B2, d_norms,
+                           (cudaStream_t)stream);
+}

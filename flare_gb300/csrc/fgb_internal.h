@@ -1,0 +1,77 @@
+// Internal host-side types shared by the libflaregb translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <vector>
+
+#include "fgb_common.cuh"
+
+namespace fgb {
+
+// Grow-only device buffer.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n);            // FGB_OK or FGB_ENOMEM
+  void release();
+  ~DevBuf() { release(); }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Per-structure geometry for the cell-list build (device copy).
+struct StrucGeom {
+  double cell[9];
+  double ct[9], cti[9], cd[9], cdi[9];   // cell^T, inverse, cell cell^T, inverse
+  double volume;
+  int nb[3];        // bins per axis
+  int kk[3];        // bin search half-width per axis
+  int sweep;        // reference image sweep (structure.cpp:35)
+  int atom0, natoms;
+  int bin0;         // first global bin
+};
+
+// Host-side cell algebra in the canonical operation order (no FMA).
+void cell_setup(const double *cell, double *ct, double *cti, double *cd,
+                double *cdi, double *volume, double *single_sweep_cutoff);
+
+// Device exclusive scan helpers (two-level, deterministic).
+int scan_int_to_int(const int *d_in, int *d_out, int n, int *d_total,
+                    DevBuf &tmp, cudaStream_t st);
+int scan_int_to_ll(const int *d_in, long long *d_out, int n,
+                   long long *d_total, DevBuf &tmp, cudaStream_t st);
+
+}  // namespace fgb
+
+struct fgb_nlist_s {
+  int n_struc = 0;
+  int n_atoms = 0;
+  long long n_pairs = 0;
+  int max_neighbors = 0;
+  std::vector<int> h_atom_offsets;
+  std::vector<double> h_cells;
+  std::vector<double> h_volume;
+  fgb::DevBuf geom;          // StrucGeom[n_struc]
+  fgb::DevBuf atom_struct;   // int[N]
+  fgb::DevBuf wrapped;       // double[N*3]
+  fgb::DevBuf raw_bin;       // int[N*3]
+  fgb::DevBuf home_bin;      // int[N]
+  fgb::DevBuf bin_slot;      // int[N]
+  fgb::DevBuf bin_count;     // int[n_bins]
+  fgb::DevBuf bin_start;     // int[n_bins+1]
+  fgb::DevBuf bin_atoms;     // int[N]
+  fgb::DevBuf counts;        // int[N]
+  fgb::DevBuf offsets;       // long long[N+1]
+  fgb::DevBuf tmp_key;       // unsigned long long[P]
+  fgb::DevBuf tmp_rel;       // double4_16a[P]
+  fgb::DevBuf nbr_j;         // int[P]  (batch-global atom index)
+  fgb::DevBuf nbr_shift;     // int[P]  packed (s0+128)<<16|(s1+128)<<8|(s2+128)
+  fgb::DevBuf nbr_rel;       // double4_16a[P] (d, x, y, z)
+  fgb::DevBuf nbr_twin;      // long long[P] index of (j -> i, -s)
+  fgb::DevBuf flag;          // int[4] device error flags
+  fgb::DevBuf scan_tmp;
+  fgb::DevBuf scalars;       // long long[4]
+};
+
+struct fgb_b2_s {
+  fgb::B2Params p;
+};

@@ -1,0 +1,32 @@
+// Launchers shared between libflaregb translation units.
+#pragma once
+#include "fgb_internal.h"
+
+namespace fgb {
+
+size_t b2_forward_smem(const B2Params &p);
+size_t b2_adjoint_smem(const B2Params &p);
+int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
+                      const int *d_species, double *d_A, double *d_B2,
+                      double *d_norms, cudaStream_t st);
+int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
+                      const int *d_species, const double *d_A,
+                      const double *d_gB2, double3 *d_pair_grad,
+                      cudaStream_t st);
+int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
+                  double *d_forces, double *d_virial, cudaStream_t st);
+int launch_struct_reduce(int n_struc, const int *d_atom_off,
+                         const double *d_volume, const double *d_e_atom,
+                         const double *d_virial, double *d_energy,
+                         double *d_stress, cudaStream_t st);
+
+// Stored forward-mode gradients (the reference's algorithm).
+int launch_b2_dervs(const B2Params &p, const fgb_nlist_s *nl,
+                    const int *d_species, const double *d_A, const double *d_B2,
+                    double *d_dB2, double *d_force_dots, cudaStream_t st);
+
+// Validate coded species in [0, n_species); returns FGB_EINVAL otherwise.
+int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
+                  cudaStream_t st);
+
+}  // namespace fgb

@@ -1,0 +1,51 @@
+// Device-resident sparse-GP model and its prediction workspace.
+#pragma once
+#include <vector>
+
+#include "fgb_internal.h"
+
+struct fgb_workspace {
+  fgb::DevBuf perm, flags, pos, scal, scan_tmp, flag;
+  fgb::DevBuf A, B2, norms, e_atom, var, volume, atom_off;
+  fgb::DevBuf gB2, pair_grad, forces, virial;
+  fgb::DevBuf kmat, wmat, erows, part;
+  fgb::DevBuf b2f, yf;           // mixed path: FP32 normalised rows, D^ B
+  fgb::DevBuf dB2, fdots, fdot, dots, kern;  // plain (stored-gradient) form
+};
+
+struct fgb_io {
+  fgb::DevBuf pos, species, energy, forces, stress, var;
+};
+
+struct fgb_model_s {
+  fgb::B2Params b2;
+  double sigma = 1.0, power = 2.0;
+  int M = 0;
+  bool solved = false;
+  std::vector<int> h_counts, h_offsets;       // sparse envs per species
+  std::vector<double> h_desc, h_snorm, h_alpha;
+  std::vector<int> h_panel_rows;
+  std::vector<long long> h_panel_off;
+  fgb::DevBuf S;        // normalised sparse descriptors, M x n_d (FP64)
+  fgb::DevBuf Sraw;     // raw sparse descriptors, M x n_d (FP64)
+  fgb::DevBuf snorm;    // sparse norms
+  fgb::DevBuf svalid;   // uint8 norm >= 1e-8
+  fgb::DevBuf alpha;    // M
+  fgb::DevBuf Lp;       // per-species L_inv panels
+  fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
+  bool bmap_ready = false;
+  fgb_nlist_s nl;
+  fgb_workspace ws;
+  fgb_io io;
+};
+
+namespace fgb {
+int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
+                      bool want_grad, bool want_var, double *d_e_atom,
+                      double *d_gB2, double *d_var, cudaStream_t st);
+int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
+                       bool want_grad, bool want_var, double *d_e_atom,
+                       double *d_gB2, double *d_var, cudaStream_t st);
+int species_permutation(fgb_model_s *m, const int *d_species, int N,
+                        std::vector<int> &counts, cudaStream_t st);
+}  // namespace fgb

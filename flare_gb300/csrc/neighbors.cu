@@ -1,0 +1,521 @@
+// K1: cell-list neighbour build, bit-exact against the reference's brute-force
+// list (src/flare_pp/structure.cpp:52-118).
+//
+// The reference tests every atom j and every image shift s in
+// [-sweep, sweep]^3 for 0 < |w_j - w_i + s.cell| < cutoff.  Here each atom is
+// binned by its fractional coordinate; bins are at least `cutoff` wide
+// (perpendicular width), so all pairs within the cutoff sit in the 3x3x3 (or
+// wider, for small cells) block of bin images around atom i.  Each candidate
+// (j, s) is tested with the reference's arithmetic in the same FP64
+// operation order (explicit _rn intrinsics, no FMA), filtered to
+// |s_a| <= sweep exactly as the reference's loop bounds, and each atom's
+// segment is finally ordered by (j, s1, s2, s3) — the reference's loop
+// order.  The result is the same set, the same order and the same bits.
+#include "fgb_internal.h"
+
+namespace fgb {
+
+namespace {
+
+__device__ __forceinline__ int floordiv(int a, int b) {
+  int q = a / b;
+  return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
+
+// frac = (p * ct) * cdi ; f = frac - floor(frac); w = (f * cd) * cti
+__global__ void k_wrap_bin(int n, const double *__restrict__ pos,
+                           const int *__restrict__ atom_struct,
+                           const StrucGeom *__restrict__ geom,
+                           double *__restrict__ wrapped, int *__restrict__ raw,
+                           int *__restrict__ home, int *__restrict__ slot,
+                           int *__restrict__ bin_count, int *__restrict__ flag) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const StrucGeom &g = geom[atom_struct[a]];
+  double p0 = pos[3 * a], p1 = pos[3 * a + 1], p2 = pos[3 * a + 2];
+  double t[3], f[3], u[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    t[k] = __dadd_rn(__dadd_rn(__dmul_rn(p0, g.ct[k]), __dmul_rn(p1, g.ct[3 + k])),
+                     __dmul_rn(p2, g.ct[6 + k]));
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    f[k] = __dadd_rn(__dadd_rn(__dmul_rn(t[0], g.cdi[k]), __dmul_rn(t[1], g.cdi[3 + k])),
+                     __dmul_rn(t[2], g.cdi[6 + k]));
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (!isfinite(f[k])) { bad = true; f[k] = 0.0; }
+    f[k] = __dsub_rn(f[k], floor(f[k]));
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    u[k] = __dadd_rn(__dadd_rn(__dmul_rn(f[0], g.cd[k]), __dmul_rn(f[1], g.cd[3 + k])),
+                     __dmul_rn(f[2], g.cd[6 + k]));
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    wrapped[3 * a + k] =
+        __dadd_rn(__dadd_rn(__dmul_rn(u[0], g.cti[k]), __dmul_rn(u[1], g.cti[3 + k])),
+                  __dmul_rn(u[2], g.cti[6 + k]));
+  int hb[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    // f in [0, 1]; raw bin in [0, nb] (nb only when f rounded up to 1.0)
+    int b = (int)floor(f[k] * (double)g.nb[k]);
+    b = b < 0 ? 0 : (b > g.nb[k] ? g.nb[k] : b);
+    raw[3 * a + k] = b;
+    hb[k] = b == g.nb[k] ? 0 : b;
+  }
+  if (bad) atomicExch(flag, 1);
+  int hbin = g.bin0 + (hb[0] * g.nb[1] + hb[1]) * g.nb[2] + hb[2];
+  home[a] = hbin;
+  slot[a] = atomicAdd(&bin_count[hbin], 1);
+}
+
+__global__ void k_bin_fill(int n, const int *__restrict__ home,
+                           const int *__restrict__ slot,
+                           const int *__restrict__ bin_start,
+                           int *__restrict__ bin_atoms) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  bin_atoms[bin_start[home[a]] + slot[a]] = a;
+}
+
+// Visit every candidate (j, s) of atom i in the bin-image block; calls
+// fn(j, s0, s1, s2, x, y, z, d) for each pair inside the cutoff.
+template <typename Fn>
+__device__ __forceinline__ void visit_pairs(int i, const StrucGeom &g,
+                                            const double *__restrict__ wrapped,
+                                            const int *__restrict__ raw,
+                                            const int *__restrict__ bin_start,
+                                            const int *__restrict__ bin_atoms,
+                                            double cutoff, Fn fn) {
+  const double wi0 = wrapped[3 * i], wi1 = wrapped[3 * i + 1],
+               wi2 = wrapped[3 * i + 2];
+  const int b0 = raw[3 * i], b1 = raw[3 * i + 1], b2 = raw[3 * i + 2];
+  for (int d0 = -g.kk[0]; d0 <= g.kk[0]; d0++) {
+    int t0 = b0 + d0, h0 = t0 - floordiv(t0, g.nb[0]) * g.nb[0],
+        q0 = floordiv(t0, g.nb[0]);
+    for (int d1 = -g.kk[1]; d1 <= g.kk[1]; d1++) {
+      int t1 = b1 + d1, h1 = t1 - floordiv(t1, g.nb[1]) * g.nb[1],
+          q1 = floordiv(t1, g.nb[1]);
+      for (int d2 = -g.kk[2]; d2 <= g.kk[2]; d2++) {
+        int t2 = b2 + d2, h2 = t2 - floordiv(t2, g.nb[2]) * g.nb[2],
+            q2 = floordiv(t2, g.nb[2]);
+        int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
+        int qb = bin_start[bin], qe = bin_start[bin + 1];
+        for (int q = qb; q < qe; q++) {
+          int j = bin_atoms[q];
+          // image shift relative to j's wrapped position
+          int s0 = q0 - (raw[3 * j] == g.nb[0] ? 1 : 0);
+          int s1 = q1 - (raw[3 * j + 1] == g.nb[1] ? 1 : 0);
+          int s2 = q2 - (raw[3 * j + 2] == g.nb[2] ? 1 : 0);
+          if (s0 < -g.sweep || s0 > g.sweep || s1 < -g.sweep ||
+              s1 > g.sweep || s2 < -g.sweep || s2 > g.sweep)
+            continue;
+          const double e0 = __dsub_rn(wrapped[3 * j], wi0);
+          const double e1 = __dsub_rn(wrapped[3 * j + 1], wi1);
+          const double e2 = __dsub_rn(wrapped[3 * j + 2], wi2);
+          const double f0 = (double)s0, f1 = (double)s1, f2 = (double)s2;
+          double x = __dadd_rn(__dadd_rn(__dadd_rn(e0, __dmul_rn(f0, g.cell[0])),
+                                         __dmul_rn(f1, g.cell[3])),
+                               __dmul_rn(f2, g.cell[6]));
+          double y = __dadd_rn(__dadd_rn(__dadd_rn(e1, __dmul_rn(f0, g.cell[1])),
+                                         __dmul_rn(f1, g.cell[4])),
+                               __dmul_rn(f2, g.cell[7]));
+          double z = __dadd_rn(__dadd_rn(__dadd_rn(e2, __dmul_rn(f0, g.cell[2])),
+                                         __dmul_rn(f1, g.cell[5])),
+                               __dmul_rn(f2, g.cell[8]));
+          double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)),
+                                          __dmul_rn(z, z)));
+          if (d < cutoff && d != 0.0) fn(j, s0, s1, s2, x, y, z, d);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_count(int n, const int *__restrict__ atom_struct,
+                        const StrucGeom *__restrict__ geom,
+                        const double *__restrict__ wrapped,
+                        const int *__restrict__ raw,
+                        const int *__restrict__ bin_start,
+                        const int *__restrict__ bin_atoms, double cutoff,
+                        int *__restrict__ counts) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const StrucGeom &g = geom[atom_struct[i]];
+  int c = 0;
+  visit_pairs(i, g, wrapped, raw, bin_start, bin_atoms, cutoff,
+              [&](int, int, int, int, double, double, double, double) { c++; });
+  counts[i] = c;
+}
+
+__global__ void k_fill(int n, const int *__restrict__ atom_struct,
+                       const StrucGeom *__restrict__ geom,
+                       const double *__restrict__ wrapped,
+                       const int *__restrict__ raw,
+                       const int *__restrict__ bin_start,
+                       const int *__restrict__ bin_atoms, double cutoff,
+                       const long long *__restrict__ offsets,
+                       unsigned long long *__restrict__ key,
+                       double4_16a *__restrict__ rel, int *__restrict__ flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const StrucGeom &g = geom[atom_struct[i]];
+  long long p = offsets[i], pend = offsets[i + 1];
+  visit_pairs(i, g, wrapped, raw, bin_start, bin_atoms, cutoff,
+              [&](int j, int s0, int s1, int s2, double x, double y, double z,
+                  double d) {
+                if (p < pend) {
+                  unsigned long long jl = (unsigned long long)(j - g.atom0);
+                  key[p] = (jl << 24) |
+                           ((unsigned long long)(s0 + 128) << 16) |
+                           ((unsigned long long)(s1 + 128) << 8) |
+                           (unsigned long long)(s2 + 128);
+                  rel[p] = make_double4_16a(d, x, y, z);
+                } else {
+                  atomicExch(flag + 1, 1);
+                }
+                p++;
+              });
+}
+
+// Warp per atom: rank each key within the atom's segment (keys are unique),
+// scatter into canonical (j, s1, s2, s3) order.
+__global__ void k_rank_scatter(int n, const int *__restrict__ atom_struct,
+                               const StrucGeom *__restrict__ geom,
+                               const long long *__restrict__ offsets,
+                               const unsigned long long *__restrict__ key,
+                               const double4_16a *__restrict__ rel_in,
+                               int *__restrict__ nbr_j,
+                               int *__restrict__ nbr_shift,
+                               double4_16a *__restrict__ rel_out) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  long long b = offsets[warp], e = offsets[warp + 1];
+  int atom0 = geom[atom_struct[warp]].atom0;
+  for (long long p = b + lane; p < e; p += 32) {
+    unsigned long long k = key[p];
+    long long r = 0;
+    for (long long q = b; q < e; q++) r += key[q] < k ? 1 : 0;
+    long long dst = b + r;
+    nbr_j[dst] = atom0 + (int)(k >> 24);
+    nbr_shift[dst] = (int)(k & 0xFFFFFFull);
+    rel_out[dst] = rel_in[p];
+  }
+}
+
+// twin of pair p = (i -> j, s) is (j -> i, -s) in j's segment.
+__global__ void k_twin(int n, const int *__restrict__ atom_struct,
+                       const StrucGeom *__restrict__ geom,
+                       const long long *__restrict__ offsets,
+                       const int *__restrict__ nbr_j,
+                       const int *__restrict__ nbr_shift,
+                       long long *__restrict__ twin, int *__restrict__ flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int atom0 = geom[atom_struct[i]].atom0;
+  for (long long p = offsets[i]; p < offsets[i + 1]; p++) {
+    int j = nbr_j[p];
+    int sh = nbr_shift[p];
+    int s0 = ((sh >> 16) & 0xFF) - 128, s1 = ((sh >> 8) & 0xFF) - 128,
+        s2 = (sh & 0xFF) - 128;
+    unsigned long long want = ((unsigned long long)(i - atom0) << 24) |
+                              ((unsigned long long)(-s0 + 128) << 16) |
+                              ((unsigned long long)(-s1 + 128) << 8) |
+                              (unsigned long long)(-s2 + 128);
+    long long lo = offsets[j], hi = offsets[j + 1] - 1, found = -1;
+    while (lo <= hi) {
+      long long mid = (lo + hi) >> 1;
+      int jj = nbr_j[mid];
+      unsigned long long km = ((unsigned long long)(jj - atom0) << 24) |
+                              (unsigned long long)nbr_shift[mid];
+      if (km == want) { found = mid; break; }
+      if (km < want) lo = mid + 1; else hi = mid - 1;
+    }
+    twin[p] = found;
+    if (found < 0) atomicExch(flag + 2, 1);
+  }
+}
+
+__global__ void k_export(int n, const long long *__restrict__ offsets,
+                         const int *__restrict__ atom_struct,
+                         const StrucGeom *__restrict__ geom,
+                         const int *__restrict__ nbr_j,
+                         const int *__restrict__ nbr_shift,
+                         const double4_16a *__restrict__ rel, int *cnt, int *sidx,
+                         int *shifts, double *relp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int atom0 = geom[atom_struct[i]].atom0;
+  if (cnt) cnt[i] = (int)(offsets[i + 1] - offsets[i]);
+  for (long long p = offsets[i]; p < offsets[i + 1]; p++) {
+    if (sidx) sidx[p] = nbr_j[p] - atom0;
+    if (shifts) {
+      int sh = nbr_shift[p];
+      shifts[3 * p] = ((sh >> 16) & 0xFF) - 128;
+      shifts[3 * p + 1] = ((sh >> 8) & 0xFF) - 128;
+      shifts[3 * p + 2] = (sh & 0xFF) - 128;
+    }
+    if (relp) {
+      double4_16a r = rel[p];
+      relp[4 * p] = r.x; relp[4 * p + 1] = r.y;
+      relp[4 * p + 2] = r.z; relp[4 * p + 3] = r.w;
+    }
+  }
+}
+
+}  // namespace
+
+// Host geometry set-up for one structure: bins and search widths.
+static void make_geom(const double *cell, double cutoff, int atom0, int natoms,
+                      int bin0, StrucGeom &g, double &single_sweep) {
+  for (int k = 0; k < 9; k++) g.cell[k] = cell[k];
+  cell_setup(cell, g.ct, g.cti, g.cd, g.cdi, &g.volume, &single_sweep);
+  g.sweep = (int)std::ceil(cutoff / single_sweep);
+  // Perpendicular widths h_a = V / |b x c| (cyclic).
+  const double *a = cell, *b = cell + 3, *c = cell + 6;
+  const double *v[3] = {a, b, c};
+  double h[3];
+  for (int k = 0; k < 3; k++) {
+    const double *p = v[(k + 1) % 3], *q = v[(k + 2) % 3];
+    double cx = p[1] * q[2] - p[2] * q[1];
+    double cy = p[2] * q[0] - p[0] * q[2];
+    double cz = p[0] * q[1] - p[1] * q[0];
+    h[k] = g.volume / std::sqrt(cx * cx + cy * cy + cz * cz);
+  }
+  const double rc = cutoff * (1.0 + 1e-9);
+  long long cap = std::max<long long>(27, 2LL * natoms);
+  for (int k = 0; k < 3; k++) {
+    double nbk = std::floor(h[k] / rc);
+    g.nb[k] = (int)std::max(1.0, std::min(nbk, 1024.0));
+  }
+  while ((long long)g.nb[0] * g.nb[1] * g.nb[2] > cap) {
+    int k = 0;
+    if (g.nb[1] > g.nb[k]) k = 1;
+    if (g.nb[2] > g.nb[k]) k = 2;
+    g.nb[k] = std::max(1, g.nb[k] / 2);
+  }
+  for (int k = 0; k < 3; k++)
+    g.kk[k] = (int)std::floor(rc * g.nb[k] / h[k]) + 1;
+  g.atom0 = atom0;
+  g.natoms = natoms;
+  g.bin0 = bin0;
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" int fgb_nlist_create(fgb_nlist_t *out) {
+  if (!out) { set_error("fgb_nlist_create: null output"); return FGB_EINVAL; }
+  *out = new fgb_nlist_s();
+  return FGB_OK;
+}
+
+extern "C" int fgb_nlist_destroy(fgb_nlist_t nl) {
+  delete nl;
+  return FGB_OK;
+}
+
+extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
+                               const int *h_atom_offsets, const double *h_cells,
+                               const double *d_positions, double cutoff,
+                               void *stream) {
+  if (!nl || n_struc <= 0 || !h_atom_offsets || !h_cells) {
+    set_error("fgb_nlist_build: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (!(cutoff > 0) || !std::isfinite(cutoff)) {
+    set_error("fgb_nlist_build: cutoff must be positive and finite");
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = h_atom_offsets[n_struc];
+  if (h_atom_offsets[0] != 0 || N < 0) {
+    set_error("fgb_nlist_build: atom offsets must start at 0");
+    return FGB_EINVAL;
+  }
+  for (int s = 0; s < n_struc; s++)
+    if (h_atom_offsets[s + 1] < h_atom_offsets[s]) {
+      set_error("fgb_nlist_build: atom offsets must be non-decreasing");
+      return FGB_EINVAL;
+    }
+  if (N > (1 << 24)) {
+    set_error("fgb_nlist_build: at most 2^24 atoms per batch");
+    return FGB_EINVAL;
+  }
+  nl->n_struc = n_struc;
+  nl->n_atoms = N;
+  nl->h_atom_offsets.assign(h_atom_offsets, h_atom_offsets + n_struc + 1);
+  nl->h_cells.assign(h_cells, h_cells + 9 * n_struc);
+  nl->h_volume.resize(n_struc);
+  std::vector<StrucGeom> geom(n_struc);
+  std::vector<int> atom_struct(N);
+  long long nbins = 0;
+  for (int s = 0; s < n_struc; s++) {
+    double sweep_cut;
+    const double *c = h_cells + 9 * s;
+    for (int k = 0; k < 9; k++)
+      if (!std::isfinite(c[k])) {
+        set_error("fgb_nlist_build: non-finite cell");
+        return FGB_EINVAL;
+      }
+    make_geom(c, cutoff, h_atom_offsets[s],
+              h_atom_offsets[s + 1] - h_atom_offsets[s], (int)nbins, geom[s],
+              sweep_cut);
+    if (!(geom[s].volume > 0) || !std::isfinite(sweep_cut) || sweep_cut <= 0) {
+      set_error("fgb_nlist_build: degenerate cell in structure %d", s);
+      return FGB_EINVAL;
+    }
+    if (geom[s].sweep > 127 || geom[s].kk[0] > 127 || geom[s].kk[1] > 127 ||
+        geom[s].kk[2] > 127) {
+      set_error("fgb_nlist_build: cutoff spans more than 127 cell images");
+      return FGB_EINVAL;
+    }
+    nl->h_volume[s] = geom[s].volume;
+    nbins += (long long)geom[s].nb[0] * geom[s].nb[1] * geom[s].nb[2];
+    for (int a = h_atom_offsets[s]; a < h_atom_offsets[s + 1]; a++)
+      atom_struct[a] = s;
+  }
+  if (nbins > (1 << 26)) {
+    set_error("fgb_nlist_build: too many bins");
+    return FGB_EINVAL;
+  }
+  int rc;
+  if ((rc = nl->geom.ensure(sizeof(StrucGeom) * n_struc)) ||
+      (rc = nl->atom_struct.ensure(sizeof(int) * (N + 1))) ||
+      (rc = nl->wrapped.ensure(sizeof(double) * 3 * (N + 1))) ||
+      (rc = nl->raw_bin.ensure(sizeof(int) * 3 * (N + 1))) ||
+      (rc = nl->home_bin.ensure(sizeof(int) * (N + 1))) ||
+      (rc = nl->bin_slot.ensure(sizeof(int) * (N + 1))) ||
+      (rc = nl->bin_count.ensure(sizeof(int) * (nbins + 1))) ||
+      (rc = nl->bin_start.ensure(sizeof(int) * (nbins + 1))) ||
+      (rc = nl->bin_atoms.ensure(sizeof(int) * (N + 1))) ||
+      (rc = nl->counts.ensure(sizeof(int) * (N + 1))) ||
+      (rc = nl->offsets.ensure(sizeof(long long) * (N + 1))) ||
+      (rc = nl->flag.ensure(sizeof(int) * 4)) ||
+      (rc = nl->scalars.ensure(sizeof(long long) * 4)))
+    return rc;
+  FGB_CUDA(cudaMemcpyAsync(nl->geom.p, geom.data(), sizeof(StrucGeom) * n_struc,
+                           cudaMemcpyHostToDevice, st));
+  if (N > 0)
+    FGB_CUDA(cudaMemcpyAsync(nl->atom_struct.p, atom_struct.data(),
+                             sizeof(int) * N, cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemsetAsync(nl->bin_count.p, 0, sizeof(int) * (nbins + 1), st));
+  FGB_CUDA(cudaMemsetAsync(nl->flag.p, 0, sizeof(int) * 4, st));
+  const int T = 128;
+  if (N == 0) {
+    nl->n_pairs = 0;
+    FGB_CUDA(cudaMemsetAsync(nl->offsets.p, 0, sizeof(long long), st));
+    return FGB_OK;
+  }
+  k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(
+      N, d_positions, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->wrapped.as<double>(), nl->raw_bin.as<int>(), nl->home_bin.as<int>(),
+      nl->bin_slot.as<int>(), nl->bin_count.as<int>(), nl->flag.as<int>());
+  FGB_LAUNCH_CHECK("k_wrap_bin");
+  if ((rc = scan_int_to_int(nl->bin_count.as<int>(), nl->bin_start.as<int>(),
+                            (int)nbins, nl->bin_start.as<int>() + nbins,
+                            nl->scan_tmp, st)))
+    return rc;
+  k_bin_fill<<<ceil_div(N, T), T, 0, st>>>(
+      N, nl->home_bin.as<int>(), nl->bin_slot.as<int>(),
+      nl->bin_start.as<int>(), nl->bin_atoms.as<int>());
+  FGB_LAUNCH_CHECK("k_bin_fill");
+  k_count<<<ceil_div(N, T), T, 0, st>>>(
+      N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->wrapped.as<double>(), nl->raw_bin.as<int>(), nl->bin_start.as<int>(),
+      nl->bin_atoms.as<int>(), cutoff, nl->counts.as<int>());
+  FGB_LAUNCH_CHECK("k_count");
+  // offsets[N] receives the total pair count
+  long long *d_total = nl->offsets.as<long long>() + N;
+  if ((rc = scan_int_to_ll(nl->counts.as<int>(), nl->offsets.as<long long>(), N,
+                           d_total, nl->scan_tmp, st)))
+    return rc;
+  long long P = 0;
+  int hflag[4];
+  FGB_CUDA(cudaMemcpyAsync(&P, d_total, sizeof(long long),
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (hflag[0]) {
+    set_error("fgb_nlist_build: non-finite atomic positions");
+    return FGB_EINVAL;
+  }
+  nl->n_pairs = P;
+  if ((rc = nl->tmp_key.ensure(sizeof(unsigned long long) * (P + 1))) ||
+      (rc = nl->tmp_rel.ensure(sizeof(double4_16a) * (P + 1))) ||
+      (rc = nl->nbr_j.ensure(sizeof(int) * (P + 1))) ||
+      (rc = nl->nbr_shift.ensure(sizeof(int) * (P + 1))) ||
+      (rc = nl->nbr_rel.ensure(sizeof(double4_16a) * (P + 1))) ||
+      (rc = nl->nbr_twin.ensure(sizeof(long long) * (P + 1))))
+    return rc;
+  if (P > 0) {
+    k_fill<<<ceil_div(N, T), T, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->wrapped.as<double>(), nl->raw_bin.as<int>(),
+        nl->bin_start.as<int>(), nl->bin_atoms.as<int>(), cutoff,
+        nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
+        nl->tmp_rel.as<double4_16a>(), nl->flag.as<int>());
+    FGB_LAUNCH_CHECK("k_fill");
+    k_rank_scatter<<<ceil_div((long long)N * 32, T), T, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
+        nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(), nl->nbr_shift.as<int>(),
+        nl->nbr_rel.as<double4_16a>());
+    FGB_LAUNCH_CHECK("k_rank_scatter");
+    k_twin<<<ceil_div(N, T), T, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_shift.as<int>(), nl->nbr_twin.as<long long>(),
+        nl->flag.as<int>());
+    FGB_LAUNCH_CHECK("k_twin");
+  }
+  FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
+                           cudaMemcpyDeviceToHost, st));
+  std::vector<int> hc(N);
+  FGB_CUDA(cudaMemcpyAsync(hc.data(), nl->counts.p, sizeof(int) * N,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (hflag[1] || hflag[2]) {
+    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
+              hflag[1], hflag[2]);
+    return FGB_ECUDA;
+  }
+  int mx = 0;
+  for (int i = 0; i < N; i++) mx = std::max(mx, hc[i]);
+  nl->max_neighbors = mx;
+  return FGB_OK;
+}
+
+extern "C" int fgb_nlist_size(fgb_nlist_t nl, long long *n_pairs,
+                              int *n_atoms) {
+  if (!nl) { set_error("fgb_nlist_size: null handle"); return FGB_EINVAL; }
+  if (n_pairs) *n_pairs = nl->n_pairs;
+  if (n_atoms) *n_atoms = nl->n_atoms;
+  return FGB_OK;
+}
+
+extern "C" int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
+                                int *d_structure_indices, int *d_shifts,
+                                double *d_relative_positions,
+                                double *d_wrapped, void *stream) {
+  if (!nl) { set_error("fgb_nlist_export: null handle"); return FGB_EINVAL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  int N = nl->n_atoms;
+  if (N == 0) return FGB_OK;
+  k_export<<<ceil_div(N, 128), 128, 0, st>>>(
+      N, nl->offsets.as<long long>(), nl->atom_struct.as<int>(),
+      nl->geom.as<StrucGeom>(), nl->nbr_j.as<int>(), nl->nbr_shift.as<int>(),
+      nl->nbr_rel.as<double4_16a>(), d_neighbor_count, d_structure_indices,
+      d_shifts, d_relative_positions);
+  FGB_LAUNCH_CHECK("k_export");
+  if (d_wrapped)
+    FGB_CUDA(cudaMemcpyAsync(d_wrapped, nl->wrapped.p, sizeof(double) * 3 * N,
+                             cudaMemcpyDeviceToDevice, st));
+  return FGB_OK;
+}

@@ -1,0 +1,568 @@
+// K3/K4: kernel against the sparse set, adjoint GEMM and local variance in
+// FP64, plus the device-resident model and the fgb_predict pipeline.
+//
+// For the atoms of species s (rows gathered through a species permutation):
+//   GEMM1 (NT)  C = B2_s S^_s^T;  epilogue c = C/|d|, k = sigma^2 c^xi,
+//               w = sigma^2 xi alpha c^(xi-1)   (normalized_dot_product.cpp:171-181)
+//   E_i = sum_t alpha_t k_it                     (sparse_gp.cpp:751 mean = K^T alpha)
+//   GEMM2 (NN)  G = W S^_s;  epilogue dE/dB2 = (G - xi E d^)/|d|
+//   GEMM3 (NT, lower-triangular)  Z = K L_s^T;  epilogue row sums of Z^2
+//   var_i = k_self - sum_r Z_ir^2                (sparse_gp.cpp:116-133)
+// L_inv of a single-kernel model is block-diagonal by species (cross-species
+// Kuu blocks are exactly zero), so species s only needs its panel of L_inv.
+#include <cstring>
+#include <vector>
+
+#include "fgb_internal.h"
+#include "fgb_kernels.h"
+#include "fgb_model.h"
+#include "fgb_gemm64.cuh"
+
+namespace fgb {
+
+namespace {
+
+constexpr int kRowChunk = 32768;
+using namespace gemm64;
+
+// GEMM1: rows = atoms of one species (through perm), cols = sparse envs.
+__global__ void __launch_bounds__(GT)
+k_kernel_gemm(int M, int N, int K, const double *__restrict__ B2,
+              const int *__restrict__ perm, const double *__restrict__ norms,
+              const double *__restrict__ S, const double *__restrict__ alpha,
+              const unsigned char *__restrict__ svalid, double sig2, double xi,
+              double *__restrict__ Kmat, double *__restrict__ Wmat) {
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  double acc[4][4];
+  gemm_mainloop<true>(acc, m0, n0, M, N, K, B2, K, perm, S, K);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int m = m0 + ty + 16 * i;
+    if (m >= M) continue;
+    double nd = norms[perm[m]];
+    bool dok = nd >= kEmptyThresh;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int n = n0 + tx + 16 * j;
+      if (n >= N) continue;
+      double kv = 0.0, wv = 0.0;
+      if (dok && svalid[n]) {
+        double c = acc[i][j] / nd;
+        kv = sig2 * powx(c, xi);
+        wv = sig2 * xi * powx(c, xi - 1.0) * alpha[n];
+      }
+      Kmat[(long long)m * N + n] = kv;
+      Wmat[(long long)m * N + n] = wv;
+    }
+  }
+}
+
+// E_m = sum_n alpha_n K[m][n]: warp per row, fixed-order shuffle tree.
+__global__ void k_row_energy(int M, int N, const double *__restrict__ Kmat,
+                             const double *__restrict__ alpha,
+                             const int *__restrict__ perm,
+                             double *__restrict__ e_rows,
+                             double *__restrict__ e_atom) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= M) return;
+  const double *row = Kmat + (long long)warp * N;
+  double acc = 0.0;
+  for (int n = lane; n < N; n += 32) acc += alpha[n] * row[n];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    e_rows[warp] = acc;
+    if (e_atom) e_atom[perm[warp]] = acc;
+  }
+}
+
+// GEMM2: G = W S (NN); epilogue dE/dB2 rows in atom order.
+__global__ void __launch_bounds__(GT)
+k_adjoint_gemm(int M, int N, int K, const double *__restrict__ Wmat,
+               const double *__restrict__ S, const int *__restrict__ perm,
+               const double *__restrict__ norms, const double *__restrict__ B2,
+               const double *__restrict__ e_rows, double xi,
+               double *__restrict__ gB2) {
+  // M rows (atoms), N = n_d columns, K = M_s
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  double acc[4][4];
+  gemm_mainloop<false>(acc, m0, n0, M, N, K, Wmat, K, nullptr, S, N);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int m = m0 + ty + 16 * i;
+    if (m >= M) continue;
+    int atom = perm[m];
+    double nd = norms[atom];
+    bool dok = nd >= kEmptyThresh;
+    double inv = dok ? 1.0 / nd : 0.0;
+    double xe = xi * e_rows[m];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int n = n0 + tx + 16 * j;
+      if (n >= N) continue;
+      double v = 0.0;
+      if (dok) {
+        double dh = B2[(long long)atom * N + n] * inv;
+        v = (acc[i][j] - xe * dh) * inv;
+      }
+      gB2[(long long)atom * N + n] = v;
+    }
+  }
+}
+
+// GEMM3: Z = K L^T over the lower-triangular panel; row sums of Z^2 per
+// column tile.
+__global__ void __launch_bounds__(GT)
+k_variance_gemm(int M, int R, int Ms, const double *__restrict__ Kmat,
+                const double *__restrict__ Lp, double *__restrict__ part,
+                int ntiles) {
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kmax = min(Ms, n0 + BN);
+  double acc[4][4];
+  gemm_mainloop<true>(acc, m0, n0, M, R, kmax, Kmat, Ms, nullptr, Lp, Ms);
+  __shared__ double red[16][BM + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int n = n0 + tx + 16 * j;
+      if (n < R) s += acc[i][j] * acc[i][j];
+    }
+    red[tx][ty + 16 * i] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < BM) {
+    int mm = threadIdx.x;
+    double s = 0.0;
+    for (int q = 0; q < 16; q++) s += red[q][mm];
+    int m = m0 + mm;
+    if (m < M) part[(long long)m * ntiles + blockIdx.x] = s;
+  }
+}
+
+__global__ void k_variance_final(int M, int ntiles, const double *__restrict__ part,
+                                 const int *__restrict__ perm,
+                                 const double *__restrict__ norms, double sig2,
+                                 double xi, double *__restrict__ var) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  int atom = perm[m];
+  double nd = norms[atom];
+  double s = 0.0;
+  for (int t = 0; t < ntiles; t++) s += part[(long long)m * ntiles + t];
+  // K_self = sig^2 (d.d/(|d||d|))^xi, zero for an empty environment.
+  double kself = nd >= kEmptyThresh ? sig2 * powx((nd * nd) / (nd * nd), xi)
+                                    : 0.0;
+  var[atom] = kself - s;
+}
+
+__global__ void k_species_flags(int n, const int *__restrict__ species, int s,
+                                int *__restrict__ flags) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flags[i] = species[i] == s ? 1 : 0;
+}
+
+__global__ void k_species_scatter(int n, const int *__restrict__ species, int s,
+                                  const int *__restrict__ pos, int base,
+                                  int *__restrict__ perm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && species[i] == s) perm[base + pos[i]] = i;
+}
+
+__global__ void k_check_species(int n, const int *__restrict__ species, int ns,
+                                int *__restrict__ flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && (species[i] < 0 || species[i] >= ns)) atomicExch(flag, 1);
+}
+
+}  // namespace
+
+int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
+                  cudaStream_t st) {
+  if (n == 0) return FGB_OK;
+  int rc = flag.ensure(sizeof(int));
+  if (rc) return rc;
+  FGB_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+  k_check_species<<<ceil_div(n, 256), 256, 0, st>>>(n, d_species, n_species,
+                                                    flag.as<int>());
+  FGB_LAUNCH_CHECK("k_check_species");
+  int h = 0;
+  FGB_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("species must lie in [0, %d)", n_species);
+    return FGB_EINVAL;
+  }
+  return FGB_OK;
+}
+
+// Species permutation: perm = atoms of species 0 (ascending), then 1, ...
+int species_permutation(fgb_model_s *m, const int *d_species, int N,
+                        std::vector<int> &counts, cudaStream_t st) {
+  const int S = m->b2.n_species;
+  counts.assign(S, 0);
+  int rc;
+  if ((rc = m->ws.perm.ensure(sizeof(int) * (N + 1))) ||
+      (rc = m->ws.flags.ensure(sizeof(int) * (N + 1))) ||
+      (rc = m->ws.pos.ensure(sizeof(int) * (N + 1))) ||
+      (rc = m->ws.scal.ensure(sizeof(int) * (S + 1))))
+    return rc;
+  std::vector<int> h(S);
+  for (int s = 0; s < S; s++) {
+    k_species_flags<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, s,
+                                                      m->ws.flags.as<int>());
+    FGB_LAUNCH_CHECK("k_species_flags");
+    if ((rc = scan_int_to_int(m->ws.flags.as<int>(), m->ws.pos.as<int>(), N,
+                              m->ws.scal.as<int>() + s, m->ws.scan_tmp, st)))
+      return rc;
+    FGB_CUDA(cudaMemcpyAsync(&h[s], m->ws.scal.as<int>() + s, sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+    int base = 0;
+    for (int q = 0; q < s; q++) base += h[q];
+    k_species_scatter<<<ceil_div(N, 256), 256, 0, st>>>(
+        N, d_species, s, m->ws.pos.as<int>(), base, m->ws.perm.as<int>());
+    FGB_LAUNCH_CHECK("k_species_scatter");
+  }
+  counts = h;
+  return FGB_OK;
+}
+
+// Kernel, energy, adjoint GEMM and variance for all species (FP64).
+int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
+                      bool want_grad, bool want_var, double *d_e_atom,
+                      double *d_gB2, double *d_var, cudaStream_t st) {
+  const B2Params &p = m->b2;
+  const int nd = p.n_d;
+  const double sig2 = m->sigma * m->sigma;
+  int base = 0;
+  for (int s = 0; s < p.n_species; s++) {
+    const int Ns = counts[s];
+    const int Ms = m->h_counts[s];
+    const int *perm_s = m->ws.perm.as<int>() + base;
+    if (Ns > 0 && Ms == 0 && want_var) {
+      // No sparse environments of this species: k = 0 and E = 0 (zero
+      // filled), var = k_self.
+      k_variance_final<<<ceil_div(Ns, 128), 128, 0, st>>>(
+          Ns, 0, nullptr, perm_s, m->ws.norms.as<double>(), sig2, m->power,
+          d_var);
+      FGB_LAUNCH_CHECK("k_variance_final");
+    }
+    for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRowChunk) {
+      const int Mr = std::min(kRowChunk, Ns - r0);
+      const int *perm = perm_s + r0;
+      int rc;
+      if ((rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms)) ||
+          (rc = m->ws.wmat.ensure(sizeof(double) * (size_t)Mr * Ms)) ||
+          (rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr)))
+        return rc;
+      dim3 g1(ceil_div(Ms, BN), ceil_div(Mr, BM));
+      k_kernel_gemm<<<g1, GT, 0, st>>>(
+          Mr, Ms, nd, m->ws.B2.as<double>(), perm, m->ws.norms.as<double>(),
+          m->S.as<double>() + (size_t)m->h_offsets[s] * nd,
+          m->alpha.as<double>() + m->h_offsets[s],
+          m->svalid.as<unsigned char>() + m->h_offsets[s], sig2, m->power,
+          m->ws.kmat.as<double>(), m->ws.wmat.as<double>());
+      FGB_LAUNCH_CHECK("k_kernel_gemm");
+      k_row_energy<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+          Mr, Ms, m->ws.kmat.as<double>(),
+          m->alpha.as<double>() + m->h_offsets[s], perm,
+          m->ws.erows.as<double>(), d_e_atom);
+      FGB_LAUNCH_CHECK("k_row_energy");
+      if (want_grad) {
+        dim3 g2(ceil_div(nd, BN), ceil_div(Mr, BM));
+        k_adjoint_gemm<<<g2, GT, 0, st>>>(
+            Mr, nd, Ms, m->ws.wmat.as<double>(),
+            m->S.as<double>() + (size_t)m->h_offsets[s] * nd, perm,
+            m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+            m->ws.erows.as<double>(), m->power, d_gB2);
+        FGB_LAUNCH_CHECK("k_adjoint_gemm");
+      }
+      if (want_var) {
+        const int R = m->h_panel_rows[s];
+        const int ntiles = ceil_div(R, BN);
+        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
+          return rc;
+        dim3 g3(ntiles, ceil_div(Mr, BM));
+        k_variance_gemm<<<g3, GT, 0, st>>>(
+            Mr, R, Ms, m->ws.kmat.as<double>(),
+            m->Lp.as<double>() + m->h_panel_off[s], m->ws.part.as<double>(),
+            ntiles);
+        FGB_LAUNCH_CHECK("k_variance_gemm");
+        k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
+            Mr, ntiles, m->ws.part.as<double>(), perm, m->ws.norms.as<double>(),
+            sig2, m->power, d_var);
+        FGB_LAUNCH_CHECK("k_variance_final");
+      }
+    }
+    base += Ns;
+  }
+  return FGB_OK;
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+// ----------------------------------------------------------------- model
+extern "C" int fgb_model_create(fgb_model_t *out, fgb_b2_t b2, double sigma,
+                                double power) {
+  if (!out || !b2) { set_error("fgb_model_create: invalid arguments"); return FGB_EINVAL; }
+  if (!std::isfinite(sigma) || !std::isfinite(power)) {
+    set_error("fgb_model_create: non-finite hyperparameters");
+    return FGB_EINVAL;
+  }
+  fgb_model_s *m = new fgb_model_s();
+  m->b2 = b2->p;
+  m->sigma = sigma;
+  m->power = power;
+  *out = m;
+  return FGB_OK;
+}
+
+extern "C" int fgb_model_destroy(fgb_model_t m) {
+  delete m;
+  return FGB_OK;
+}
+
+extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
+                             const double *h_desc, const double *h_alpha,
+                             const double *h_L_inv) {
+  if (!m || !h_counts) { set_error("fgb_model_set: invalid arguments"); return FGB_EINVAL; }
+  const int S = m->b2.n_species, nd = m->b2.n_d;
+  m->h_counts.assign(h_counts, h_counts + S);
+  m->h_offsets.assign(S + 1, 0);
+  for (int s = 0; s < S; s++) {
+    if (h_counts[s] < 0) { set_error("fgb_model_set: negative count"); return FGB_EINVAL; }
+    m->h_offsets[s + 1] = m->h_offsets[s] + h_counts[s];
+  }
+  const int M = m->h_offsets[S];
+  m->M = M;
+  if (M > 0 && !h_desc) { set_error("fgb_model_set: descriptors required"); return FGB_EINVAL; }
+  // normalised sparse descriptors, validity flags (norm >= 1e-8)
+  std::vector<double> Sh((size_t)M * nd);
+  std::vector<unsigned char> valid(M);
+  std::vector<double> snorm(M);
+  for (int t = 0; t < M; t++) {
+    const double *row = h_desc + (size_t)t * nd;
+    double nn = 0;
+    for (int q = 0; q < nd; q++) nn += row[q] * row[q];
+    double n = std::sqrt(nn);
+    snorm[t] = n;
+    valid[t] = n >= kEmptyThresh;
+    for (int q = 0; q < nd; q++) Sh[(size_t)t * nd + q] = valid[t] ? row[q] / n : 0.0;
+  }
+  m->h_snorm = snorm;
+  m->h_desc.assign(h_desc, h_desc + (size_t)M * nd);
+  int rc;
+  if ((rc = m->S.ensure(sizeof(double) * (size_t)M * nd)) ||
+      (rc = m->svalid.ensure(M + 1)) ||
+      (rc = m->Sraw.ensure(sizeof(double) * (size_t)M * nd)) ||
+      (rc = m->snorm.ensure(sizeof(double) * (M + 1))))
+    return rc;
+  if (M > 0) {
+    FGB_CUDA(cudaMemcpy(m->S.p, Sh.data(), sizeof(double) * (size_t)M * nd,
+                        cudaMemcpyHostToDevice));
+    FGB_CUDA(cudaMemcpy(m->Sraw.p, h_desc, sizeof(double) * (size_t)M * nd,
+                        cudaMemcpyHostToDevice));
+    FGB_CUDA(cudaMemcpy(m->svalid.p, valid.data(), M, cudaMemcpyHostToDevice));
+    FGB_CUDA(cudaMemcpy(m->snorm.p, snorm.data(), sizeof(double) * M,
+                        cudaMemcpyHostToDevice));
+  }
+  m->solved = false;
+  if (!h_alpha || !h_L_inv) return FGB_OK;
+  if ((rc = m->alpha.ensure(sizeof(double) * (M + 1)))) return rc;
+  if (M > 0)
+    FGB_CUDA(cudaMemcpy(m->alpha.p, h_alpha, sizeof(double) * M,
+                        cudaMemcpyHostToDevice));
+  m->h_alpha.assign(h_alpha, h_alpha + M);
+  // L_inv panels: species s uses rows [c_s, c_s + R_s) and columns
+  // [c_s, c_s + M_s); R_s = M_s when everything below the diagonal block is
+  // exactly zero (the single-kernel case), else M - c_s.
+  std::vector<double> panels;
+  m->h_panel_rows.assign(S, 0);
+  m->h_panel_off.assign(S, 0);
+  for (int s = 0; s < S; s++) {
+    const int cs = m->h_offsets[s], Ms = h_counts[s];
+    bool below_zero = true;
+    for (int r = cs + Ms; r < M && below_zero; r++)
+      for (int c = cs; c < cs + Ms; c++)
+        if (h_L_inv[(size_t)r * M + c] != 0.0) { below_zero = false; break; }
+    const int R = below_zero ? Ms : M - cs;
+    m->h_panel_rows[s] = R;
+    m->h_panel_off[s] = (long long)panels.size();
+    for (int r = 0; r < R; r++)
+      for (int c = 0; c < Ms; c++)
+        panels.push_back(h_L_inv[(size_t)(cs + r) * M + cs + c]);
+  }
+  if ((rc = m->Lp.ensure(sizeof(double) * (panels.size() + 1)))) return rc;
+  if (!panels.empty())
+    FGB_CUDA(cudaMemcpy(m->Lp.p, panels.data(), sizeof(double) * panels.size(),
+                        cudaMemcpyHostToDevice));
+  m->solved = true;
+  return FGB_OK;
+}
+
+// ------------------------------------------------------------- predict
+static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
+                        const double *h_cells, const double *d_positions,
+                        const int *d_species, double cutoff, int want,
+                        int precision, double *d_energy, double *d_forces,
+                        double *d_stress, double *d_local_var,
+                        cudaStream_t st) {
+  if (!m->solved) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  if (precision != FGB_PREC_FP64 && precision != FGB_PREC_MIXED) {
+    set_error("fgb_predict: unknown precision %d", precision);
+    return FGB_EINVAL;
+  }
+  int rc;
+  if ((rc = fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
+                            d_positions, cutoff, st)))
+    return rc;
+  const B2Params &p = m->b2;
+  const int N = m->nl.n_atoms;
+  const long long P = m->nl.n_pairs;
+  if ((rc = check_species(d_species, N, p.n_species, m->ws.flag, st))) return rc;
+  const bool want_e = want & FGB_WANT_ENERGY, want_f = want & FGB_WANT_FORCES,
+             want_s = want & FGB_WANT_STRESS, want_v = want & FGB_WANT_LOCAL_VAR;
+  const bool want_grad = want_f || want_s;
+  if ((rc = m->ws.A.ensure(sizeof(double) * ((size_t)N * p.n_A + 1))) ||
+      (rc = m->ws.B2.ensure(sizeof(double) * ((size_t)N * p.n_d + 1))) ||
+      (rc = m->ws.norms.ensure(sizeof(double) * (N + 1))) ||
+      (rc = m->ws.e_atom.ensure(sizeof(double) * (N + 1))) ||
+      (rc = m->ws.var.ensure(sizeof(double) * (N + 1))) ||
+      (rc = m->ws.volume.ensure(sizeof(double) * (n_struc + 1))) ||
+      (rc = m->ws.atom_off.ensure(sizeof(int) * (n_struc + 1))))
+    return rc;
+  if (want_grad &&
+      ((rc = m->ws.gB2.ensure(sizeof(double) * ((size_t)N * p.n_d + 1))) ||
+       (rc = m->ws.pair_grad.ensure(sizeof(double3) * (P + 1))) ||
+       (rc = m->ws.forces.ensure(sizeof(double) * (3 * (size_t)N + 1))) ||
+       (rc = m->ws.virial.ensure(sizeof(double) * (6 * (size_t)N + 1)))))
+    return rc;
+  FGB_CUDA(cudaMemcpyAsync(m->ws.volume.p, m->nl.h_volume.data(),
+                           sizeof(double) * n_struc, cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(m->ws.atom_off.p, h_atom_offsets,
+                           sizeof(int) * (n_struc + 1), cudaMemcpyHostToDevice,
+                           st));
+  if (N > 0) {
+    FGB_CUDA(cudaMemsetAsync(m->ws.e_atom.p, 0, sizeof(double) * N, st));
+    FGB_CUDA(cudaMemsetAsync(m->ws.var.p, 0, sizeof(double) * N, st));
+    if (want_grad)
+      FGB_CUDA(cudaMemsetAsync(m->ws.gB2.p, 0, sizeof(double) * (size_t)N * p.n_d, st));
+  }
+  if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
+                              m->ws.B2.as<double>(), m->ws.norms.as<double>(),
+                              st)))
+    return rc;
+  std::vector<int> counts;
+  if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
+  if (precision == FGB_PREC_MIXED) {
+    if ((rc = kernel_stage_mixed(m, N, counts, want_grad, want_v,
+                                 m->ws.e_atom.as<double>(),
+                                 m->ws.gB2.as<double>(), m->ws.var.as<double>(),
+                                 st)))
+      return rc;
+  } else {
+    if ((rc = kernel_stage_fp64(m, N, counts, want_grad, want_v,
+                                m->ws.e_atom.as<double>(),
+                                m->ws.gB2.as<double>(), m->ws.var.as<double>(),
+                                st)))
+      return rc;
+  }
+  if (want_grad) {
+    if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
+                                m->ws.gB2.as<double>(),
+                                m->ws.pair_grad.as<double3>(), st)))
+      return rc;
+    if ((rc = launch_forces(&m->nl, m->ws.pair_grad.as<double3>(),
+                            m->ws.forces.as<double>(), m->ws.virial.as<double>(),
+                            st)))
+      return rc;
+    if (d_forces && want_f && N > 0)
+      FGB_CUDA(cudaMemcpyAsync(d_forces, m->ws.forces.p,
+                               sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice,
+                               st));
+  }
+  if ((want_e && d_energy) || (want_s && d_stress))
+    if ((rc = launch_struct_reduce(
+             n_struc, m->ws.atom_off.as<int>(), m->ws.volume.as<double>(),
+             m->ws.e_atom.as<double>(),
+             want_grad ? m->ws.virial.as<double>() : nullptr,
+             want_e ? d_energy : nullptr, want_s ? d_stress : nullptr, st)))
+      return rc;
+  if (want_v && d_local_var && N > 0)
+    FGB_CUDA(cudaMemcpyAsync(d_local_var, m->ws.var.p, sizeof(double) * N,
+                             cudaMemcpyDeviceToDevice, st));
+  return FGB_OK;
+}
+
+extern "C" int fgb_predict(fgb_model_t m, int n_struc, const int *h_atom_offsets,
+                           const double *h_cells, const double *d_positions,
+                           const int *d_species, double cutoff, int want,
+                           int precision, double *d_energy, double *d_forces,
+                           double *d_stress, double *d_local_var, void *stream) {
+  if (!m) { set_error("fgb_predict: null model"); return FGB_EINVAL; }
+  return predict_impl(m, n_struc, h_atom_offsets, h_cells, d_positions,
+                      d_species, cutoff, want, precision, d_energy, d_forces,
+                      d_stress, d_local_var, (cudaStream_t)stream);
+}
+
+extern "C" int fgb_predict_host(fgb_model_t m, int n_struc,
+                                const int *h_atom_offsets, const double *h_cells,
+                                const double *h_positions, const int *h_species,
+                                double cutoff, int want, int precision,
+                                double *h_energy, double *h_forces,
+                                double *h_stress, double *h_local_var,
+                                void *stream) {
+  if (!m || n_struc <= 0 || !h_atom_offsets) {
+    set_error("fgb_predict_host: invalid arguments");
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = h_atom_offsets[n_struc];
+  int rc;
+  if ((rc = m->io.pos.ensure(sizeof(double) * (3 * (size_t)N + 1))) ||
+      (rc = m->io.species.ensure(sizeof(int) * (N + 1))) ||
+      (rc = m->io.energy.ensure(sizeof(double) * (n_struc + 1))) ||
+      (rc = m->io.forces.ensure(sizeof(double) * (3 * (size_t)N + 1))) ||
+      (rc = m->io.stress.ensure(sizeof(double) * (6 * (size_t)n_struc + 1))) ||
+      (rc = m->io.var.ensure(sizeof(double) * (N + 1))))
+    return rc;
+  if (N > 0) {
+    FGB_CUDA(cudaMemcpyAsync(m->io.pos.p, h_positions, sizeof(double) * 3 * N,
+                             cudaMemcpyHostToDevice, st));
+    FGB_CUDA(cudaMemcpyAsync(m->io.species.p, h_species, sizeof(int) * N,
+                             cudaMemcpyHostToDevice, st));
+  }
+  rc = predict_impl(m, n_struc, h_atom_offsets, h_cells, m->io.pos.as<double>(),
+                    m->io.species.as<int>(), cutoff, want, precision,
+                    m->io.energy.as<double>(), m->io.forces.as<double>(),
+                    m->io.stress.as<double>(), m->io.var.as<double>(), st);
+  if (rc) return rc;
+  if (h_energy && (want & FGB_WANT_ENERGY))
+    FGB_CUDA(cudaMemcpyAsync(h_energy, m->io.energy.p, sizeof(double) * n_struc,
+                             cudaMemcpyDeviceToHost, st));
+  if (h_forces && (want & FGB_WANT_FORCES) && N > 0)
+    FGB_CUDA(cudaMemcpyAsync(h_forces, m->io.forces.p, sizeof(double) * 3 * N,
+                             cudaMemcpyDeviceToHost, st));
+  if (h_stress && (want & FGB_WANT_STRESS))
+    FGB_CUDA(cudaMemcpyAsync(h_stress, m->io.stress.p,
+                             sizeof(double) * 6 * n_struc, cudaMemcpyDeviceToHost,
+                             st));
+  if (h_local_var && (want & FGB_WANT_LOCAL_VAR) && N > 0)
+    FGB_CUDA(cudaMemcpyAsync(h_local_var, m->io.var.p, sizeof(double) * N,
+                             cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  return FGB_OK;
+}

@@ -1,0 +1,195 @@
+/*
+ * libflaregb — GB300-native (sm_103a) sparse-GP prediction for FLARE's
+ * B2 / NormalizedDotProduct / SparseGP path, behind a plain C ABI.
+ *
+ * Every entry point returns an int status (FGB_OK = 0) and never aborts;
+ * fgb_last_error() returns the message of the last failure on this thread.
+ * Pointers named d_* are device pointers on the current CUDA device, h_* are
+ * host pointers.  `stream` is a cudaStream_t passed as void* (NULL = legacy
+ * default stream).  No entry point takes or returns framework (torch) types.
+ *
+ * Reference interfaces replaced (paths inside mir-group/flare):
+ *   Structure(cell, species, positions, cutoff, descriptors)
+ *       src/flare_pp/structure.cpp:27-118, bound at src/ace_binding.cpp:30-35
+ *   B2(radial_basis, cutoff_function, radial_hyps, cutoff_hyps, settings[, cutoffs])
+ *       src/flare_pp/descriptors/b2.cpp:13-50,76-242, bound at src/ace_binding.cpp:125-138
+ *   NormalizedDotProduct(sigma, power).envs_struc / envs_envs
+ *       src/flare_pp/kernels/normalized_dot_product.cpp:15-214, bound at src/ace_binding.cpp:168-176
+ *   SparseGP.update_matrices_QR / predict_{mean,SOR,local_uncertainties}
+ *       src/flare_pp/bffs/sparse_gp.cpp:607-757, bound at src/ace_binding.cpp:195-213
+ */
+#ifndef FLAREGB_H
+#define FLAREGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status */
+enum {
+  FGB_OK = 0,
+  FGB_EINVAL = 1,   /* bad argument (reference: std::invalid_argument)     */
+  FGB_ENOMEM = 2,   /* device allocation failed                            */
+  FGB_ECUDA = 3,    /* CUDA runtime / library error                        */
+  FGB_ETIMEOUT = 4, /* a bounded device wait ran out                       */
+  FGB_ESTALE = 5,   /* model weights not solved (reference: runtime_error
+                       "L_inv must be up to date", sparse_gp.cpp:644-649)  */
+  FGB_ENOTSUP = 6   /* valid in the reference but not built here           */
+};
+
+/* radial bases (radial.cpp:381-408) and cutoffs (cutoffs.cpp:87-103) */
+enum { FGB_RADIAL_CHEBYSHEV = 0 };
+enum {
+  FGB_CUTOFF_QUADRATIC = 0,
+  FGB_CUTOFF_HARD = 1,
+  FGB_CUTOFF_COSINE = 2,
+  FGB_CUTOFF_POLYNOMIAL = 3,
+  FGB_CUTOFF_POWER = 4
+};
+
+/* prediction precision */
+enum {
+  FGB_PREC_FP64 = 0,  /* FP64 adjoint path                                   */
+  FGB_PREC_MIXED = 1  /* FP64 descriptors/variance, FP32 tensor-core E and F */
+};
+
+/* prediction outputs */
+enum {
+  FGB_WANT_ENERGY = 1,
+  FGB_WANT_FORCES = 2,
+  FGB_WANT_STRESS = 4,
+  FGB_WANT_LOCAL_VAR = 8
+};
+
+const char *fgb_last_error(void);
+int fgb_version(void);
+
+/* ----------------------------------------------------- neighbour list
+ * Cell-list neighbour build for a batch of periodic structures.  Replaces
+ * Structure::compute_neighbors (structure.cpp:52-118): the same pairs
+ * (0 < d < cutoff, image shifts |s| <= sweep with sweep from
+ * get_single_sweep_cutoff, structure.cpp:35,135-165), in the reference's
+ * order (i, then j ascending, then s1, s2, s3 ascending), with relative
+ * vectors computed in the same FP64 operation order, so the lists are
+ * bit-exact against the reference.  Structures are packed: structure s owns
+ * atoms [h_atom_offsets[s], h_atom_offsets[s+1]).
+ */
+typedef struct fgb_nlist_s *fgb_nlist_t;
+int fgb_nlist_create(fgb_nlist_t *out);
+int fgb_nlist_destroy(fgb_nlist_t nl);
+int fgb_nlist_build(fgb_nlist_t nl, int n_struc, const int *h_atom_offsets,
+                    const double *h_cells, const double *d_positions,
+                    double cutoff, void *stream);
+/* total pairs and atoms of the last build */
+int fgb_nlist_size(fgb_nlist_t nl, long long *n_pairs, int *n_atoms);
+/* Copy out in the reference's Structure layout (device pointers; any may be
+ * NULL): neighbor_count[N], structure_indices[P] (index within the
+ * structure), shifts[P*3], relative_positions[P*4] = (d, x, y, z),
+ * wrapped_positions[N*3]. */
+int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
+                     int *d_structure_indices, int *d_shifts,
+                     double *d_relative_positions, double *d_wrapped,
+                     void *stream);
+
+/* ------------------------------------------------------- B2 descriptor
+ * B2(radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
+ *    [n_species, n_max, l_max], cutoffs[n_species^2]) — b2.cpp:13-50.
+ * radial_hyps = [r1, r2(, ...)]; cutoffs == NULL means r2 for every pair.
+ */
+typedef struct fgb_b2_s *fgb_b2_t;
+int fgb_b2_create(fgb_b2_t *out, int radial_basis, int cutoff_function,
+                  const double *radial_hyps, int n_radial_hyps,
+                  const double *cutoff_hyps, int n_cutoff_hyps, int n_species,
+                  int n_max, int l_max, const double *h_cutoffs);
+int fgb_b2_destroy(fgb_b2_t b2);
+int fgb_b2_size(fgb_b2_t b2, int *n_descriptors, int *n_single_bond);
+
+/* B2 values and norms in atom order (B2::compute_struc values,
+ * b2.cpp:181-242 without the stored gradients): d_B2[N * n_d], d_norms[N].
+ * d_species[N] are the coded species (0..n_species-1). */
+int fgb_b2_forward(fgb_b2_t b2, fgb_nlist_t nl, const int *d_species,
+                   double *d_B2, double *d_norms, void *stream);
+
+/* Stored forward-mode gradients, the reference's algorithm (b2.cpp:181-242):
+ * over the neighbour list of `nl` (pairs filtered by the per-pair cutoff
+ * get zero rows): d_dB2[3P * n_d] with row 3p+c = dB2_i/dr_ij,c and
+ * d_force_dots[3P] = dB2/dr . B2. */
+int fgb_b2_forward_dervs(fgb_b2_t b2, fgb_nlist_t nl, const int *d_species,
+                         double *d_B2, double *d_norms, double *d_dB2,
+                         double *d_force_dots, void *stream);
+
+/* ------------------------------------------------------------- model
+ * Device-resident sparse GP: B2 settings, NormalizedDotProduct(sigma,
+ * power), sparse set grouped by species (sparse_gp.cpp sparse_descriptors),
+ * alpha and L_inv (sparse_gp.cpp:607-641).
+ */
+typedef struct fgb_model_s *fgb_model_t;
+int fgb_model_create(fgb_model_t *out, fgb_b2_t b2, double sigma,
+                     double power);
+int fgb_model_destroy(fgb_model_t m);
+/* h_counts[n_species]: sparse environments per species; h_desc[M * n_d]
+ * species-grouped rows (species 0 first); h_alpha[M]; h_L_inv[M * M]
+ * row-major (the kernel's block of L_inv).  h_alpha/h_L_inv may be NULL to
+ * load only the sparse set (model is then stale for prediction). */
+int fgb_model_set(fgb_model_t m, const int *h_counts, const double *h_desc,
+                  const double *h_alpha, const double *h_L_inv);
+
+/* Full prediction for a packed batch of structures (device pointers):
+ * neighbours (cutoff = Structure cutoff), B2, kernel against the sparse set,
+ * mean energy / forces / stress by the reverse-mode adjoint and the local
+ * variance sigma^2 - |L_inv k|^2 (sparse_gp.cpp:94-139, 731-757).
+ * Outputs (any may be NULL if not wanted):
+ *   d_energy[n_struc], d_forces[N*3] (atom order),
+ *   d_stress[n_struc*6] (flare order xx, xy, xz, yy, yz, zz: mean_efs[-6:]),
+ *   d_local_var[N] (atom order; the calculator's sort_variances applied). */
+int fgb_predict(fgb_model_t m, int n_struc, const int *h_atom_offsets,
+                const double *h_cells, const double *d_positions,
+                const int *d_species, double cutoff, int want, int precision,
+                double *d_energy, double *d_forces, double *d_stress,
+                double *d_local_var, void *stream);
+
+/* Same with HOST input/output buffers: copies in, predicts, copies out on
+ * `stream` and synchronises it. */
+int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
+                     const double *h_cells, const double *h_positions,
+                     const int *h_species, double cutoff, int want,
+                     int precision, double *h_energy, double *h_forces,
+                     double *h_stress, double *h_local_var, void *stream);
+
+/* NormalizedDotProduct::envs_envs (normalized_dot_product.cpp:28-89) for
+ * one species block in FP64: d_kern[n1 * n2] (row-major) =
+ * sig2 * (d1.d2 / (norm1 norm2))^power, zero where either norm < 1e-8.
+ * d_desc1[n1 * n_desc], d_norm1[n1], d_desc2[n2 * n_desc], d_norm2[n2]. */
+int fgb_envs_envs(const double *d_desc1, const double *d_norm1, int n1,
+                  const double *d_desc2, const double *d_norm2, int n2,
+                  int n_desc, double sig2, double power, double *d_kern,
+                  void *stream);
+
+/* NormalizedDotProduct::envs_struc (normalized_dot_product.cpp:117-214) on
+ * the GPU in FP64, the reference algorithm with stored gradients: the model's
+ * sparse set against ONE structure (n_struc == 1 build of `nl`).
+ * d_kern[M * (1 + 3N + 6)] row-major. */
+int fgb_envs_struc(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
+                   double *d_kern, void *stream);
+
+/* Plain FP64 form of SparseGP::predict_local_uncertainties for one
+ * structure: envs_struc (stored gradients), mean_efs = K^T alpha, and the
+ * local variances via the envs_envs route.  d_mean_efs[1+3N+6],
+ * d_local_var[N] (atom order). */
+int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
+                      double *d_mean_efs, double *d_local_var, void *stream);
+
+/* SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 on the GPU:
+ * Cholesky of Kuu + jitter I, L_inv, QR of [diag(sqrt(noise)) Kuf^T ; L^T],
+ * alpha = R^-1 Q^T b.  All device pointers, row-major.
+ * d_Kuu[M*M], d_Kuf[M*n_labels], d_y[n_labels], d_noise[n_labels] ->
+ * d_alpha[M], d_L_inv[M*M], d_R_inv[M*M] (may be NULL). */
+int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
+                 const double *d_Kuf, const double *d_y,
+                 const double *d_noise, double jitter, double *d_alpha,
+                 double *d_L_inv, double *d_R_inv, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLAREGB_H */

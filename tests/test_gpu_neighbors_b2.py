@@ -1,0 +1,94 @@
+"""GPU: cell-list neighbour list bit-exact against the oracle's brute-force
+list (structure.cpp:52-118), and B2 against the oracle (b2.cpp)."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import b2_args, random_atoms
+from flare_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def cases():
+    out = []
+    out.append(("fcc256", *syn.fcc_al(seed=1100), 5.0))
+    out.append(("alloy1000", *syn.random_alloy(1000, seed=2100), 5.5))
+    out.append(("tiny_box_sweep3", *random_atoms(seed=11), 5.0))
+    # skewed triclinic cell (reference sweep can be conservative here)
+    c, s, p = syn.random_alloy(200, seed=7)
+    sk = np.array([[1.0, 0.0, 0.0], [0.35, 1.0, 0.0], [0.2, -0.3, 1.0]])
+    out.append(("triclinic", c @ sk, s, p @ sk, 5.0))
+    # atoms outside the cell (wrapping) and one exactly on a face
+    c, s, p = syn.fcc_al(n_cells=3, seed=5)
+    p = p + np.array([16.2, -8.1, 3 * 4.05 * 2])
+    p[0] = [0.0, 0.0, 0.0]
+    out.append(("unwrapped", c, s, p, 5.0))
+    out.append(("sparse_gas", np.eye(3) * 30.0, np.zeros(3, int),
+                np.array([[0, 0, 0], [1, 1, 1], [15, 15, 15.]]), 5.0))
+    return out
+
+
+@pytest.mark.parametrize("case", cases(), ids=lambda c: c[0])
+def test_neighbor_list_bit_exact(case):
+    import flare_gb300 as fg
+    name, cell, sp, pos, rc = case
+    o = oracle.Structure(cell, sp, pos, rc, [])
+    g = fg.Structure(cell, sp, pos, rc, [])
+    a = g.neighbor_arrays()
+    np.testing.assert_array_equal(a["neighbor_count"], o.neighbor_count)
+    np.testing.assert_array_equal(a["structure_indices"], o.structure_indices)
+    np.testing.assert_array_equal(a["shifts"], o.shifts)
+    # bit-exact relative vectors and distances
+    np.testing.assert_array_equal(a["relative_positions"], o.relative_positions)
+    np.testing.assert_array_equal(a["wrapped_positions"], o.wrapped_positions)
+
+
+def test_empty_structure_and_isolated_atom():
+    import flare_gb300 as fg
+    g = fg.Structure(np.eye(3) * 30.0, [0], [[1.0, 2.0, 3.0]], 5.0, [])
+    a = g.neighbor_arrays()
+    assert a["neighbor_count"].tolist() == [0]
+
+
+def test_nonfinite_positions_raise():
+    import flare_gb300 as fg
+    g = fg.Structure(np.eye(3) * 10.0, [0, 0], [[0, 0, 0], [np.nan, 1, 1]],
+                     5.0, [])
+    with pytest.raises(ValueError):
+        g.neighbor_arrays()
+
+
+@pytest.mark.parametrize("S,nmax,lmax,cut", [(1, 8, 3, "quadratic"),
+                                             (2, 8, 4, "quadratic"),
+                                             (2, 3, 2, "cosine"),
+                                             (1, 10, 6, "quadratic"),
+                                             (3, 4, 10, "polynomial")])
+def test_b2_matches_oracle(S, nmax, lmax, cut):
+    import flare_gb300 as fg
+    cell, sp, pos = syn.random_alloy(150, fractions=[1.0 / S] * S, seed=31 + S)
+    ch = [6.0] if cut == "polynomial" else []
+    args = ("chebyshev", cut, [0.0, 5.0], ch, [S, nmax, lmax])
+    o = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*args)],
+                         compute_dervs=False)
+    g = fg.Structure(cell, sp, pos, 5.0, [fg.B2(*args)])
+    B, n = g.b2_values()
+    ob = o.descriptors[0].atom_B2
+    np.testing.assert_allclose(B.cpu().numpy(), ob, rtol=1e-11,
+                               atol=1e-12 * np.abs(ob).max())
+    np.testing.assert_allclose(n.cpu().numpy(), o.descriptors[0].atom_norms,
+                               rtol=1e-12)
+
+
+def test_b2_per_pair_cutoff_matrix():
+    """b2.cpp:274-277: pairs beyond cutoffs(s_i, s_j) are skipped."""
+    import flare_gb300 as fg
+    cell, sp, pos = random_atoms(seed=21)
+    cut = 5.0 * np.ones((2, 2)) + np.eye(2) - 1
+    args = b2_args(2, 3, 2, 5.0, cutoffs=cut)
+    o = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*args)],
+                         compute_dervs=False)
+    g = fg.Structure(cell, sp, pos, 5.0, [fg.B2(*args[:5], cutoffs=cut)])
+    B, _ = g.b2_values()
+    np.testing.assert_allclose(B.cpu().numpy(), o.descriptors[0].atom_B2,
+                               rtol=1e-11, atol=1e-13)

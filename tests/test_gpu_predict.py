@@ -1,0 +1,137 @@
+"""GPU: mean energy, forces, stress and local variance against the FP64
+oracle (sparse_gp.cpp:643-757 + calculator.py post-processing), on the
+same trained weights."""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import (b2_args, c1_model, random_atoms, small_two_species,
+                     to_gpu_sgp)
+from flare_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+# FP64 path: tolerances for FP64 arithmetic in a different summation order.
+E_TOL = 1e-9      # eV (absolute, whole structure) scaled by |E| below
+F_TOL = 1e-8      # eV/A
+S_TOL = 1e-10     # eV/A^3
+V_TOL = 1e-10     # variance (absolute)
+
+
+def oracle_predict(ogp, b2a, cell, sp, pos, cutoff=5.0):
+    st = oracle.Structure(cell, sp, pos, cutoff, [oracle.B2Settings(*b2a)])
+    ogp.predict_local_uncertainties(st)
+    m = st.mean_efs
+    var = oracle.sort_variances(st, st.local_uncertainties[0])
+    return m[0], m[1:-6].reshape(-1, 3), m[-6:], var
+
+
+def gpu_predict(ggp, calc, structures_np, cutoff=5.0, precision="fp64"):
+    import flare_gb300 as fg
+    strucs = [fg.Structure(c, s, p, cutoff, [calc]) for c, s, p in structures_np]
+    return ggp.predict_batch(strucs, precision=precision)
+
+
+@pytest.mark.parametrize("power", [1, 2])
+def test_small_two_species_fp64(power):
+    ogp, b2a = small_two_species(seed=5, n_train=3, power=power)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    cell, sp, pos = random_atoms(seed=55)
+    E, F, S, V = oracle_predict(ogp, b2a, cell, sp, pos)
+    r = gpu_predict(ggp, calc, [(cell, sp, pos)])
+    assert abs(r["energy"][0] - E) < E_TOL * max(1, abs(E))
+    np.testing.assert_allclose(r["forces"], F, atol=F_TOL)
+    np.testing.assert_allclose(r["stress"][0], S, atol=S_TOL)
+    np.testing.assert_allclose(r["local_var"], V, atol=V_TOL)
+
+
+def test_multicut_model_fp64():
+    ogp, b2a = small_two_species(seed=6, n_train=2, multicut=True)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    cell, sp, pos = random_atoms(seed=66)
+    E, F, S, V = oracle_predict(ogp, b2a, cell, sp, pos)
+    r = gpu_predict(ggp, calc, [(cell, sp, pos)])
+    assert abs(r["energy"][0] - E) < E_TOL * max(1, abs(E))
+    np.testing.assert_allclose(r["forces"], F, atol=F_TOL)
+    np.testing.assert_allclose(r["stress"][0], S, atol=S_TOL)
+    np.testing.assert_allclose(r["local_var"], V, atol=V_TOL)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    ogp, b2a = c1_model()
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    return ogp, b2a, ggp, calc
+
+
+def test_fcc256_fp64(c1):
+    ogp, b2a, ggp, calc = c1
+    cell, sp, pos = syn.fcc_al(seed=1100)
+    E, F, S, V = oracle_predict(ogp, b2a, cell, sp, pos)
+    r = gpu_predict(ggp, calc, [(cell, sp, pos)])
+    # |alpha| ~ 1e4 makes the sum of kernel terms cancel; FP64 agreement
+    # is limited by that cancellation (oracle vs long double: ~1e-9 eV).
+    assert abs(r["energy"][0] - E) < 1e-7
+    np.testing.assert_allclose(r["forces"], F, atol=1e-7)
+    np.testing.assert_allclose(r["stress"][0], S, atol=1e-9)
+    np.testing.assert_allclose(r["local_var"], V, atol=1e-12)
+
+
+def test_batch_equals_alone(c1):
+    """Each structure's result is the same alone and in a batch (bitwise:
+    no float atomics, fixed reduction orders)."""
+    ogp, b2a, ggp, calc = c1
+    items = [syn.fcc_al(seed=s) for s in (1100, 1101, 1102)]
+    items.append(syn.fcc_al(n_cells=3, seed=1103))
+    batch = gpu_predict(ggp, calc, items)
+    off = batch["offsets"]
+    for k, it in enumerate(items):
+        alone = gpu_predict(ggp, calc, [it])
+        assert alone["energy"][0] == batch["energy"][k]
+        np.testing.assert_array_equal(alone["forces"],
+                                      batch["forces"][off[k]:off[k + 1]])
+        np.testing.assert_array_equal(alone["stress"][0], batch["stress"][k])
+        np.testing.assert_array_equal(alone["local_var"],
+                                      batch["local_var"][off[k]:off[k + 1]])
+
+
+def test_deterministic_repeat(c1):
+    ogp, b2a, ggp, calc = c1
+    it = [syn.fcc_al(seed=1105)]
+    a = gpu_predict(ggp, calc, it)
+    b = gpu_predict(ggp, calc, it)
+    for k in ("energy", "forces", "stress", "local_var"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_forces_are_energy_gradient(c1):
+    """Adjoint forces against central differences of the GPU energy."""
+    ogp, b2a, ggp, calc = c1
+    cell, sp, pos = syn.fcc_al(n_cells=2, seed=1107)
+    r = gpu_predict(ggp, calc, [(cell, sp, pos)])
+    h = 1e-4
+    for atom, c in [(0, 0), (3, 2), (17, 1)]:
+        p1 = pos.copy(); p1[atom, c] += h
+        p2 = pos.copy(); p2[atom, c] -= h
+        e1 = gpu_predict(ggp, calc, [(cell, sp, p1)])["energy"][0]
+        e2 = gpu_predict(ggp, calc, [(cell, sp, p2)])["energy"][0]
+        assert abs(r["forces"][atom, c] + (e1 - e2) / (2 * h)) < 1e-5
+
+
+def test_stale_model_raises():
+    import flare_gb300 as fg
+    calc = fg.B2(*b2_args(1, 4, 2, 5.0)[:5])
+    gp = fg.SparseGP([fg.NormalizedDotProduct(1.0, 2)], 0.1, 0.1, 0.1)
+    cell, sp, pos = syn.fcc_al(n_cells=2, seed=1)
+    with pytest.raises(RuntimeError, match="L_inv must be up to date"):
+        gp.predict_mean(fg.Structure(cell, sp, pos, 5.0, [calc]))
+
+
+def test_species_out_of_range_raises(c1):
+    ogp, b2a, ggp, calc = c1
+    import flare_gb300 as fg
+    cell, sp, pos = syn.fcc_al(n_cells=2, seed=1)
+    sp = sp.copy()
+    sp[3] = 4
+    with pytest.raises(ValueError):
+        ggp.predict_batch([fg.Structure(cell, sp, pos, 5.0, [calc])])

@@ -1,0 +1,133 @@
+"""CPU: the oracle against the reference's golden vectors and the
+relations the reference's own tests check."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import b2_args, random_atoms, small_two_species
+from flare_gb300 import synthetic as syn
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "per_pair.npz")
+
+
+def test_ylm_matches_reference_golden():
+    """y_grad.cpp get_Y values and gradients, l <= 10 (golden from the
+    reference's compiled source)."""
+    g = np.load(GOLD)
+    L = int(g["ylm_lmax"])
+    for i, p in enumerate(g["ylm_points"]):
+        mine = np.stack(oracle.ylm(*p, L))
+        ref = g["ylm"][i]
+        np.testing.assert_allclose(mine, ref, rtol=1e-12,
+                                   atol=1e-13 * max(1, np.abs(ref).max()))
+
+
+@pytest.mark.parametrize("cut", ["quadratic", "hard", "cosine", "polynomial",
+                                 "power"])
+def test_radial_matches_reference_golden(cut):
+    """calculate_radial (radial.cpp:344) with the Chebyshev basis."""
+    g = np.load(GOLD)
+    for i, p in enumerate(g["radial_points"]):
+        mine = np.stack(oracle.radial(
+            "chebyshev", cut, *p, g["radial_r"][i], float(g["radial_rcut"]),
+            int(g["radial_nmax"]), 0.0, list(g["cutoff_hyps_" + cut])))
+        np.testing.assert_array_equal(mine, g["radial_" + cut][i])
+
+
+def test_ylm_gradient_finite_difference():
+    """test_y_grad.cpp: gradients against central differences."""
+    r = np.random.Generator(np.random.PCG64(5))
+    for _ in range(10):
+        p = r.normal(size=3)
+        Y, Yx, Yy, Yz = oracle.ylm(*p, 6)
+        h = 1e-6
+        for k, G in enumerate([Yx, Yy, Yz]):
+            dp = np.zeros(3)
+            dp[k] = h
+            fd = (oracle.ylm(*(p + dp), 6)[0] - oracle.ylm(*(p - dp), 6)[0]) / (2 * h)
+            np.testing.assert_allclose(G, fd, atol=1e-7)
+
+
+def _rot(seed):
+    q, _ = np.linalg.qr(np.random.Generator(np.random.PCG64(seed)).normal(size=(3, 3)))
+    return q
+
+
+def test_b2_rotation_invariance():
+    """test_descriptor.cpp:49-69: B2 invariant under rotation (1e-10)."""
+    cell, sp, pos = random_atoms(seed=3)
+    b2 = oracle.B2Settings(*b2_args(2, 4, 3, 5.0))
+    R = _rot(1)
+    s1 = oracle.Structure(cell, sp, pos, 5.0, [b2], compute_dervs=False)
+    s2 = oracle.Structure(cell @ R, sp, pos @ R, 5.0, [b2], compute_dervs=False)
+    np.testing.assert_allclose(s1.descriptors[0].atom_B2,
+                               s2.descriptors[0].atom_B2, rtol=1e-10, atol=1e-10)
+
+
+def test_neighbor_list_symmetric():
+    cell, sp, pos = syn.fcc_al(n_cells=2, seed=4)
+    s = oracle.Structure(cell, sp, pos, 5.0, [])
+    pairs = set()
+    off = s.cumulative_neighbor_count
+    for i in range(s.noa):
+        for p in range(off[i], off[i + 1]):
+            pairs.add((i, int(s.structure_indices[p]), tuple(s.shifts[p])))
+    for (i, j, sh) in pairs:
+        assert (j, i, tuple(-np.asarray(sh))) in pairs
+
+
+def test_envs_sum_equals_energy_kernel():
+    """test_kernels.cpp:35-75 relation: the energy column of envs_struc is
+    the sum of envs_envs over the structure's atoms."""
+    gp, b2a = small_two_species(seed=1, n_train=1)
+    k = gp.kernels[0]
+    cell, sp, pos = random_atoms(seed=77)
+    st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    K = k.envs_struc(gp.sparse_descriptors[0], st.descriptors[0])
+    cd = oracle.ClusterDescriptor.from_values(st.descriptors[0])
+    Kee = k.envs_envs(gp.sparse_descriptors[0], cd)
+    np.testing.assert_allclose(K[:, 0], Kee.sum(1), rtol=1e-10, atol=1e-10)
+
+
+def test_force_and_stress_columns_finite_difference():
+    """test_kernels.cpp:140-400: force/stress kernel columns against central
+    differences of the energy column (delta 1e-4, tolerance 1e-4)."""
+    gp, b2a = small_two_species(seed=2, n_train=1)
+    k = gp.kernels[0]
+    b2 = oracle.B2Settings(*b2a)
+    cell, sp, pos = random_atoms(seed=9)
+    st = oracle.Structure(cell, sp, pos, 5.0, [b2])
+    K = k.envs_struc(gp.sparse_descriptors[0], st.descriptors[0])
+    d = 1e-4
+    for atom in [0, 5]:
+        for c in range(3):
+            p1 = pos.copy(); p1[atom, c] += d
+            p2 = pos.copy(); p2[atom, c] -= d
+            e1 = k.envs_struc(gp.sparse_descriptors[0], oracle.Structure(
+                cell, sp, p1, 5.0, [b2]).descriptors[0])[:, 0]
+            e2 = k.envs_struc(gp.sparse_descriptors[0], oracle.Structure(
+                cell, sp, p2, 5.0, [b2]).descriptors[0])[:, 0]
+            np.testing.assert_allclose(K[:, 1 + 3 * atom + c],
+                                       -(e1 - e2) / (2 * d), atol=1e-4)
+    # stress xx: strain the cell and positions together
+    eps = np.eye(3)
+    eps[0, 0] += d
+    e1 = k.envs_struc(gp.sparse_descriptors[0], oracle.Structure(
+        cell @ eps, sp, pos @ eps, 5.0, [b2]).descriptors[0])[:, 0]
+    eps[0, 0] -= 2 * d
+    e2 = k.envs_struc(gp.sparse_descriptors[0], oracle.Structure(
+        cell @ eps, sp, pos @ eps, 5.0, [b2]).descriptors[0])[:, 0]
+    vol = abs(np.linalg.det(cell))
+    np.testing.assert_allclose(K[:, 1 + 3 * st.noa], -(e1 - e2) / (2 * d) / vol,
+                               atol=1e-4)
+
+
+def test_local_variances_nonnegative_and_sparse_points_small():
+    """test_sparse_gp.cpp:55-119: variances >= 0 (to rounding)."""
+    gp, b2a = small_two_species(seed=3, n_train=2)
+    cell, sp, pos = random_atoms(seed=123)
+    st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    v = gp.compute_cluster_uncertainties(st)[0]
+    assert np.all(v > -1e-8)
