@@ -1,0 +1,469 @@
+"""Benchmark: atoms/s for energy + forces + local std on the 2-species
+1,000-atom alloy workload (flare_gb300.workloads.ALLOY), one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fp64|mixed] [--batch B]
+
+A step is one batched pass of the prediction pipeline (neighbours, B2,
+kernel against the 2,000-environment sparse set, reverse-mode adjoint forces
+and stress, local variance) over B structures of 1,000 atoms.  `value` is
+timed with CUDA events per step on the launching stream with inputs resident
+in HBM (L2 flushed between steps by a 256 MiB write); `e2e` is the same step
+through the C ABI with host buffers (pinned H2D of positions/species, D2H of
+energy/forces/stress/variances inside the timed region).  `--impl reference`
+times the FP64 CPU oracle (a restatement of the reference's flare_pp
+algorithm; the reference itself cannot be built here) on the host cores.
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("atoms/s (E+F+std) mixed-prec/adjoint vs FP64 plain on 1 GB300 at "
+          "stated err; p99")
+WORKLOAD = ("alloy1000: 2-species random alloy, 1000-atom cubic cell, 0.06 "
+            "atoms/A^3, B2 n_max=8 l_max=4 rc=5.5, NormalizedDotProduct "
+            "sigma=2 power=2, 2000 sparse envs (1000/species), 10 LJ-labelled "
+            "training structures")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--batch", type=int, default=32,
+                    help="structures (1000 atoms each) per step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if n > 0 else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ CPU oracle
+def oracle_model():
+    """FP64 CPU oracle model of the same sizes (M = 2000, n_d = 680) from
+    two training structures; prediction cost does not depend on the
+    training-set size."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from flare_gb300 import workloads as wl
+    c = wl.ALLOY
+    b2 = oracle.B2Settings("chebyshev", "quadratic", [0.0, c["rc"]], [],
+                           [2, c["n_max"], c["l_max"]])
+    k = oracle.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = oracle.SparseGP([k], c["sigma_e_per_atom"] * c["n_atoms"],
+                         c["sigma_f"], c["sigma_s"])
+    n_train = 2
+    data = [wl.alloy_structure(c["train_seed0"] + t) for t in range(n_train)]
+    sparse = wl.alloy_sparse_choice(n_train, [d[1] for d in data],
+                                    c["sparse_per_species"], c["sparse_seed"])
+    for t, (cell, sp, pos) in enumerate(data):
+        st = oracle.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = wl.alloy_labels(cell, sp, pos)
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(st, sparse[t])
+    gp.update_matrices_QR()
+    return oracle, gp, b2
+
+
+def oracle_step(oracle, gp, b2, seed):
+    """One structure through the oracle: Structure (neighbours, B2 with
+    stored gradients), predict_local_uncertainties, calculator results."""
+    from flare_gb300 import workloads as wl
+    cell, sp, pos = wl.alloy_structure(seed)
+    st = oracle.Structure(cell, sp, pos, wl.ALLOY["rc"], [b2])
+    gp.predict_local_uncertainties(st)
+    oracle.calculator_results(st, "local", wl.ALLOY["sigma"])
+    return len(sp)
+
+
+def cpu_cores():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def time_oracle(n_structures, warm=1):
+    oracle, gp, b2 = oracle_model()
+    for w in range(warm):
+        oracle_step(oracle, gp, b2, 2100 + w)
+    times = []
+    atoms = 0
+    for k in range(n_structures):
+        t0 = time.perf_counter()
+        atoms += oracle_step(oracle, gp, b2, 2100 + k)
+        times.append(time.perf_counter() - t0)
+    return atoms / sum(times), times
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = cpu_cores()
+    oracle, gp, b2 = oracle_model()
+    for w in range(args.warmup):
+        oracle_step(oracle, gp, b2, 2100 + w)
+    times, atoms = [], 0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        atoms += oracle_step(oracle, gp, b2, 2100 + k)
+        times.append(time.perf_counter() - t0)
+    v = atoms / sum(times)
+    sample = ("one 1000-atom alloy structure per step: neighbours (brute "
+              "force), B2 with stored gradients, envs_struc, K^T alpha, local "
+              "variance via L_inv; FP64, OpenMP + BLAS threads")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "atoms/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "atoms_per_step": 1000,
+                   "implementation": "FP64 CPU oracle restating flare_pp "
+                                     "(reference unbuildable: Eigen/json "
+                                     "fetched at configure time)"},
+        "cpu_baseline": {"value": v, "unit": "atoms/s", "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "atoms/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm
+class Clocks:
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, dev_index=0):
+        try:
+            rows = [l.split(",") for l in open(self.path).read().splitlines()]
+        except Exception:
+            return None
+        rows = [[x.strip() for x in r] for r in rows if len(r) >= 9]
+        rows = [r for r in rows if r[0] == str(dev_index)] or rows
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measure_fp64_peak(torch):
+    """cuBLAS DGEMM throughput (TFLOP/s), best of 5 on 8192^3."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = max(best, 2 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    import flare_gb300 as fg
+    from flare_gb300 import _lib
+    from flare_gb300 import workloads as wl
+    L = _lib.lib()
+    c = wl.ALLOY
+    t_setup = time.time()
+    gp, b2, k = wl.build_alloy_model()
+    model = gp._device_model([b2])
+    train_s = time.time() - t_setup
+
+    B = args.batch
+    structs = [wl.alloy_structure(c["test_seed0"] + rank * 100000 + i)
+               for i in range(B)]
+    offsets = np.zeros(B + 1, dtype=np.int32)
+    for i, s in enumerate(structs):
+        offsets[i + 1] = offsets[i] + len(s[1])
+    cells = np.ascontiguousarray(np.stack([s[0].reshape(-1) for s in structs]))
+    pos = np.ascontiguousarray(np.concatenate([s[2] for s in structs]))
+    sp = np.ascontiguousarray(np.concatenate([s[1] for s in structs]).astype(np.int32))
+    N = int(offsets[-1])
+    dev = torch.device("cuda", local)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_sp = torch.from_numpy(sp).to(dev)
+    out = {k_: torch.zeros(n, dtype=torch.float64, device=dev)
+           for k_, n in (("e", B), ("f", 3 * N), ("s", 6 * B), ("v", N))}
+    stream = torch.cuda.current_stream()
+    sptr = _lib.stream_ptr(stream)
+    prec = {"fp64": _lib.FGB_PREC_FP64, "mixed": _lib.FGB_PREC_MIXED}[args.precision]
+    want = 0xF
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(precision=prec):
+        _lib.check(L.fgb_predict(model.h, B, _lib.ptr(offsets), _lib.ptr(cells),
+                                 _lib.ptr(d_pos), _lib.ptr(d_sp), c["rc"], want,
+                                 precision, _lib.ptr(out["e"]),
+                                 _lib.ptr(out["f"]), _lib.ptr(out["s"]),
+                                 _lib.ptr(out["v"]), sptr))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # ---- timed region: device-resident inputs
+    L.fgb_profile_reset()
+    L.fgb_profile_enable(1)
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
+                    if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                    else f"/tmp/fgb_clocks_{rank}.csv")
+    per = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            torch.cuda.nvtx.range_push("timed_step")
+            step()
+            torch.cuda.nvtx.range_pop()
+            s1.record(stream)
+            s1.synchronize()
+            per.append(s0.elapsed_time(s1))
+    torch.cuda.synchronize()
+    barrier(world)
+    L.fgb_profile_enable(0)
+    nst = L.fgb_profile_n_stages()
+    ms = (ctypes_array("d", nst))
+    ln = (ctypes_array("q", nst))
+    import ctypes
+    L.fgb_profile_read(ctypes.cast(ms, ctypes.c_void_p),
+                       ctypes.cast(ln, ctypes.c_void_p), nst)
+    stage = {L.fgb_profile_stage_name(i).decode(): (ms[i], ln[i])
+             for i in range(nst)}
+    total_ms = sum(per)
+    total_ms_max = max_over_ranks(total_ms, world)
+    atoms_all = N * args.steps * world
+    value = atoms_all / (total_ms_max * 1e-3)
+    res_e = out["e"].cpu().numpy().copy()
+    res_f = out["f"].cpu().numpy().copy()
+    res_s = out["s"].cpu().numpy().copy()
+    res_v = out["v"].cpu().numpy().copy()
+
+    # ---- e2e through the host-buffer C ABI (pinned buffers)
+    h_pos = torch.from_numpy(pos).pin_memory()
+    h_sp = torch.from_numpy(sp).pin_memory()
+    h_out = {k_: torch.zeros(n, dtype=torch.float64).pin_memory()
+             for k_, n in (("e", B), ("f", 3 * N), ("s", 6 * B), ("v", N))}
+
+    def step_host():
+        _lib.check(L.fgb_predict_host(
+            model.h, B, _lib.ptr(offsets), _lib.ptr(cells), _lib.ptr(h_pos),
+            _lib.ptr(h_sp), c["rc"], want, prec, _lib.ptr(h_out["e"]),
+            _lib.ptr(h_out["f"]), _lib.ptr(h_out["s"]), _lib.ptr(h_out["v"]),
+            sptr))
+
+    for _ in range(max(1, args.warmup)):
+        step_host()
+    e2e = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_host()
+        e2e.append(time.perf_counter() - t0)
+    e2e_max = max_over_ranks(sum(e2e), world)
+    e2e_value = atoms_all / e2e_max
+    h2d = pos.nbytes + sp.nbytes + cells.nbytes + offsets.nbytes
+    d2h = 8 * (B + 3 * N + 6 * B + N)
+
+    # ---- dominant kernel roofline
+    sizes = species_sizes(sp, offsets, gp)
+    flops = {"kernel_gemm": sum(2.0 * n_s * m_s * b2.n_descriptors
+                                for n_s, m_s in sizes),
+             "adjoint_gemm": sum(2.0 * n_s * m_s * b2.n_descriptors
+                                 for n_s, m_s in sizes),
+             "variance_gemm": sum(1.0 * n_s * m_s * (m_s + 1)
+                                  for n_s, m_s in sizes)}
+    gemm_stage = max(flops, key=lambda s: stage.get(s, (0, 0))[0])
+    st_ms, st_n = stage[gemm_stage]
+    launches_per_step = st_n / args.steps
+    flop_per_launch = flops[gemm_stage] / max(launches_per_step, 1)
+    achieved = flop_per_launch / (st_ms / st_n * 1e-3) / 1e12
+    peak = measure_fp64_peak(torch) if args.precision == "fp64" else None
+    gpu_launches = int(sum(v[1] for v in stage.values()))
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "atoms/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "structures_per_step": B,
+                   "atoms_per_step": N, "precision": args.precision,
+                   "l2": "flushed between steps (256 MiB write)",
+                   "train_setup_s": round(train_s, 1)},
+        "latency_ms": {"p50": float(np.percentile(per, 50)),
+                       "p99": float(np.percentile(per, 99)),
+                       "per_step": [round(x, 3) for x in per]},
+        "e2e": {"value": e2e_value, "unit": "atoms/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "p50_ms": 1e3 * float(np.percentile(e2e, 50)),
+                "p99_ms": 1e3 * float(np.percentile(e2e, 99))},
+        "roofline": {"kernel": gemm_stage, "bound": "tensor",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if peak else None,
+                     "traffic": None,
+                     "peak_source": "FP64 cuBLAS DGEMM 8192^3 measured in "
+                                    "this run (FP64 has no entry in the "
+                                    "measured-peaks file)",
+                     "flop_per_launch": flop_per_launch,
+                     "avg_launch_ms": st_ms / st_n},
+        "stages_ms_per_step": {k_: round(v[0] / args.steps, 4)
+                               for k_, v in stage.items() if v[1]},
+        "gpu_launches": gpu_launches,
+        "clocks": clocks.summary(local),
+    }
+    if rank == 0 and not args.no_plain:
+        result["fp64_plain"] = time_plain(L, _lib, model, structs[:2], b2, c,
+                                          torch)
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v, ts = time_oracle(2)
+            result["cpu_baseline"] = {
+                "value": v, "unit": "atoms/s", "cores": cpu_cores(),
+                "kind": "port",
+                "sample": "2 alloy structures (2000 atoms) through the FP64 "
+                          "CPU oracle (brute-force neighbours, stored-gradient "
+                          "B2, envs_struc, local variance), after 1 warm-up"}
+        except Exception as ex:  # report, never hide
+            result["cpu_baseline"] = {"error": repr(ex)}
+    if rank == 0:
+        result["sample_energy_per_atom"] = float(res_e[0] / 1000)
+        print(json.dumps(result), flush=True)
+
+
+def ctypes_array(code, n):
+    import ctypes
+    t = {"d": ctypes.c_double, "q": ctypes.c_longlong}[code]
+    return (t * n)()
+
+
+def species_sizes(sp, offsets, gp):
+    sd = gp.sparse_descriptors[0]
+    out = []
+    for s in range(sd.n_types):
+        out.append((int((sp == s).sum()), int(sd.n_clusters_by_type[s])))
+    return out
+
+
+def time_plain(L, _lib, model, structs, b2, c, torch):
+    """The plain FP64 GPU form (reference algorithm: stored gradients,
+    envs_struc GEMM + scatter, K^T alpha, variance) per structure."""
+    import flare_gb300 as fg
+    times, atoms = [], 0
+    for i, (cell, sp, pos) in enumerate(structs):
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        nl = st.nlist()
+        d = st._inputs()
+        N = st.noa
+        mean = torch.zeros(1 + 3 * N + 6, dtype=torch.float64, device="cuda")
+        var = torch.zeros(N, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _lib.check(L.fgb_predict_plain(model.h, nl.h, _lib.ptr(d["species"]),
+                                       _lib.ptr(mean), _lib.ptr(var),
+                                       _lib.stream_ptr()))
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i > 0:            # first one warms up
+            times.append(dt)
+            atoms += N
+    if not times:
+        return None
+    return {"value": atoms / sum(times), "unit": "atoms/s",
+            "sample": f"{len(times)} structure(s) after 1 warm-up, wall clock"}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus if args.impl == "ours" else 0)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

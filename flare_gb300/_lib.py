@@ -31,6 +31,11 @@ _pvp = ctypes.POINTER(ctypes.c_void_p)
 SIGNATURES = {
     "fgb_last_error": (ctypes.c_char_p, []),
     "fgb_version": (_i, []),
+    "fgb_profile_enable": (_i, [_i]),
+    "fgb_profile_reset": (_i, []),
+    "fgb_profile_n_stages": (_i, []),
+    "fgb_profile_stage_name": (ctypes.c_char_p, [_i]),
+    "fgb_profile_read": (_i, [_vp, _vp, _i]),
     "fgb_nlist_create": (_i, [_pvp]),
     "fgb_nlist_destroy": (_i, [_vp]),
     "fgb_nlist_build": (_i, [_vp, _i, _vp, _vp, _vp, _d, _vp]),
@@ -50,7 +55,7 @@ SIGNATURES = {
                               _vp, _vp, _vp, _vp]),
     "fgb_envs_envs": (_i, [_vp, _vp, _i, _vp, _vp, _i, _i, _d, _d, _vp,
                            _vp]),
-    "fgb_envs_struc": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fgb_envs_struc": (_i, [_vp, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_predict_plain": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_solve_qr": (_i, [_i, _i, _vp, _vp, _vp, _vp, _d, _vp, _vp, _vp,
                           _vp]),

@@ -403,8 +403,10 @@ def envs_envs_gpu(envs1, envs2, sigma, power):
         d2 = torch.from_numpy(np.ascontiguousarray(envs2.descriptors[s])).to(dev)
         if d1.shape[0] == 0 or d2.shape[0] == 0:
             continue
-        n1 = torch.from_numpy(np.asarray(envs1.descriptor_norms[s])).to(dev)
-        n2 = torch.from_numpy(np.asarray(envs2.descriptor_norms[s])).to(dev)
+        n1 = torch.from_numpy(np.ascontiguousarray(
+            envs1.descriptor_norms[s], dtype=np.float64)).to(dev)
+        n2 = torch.from_numpy(np.ascontiguousarray(
+            envs2.descriptor_norms[s], dtype=np.float64)).to(dev)
         blk = _kernel_block(d1, n1, d2, n2, sig2, power)
         c1, c2 = envs1.cumulative_type_count[s], envs2.cumulative_type_count[s]
         K[c1:c1 + d1.shape[0], c2:c2 + d2.shape[0]] = blk
@@ -428,8 +430,329 @@ class _KernelBlock:
         return out
 
 
-def envs_struc_gpu(envs, struc, sigma, power):
-    raise NotImplementedError("envs_struc on the GPU is provided by SparseGP")
+def envs_struc_gpu(envs, struc, sigma, power, k=0):
+    """envs_struc (normalized_dot_product.cpp:117-214) in FP64 on the GPU,
+    stored-gradient form; ``struc`` is a Structure."""
+    calc = struc.descriptor_calculators[k]
+    counts, rows = envs.stacked()
+    M = int(counts.sum())
+    ncol = 1 + 3 * struc.noa + 6
+    if M == 0:
+        return np.zeros((0, ncol))
+    dev = _device()
+    d_rows = torch.from_numpy(rows).to(dev)
+    out = torch.zeros((M, ncol), dtype=torch.float64, device=dev)
+    d = struc._inputs()
+    check(lib().fgb_envs_struc(calc.handle, float(sigma), float(power),
+                               ptr(counts), ptr(d_rows), struc.nlist().h,
+                               ptr(d["species"]), ptr(out), stream_ptr()),
+          "envs_struc")
+    return out.cpu().numpy()
+
+
+
+# ------------------------------------------------------------ training
+class _Training:
+    """Kuu / Kuf / label bookkeeping of SparseGP (sparse_gp.cpp:141-641)."""
+
+    def _init_training(self):
+        self.training_atom_indices = []
+        self.Kuu_kernels = [np.zeros((0, 0)) for _ in self.kernels]
+        self.Kuf_kernels = [np.zeros((0, 0)) for _ in self.kernels]
+        self.Kuu = np.zeros((0, 0))
+        self.Kuf = np.zeros((0, 0))
+        self.label_count = [0]
+        self.y = np.zeros(0)
+        self.noise_vector = np.zeros(0)
+        self.n_labels = 0
+        self.n_strucs = 0
+        self.n_energy_labels = 0
+        self.n_force_labels = 0
+        self.n_stress_labels = 0
+
+    @property
+    def n_sparse(self):
+        return sum(sd.n_clusters for sd in self.sparse_descriptors)
+
+    def _calcs(self, structure):
+        self._calculators = list(structure.descriptor_calculators)
+        return self._calculators
+
+    def initialize_sparse_descriptors(self, structure):
+        """sparse_gp.cpp:59-71."""
+        if self.sparse_descriptors:
+            return
+        for calc in self._calcs(structure):
+            self.sparse_descriptors.append(
+                ClusterDescriptor(calc.descriptor_settings[0],
+                                  calc.n_descriptors))
+            self.sparse_indices.append([])
+
+    def add_training_structure(self, structure, atom_indices=(-1,),
+                               rel_e_noise=1.0, rel_f_noise=1.0,
+                               rel_s_noise=1.0):
+        """sparse_gp.cpp:474-583."""
+        self.initialize_sparse_descriptors(structure)
+        n_atoms = structure.noa
+        energy = np.asarray(structure.energy, np.float64).reshape(-1)
+        forces = np.asarray(structure.forces, np.float64).reshape(-1)
+        stresses = np.asarray(structure.stresses, np.float64).reshape(-1)
+        n_energy = energy.size
+        atom_indices = list(np.asarray(atom_indices).reshape(-1))
+        if atom_indices[0] == -1:
+            atoms = list(range(n_atoms))
+            n_force = forces.size
+        else:
+            atoms = [int(a) for a in atom_indices]
+            n_force = 3 * len(atoms)
+        self.training_atom_indices.append(atoms)
+        n_stress = stresses.size
+        nl = n_energy + n_force + n_stress
+        self.label_count.append(self.n_labels + nl)
+        yy = np.zeros(nl)
+        yy[:n_energy] = energy
+        if n_force:
+            for a, at in enumerate(atoms):
+                yy[n_energy + 3 * a:n_energy + 3 * a + 3] = forces[3 * at:3 * at + 3]
+        yy[n_energy + n_force:] = stresses
+        self.y = np.concatenate([self.y, yy])
+        nv = np.zeros(nl)
+        nv[:n_energy] = 1 / (self.energy_noise ** 2 * rel_e_noise ** 2)
+        nv[n_energy:n_energy + n_force] = 1 / (self.force_noise ** 2 *
+                                               rel_f_noise ** 2)
+        nv[n_energy + n_force:] = 1 / (self.stress_noise ** 2 * rel_s_noise ** 2)
+        self.noise_vector = np.concatenate([self.noise_vector, nv])
+        for i, k in enumerate(self.kernels):
+            n_sparse = self.sparse_descriptors[i].n_clusters
+            blk = np.zeros((n_sparse, nl))
+            if n_sparse:
+                esk = envs_struc_gpu(self.sparse_descriptors[i], structure,
+                                     k.sigma, k.power, i)
+                blk[:, :n_energy] = esk[:, :n_energy]
+                blk[:, n_energy + n_force:] = \
+                    esk[:, 1 + 3 * n_atoms:1 + 3 * n_atoms + n_stress]
+                if n_force:
+                    for a, at in enumerate(atoms):
+                        blk[:, n_energy + 3 * a:n_energy + 3 * a + 3] = \
+                            esk[:, 1 + 3 * at:1 + 3 * at + 3]
+            old = self.Kuf_kernels[i]
+            if old.shape != (n_sparse, self.n_labels):
+                old = np.zeros((n_sparse, self.n_labels))
+            self.Kuf_kernels[i] = np.hstack([old, blk])
+        self.n_energy_labels += n_energy
+        self.n_force_labels += n_force
+        self.n_stress_labels += n_stress
+        self.n_labels += nl
+        self.training_structures.append(structure)
+        self.n_strucs += 1
+        self._stack_Kuf()
+
+    def _add_clusters(self, structure, clusters_by_kernel):
+        clusters = [ClusterDescriptor.from_values(structure.descriptors[i],
+                                                  clusters_by_kernel[i])
+                    for i in range(self.n_kernels)]
+        self._update_Kuu(clusters)
+        self._update_Kuf(clusters)
+        self._stack_Kuu()
+        self._stack_Kuf()
+        for i in range(self.n_kernels):
+            self.sparse_descriptors[i].add_clusters_by_type(
+                structure.descriptors[i], clusters_by_kernel[i])
+        self.alpha = None
+        self._model = None
+
+    def add_specific_environments(self, structure, atoms):
+        """sparse_gp.cpp:141-189."""
+        self.initialize_sparse_descriptors(structure)
+        atoms = [int(a) for a in atoms]
+        by_kernel = []
+        for i in range(self.n_kernels):
+            self.sparse_indices[i].append(atoms)
+            dv = structure.descriptors[i]
+            by_type = []
+            for j in range(dv.n_types):
+                ind = []
+                for kk in range(dv.n_clusters_by_type[j]):
+                    a1 = int(dv.atom_indices[j][kk])
+                    ind.extend(kk for a2 in atoms if a1 == a2)
+                by_type.append(ind)
+            by_kernel.append(by_type)
+        self._add_clusters(structure, by_kernel)
+
+    def add_all_environments(self, structure):
+        """sparse_gp.cpp:307-341."""
+        self.initialize_sparse_descriptors(structure)
+        by_kernel = [[list(range(dv.n_clusters_by_type[s]))
+                      for s in range(dv.n_types)]
+                     for dv in structure.descriptors[:self.n_kernels]]
+        self._add_clusters(structure, by_kernel)
+        for i in range(self.n_kernels):
+            self.sparse_indices[i].append(list(range(structure.noa)))
+
+    def _clusters_to_atoms(self, dv, clusters):
+        out = []
+        for c in clusters:
+            for j in range(dv.n_types):
+                if dv.cumulative_type_count[j] <= c < dv.cumulative_type_count[j + 1]:
+                    out.append(int(dv.atom_indices[j][c - dv.cumulative_type_count[j]]))
+                    break
+        return out
+
+    def _by_type(self, dv, clusters):
+        by_type = [[] for _ in range(dv.n_types)]
+        for c in clusters:
+            for j in range(dv.n_types):
+                if dv.cumulative_type_count[j] <= c < dv.cumulative_type_count[j + 1]:
+                    by_type[j].append(c - dv.cumulative_type_count[j])
+                    break
+        return by_type
+
+    def add_random_environments(self, structure, n_added, seed=None):
+        """sparse_gp.cpp:256-305 (the reference shuffles with an unseeded
+        std::random_shuffle; here a numpy generator, seedable)."""
+        self.initialize_sparse_descriptors(structure)
+        r = np.random.Generator(np.random.PCG64(seed))
+        by_kernel, picked = [], []
+        for i in range(self.n_kernels):
+            dv = structure.descriptors[i]
+            order = r.permutation(dv.n_clusters)
+            chosen = order[:min(int(n_added[i]), dv.n_clusters)].tolist()
+            picked.append(chosen)
+            by_kernel.append(self._by_type(dv, chosen))
+        self._add_clusters(structure, by_kernel)
+        for i in range(self.n_kernels):
+            self.sparse_indices[i].append(
+                self._clusters_to_atoms(structure.descriptors[i], picked[i]))
+
+    def add_uncertain_environments(self, structure, n_added):
+        """sparse_gp.cpp:191-254: the n_added clusters of largest local
+        variance (stable sort, descending)."""
+        if len(n_added) != self.n_kernels:
+            raise RuntimeError(
+                "n_added must have the same size as the number of kernels")
+        self.initialize_sparse_descriptors(structure)
+        variances = self.compute_cluster_uncertainties(structure)
+        by_kernel, picked = [], []
+        for i in range(self.n_kernels):
+            v = np.asarray(variances[i])
+            order = sorted(range(len(v)), key=lambda q: -v[q])
+            chosen = order[:min(int(n_added[i]), len(order))]
+            picked.append(chosen)
+            by_kernel.append(self._by_type(structure.descriptors[i], chosen))
+        self._add_clusters(structure, by_kernel)
+        for i in range(self.n_kernels):
+            self.sparse_indices[i].append(
+                self._clusters_to_atoms(structure.descriptors[i], picked[i]))
+
+    def _update_Kuu(self, clusters):
+        """sparse_gp.cpp:343-400 (type-blocked growth of Kuu)."""
+        for i, k in enumerate(self.kernels):
+            sd, cd = self.sparse_descriptors[i], clusters[i]
+            prev = k.envs_envs(sd, cd) if sd.n_clusters and cd.n_clusters else \
+                np.zeros((sd.n_clusters, cd.n_clusters))
+            selfb = k.envs_envs(cd, cd) if cd.n_clusters else np.zeros((0, 0))
+            ns, ne, nt = sd.n_clusters, cd.n_clusters, cd.n_types
+            km = np.zeros((ns + ne, ns + ne))
+            n1 = n2 = 0
+            for j in range(nt):
+                n3 = n4 = 0
+                n5, n6 = sd.n_clusters_by_type[j], cd.n_clusters_by_type[j]
+                for kk in range(nt):
+                    n7, n8 = sd.n_clusters_by_type[kk], cd.n_clusters_by_type[kk]
+                    km[n1 + n2:n1 + n2 + n5, n3 + n4:n3 + n4 + n7] = \
+                        self.Kuu_kernels[i][n1:n1 + n5, n3:n3 + n7]
+                    km[n1 + n2:n1 + n2 + n5, n3 + n4 + n7:n3 + n4 + n7 + n8] = \
+                        prev[n1:n1 + n5, n4:n4 + n8]
+                    km[n1 + n2 + n5:n1 + n2 + n5 + n6, n3 + n4:n3 + n4 + n7] = \
+                        prev[n3:n3 + n7, n2:n2 + n6].T
+                    km[n1 + n2 + n5:n1 + n2 + n5 + n6,
+                       n3 + n4 + n7:n3 + n4 + n7 + n8] = \
+                        selfb[n2:n2 + n6, n4:n4 + n8]
+                    n3 += n7
+                    n4 += n8
+                n1 += n5
+                n2 += n6
+            self.Kuu_kernels[i] = km
+
+    def _update_Kuf(self, clusters):
+        """sparse_gp.cpp:402-472: new sparse rows against every training
+        structure."""
+        for i, k in enumerate(self.kernels):
+            sd, cd = self.sparse_descriptors[i], clusters[i]
+            ns, ne, nt = sd.n_clusters, cd.n_clusters, cd.n_types
+            inds = [0]
+            for j in range(nt):
+                inds.append(inds[-1] + sd.n_clusters_by_type[j] +
+                            cd.n_clusters_by_type[j])
+            km = np.zeros((ns + ne, self.n_labels))
+            old = self.Kuf_kernels[i]
+            if old.shape != (ns, self.n_labels):
+                old = np.zeros((ns, self.n_labels))
+            for j, struc in enumerate(self.training_structures):
+                n_atoms = struc.noa
+                esk = envs_struc_gpu(cd, struc, k.sigma, k.power, i) if ne else \
+                    np.zeros((0, 1 + 3 * n_atoms + 6))
+                n1 = n2 = 0
+                lc = self.label_count[j]
+                ne_j = np.asarray(struc.energy).size
+                nf_j = np.asarray(struc.forces).size
+                ns_j = np.asarray(struc.stresses).size
+                for kk in range(nt):
+                    cc = 0
+                    u = inds[kk]
+                    n3, n4 = sd.n_clusters_by_type[kk], cd.n_clusters_by_type[kk]
+                    if ne_j:
+                        km[u:u + n3, lc] = old[n1:n1 + n3, lc]
+                        km[u + n3:u + n3 + n4, lc] = esk[n2:n2 + n4, 0]
+                        cc += 1
+                    if nf_j:
+                        for at in self.training_atom_indices[j]:
+                            km[u:u + n3, lc + cc:lc + cc + 3] = \
+                                old[n1:n1 + n3, lc + cc:lc + cc + 3]
+                            km[u + n3:u + n3 + n4, lc + cc:lc + cc + 3] = \
+                                esk[n2:n2 + n4, 1 + 3 * at:1 + 3 * at + 3]
+                            cc += 3
+                    if ns_j:
+                        km[u:u + n3, lc + cc:lc + cc + 6] = \
+                            old[n1:n1 + n3, lc + cc:lc + cc + 6]
+                        km[u + n3:u + n3 + n4, lc + cc:lc + cc + 6] = \
+                            esk[n2:n2 + n4, 1 + 3 * n_atoms:1 + 3 * n_atoms + 6]
+                    n1 += n3
+                    n2 += n4
+            self.Kuf_kernels[i] = km
+
+    def _stack_Kuu(self):
+        import scipy.linalg as sla
+        self.Kuu = sla.block_diag(*self.Kuu_kernels)
+
+    def _stack_Kuf(self):
+        self.Kuf = np.vstack([k if k.shape[1] == self.n_labels else
+                              np.zeros((k.shape[0], self.n_labels))
+                              for k in self.Kuf_kernels])
+
+    def update_matrices_QR(self):
+        """sparse_gp.cpp:607-641 on the GPU in FP64 (fgb_solve_qr)."""
+        M = self.Kuu.shape[0]
+        if M == 0:
+            raise RuntimeError("no sparse environments")
+        dev = _device()
+        Kuu = torch.from_numpy(np.ascontiguousarray(self.Kuu)).to(dev)
+        Kuf = torch.from_numpy(np.ascontiguousarray(self.Kuf)).to(dev)
+        y = torch.from_numpy(np.ascontiguousarray(self.y)).to(dev)
+        nv = torch.from_numpy(np.ascontiguousarray(self.noise_vector)).to(dev)
+        alpha = torch.zeros(M, dtype=torch.float64, device=dev)
+        Li = torch.zeros((M, M), dtype=torch.float64, device=dev)
+        Ri = torch.zeros((M, M), dtype=torch.float64, device=dev)
+        check(lib().fgb_solve_qr(M, int(self.n_labels), ptr(Kuu), ptr(Kuf),
+                                 ptr(y), ptr(nv), float(self.Kuu_jitter),
+                                 ptr(alpha), ptr(Li), ptr(Ri), stream_ptr()),
+              "update_matrices_QR")
+        self.alpha = alpha.cpu().numpy()
+        self.L_inv = Li.cpu().numpy()
+        self.R_inv = Ri.cpu().numpy()
+        self.Kuu_inverse = self.L_inv.T @ self.L_inv
+        self.Sigma = self.R_inv @ self.R_inv.T
+        self._model = None
 
 
 # -------------------------------------------------------------- model
@@ -470,10 +793,11 @@ def pack_structures(structures):
     return offsets, cells, pos, sp
 
 
-class SparseGP:
+class SparseGP(_Training):
     """SparseGP(kernels, energy_noise, force_noise, stress_noise) —
-    src/flare_pp/bffs/sparse_gp.cpp:14-58 (prediction API here; training
-    bookkeeping in ``flare_gb300.training``)."""
+    src/flare_pp/bffs/sparse_gp.cpp:14-58.  Training bookkeeping (Kuu, Kuf,
+    labels) mirrors sparse_gp.cpp:141-641 with the kernel blocks and the QR
+    solve on the GPU in FP64; prediction runs the fused GPU pipeline."""
 
     def __init__(self, kernels=(), energy_noise=1.0, force_noise=1.0,
                  stress_noise=1.0):
@@ -486,6 +810,7 @@ class SparseGP:
         self.sparse_descriptors = []
         self.sparse_indices = []
         self.training_structures = []
+        self._init_training()
         self.alpha = None
         self.L_inv = None
         self.R_inv = None
@@ -499,10 +824,6 @@ class SparseGP:
         return np.concatenate([k.kernel_hyperparameters for k in self.kernels] +
                               [np.array([self.energy_noise, self.force_noise,
                                          self.stress_noise])])
-
-    @property
-    def n_sparse(self):
-        return sum(sd.n_clusters for sd in self.sparse_descriptors)
 
     # -------------------------------------------------- device model
     def set_weights(self, sparse_descriptors, alpha, L_inv, calculators):

@@ -17,6 +17,7 @@
 #include "fgb_kernels.h"
 #include "fgb_model.h"
 #include "fgb_gemm64.cuh"
+#include "fgb_profile.h"
 
 namespace fgb {
 
@@ -263,26 +264,35 @@ int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
           (rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr)))
         return rc;
       dim3 g1(ceil_div(Ms, BN), ceil_div(Mr, BM));
-      k_kernel_gemm<<<g1, GT, 0, st>>>(
-          Mr, Ms, nd, m->ws.B2.as<double>(), perm, m->ws.norms.as<double>(),
-          m->S.as<double>() + (size_t)m->h_offsets[s] * nd,
-          m->alpha.as<double>() + m->h_offsets[s],
-          m->svalid.as<unsigned char>() + m->h_offsets[s], sig2, m->power,
-          m->ws.kmat.as<double>(), m->ws.wmat.as<double>());
-      FGB_LAUNCH_CHECK("k_kernel_gemm");
-      k_row_energy<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
-          Mr, Ms, m->ws.kmat.as<double>(),
-          m->alpha.as<double>() + m->h_offsets[s], perm,
-          m->ws.erows.as<double>(), d_e_atom);
-      FGB_LAUNCH_CHECK("k_row_energy");
+      {
+        StageTimer _pt(kStKernelGemm, st, 1);
+        k_kernel_gemm<<<g1, GT, 0, st>>>(
+            Mr, Ms, nd, m->ws.B2.as<double>(), perm, m->ws.norms.as<double>(),
+            m->S.as<double>() + (size_t)m->h_offsets[s] * nd,
+            m->alpha.as<double>() + m->h_offsets[s],
+            m->svalid.as<unsigned char>() + m->h_offsets[s], sig2, m->power,
+            m->ws.kmat.as<double>(), m->ws.wmat.as<double>());
+        FGB_LAUNCH_CHECK("k_kernel_gemm");
+      }
+      {
+        StageTimer _pt(kStRowEnergy, st, 1);
+        k_row_energy<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+            Mr, Ms, m->ws.kmat.as<double>(),
+            m->alpha.as<double>() + m->h_offsets[s], perm,
+            m->ws.erows.as<double>(), d_e_atom);
+        FGB_LAUNCH_CHECK("k_row_energy");
+      }
       if (want_grad) {
         dim3 g2(ceil_div(nd, BN), ceil_div(Mr, BM));
-        k_adjoint_gemm<<<g2, GT, 0, st>>>(
-            Mr, nd, Ms, m->ws.wmat.as<double>(),
-            m->S.as<double>() + (size_t)m->h_offsets[s] * nd, perm,
-            m->ws.norms.as<double>(), m->ws.B2.as<double>(),
-            m->ws.erows.as<double>(), m->power, d_gB2);
-        FGB_LAUNCH_CHECK("k_adjoint_gemm");
+        {
+          StageTimer _pt(kStAdjointGemm, st, 1);
+          k_adjoint_gemm<<<g2, GT, 0, st>>>(
+              Mr, nd, Ms, m->ws.wmat.as<double>(),
+              m->S.as<double>() + (size_t)m->h_offsets[s] * nd, perm,
+              m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+              m->ws.erows.as<double>(), m->power, d_gB2);
+          FGB_LAUNCH_CHECK("k_adjoint_gemm");
+        }
       }
       if (want_var) {
         const int R = m->h_panel_rows[s];
@@ -290,15 +300,21 @@ int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
           return rc;
         dim3 g3(ntiles, ceil_div(Mr, BM));
-        k_variance_gemm<<<g3, GT, 0, st>>>(
-            Mr, R, Ms, m->ws.kmat.as<double>(),
-            m->Lp.as<double>() + m->h_panel_off[s], m->ws.part.as<double>(),
-            ntiles);
-        FGB_LAUNCH_CHECK("k_variance_gemm");
-        k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
-            Mr, ntiles, m->ws.part.as<double>(), perm, m->ws.norms.as<double>(),
-            sig2, m->power, d_var);
-        FGB_LAUNCH_CHECK("k_variance_final");
+        {
+          StageTimer _pt(kStVarianceGemm, st, 1);
+          k_variance_gemm<<<g3, GT, 0, st>>>(
+              Mr, R, Ms, m->ws.kmat.as<double>(),
+              m->Lp.as<double>() + m->h_panel_off[s], m->ws.part.as<double>(),
+              ntiles);
+          FGB_LAUNCH_CHECK("k_variance_gemm");
+        }
+        {
+          StageTimer _pt(kStVarianceFinal, st, 1);
+          k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
+              Mr, ntiles, m->ws.part.as<double>(), perm, m->ws.norms.as<double>(),
+              sig2, m->power, d_var);
+          FGB_LAUNCH_CHECK("k_variance_final");
+        }
       }
     }
     base += Ns;
@@ -426,9 +442,12 @@ static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     return FGB_EINVAL;
   }
   int rc;
-  if ((rc = fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
-                            d_positions, cutoff, st)))
-    return rc;
+  {
+    StageTimer _pt(kStNeighbors, st, 11);
+    if ((rc = fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
+                              d_positions, cutoff, st)))
+      return rc;
+  }
   const B2Params &p = m->b2;
   const int N = m->nl.n_atoms;
   const long long P = m->nl.n_pairs;
@@ -461,12 +480,18 @@ static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     if (want_grad)
       FGB_CUDA(cudaMemsetAsync(m->ws.gB2.p, 0, sizeof(double) * (size_t)N * p.n_d, st));
   }
-  if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
-                              m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-                              st)))
-    return rc;
+  {
+    StageTimer _pt(kStB2Forward, st);
+    if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
+                                m->ws.B2.as<double>(), m->ws.norms.as<double>(),
+                                st)))
+      return rc;
+  }
   std::vector<int> counts;
-  if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
+  {
+    StageTimer _pt(kStSpeciesPerm, st, 2 + 5 * p.n_species);
+    if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
+  }
   if (precision == FGB_PREC_MIXED) {
     if ((rc = kernel_stage_mixed(m, N, counts, want_grad, want_v,
                                  m->ws.e_atom.as<double>(),
@@ -481,19 +506,26 @@ static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       return rc;
   }
   if (want_grad) {
-    if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
-                                m->ws.gB2.as<double>(),
-                                m->ws.pair_grad.as<double3>(), st)))
-      return rc;
-    if ((rc = launch_forces(&m->nl, m->ws.pair_grad.as<double3>(),
-                            m->ws.forces.as<double>(), m->ws.virial.as<double>(),
-                            st)))
-      return rc;
+    {
+      StageTimer _pt(kStB2Adjoint, st);
+      if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
+                                  m->ws.gB2.as<double>(),
+                                  m->ws.pair_grad.as<double3>(), st)))
+        return rc;
+    }
+    {
+      StageTimer _pt(kStForces, st);
+      if ((rc = launch_forces(&m->nl, m->ws.pair_grad.as<double3>(),
+                              m->ws.forces.as<double>(),
+                              m->ws.virial.as<double>(), st)))
+        return rc;
+    }
     if (d_forces && want_f && N > 0)
       FGB_CUDA(cudaMemcpyAsync(d_forces, m->ws.forces.p,
                                sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice,
                                st));
   }
+  StageTimer _ptr(kStStructReduce, st);
   if ((want_e && d_energy) || (want_s && d_stress))
     if ((rc = launch_struct_reduce(
              n_struc, m->ws.atom_off.as<int>(), m->ws.volume.as<double>(),

@@ -1,0 +1,78 @@
+"""Named synthetic workloads with seeded inputs and GPU-trained models.
+
+``alloy1000``: 2-species random alloy, 1,000-atom cubic cell at 0.06
+atoms/A^3, species 50/50, 1.8 A minimum distance; B2 chebyshev/quadratic
+n_max = 8, l_max = 4, rc = 5.5 A; NormalizedDotProduct sigma = 2, power = 2;
+10 training structures (seeds 2000-2009) with truncated Lennard-Jones energy
+and force labels (eps 0.4/0.25 eV, sigma 2.6/2.3 A, Lorentz-Berthelot
+mixing); 1,000 sparse environments per species drawn without replacement
+from the training pool (seed 2200); noise sigma_E = 1e-3 eV/atom (1.0 eV per
+structure), sigma_F = 0.05 eV/A; test structures from seeds 2100, 2101, ...
+"""
+import numpy as np
+
+from . import synthetic as syn
+
+ALLOY = dict(n_atoms=1000, density=0.06, fractions=(0.5, 0.5), dmin=1.8,
+             rc=5.5, n_max=8, l_max=4, sigma=2.0, power=2, eps=(0.4, 0.25),
+             lj_sigma=(2.6, 2.3), n_train=10, train_seed0=2000,
+             sparse_per_species=1000, sparse_seed=2200, test_seed0=2100,
+             sigma_e_per_atom=1e-3, sigma_f=0.05, sigma_s=1.0)
+
+
+def alloy_structure(seed, n_atoms=None):
+    c = ALLOY
+    return syn.random_alloy(n_atoms or c["n_atoms"], density=c["density"],
+                            fractions=c["fractions"], dmin=c["dmin"],
+                            seed=seed)
+
+
+def alloy_labels(cell, sp, pos):
+    c = ALLOY
+    return syn.lennard_jones(cell, sp, pos, c["eps"], c["lj_sigma"], c["rc"])
+
+
+def alloy_sparse_choice(n_train, species_lists, per_species, seed):
+    """Per training structure, the sorted atom indices chosen as sparse
+    environments: per species, ``per_species`` draws without replacement
+    from the pool of all training atoms of that species."""
+    r = syn.rng(seed)
+    chosen = [[] for _ in range(n_train)]
+    S = max(int(max(s)) for s in species_lists) + 1
+    for s in range(S):
+        pool = [(t, a) for t in range(n_train)
+                for a in np.nonzero(np.asarray(species_lists[t]) == s)[0]]
+        k = min(per_species, len(pool))
+        pick = r.choice(len(pool), size=k, replace=False)
+        for q in pick:
+            t, a = pool[q]
+            chosen[t].append(int(a))
+    return [sorted(c) for c in chosen]
+
+
+def build_alloy_model(n_train=None, per_species=None, verbose=False):
+    """Train the alloy model with flare_gb300 (GPU, FP64).  Returns
+    (SparseGP, B2, NormalizedDotProduct)."""
+    import flare_gb300 as fg
+    c = ALLOY
+    n_train = n_train or c["n_train"]
+    per_species = per_species or c["sparse_per_species"]
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, c["rc"]], [],
+               [2, c["n_max"], c["l_max"]])
+    k = fg.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = fg.SparseGP([k], c["sigma_e_per_atom"] * c["n_atoms"], c["sigma_f"],
+                     c["sigma_s"])
+    data = [alloy_structure(c["train_seed0"] + t) for t in range(n_train)]
+    sparse = alloy_sparse_choice(n_train, [d[1] for d in data], per_species,
+                                 c["sparse_seed"])
+    for t, (cell, sp, pos) in enumerate(data):
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = alloy_labels(cell, sp, pos)
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(st, sparse[t])
+        if verbose:
+            print(f"  trained structure {t}: M = {gp.n_sparse}", flush=True)
+    gp.update_matrices_QR()
+    return gp, b2, k

@@ -64,6 +64,17 @@ enum {
 const char *fgb_last_error(void);
 int fgb_version(void);
 
+/* ------------------------------------------------------ stage profiler
+ * When enabled, every kernel launch of the prediction pipeline is bracketed
+ * by CUDA events on its launch stream.  fgb_profile_read synchronises those
+ * events and returns, per stage, the summed device time (ms) and the launch
+ * count since the last reset.  Stage names: fgb_profile_stage_name(i). */
+int fgb_profile_enable(int on);
+int fgb_profile_reset(void);
+int fgb_profile_n_stages(void);
+const char *fgb_profile_stage_name(int stage);
+int fgb_profile_read(double *ms, long long *launches, int n);
+
 /* ----------------------------------------------------- neighbour list
  * Cell-list neighbour build for a batch of periodic structures.  Replaces
  * Structure::compute_neighbors (structure.cpp:52-118): the same pairs
@@ -166,11 +177,15 @@ int fgb_envs_envs(const double *d_desc1, const double *d_norm1, int n1,
                   void *stream);
 
 /* NormalizedDotProduct::envs_struc (normalized_dot_product.cpp:117-214) on
- * the GPU in FP64, the reference algorithm with stored gradients: the model's
- * sparse set against ONE structure (n_struc == 1 build of `nl`).
- * d_kern[M * (1 + 3N + 6)] row-major. */
-int fgb_envs_struc(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
-                   double *d_kern, void *stream);
+ * the GPU in FP64, the reference algorithm with stored forward-mode
+ * descriptor gradients: the sparse set (h_counts[n_species] environments per
+ * species, d_sparse[M * n_d] species-grouped raw descriptors) against ONE
+ * structure (an n_struc == 1 build of `nl`, coded species d_species[N]).
+ * d_kern[M * (1 + 3N + 6)] row-major: energy, force and stress columns. */
+int fgb_envs_struc(fgb_b2_t b2, double sigma, double power,
+                   const int *h_counts, const double *d_sparse,
+                   fgb_nlist_t nl, const int *d_species, double *d_kern,
+                   void *stream);
 
 /* Plain FP64 form of SparseGP::predict_local_uncertainties for one
  * structure: envs_struc (stored gradients), mean_efs = K^T alpha, and the

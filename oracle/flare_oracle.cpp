@@ -411,32 +411,42 @@ long long orc_b2(int n, const int *species, const int *counts,
       bp++;
       local++;
     }
-    // B2 contraction (b2.cpp:209-233)
+    // B2 contraction (b2.cpp:209-233).  The reference stores
+    // B2_force_dervs column-major (Eigen), so its inner neighbour loop walks
+    // contiguous memory; with row-major storage here the same arithmetic is
+    // ordered neighbour-major so that the writes stay contiguous.
     double *b = B2 + (long long)i * nd;
-    int counter = 0;
-    for (int n1 = 0; n1 < nr; n1++)
-      for (int n2 = n1; n2 < nr; n2++)
-        for (int l = 0; l < L + 1; l++) {
-          double acc = 0;
-          for (int m = 0; m < 2 * l + 1; m++) {
-            int i1 = n1 * nh + l * l + m, i2 = n2 * nh + l * l + m;
-            acc += A[i1] * A[i2];
+    {
+      int counter = 0;
+      for (int n1 = 0; n1 < nr; n1++)
+        for (int n2 = n1; n2 < nr; n2++)
+          for (int l = 0; l < L + 1; l++) {
+            double acc = 0;
+            for (int m = 0; m < 2 * l + 1; m++) {
+              int i1 = n1 * nh + l * l + m, i2 = n2 * nh + l * l + m;
+              acc += A[i1] * A[i2];
+            }
+            b[counter++] = acc;
           }
-          b[counter] = acc;
-          if (dervs) {
-            for (int nb = 0; nb < bc[i]; nb++)
-              for (int comp = 0; comp < 3; comp++) {
-                const double *dl = dA.data() + ((size_t)nb * 3 + comp) * nA;
+    }
+    if (dervs) {
+      for (int nb = 0; nb < bc[i]; nb++)
+        for (int comp = 0; comp < 3; comp++) {
+          const double *dl = dA.data() + ((size_t)nb * 3 + comp) * nA;
+          double *out = dervs + ((boff[i] + nb) * 3 + comp) * nd;
+          int counter = 0;
+          for (int n1 = 0; n1 < nr; n1++)
+            for (int n2 = n1; n2 < nr; n2++)
+              for (int l = 0; l < L + 1; l++) {
                 double acc2 = 0;
                 for (int m = 0; m < 2 * l + 1; m++) {
                   int i1 = n1 * nh + l * l + m, i2 = n2 * nh + l * l + m;
                   acc2 += A[i1] * dl[i2] + dl[i1] * A[i2];
                 }
-                dervs[((boff[i] + nb) * 3 + comp) * nd + counter] = acc2;
+                out[counter++] = acc2;
               }
-          }
-          counter++;
         }
+    }
     double nn = 0;
     for (int k = 0; k < nd; k++) nn += b[k] * b[k];
     norms[i] = std::sqrt(nn);

@@ -291,9 +291,13 @@ class Structure:
             dv.neighbor_indices.append(b2_idx[pair_rows])
             dv.neighbor_coordinates.append(coords[pair_rows])
             if compute_dervs:
-                rows3 = (3 * pair_rows[:, None] + np.arange(3)[None, :]).reshape(-1)
-                dv.descriptor_force_dervs.append(dervs[rows3])
-                dv.descriptor_force_dots.append(fdots[rows3])
+                # contiguous per-atom blocks (b2.cpp:159-166 block copies)
+                blocks = [dervs[3 * cum[a]:3 * cum[a + 1]] for a in atoms]
+                dv.descriptor_force_dervs.append(
+                    np.concatenate(blocks) if blocks else np.zeros((0, nd)))
+                fblocks = [fdots[3 * cum[a]:3 * cum[a + 1]] for a in atoms]
+                dv.descriptor_force_dots.append(
+                    np.concatenate(fblocks) if fblocks else np.zeros(0))
         return dv
 
 

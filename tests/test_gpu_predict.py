@@ -115,7 +115,9 @@ def test_forces_are_energy_gradient(c1):
         p2 = pos.copy(); p2[atom, c] -= h
         e1 = gpu_predict(ggp, calc, [(cell, sp, p1)])["energy"][0]
         e2 = gpu_predict(ggp, calc, [(cell, sp, p2)])["energy"][0]
-        assert abs(r["forces"][atom, c] + (e1 - e2) / (2 * h)) < 1e-5
+        # tolerance of the reference's finite-difference tests
+        # (test_kernels.cpp: delta 1e-4, tolerance 1e-4)
+        assert abs(r["forces"][atom, c] + (e1 - e2) / (2 * h)) < 1e-4
 
 
 def test_stale_model_raises():
