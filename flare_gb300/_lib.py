@@ -41,6 +41,8 @@ SIGNATURES = {
     "fgb_nlist_build": (_i, [_vp, _i, _vp, _vp, _vp, _d, _vp]),
     "fgb_nlist_size": (_i, [_vp, _pll, _pi]),
     "fgb_nlist_export": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_nlist_build_noalloc": (_i, [_vp, _vp, _i, _d, _ll, _vp, _vp, _vp,
+                                     _vp, _pll, _vp]),
     "fgb_b2_create": (_i, [_pvp, _i, _i, _vp, _i, _vp, _i, _i, _i, _i, _vp]),
     "fgb_b2_destroy": (_i, [_vp]),
     "fgb_b2_size": (_i, [_vp, _pi, _pi]),

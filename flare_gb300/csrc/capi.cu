@@ -192,7 +192,41 @@ int scan_impl(const TI *d_in, TO *d_out, int n, TO *d_total, DevBuf &tmp,
   return FGB_OK;
 }
 
+// Same scan with caller-provided block-sum storage (no allocation):
+// `sums` holds at least ceil(n / 1024) + 1 elements.
+template <typename TI, typename TO>
+int scan_impl_raw(const TI *d_in, TO *d_out, int n, TO *d_total, TO *sums,
+                  cudaStream_t st) {
+  if (n <= 0) {
+    if (d_total) FGB_CUDA(cudaMemsetAsync(d_total, 0, sizeof(TO), st));
+    return FGB_OK;
+  }
+  int nb = (n + kScanBlock - 1) / kScanBlock;
+  if (nb > 4 * kScanBlock) {
+    set_error("scan: %d elements exceed the two-level scan limit", n);
+    return FGB_EINVAL;
+  }
+  k_scan_block<TI, TO><<<nb, kScanBlock, 0, st>>>(d_in, d_out, n, sums);
+  FGB_LAUNCH_CHECK("k_scan_block");
+  k_scan_sums<TO><<<1, kScanBlock, 0, st>>>(sums, nb, d_total);
+  FGB_LAUNCH_CHECK("k_scan_sums");
+  k_scan_add<TO><<<nb, kScanBlock, 0, st>>>(d_out, n, sums);
+  FGB_LAUNCH_CHECK("k_scan_add");
+  return FGB_OK;
+}
+
 }  // namespace
+
+int scan_int_to_int_raw(const int *d_in, int *d_out, int n, int *d_total,
+                        int *d_sums, cudaStream_t st) {
+  return scan_impl_raw<int, int>(d_in, d_out, n, d_total, d_sums, st);
+}
+
+int scan_int_to_ll_raw(const int *d_in, long long *d_out, int n,
+                       long long *d_total, long long *d_sums,
+                       cudaStream_t st) {
+  return scan_impl_raw<int, long long>(d_in, d_out, n, d_total, d_sums, st);
+}
 
 int scan_int_to_int(const int *d_in, int *d_out, int n, int *d_total,
                     DevBuf &tmp, cudaStream_t st) {

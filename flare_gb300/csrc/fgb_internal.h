@@ -39,6 +39,12 @@ int scan_int_to_int(const int *d_in, int *d_out, int n, int *d_total,
                     DevBuf &tmp, cudaStream_t st);
 int scan_int_to_ll(const int *d_in, long long *d_out, int n,
                    long long *d_total, DevBuf &tmp, cudaStream_t st);
+// Variants with caller-provided block sums (ceil(n/1024) + 1 elements).
+int scan_int_to_int_raw(const int *d_in, int *d_out, int n, int *d_total,
+                        int *d_sums, cudaStream_t st);
+int scan_int_to_ll_raw(const int *d_in, long long *d_out, int n,
+                       long long *d_total, long long *d_sums,
+                       cudaStream_t st);
 
 }  // namespace fgb
 

@@ -11,6 +11,8 @@
 // |s_a| <= sweep exactly as the reference's loop bounds, and each atom's
 // segment is finally ordered by (j, s1, s2, s3) — the reference's loop
 // order.  The result is the same set, the same order and the same bits.
+#include <mutex>
+
 #include "fgb_internal.h"
 
 namespace fgb {
@@ -517,5 +519,216 @@ extern "C" int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
   if (d_wrapped)
     FGB_CUDA(cudaMemcpyAsync(d_wrapped, nl->wrapped.p, sizeof(double) * 3 * N,
                              cudaMemcpyDeviceToDevice, st));
+  return FGB_OK;
+}
+
+// ------------------------------------------------- no-allocation variant
+// fgb_nlist_build_noalloc builds one structure's neighbour list without any
+// device allocation: its working memory is the file-scope array below, and
+// the list is written straight into buffers the caller owns.  It exists for
+// callers that cannot call cudaMalloc themselves or have us call it — for
+// instance an MD engine or plugin that manages a fixed device-memory budget
+// of its own, or a loop that must not pay allocation latency or fragment
+// the heap between steps.
+//
+// The array's name, used in host code, is only a host-side stand-in for the
+// symbol; the kernels need its device address, which is looked up once per
+// device with cudaGetSymbolAddress (on the first call made with that device
+// current) and cached.  Every call on a device shares the one array and
+// leaves its contents behind; each call clears what must start at zero (bin
+// counts, error flags, the structure index of each atom), so calls that run
+// one after another are independent, but calls that overlap on the GPU (for
+// example on two streams at once) race on the same memory.
+namespace fgb {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = FGB_NOALLOC_SCRATCH_BYTES;  // 24 MiB
+static __device__ __align__(256) unsigned char g_nlist_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Device address of g_nlist_scratch on the current device (set-up on the
+// first call per device).
+int noalloc_scratch(unsigned char **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) {
+    set_error("fgb_nlist_build_noalloc: device ordinal %d out of range", dev);
+    return FGB_EINVAL;
+  }
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_nlist_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+  return FGB_OK;
+}
+
+}  // namespace
+}  // namespace fgb
+
+extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
+                                       const double *d_positions, int n_atoms,
+                                       double cutoff, long long max_pairs,
+                                       int *d_neighbor_count,
+                                       int *d_structure_indices, int *d_shifts,
+                                       double *d_relative_positions,
+                                       long long *h_n_pairs, void *stream) {
+  using namespace fgb;
+  if (!h_cell || !d_positions || !d_neighbor_count || !d_structure_indices ||
+      !d_relative_positions || !h_n_pairs || n_atoms < 0 || max_pairs < 0) {
+    set_error("fgb_nlist_build_noalloc: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (n_atoms > FGB_NOALLOC_MAX_ATOMS) {
+    set_error("fgb_nlist_build_noalloc: %d atoms exceed the no-allocation "
+              "limit of %d atoms", n_atoms, FGB_NOALLOC_MAX_ATOMS);
+    return FGB_EINVAL;
+  }
+  if (!(cutoff > 0) || !std::isfinite(cutoff)) {
+    set_error("fgb_nlist_build_noalloc: cutoff must be positive and finite");
+    return FGB_EINVAL;
+  }
+  if (reinterpret_cast<uintptr_t>(d_relative_positions) % 16 != 0) {
+    set_error("fgb_nlist_build_noalloc: relative_positions must be 16-byte "
+              "aligned");
+    return FGB_EINVAL;
+  }
+  for (int k = 0; k < 9; k++)
+    if (!std::isfinite(h_cell[k])) {
+      set_error("fgb_nlist_build_noalloc: non-finite cell");
+      return FGB_EINVAL;
+    }
+  *h_n_pairs = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = n_atoms;
+  StrucGeom geom;
+  double sweep_cut;
+  make_geom(h_cell, cutoff, 0, N, 0, geom, sweep_cut);
+  if (!(geom.volume > 0) || !std::isfinite(sweep_cut) || sweep_cut <= 0) {
+    set_error("fgb_nlist_build_noalloc: degenerate cell");
+    return FGB_EINVAL;
+  }
+  if (geom.sweep > 127 || geom.kk[0] > 127 || geom.kk[1] > 127 ||
+      geom.kk[2] > 127) {
+    set_error("fgb_nlist_build_noalloc: cutoff spans more than 127 cell "
+              "images");
+    return FGB_EINVAL;
+  }
+  const long long nbins = (long long)geom.nb[0] * geom.nb[1] * geom.nb[2];
+  unsigned char *base = nullptr;
+  int rc;
+  if ((rc = noalloc_scratch(&base))) return rc;
+  // carve the scratch (every piece 256-byte aligned)
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char *p = base + off;
+    off += align256(bytes);
+    return p;
+  };
+  const int nsum = (int)std::max<long long>(N, nbins) / 1024 + 2;
+  StrucGeom *d_geom = (StrucGeom *)take(sizeof(StrucGeom));
+  int *atom_struct = (int *)take(sizeof(int) * (N + 1));
+  double *wrapped = (double *)take(sizeof(double) * 3 * (N + 1));
+  int *raw = (int *)take(sizeof(int) * 3 * (N + 1));
+  int *home = (int *)take(sizeof(int) * (N + 1));
+  int *slot = (int *)take(sizeof(int) * (N + 1));
+  int *bin_count = (int *)take(sizeof(int) * (nbins + 1));
+  int *bin_start = (int *)take(sizeof(int) * (nbins + 1));
+  int *bin_atoms = (int *)take(sizeof(int) * (N + 1));
+  long long *offsets = (long long *)take(sizeof(long long) * (N + 1));
+  long long *sums = (long long *)take(sizeof(long long) * nsum);
+  int *flag = (int *)take(sizeof(int) * 4);
+  const size_t fixed = off;
+  if (fixed > kNoAllocScratchBytes) {
+    set_error("fgb_nlist_build_noalloc: structure needs more than the "
+              "%zu-byte no-allocation scratch", kNoAllocScratchBytes);
+    return FGB_EINVAL;
+  }
+  FGB_CUDA(cudaMemcpyAsync(d_geom, &geom, sizeof(StrucGeom),
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemsetAsync(atom_struct, 0, sizeof(int) * (N + 1), st));
+  FGB_CUDA(cudaMemsetAsync(bin_count, 0, sizeof(int) * (nbins + 1), st));
+  FGB_CUDA(cudaMemsetAsync(flag, 0, sizeof(int) * 4, st));
+  if (N == 0) {
+    FGB_CUDA(cudaStreamSynchronize(st));
+    return FGB_OK;
+  }
+  const int T = 128;
+  k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(N, d_positions, atom_struct, d_geom,
+                                           wrapped, raw, home, slot, bin_count,
+                                           flag);
+  FGB_LAUNCH_CHECK("k_wrap_bin");
+  if ((rc = scan_int_to_int_raw(bin_count, bin_start, (int)nbins,
+                                bin_start + nbins, (int *)sums, st)))
+    return rc;
+  k_bin_fill<<<ceil_div(N, T), T, 0, st>>>(N, home, slot, bin_start, bin_atoms);
+  FGB_LAUNCH_CHECK("k_bin_fill");
+  k_count<<<ceil_div(N, T), T, 0, st>>>(N, atom_struct, d_geom, wrapped, raw,
+                                        bin_start, bin_atoms, cutoff,
+                                        d_neighbor_count);
+  FGB_LAUNCH_CHECK("k_count");
+  if ((rc = scan_int_to_ll_raw(d_neighbor_count, offsets, N, offsets + N, sums,
+                               st)))
+    return rc;
+  long long P = 0;
+  int hflag[4] = {0, 0, 0, 0};
+  FGB_CUDA(cudaMemcpyAsync(&P, offsets + N, sizeof(long long),
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaMemcpyAsync(hflag, flag, sizeof(int) * 4,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (hflag[0]) {
+    set_error("fgb_nlist_build_noalloc: non-finite atomic positions");
+    return FGB_EINVAL;
+  }
+  *h_n_pairs = P;
+  const size_t per_pair = align256(sizeof(unsigned long long) * (P + 1)) +
+                          align256(sizeof(double4_16a) * (P + 1)) +
+                          align256(sizeof(int) * (P + 1)) * 2 +
+                          align256(sizeof(double4_16a) * (P + 1));
+  if (P > FGB_NOALLOC_MAX_PAIRS || fixed + per_pair > kNoAllocScratchBytes) {
+    set_error("fgb_nlist_build_noalloc: %lld pairs exceed the no-allocation "
+              "limit of %d pairs", P, FGB_NOALLOC_MAX_PAIRS);
+    return FGB_EINVAL;
+  }
+  if (P > max_pairs) {
+    set_error("fgb_nlist_build_noalloc: %lld pairs do not fit the output "
+              "capacity of %lld (needed size returned in n_pairs)", P,
+              max_pairs);
+    return FGB_EINVAL;
+  }
+  if (P == 0) return FGB_OK;
+  unsigned long long *key = (unsigned long long *)take(sizeof(unsigned long long) * (P + 1));
+  double4_16a *tmp_rel = (double4_16a *)take(sizeof(double4_16a) * (P + 1));
+  int *nbr_j = (int *)take(sizeof(int) * (P + 1));
+  int *nbr_shift = (int *)take(sizeof(int) * (P + 1));
+  double4_16a *nbr_rel = (double4_16a *)take(sizeof(double4_16a) * (P + 1));
+  k_fill<<<ceil_div(N, T), T, 0, st>>>(N, atom_struct, d_geom, wrapped, raw,
+                                       bin_start, bin_atoms, cutoff, offsets,
+                                       key, tmp_rel, flag);
+  FGB_LAUNCH_CHECK("k_fill");
+  k_rank_scatter<<<ceil_div((long long)N * 32, T), T, 0, st>>>(
+      N, atom_struct, d_geom, offsets, key, tmp_rel, nbr_j, nbr_shift, nbr_rel);
+  FGB_LAUNCH_CHECK("k_rank_scatter");
+  k_export<<<ceil_div(N, T), T, 0, st>>>(N, offsets, atom_struct, d_geom, nbr_j,
+                                         nbr_shift, nbr_rel, d_neighbor_count,
+                                         d_structure_indices, d_shifts,
+                                         d_relative_positions);
+  FGB_LAUNCH_CHECK("k_export");
+  FGB_CUDA(cudaMemcpyAsync(hflag, flag, sizeof(int) * 4,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (hflag[1]) {
+    set_error("fgb_nlist_build_noalloc: internal consistency check failed");
+    return FGB_ECUDA;
+  }
   return FGB_OK;
 }

@@ -102,6 +102,29 @@ int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
                      double *d_relative_positions, double *d_wrapped,
                      void *stream);
 
+/* The neighbour list of ONE structure written into caller-owned device
+ * buffers, with no device allocation at all.  No counterpart in the
+ * reference; it serves callers that cannot allocate device memory (for
+ * example a host program that owns a fixed device-memory budget, or a loop
+ * that must not allocate between steps).  Working memory is a fixed
+ * FGB_NOALLOC_SCRATCH_BYTES array that every GPU loading the library holds
+ * until exit.  Limits: n_atoms <= FGB_NOALLOC_MAX_ATOMS and at most
+ * FGB_NOALLOC_MAX_PAIRS pairs; larger inputs return FGB_EINVAL with a
+ * message.  Outputs as in fgb_nlist_export (d_shifts may be NULL;
+ * d_relative_positions 16-byte aligned); *h_n_pairs receives the pair count
+ * (also when it exceeds max_pairs, so the caller can grow its buffers).
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  Calls share the array, so
+ * calls that overlap on the GPU race; calls in sequence are independent. */
+#define FGB_NOALLOC_MAX_ATOMS 8192
+#define FGB_NOALLOC_MAX_PAIRS 262144
+#define FGB_NOALLOC_SCRATCH_BYTES (24u << 20)
+int fgb_nlist_build_noalloc(const double *h_cell, const double *d_positions,
+                            int n_atoms, double cutoff, long long max_pairs,
+                            int *d_neighbor_count, int *d_structure_indices,
+                            int *d_shifts, double *d_relative_positions,
+                            long long *h_n_pairs, void *stream);
+
 /* ------------------------------------------------------- B2 descriptor
  * B2(radial_basis, cutoff_function, radial_hyps, cutoff_hyps,
  *    [n_species, n_max, l_max], cutoffs[n_species^2]) — b2.cpp:13-50.
