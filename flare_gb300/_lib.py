@@ -51,6 +51,8 @@ SIGNATURES = {
     "fgb_model_create": (_i, [_pvp, _vp, _d, _d]),
     "fgb_model_destroy": (_i, [_vp]),
     "fgb_model_set": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fgb_model_set_R_inv": (_i, [_vp, _vp]),
+    "fgb_predict_sor": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_predict": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp,
                          _vp, _vp, _vp]),
     "fgb_predict_host": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _i, _vp,

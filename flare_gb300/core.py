@@ -852,6 +852,9 @@ class SparseGP(_Training):
             counts, desc = self.sparse_descriptors[0].stacked()
             M = desc.shape[0]
             m.set(counts, desc, self.alpha[:M], self.L_inv[:M, :M])
+            if self.R_inv is not None:
+                R = np.ascontiguousarray(self.R_inv[:M, :M], np.float64)
+                check(lib().fgb_model_set_R_inv(m.h, ptr(R)), "SparseGP")
             self._model = m
         return self._model
 
@@ -907,6 +910,30 @@ class SparseGP(_Training):
         S = structure.descriptor_calculators[0].descriptor_settings[0]
         order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
         structure.local_uncertainties = [r["local_var"][order]]
+
+    def predict_SOR(self, structure):
+        """sparse_gp.cpp:667-692: mean_efs and the SOR variances
+        diag(K^T R_inv R_inv^T K) over all 1 + 3N + 6 outputs (FP64)."""
+        if self.R_inv is None:
+            raise RuntimeError(
+                "L_inv must be up to date to make predictions. Please call "
+                "update_matrices_QR and try again.")
+        m = self._device_model(structure.descriptor_calculators)
+        dev = _device()
+        n_out = 1 + 3 * structure.noa + 6
+        mean = torch.zeros(n_out, dtype=torch.float64, device=dev)
+        var = torch.zeros(n_out, dtype=torch.float64, device=dev)
+        d = structure._inputs()
+        check(lib().fgb_predict_sor(m.h, structure.nlist().h, ptr(d["species"]),
+                                    ptr(mean), ptr(var), stream_ptr()),
+              "predict_SOR")
+        structure.mean_efs = mean.cpu().numpy()
+        structure.variance_efs = var.cpu().numpy()
+
+    def predict_DTC(self, structure):
+        raise NotImplementedError(
+            "predict_DTC needs self_kernel_struc "
+            "(normalized_dot_product.cpp:451-586), which is not built")
 
     def compute_cluster_uncertainties(self, structure):
         """sparse_gp.cpp:94-139 (species-sorted variances)."""

@@ -32,6 +32,8 @@ struct fgb_model_s {
   fgb::DevBuf svalid;   // uint8 norm >= 1e-8
   fgb::DevBuf alpha;    // M
   fgb::DevBuf Lp;       // per-species L_inv panels
+  fgb::DevBuf RinvT;    // R_inv^T (M x M, lower triangular) for SOR
+  bool has_rinv = false;
   fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
   bool bmap_ready = false;
   fgb_nlist_s nl;
@@ -48,4 +50,8 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        double *d_gB2, double *d_var, cudaStream_t st);
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st);
+int envs_struc_impl(const B2Params &p, double sigma, double power,
+                    const int *h_counts, const double *d_sparse,
+                    fgb_nlist_s *nl, const int *d_species, double *d_kern,
+                    fgb_workspace &ws, cudaStream_t st);
 }  // namespace fgb

@@ -360,7 +360,7 @@ extern "C" int fgb_b2_forward_dervs(fgb_b2_t b2, fgb_nlist_t nl,
 namespace fgb {
 // envs_struc for one structure into d_kern; B2/norms of the structure are
 // left in ws (for the plain prediction's variance stage).
-static int envs_struc_impl(const B2Params &p, double sigma, double power,
+int envs_struc_impl(const B2Params &p, double sigma, double power,
                            const int *h_counts, const double *d_sparse,
                            fgb_nlist_s *nl, const int *d_species,
                            double *d_kern, fgb_workspace &ws,

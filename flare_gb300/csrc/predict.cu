@@ -163,6 +163,33 @@ __global__ void k_variance_final(int M, int ntiles, const double *__restrict__ p
   var[atom] = kself - s;
 }
 
+__global__ void k_transpose_rm(int R, int C, const double *__restrict__ in,
+                               double *__restrict__ out) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)R * C) return;
+  int r = (int)(idx / C), c = (int)(idx % C);
+  out[(long long)c * R + r] = in[idx];
+}
+
+__global__ void k_sum_parts(int M, int ntiles, const double *__restrict__ part,
+                            double *__restrict__ out) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  double s = 0.0;
+  for (int t = 0; t < ntiles; t++) s += part[(long long)m * ntiles + t];
+  out[m] = s;
+}
+
+__global__ void k_kt_alpha(int M, long long ncol, const double *__restrict__ KT,
+                           const double *__restrict__ alpha,
+                           double *__restrict__ out) {
+  long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= ncol) return;
+  double acc = 0.0;
+  for (int i = 0; i < M; i++) acc += KT[o * M + i] * alpha[i];
+  out[o] = acc;
+}
+
 __global__ void k_species_flags(int n, const int *__restrict__ species, int s,
                                 int *__restrict__ flags) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -595,6 +622,75 @@ extern "C" int fgb_predict_host(fgb_model_t m, int n_struc,
   if (h_local_var && (want & FGB_WANT_LOCAL_VAR) && N > 0)
     FGB_CUDA(cudaMemcpyAsync(h_local_var, m->io.var.p, sizeof(double) * N,
                              cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  return FGB_OK;
+}
+
+extern "C" int fgb_model_set_R_inv(fgb_model_t m, const double *h_R_inv) {
+  if (!m || !h_R_inv) { set_error("fgb_model_set_R_inv: invalid arguments"); return FGB_EINVAL; }
+  const int M = m->M;
+  std::vector<double> t((size_t)M * M);
+  for (int r = 0; r < M; r++)
+    for (int c = 0; c < M; c++) t[(size_t)c * M + r] = h_R_inv[(size_t)r * M + c];
+  int rc;
+  if ((rc = m->RinvT.ensure(sizeof(double) * ((size_t)M * M + 1)))) return rc;
+  if (M > 0)
+    FGB_CUDA(cudaMemcpy(m->RinvT.p, t.data(), sizeof(double) * (size_t)M * M,
+                        cudaMemcpyHostToDevice));
+  m->has_rinv = true;
+  return FGB_OK;
+}
+
+extern "C" int fgb_predict_sor(fgb_model_t m, fgb_nlist_t nl,
+                               const int *d_species, double *d_mean_efs,
+                               double *d_variance_efs, void *stream) {
+  if (!m || !nl || !d_mean_efs || !d_variance_efs) {
+    set_error("fgb_predict_sor: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (!m->solved || !m->has_rinv) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = nl->n_atoms, M = m->M;
+  const long long ncol = 1 + 3LL * N + 6;
+  if (ncol > (1LL << 30)) { set_error("fgb_predict_sor: structure too large"); return FGB_EINVAL; }
+  int rc;
+  DevBuf kern, kt, part;
+  const int ntiles = ceil_div(M, BN);
+  if ((rc = kern.ensure(sizeof(double) * ((size_t)M * ncol + 1))) ||
+      (rc = kt.ensure(sizeof(double) * ((size_t)M * ncol + 1))) ||
+      (rc = part.ensure(sizeof(double) * ((size_t)ncol * ntiles + 1))))
+    return rc;
+  if ((rc = envs_struc_impl(m->b2, m->sigma, m->power, m->h_counts.data(),
+                            m->Sraw.as<double>(), nl, d_species,
+                            kern.as<double>(), m->ws, st)))
+    return rc;
+  if (M == 0) {
+    FGB_CUDA(cudaMemsetAsync(d_mean_efs, 0, sizeof(double) * ncol, st));
+    FGB_CUDA(cudaMemsetAsync(d_variance_efs, 0, sizeof(double) * ncol, st));
+    return FGB_OK;
+  }
+  k_transpose_rm<<<ceil_div((long long)M * ncol, 256), 256, 0, st>>>(
+      M, (int)ncol, kern.as<double>(), kt.as<double>());
+  FGB_LAUNCH_CHECK("k_transpose_rm");
+  k_kt_alpha<<<ceil_div(ncol, 128), 128, 0, st>>>(M, ncol, kt.as<double>(),
+                                                  m->alpha.as<double>(),
+                                                  d_mean_efs);
+  FGB_LAUNCH_CHECK("k_kt_alpha");
+  // V = K^T R_inv = K^T (R_inv^T)^T: the triangular NT GEMM with the lower
+  // factor R_inv^T; variance_efs = row sums of V^2 (sparse_gp.cpp:689-691).
+  dim3 g(ntiles, ceil_div(ncol, BM));
+  k_variance_gemm<<<g, GT, 0, st>>>((int)ncol, M, M, kt.as<double>(),
+                                    m->RinvT.as<double>(), part.as<double>(),
+                                    ntiles);
+  FGB_LAUNCH_CHECK("k_variance_gemm");
+  k_sum_parts<<<ceil_div(ncol, 128), 128, 0, st>>>((int)ncol, ntiles,
+                                                   part.as<double>(),
+                                                   d_variance_efs);
+  FGB_LAUNCH_CHECK("k_sum_parts");
   FGB_CUDA(cudaStreamSynchronize(st));
   return FGB_OK;
 }

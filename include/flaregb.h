@@ -168,6 +168,16 @@ int fgb_model_destroy(fgb_model_t m);
 int fgb_model_set(fgb_model_t m, const int *h_counts, const double *h_desc,
                   const double *h_alpha, const double *h_L_inv);
 
+/* R_inv (sparse_gp.cpp:635, upper triangular, row-major M x M) for the SOR
+ * variance. */
+int fgb_model_set_R_inv(fgb_model_t m, const double *h_R_inv);
+
+/* SparseGP::predict_SOR (sparse_gp.cpp:667-692) for ONE structure in FP64:
+ * mean_efs = K^T alpha and variance_efs = diag(K^T R_inv R_inv^T K) with K
+ * from envs_struc.  d_mean_efs, d_variance_efs: [1 + 3N + 6]. */
+int fgb_predict_sor(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
+                    double *d_mean_efs, double *d_variance_efs, void *stream);
+
 /* Full prediction for a packed batch of structures (device pointers):
  * neighbours (cutoff = Structure cutoff), B2, kernel against the sparse set,
  * mean energy / forces / stress by the reverse-mode adjoint and the local
