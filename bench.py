@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=32,
                     help="structures (1000 atoms each) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -320,6 +320,26 @@ def run_ours(args, rank, world, local):
     res_s = out["s"].cpu().numpy().copy()
     res_v = out["v"].cpu().numpy().copy()
 
+    # ---- errors of this precision against the FP64 path, same batch
+    errors = None
+    if args.precision != "fp64":
+        step(_lib.FGB_PREC_FP64)
+        torch.cuda.synchronize()
+        e64 = out["e"].cpu().numpy()
+        f64 = out["f"].cpu().numpy()
+        s64 = out["s"].cpu().numpy()
+        v64 = out["v"].cpu().numpy()
+        nat = np.diff(offsets)
+        std = lambda v: np.where(v > 0, np.sqrt(np.abs(v)), -np.sqrt(np.abs(v))) / c["sigma"]
+        errors = {
+            "energy_ev_per_atom_max": float(np.max(np.abs(res_e - e64) / nat)),
+            "force_mae_ev_per_a": float(np.mean(np.abs(res_f - f64))),
+            "force_max_ev_per_a": float(np.max(np.abs(res_f - f64))),
+            "stress_max_ev_per_a3": float(np.max(np.abs(res_s - s64))),
+            "local_std_max_abs": float(np.max(np.abs(std(res_v) - std(v64)))),
+            "reference": "FP64 path of this library on the same batch "
+                         "(itself checked against the FP64 CPU oracle)"}
+
     # ---- e2e through the host-buffer C ABI (pinned buffers)
     h_pos = torch.from_numpy(pos).pin_memory()
     h_sp = torch.from_numpy(sp).pin_memory()
@@ -360,7 +380,7 @@ def run_ours(args, rank, world, local):
     launches_per_step = st_n / args.steps
     flop_per_launch = flops[gemm_stage] / max(launches_per_step, 1)
     achieved = flop_per_launch / (st_ms / st_n * 1e-3) / 1e12
-    peak = measure_fp64_peak(torch) if args.precision == "fp64" else None
+    peak = measure_fp64_peak(torch)
     gpu_launches = int(sum(v[1] for v in stage.values()))
 
     result = {
@@ -393,6 +413,7 @@ def run_ours(args, rank, world, local):
         "stages_ms_per_step": {k_: round(v[0] / args.steps, 4)
                                for k_, v in stage.items() if v[1]},
         "gpu_launches": gpu_launches,
+        "errors_vs_fp64": errors,
         "clocks": clocks.summary(local),
     }
     if rank == 0 and not args.no_plain:

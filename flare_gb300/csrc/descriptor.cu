@@ -115,32 +115,35 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   if (t == 0) norms[i] = sqrt(nrm);
 }
 
-// Shared memory: u[nA] | A[nA]
+// Shared memory: u[nA] | A[nA] (compute type T: double, or float in the
+// mixed-precision path)
+template <typename T>
 __global__ void __launch_bounds__(kChunk)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
              const double *__restrict__ gB2, double3 *__restrict__ pair_grad) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *smem = reinterpret_cast<T *>(smem_raw);
   const int i = blockIdx.x;
   if (i >= n_atoms) return;
   const int nA = p.n_A, nh = p.n_harm, nm = p.n_max, nr = p.n_rad,
             L1 = p.l_max + 1, nd = p.n_d;
-  double *u = smem;
-  double *A = u + nA;
+  T *u = smem;
+  T *A = u + nA;
   const int t = threadIdx.x;
-  for (int e = t; e < nA; e += blockDim.x) A[e] = A_in[(long long)i * nA + e];
+  for (int e = t; e < nA; e += blockDim.x) A[e] = T(A_in[(long long)i * nA + e]);
   __syncthreads();
   const double *w = gB2 + (long long)i * nd;
   for (int e = t; e < nA; e += blockDim.x) {
     int c = e / nh, lm = e % nh;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
-    double acc = 0.0;
+    T acc = T(0);
     for (int bb = 0; bb < nr; bb++) {
       int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
-      double wv = w[pair_index(lo, hi, nr) * L1 + l];
-      double f = (bb == c) ? 2.0 : 1.0;
+      T wv = T(w[pair_index(lo, hi, nr) * L1 + l]);
+      T f = (bb == c) ? T(2) : T(1);
       acc += f * wv * A[bb * nh + lm];
     }
     u[e] = acc;
@@ -155,30 +158,30 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     double rc = p.cutoffs[si * kMaxSpecies + sj];
     double3 out = make_double3(0.0, 0.0, 0.0);
     if (r.x <= rc) {
-      double g[kMaxNmax], dg[kMaxNmax];
-      double Y[kMaxHarm], Yd[3 * kMaxHarm];
-      radial_eval<double>(p, r.x, rc, g, dg);
-      ylm_eval<double>(p.l_max, r.y, r.z, r.w, Y, Yd);
-      const double ir = 1.0 / r.x;
-      const double ex = r.y * ir, ey = r.z * ir, ez = r.w * ir;
-      const double *us = u + sj * nm * nh;
-      double ox = 0.0, oy = 0.0, oz = 0.0;
+      T g[kMaxNmax], dg[kMaxNmax];
+      T Y[kMaxHarm], Yd[3 * kMaxHarm];
+      radial_eval<T>(p, T(r.x), T(rc), g, dg);
+      ylm_eval<T>(p.l_max, T(r.y), T(r.z), T(r.w), Y, Yd);
+      const T ir = T(1) / T(r.x);
+      const T ex = T(r.y) * ir, ey = T(r.z) * ir, ez = T(r.w) * ir;
+      const T *us = u + sj * nm * nh;
+      T ox = T(0), oy = T(0), oz = T(0);
       for (int n = 0; n < nm; n++) {
-        const double *un = us + n * nh;
-        double t1 = 0.0, tx = 0.0, ty = 0.0, tz = 0.0;
+        const T *un = us + n * nh;
+        T t1 = T(0), tx = T(0), ty = T(0), tz = T(0);
         for (int lm = 0; lm < nh; lm++) {
-          double uv = un[lm];
+          T uv = un[lm];
           t1 += uv * Y[lm];
           tx += uv * Yd[3 * lm];
           ty += uv * Yd[3 * lm + 1];
           tz += uv * Yd[3 * lm + 2];
         }
-        double dgr = dg[n];
+        T dgr = dg[n];
         ox += dgr * ex * t1 + g[n] * tx;
         oy += dgr * ey * t1 + g[n] * ty;
         oz += dgr * ez * t1 + g[n] * tz;
       }
-      out = make_double3(ox, oy, oz);
+      out = make_double3((double)ox, (double)oy, (double)oz);
     }
     pair_grad[pp] = out;
   }
@@ -280,20 +283,29 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
                       const double *d_gB2, double3 *d_pair_grad,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool fp32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
-  size_t sm = b2_adjoint_smem(p);
+  size_t sm = fp32 ? b2_adjoint_smem(p) / 2 : b2_adjoint_smem(p);
   if (sm > 200 * 1024) {
     set_error("B2 adjoint needs %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sm));
-  k_b2_adjoint<<<N, kChunk, sm, st>>>(
-      p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-      nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
+  if (fp32) {
+    FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint<float>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
+    k_b2_adjoint<float><<<N, kChunk, sm, st>>>(
+        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
+  } else {
+    FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint<double>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
+    k_b2_adjoint<double><<<N, kChunk, sm, st>>>(
+        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
+  }
   FGB_LAUNCH_CHECK("k_b2_adjoint");
   return FGB_OK;
 }

@@ -12,7 +12,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
                       const double *d_gB2, double3 *d_pair_grad,
-                      cudaStream_t st);
+                      cudaStream_t st, bool fp32 = false);
 int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
                   double *d_forces, double *d_virial, cudaStream_t st);
 int launch_struct_reduce(int n_struc, const int *d_atom_off,

@@ -1,12 +1,222 @@
 // Mixed-precision kernel stage.
+//
+// The energy and the local variance keep the FP64 kernel GEMM and the FP64
+// variance GEMM (the sparse-set sum and sigma^2 - |L_inv k|^2 cancel too many
+// digits for any 24-bit arithmetic).  The forces, which only need 1e-4 eV/A,
+// use the alpha-weighted sum folded into the sparse set before the GEMM:
+//   power 2:  E_i = sigma^2 d^_i^T B_s d^_i,  B_s = S^_s^T diag(alpha_s) S^_s
+//             dE/dd^ = 2 sigma^2 B_s d^   (one FP32 GEMM, n_d x n_d per species)
+//   power 1:  E_i = sigma^2 beta_s . d^_i,  beta_s = S^_s^T alpha_s
+// B_s / beta_s are built once per model in FP64 on the GPU and rounded to
+// FP32.  dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d|; the per-pair adjoint then
+// runs in FP32.  Other powers use the FP64 adjoint GEMM.
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 #include "fgb_model.h"
+#include "fgb_gemm64.cuh"
+#include "fgb_profile.h"
 
 namespace fgb {
-int kernel_stage_mixed(fgb_model_s *, int, const std::vector<int> &, bool,
-                       bool, double *, double *, double *, cudaStream_t) {
-  set_error("mixed precision stage not built yet");
-  return FGB_ENOTSUP;
+namespace {
+using namespace gemm64;
+
+constexpr int kRowChunkMixed = 32768;
+
+// S^T (M x nd) -> ST (nd x M) scaled by alpha*valid (for B = S^T diag(a) S)
+__global__ void k_scaled_transpose(int M, int nd, const double *__restrict__ S,
+                                   const double *__restrict__ alpha,
+                                   const unsigned char *__restrict__ valid,
+                                   double *__restrict__ ST,
+                                   double *__restrict__ STa) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)M * nd) return;
+  int t = (int)(idx / nd), q = (int)(idx % nd);
+  double v = S[idx];
+  ST[(long long)q * M + t] = v;
+  STa[(long long)q * M + t] = valid[t] ? v * alpha[t] : 0.0;
 }
+
+// B = ST STa^T (nd x nd), written as FP32.
+__global__ void __launch_bounds__(GT)
+k_fold_gemm(int nd, int M, const double *__restrict__ ST,
+            const double *__restrict__ STa, float *__restrict__ B) {
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  double acc[4][4];
+  gemm_mainloop<true>(acc, m0, n0, nd, nd, M, ST, M, nullptr, STa, M);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int m = m0 + ty + 16 * i;
+    if (m >= nd) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int n = n0 + tx + 16 * j;
+      if (n < nd) B[(long long)m * nd + n] = (float)acc[i][j];
+    }
+  }
+}
+
+// beta = S^T (alpha * valid), FP32 output
+__global__ void k_fold_vec(int M, int nd, const double *__restrict__ S,
+                           const double *__restrict__ alpha,
+                           const unsigned char *__restrict__ valid,
+                           float *__restrict__ beta) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nd) return;
+  double acc = 0.0;
+  for (int t = 0; t < M; t++)
+    if (valid[t]) acc += alpha[t] * S[(long long)t * nd + q];
+  beta[q] = (float)acc;
+}
+
+// FP32 normalised descriptor rows of one species chunk (gathered)
+__global__ void k_gather_dhat(int Mr, int nd, const int *__restrict__ perm,
+                              const double *__restrict__ B2,
+                              const double *__restrict__ norms,
+                              float *__restrict__ out) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)Mr * nd) return;
+  int m = (int)(idx / nd), q = (int)(idx % nd);
+  int atom = perm[m];
+  double n = norms[atom];
+  out[idx] = n >= kEmptyThresh ? (float)(B2[(long long)atom * nd + q] / n) : 0.f;
+}
+
+// Y = Dh B (FP32): rows Mr, cols nd, K = nd (B symmetric, row-major)
+__global__ void __launch_bounds__(GT)
+k_mapped_gemm(int Mr, int nd, const float *__restrict__ Dh,
+              const float *__restrict__ B, float *__restrict__ Y) {
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  float acc[4][4];
+  gemm_mainloop_t<float, true>(acc, m0, n0, Mr, nd, nd, Dh, nd, nullptr, B, nd);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int m = m0 + ty + 16 * i;
+    if (m >= Mr) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      int n = n0 + tx + 16 * j;
+      if (n < nd) Y[(long long)m * nd + n] = acc[i][j];
+    }
+  }
+}
+
+// dE/dB2 rows from g = dE/dd^ (power 2: g = 2 sig2 Y; power 1: g = sig2 beta)
+// warp per row: q = d^ . g, dE/dB2 = (g - q d^) / |d|
+__global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
+                              const double *__restrict__ norms,
+                              const float *__restrict__ Dh,
+                              const float *__restrict__ Y,
+                              const float *__restrict__ beta, float scale,
+                              double *__restrict__ gB2) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= Mr) return;
+  const float *d = Dh + (long long)warp * nd;
+  const float *y = Y ? Y + (long long)warp * nd : nullptr;
+  float q = 0.f;
+  for (int k = lane; k < nd; k += 32) q += d[k] * (y ? y[k] : beta[k]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+  int atom = perm[warp];
+  double n = norms[atom];
+  double inv = n >= kEmptyThresh ? 1.0 / n : 0.0;
+  for (int k = lane; k < nd; k += 32) {
+    float g = scale * (y ? y[k] : beta[k]);
+    float v = g - scale * q * d[k];
+    gB2[(long long)atom * nd + k] = (double)v * inv;
+  }
+}
+
+}  // namespace
+
+static int build_fold(fgb_model_s *m, cudaStream_t st) {
+  const B2Params &p = m->b2;
+  const int nd = p.n_d, S = p.n_species;
+  const bool quad = m->power == 2.0;
+  size_t per = quad ? (size_t)nd * nd : (size_t)nd;
+  int rc;
+  if ((rc = m->Bmap.ensure(sizeof(float) * (per * S + 1)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(m->Bmap.p, 0, sizeof(float) * per * S, st));
+  DevBuf ST, STa;
+  for (int s = 0; s < S; s++) {
+    const int Ms = m->h_counts[s], c = m->h_offsets[s];
+    if (Ms == 0) continue;
+    const double *Ss = m->S.as<double>() + (size_t)c * nd;
+    float *Bs = m->Bmap.as<float>() + per * s;
+    if (quad) {
+      if ((rc = ST.ensure(sizeof(double) * (size_t)Ms * nd)) ||
+          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)))
+        return rc;
+      k_scaled_transpose<<<ceil_div((long long)Ms * nd, 256), 256, 0, st>>>(
+          Ms, nd, Ss, m->alpha.as<double>() + c,
+          m->svalid.as<unsigned char>() + c, ST.as<double>(), STa.as<double>());
+      FGB_LAUNCH_CHECK("k_scaled_transpose");
+      dim3 g(ceil_div(nd, BN), ceil_div(nd, BM));
+      k_fold_gemm<<<g, GT, 0, st>>>(nd, Ms, ST.as<double>(), STa.as<double>(),
+                                    Bs);
+      FGB_LAUNCH_CHECK("k_fold_gemm");
+      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa reused next species
+    } else {
+      k_fold_vec<<<ceil_div(nd, 128), 128, 0, st>>>(
+          Ms, nd, Ss, m->alpha.as<double>() + c,
+          m->svalid.as<unsigned char>() + c, Bs);
+      FGB_LAUNCH_CHECK("k_fold_vec");
+    }
+  }
+  FGB_CUDA(cudaStreamSynchronize(st));
+  m->bmap_ready = true;
+  return FGB_OK;
+}
+
+int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
+                       bool want_grad, bool want_var, double *d_e_atom,
+                       double *d_gB2, double *d_var, cudaStream_t st) {
+  const bool foldable = m->power == 2.0 || m->power == 1.0;
+  // Energy (FP64) and variance (FP64); the FP64 adjoint GEMM only when the
+  // power cannot be folded.
+  int rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
+                             d_e_atom, d_gB2, d_var, st);
+  if (rc || !want_grad || !foldable) return rc;
+  if (!m->bmap_ready && (rc = build_fold(m, st))) return rc;
+  const B2Params &p = m->b2;
+  const int nd = p.n_d;
+  const bool quad = m->power == 2.0;
+  const float sig2 = (float)(m->sigma * m->sigma);
+  const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
+  int base = 0;
+  for (int s = 0; s < p.n_species; s++) {
+    const int Ns = counts[s];
+    const int *perm_s = m->ws.perm.as<int>() + base;
+    base += Ns;
+    if (Ns == 0 || m->h_counts[s] == 0) continue;   // gB2 stays zero
+    const float *Bs = m->Bmap.as<float>() + per * s;
+    for (int r0 = 0; r0 < Ns; r0 += kRowChunkMixed) {
+      const int Mr = std::min(kRowChunkMixed, Ns - r0);
+      const int *perm = perm_s + r0;
+      if ((rc = m->ws.b2f.ensure(sizeof(float) * (size_t)Mr * nd)) ||
+          (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
+        return rc;
+      StageTimer _pt(kStMappedGemm, st, quad ? 3 : 2);
+      k_gather_dhat<<<ceil_div((long long)Mr * nd, 256), 256, 0, st>>>(
+          Mr, nd, perm, m->ws.B2.as<double>(), m->ws.norms.as<double>(),
+          m->ws.b2f.as<float>());
+      FGB_LAUNCH_CHECK("k_gather_dhat");
+      if (quad) {
+        dim3 g(ceil_div(nd, BN), ceil_div(Mr, BM));
+        k_mapped_gemm<<<g, GT, 0, st>>>(Mr, nd, m->ws.b2f.as<float>(), Bs,
+                                        m->ws.yf.as<float>());
+        FGB_LAUNCH_CHECK("k_mapped_gemm");
+      }
+      k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.b2f.as<float>(),
+          quad ? m->ws.yf.as<float>() : nullptr, quad ? nullptr : Bs,
+          quad ? 2.f * sig2 : sig2, d_gB2);
+      FGB_LAUNCH_CHECK("k_mapped_grad");
+    }
+  }
+  return FGB_OK;
+}
+
 }  // namespace fgb

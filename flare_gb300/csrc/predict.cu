@@ -419,6 +419,7 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
                         cudaMemcpyHostToDevice));
   }
   m->solved = false;
+  m->bmap_ready = false;
   if (!h_alpha || !h_L_inv) return FGB_OK;
   if ((rc = m->alpha.ensure(sizeof(double) * (M + 1)))) return rc;
   if (M > 0)
@@ -537,7 +538,8 @@ static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       StageTimer _pt(kStB2Adjoint, st);
       if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
                                   m->ws.gB2.as<double>(),
-                                  m->ws.pair_grad.as<double3>(), st)))
+                                  m->ws.pair_grad.as<double3>(), st,
+                                  precision == FGB_PREC_MIXED)))
         return rc;
     }
     {

@@ -137,3 +137,47 @@ def test_species_out_of_range_raises(c1):
     sp[3] = 4
     with pytest.raises(ValueError):
         ggp.predict_batch([fg.Structure(cell, sp, pos, 5.0, [calc])])
+
+
+def test_autograd_energy_gradient_is_minus_forces(c1):
+    import torch
+    import flare_gb300 as fg
+    from flare_gb300.autograd import energy
+    ogp, b2a, ggp, calc = c1
+    items = [syn.fcc_al(seed=1110), syn.fcc_al(seed=1111)]
+    strucs = [fg.Structure(c, s, p, 5.0, [calc]) for c, s, p in items]
+    pos = torch.from_numpy(np.concatenate([p for _, _, p in items])).cuda()
+    pos.requires_grad_(True)
+    e = energy(pos, ggp, strucs)
+    w = torch.tensor([1.0, -2.5], dtype=torch.float64, device="cuda")
+    (g,) = torch.autograd.grad((e * w).sum(), pos)
+    r = ggp.predict_batch(strucs)
+    F = r["forces"]
+    np.testing.assert_allclose(g[:256].cpu().numpy(), -F[:256] * 1.0, atol=1e-12)
+    np.testing.assert_allclose(g[256:].cpu().numpy(), -F[256:] * -2.5, atol=1e-12)
+    np.testing.assert_allclose(e.detach().cpu().numpy(), r["energy"], rtol=0,
+                               atol=0)
+
+
+@pytest.mark.parametrize("power", [2, 1])
+def test_mixed_precision_within_budget(power):
+    """Mixed path against the FP64 path: energy and local variance come from
+    the same FP64 GEMMs (identical); forces from the alpha-folded FP32 GEMM
+    and the FP32 adjoint must stay within MAE <= 1e-4 eV/A, stress within
+    1e-5 eV/A^3."""
+    if power == 2:
+        ogp, b2a = c1_model(n_train=8, n_sparse=120)
+    else:
+        ogp, b2a = small_two_species(seed=12, n_train=3, power=1)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    if power == 2:
+        items = [syn.fcc_al(seed=1120 + k) for k in range(3)]
+    else:
+        items = [random_atoms(seed=120 + k) for k in range(3)]
+    a = gpu_predict(ggp, calc, items, precision="fp64")
+    b = gpu_predict(ggp, calc, items, precision="mixed")
+    np.testing.assert_array_equal(a["energy"], b["energy"])
+    np.testing.assert_array_equal(a["local_var"], b["local_var"])
+    mae = np.abs(a["forces"] - b["forces"]).mean()
+    assert mae <= 1e-4, mae
+    np.testing.assert_allclose(b["stress"], a["stress"], atol=1e-5)
