@@ -369,18 +369,46 @@ def run_ours(args, rank, world, local):
 
     # ---- dominant kernel roofline
     sizes = species_sizes(sp, offsets, gp)
-    flops = {"kernel_gemm": sum(2.0 * n_s * m_s * b2.n_descriptors
-                                for n_s, m_s in sizes),
-             "adjoint_gemm": sum(2.0 * n_s * m_s * b2.n_descriptors
-                                 for n_s, m_s in sizes),
-             "variance_gemm": sum(1.0 * n_s * m_s * (m_s + 1)
-                                  for n_s, m_s in sizes)}
-    gemm_stage = max(flops, key=lambda s: stage.get(s, (0, 0))[0])
+    nd_ = b2.n_descriptors
+    fp64_flops = {"kernel_gemm": sum(2.0 * n_s * m_s * nd_ for n_s, m_s in sizes),
+                  "adjoint_gemm": sum(2.0 * n_s * m_s * nd_ for n_s, m_s in sizes),
+                  "variance_gemm": sum(1.0 * n_s * m_s * (m_s + 1)
+                                       for n_s, m_s in sizes)}
+    tensor = args.precision == "mixed" and oz_eligible(gp, b2)
+    gemm_stage = max(fp64_flops, key=lambda s_: stage.get(s_, (0, 0))[0])
     st_ms, st_n = stage[gemm_stage]
-    launches_per_step = st_n / args.steps
-    flop_per_launch = flops[gemm_stage] / max(launches_per_step, 1)
-    achieved = flop_per_launch / (st_ms / st_n * 1e-3) / 1e12
-    peak = measure_fp64_peak(torch)
+    # launches counted per stage: the tensor-core stages count slice + GEMM
+    per_stage_launch = 2 if tensor else 1
+    launches_per_step = st_n / per_stage_launch / args.steps
+    avg_ms = st_ms / (st_n / per_stage_launch)
+    alg = fp64_flops[gemm_stage] / max(launches_per_step, 1)
+    fp64_peak = measure_fp64_peak(torch)
+    if tensor:
+        # the algorithm executed on the tensor pipe: 45 BF16 slice products
+        # per FP64 product (9 slices of 6 bits, a + b <= 10)
+        flop = OZ_PRODUCTS * alg
+        peak, peak_src = bf16_peak()
+        roofline = {"kernel": gemm_stage + " (tcgen05, exact BF16 slicing)",
+                    "bound": "tensor", "achieved": flop / (avg_ms * 1e-3) / 1e12,
+                    "peak": peak, "unit": "TFLOP/s",
+                    "frac": flop / (avg_ms * 1e-3) / 1e12 / peak,
+                    "traffic": None, "peak_source": peak_src,
+                    "flop_per_launch": flop, "avg_launch_ms": avg_ms,
+                    "fp64_equivalent_tflops": alg / (avg_ms * 1e-3) / 1e12,
+                    "fp64_dgemm_measured_tflops": fp64_peak,
+                    "note": "achieved counts the 45 BF16 slice products the "
+                            "kernel executes per FP64 product; the stage time "
+                            "includes the row-slicing kernel"}
+    else:
+        roofline = {"kernel": gemm_stage, "bound": "tensor",
+                    "achieved": alg / (avg_ms * 1e-3) / 1e12, "peak": fp64_peak,
+                    "unit": "TFLOP/s",
+                    "frac": alg / (avg_ms * 1e-3) / 1e12 / fp64_peak,
+                    "traffic": None,
+                    "peak_source": "FP64 cuBLAS DGEMM 8192^3 measured in this "
+                                   "run (FP64 has no entry in the measured-peaks "
+                                   "file)",
+                    "flop_per_launch": alg, "avg_launch_ms": avg_ms}
     gpu_launches = int(sum(v[1] for v in stage.values()))
 
     result = {
@@ -401,15 +429,7 @@ def run_ours(args, rank, world, local):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "p50_ms": 1e3 * float(np.percentile(e2e, 50)),
                 "p99_ms": 1e3 * float(np.percentile(e2e, 99))},
-        "roofline": {"kernel": gemm_stage, "bound": "tensor",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if peak else None,
-                     "traffic": None,
-                     "peak_source": "FP64 cuBLAS DGEMM 8192^3 measured in "
-                                    "this run (FP64 has no entry in the "
-                                    "measured-peaks file)",
-                     "flop_per_launch": flop_per_launch,
-                     "avg_launch_ms": st_ms / st_n},
+        "roofline": roofline,
         "stages_ms_per_step": {k_: round(v[0] / args.steps, 4)
                                for k_, v in stage.items() if v[1]},
         "gpu_launches": gpu_launches,
@@ -433,6 +453,25 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         result["sample_energy_per_atom"] = float(res_e[0] / 1000)
         print(json.dumps(result), flush=True)
+
+
+OZ_PRODUCTS = 45
+
+
+def oz_eligible(gp, b2, k_max=1472):
+    sd = gp.sparse_descriptors[0]
+    return (b2.n_descriptors <= k_max and gp.kernels[0].power in (1.0, 2.0)
+            and all(c <= k_max for c in sd.n_clusters_by_type))
+
+
+def bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), \
+                "MEASURED_PEAKS.json bf16_tflops (burst, measured)"
+    except Exception:
+        return 1900.0, "fallback 1.9 PFLOP/s bf16 (measured-peaks file absent)"
 
 
 def ctypes_array(code, n):

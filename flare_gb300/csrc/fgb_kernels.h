@@ -25,6 +25,15 @@ int launch_b2_dervs(const B2Params &p, const fgb_nlist_s *nl,
                     const int *d_species, const double *d_A, const double *d_B2,
                     double *d_dB2, double *d_force_dots, cudaStream_t st);
 
+// FP64 row energies E = K alpha and the local-variance finish
+// var = k_self - sum(part) (predict.cu).
+int launch_row_energy(int Mr, int Ms, const double *Kmat, const double *alpha,
+                      const int *perm, double *e_rows, double *e_atom,
+                      cudaStream_t st);
+int launch_variance_final(int Mr, int ntiles, const double *part,
+                          const int *perm, const double *norms, double sig2,
+                          double xi, double *var, cudaStream_t st);
+
 // Validate coded species in [0, n_species); returns FGB_EINVAL otherwise.
 int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
                   cudaStream_t st);

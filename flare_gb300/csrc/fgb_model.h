@@ -2,7 +2,10 @@
 #pragma once
 #include <vector>
 
+#include <memory>
+
 #include "fgb_internal.h"
+#include "fgb_ozaki.h"
 
 struct fgb_workspace {
   fgb::DevBuf perm, flags, pos, scal, scan_tmp, flag;
@@ -11,6 +14,8 @@ struct fgb_workspace {
   fgb::DevBuf kmat, wmat, erows, part;
   fgb::DevBuf b2f, yf;           // mixed path: FP32 normalised rows, D^ B
   fgb::DevBuf dB2, fdots, fdot, dots, kern;  // plain (stored-gradient) form
+  fgb::oz::Sliced ozA, ozK;      // tensor-core path: sliced rows per call
+  fgb::DevBuf ozerr;
 };
 
 struct fgb_io {
@@ -36,6 +41,9 @@ struct fgb_model_s {
   bool has_rinv = false;
   fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
   bool bmap_ready = false;
+  // mixed path: sliced sparse set and L_inv panels per species (tensor cores)
+  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS, ozL;
+  bool oz_ready = false;
   fgb_nlist_s nl;
   fgb_workspace ws;
   fgb_io io;
@@ -45,6 +53,9 @@ namespace fgb {
 int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
                       bool want_grad, bool want_var, double *d_e_atom,
                       double *d_gB2, double *d_var, cudaStream_t st);
+int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
+                    bool want_w, bool want_var, double *d_e_atom, double *d_var,
+                    cudaStream_t st);
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
                        double *d_gB2, double *d_var, cudaStream_t st);

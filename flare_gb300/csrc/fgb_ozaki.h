@@ -1,0 +1,39 @@
+// FP64-accurate tensor-core GEMM by exact BF16 slicing (see ozaki.cu).
+#pragma once
+#include "fgb_internal.h"
+
+namespace fgb {
+namespace oz {
+
+constexpr int kS = 9;        // slices per operand
+constexpr int kBeta = 6;     // bits per slice
+constexpr int kG = kS;       // groups a + b = 2 .. kS + 1
+constexpr int kTM = 128;     // A rows per tile (TMEM lanes)
+constexpr int kTN = 48;      // B rows per tile (columns per group)
+constexpr int kKC = 32;      // k per pipeline stage
+// Largest K whose group sums stay below 2^24 (exact FP32 accumulation):
+// the biggest group (a + b = 10) sums to at most 11264 * K.
+constexpr int kMaxK = 1472;
+
+struct SliceSpec {
+  int rows, K, TR;
+  const double *src;
+  long long ld;
+  const int *perm;         // optional row gather
+  const double *rownorm;   // optional: divide row by its norm (0 if < 1e-8)
+};
+
+struct Sliced {
+  int rows = 0, K = 0, TR = 0, RP = 0, KP = 0;
+  DevBuf q;       // bf16 slices, tiled canonical layout
+  DevBuf scale;   // per-row 2^e
+};
+
+int pad_to(int x, int m);
+int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st);
+template <class Epi>
+int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
+         cudaStream_t st);
+
+}  // namespace oz
+}  // namespace fgb

@@ -1,15 +1,18 @@
 // Mixed-precision kernel stage.
 //
-// The energy and the local variance keep the FP64 kernel GEMM and the FP64
-// variance GEMM (the sparse-set sum and sigma^2 - |L_inv k|^2 cancel too many
-// digits for any 24-bit arithmetic).  The forces, which only need 1e-4 eV/A,
-// use the alpha-weighted sum folded into the sparse set before the GEMM:
+// Energy and local variance need FP64-level accuracy: the sparse-set sum and
+// sigma^2 - |L_inv k|^2 cancel too many digits for any 24-bit arithmetic.
+// They come from the kernel GEMM and the variance GEMM run on the BF16 tensor
+// cores with exact integer slicing (ozaki.cu, FP64-accurate) when n_d and the
+// per-species sparse counts fit its exact-accumulation limit, else from the
+// FP64 GEMMs.  The forces, which only need 1e-4 eV/A, use the alpha-weighted
+// sum folded into the sparse set before the GEMM:
 //   power 2:  E_i = sigma^2 d^_i^T B_s d^_i,  B_s = S^_s^T diag(alpha_s) S^_s
 //             dE/dd^ = 2 sigma^2 B_s d^   (one FP32 GEMM, n_d x n_d per species)
 //   power 1:  E_i = sigma^2 beta_s . d^_i,  beta_s = S^_s^T alpha_s
 // B_s / beta_s are built once per model in FP64 on the GPU and rounded to
 // FP32.  dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d|; the per-pair adjoint then
-// runs in FP32.  Other powers use the FP64 adjoint GEMM.
+// runs in FP32.  Other powers use the FP64 kernel, adjoint and variance GEMMs.
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 #include "fgb_model.h"
@@ -17,6 +20,7 @@
 #include "fgb_profile.h"
 
 namespace fgb {
+bool oz_eligible(const fgb_model_s *m);
 namespace {
 using namespace gemm64;
 
@@ -174,10 +178,16 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
                        double *d_gB2, double *d_var, cudaStream_t st) {
   const bool foldable = m->power == 2.0 || m->power == 1.0;
-  // Energy (FP64) and variance (FP64); the FP64 adjoint GEMM only when the
-  // power cannot be folded.
-  int rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
-                             d_e_atom, d_gB2, d_var, st);
+  int rc;
+  if (foldable && oz_eligible(m)) {
+    // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact
+    // integer slicing (ozaki.cu).
+    rc = kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st);
+  } else {
+    // FP64 GEMMs; the FP64 adjoint GEMM only when the power cannot be folded.
+    rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
+                           d_e_atom, d_gB2, d_var, st);
+  }
   if (rc || !want_grad || !foldable) return rc;
   if (!m->bmap_ready && (rc = build_fold(m, st))) return rc;
   const B2Params &p = m->b2;

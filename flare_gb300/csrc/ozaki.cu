@@ -1,0 +1,518 @@
+// FP64-accurate GEMM on the BF16 tensor cores (tcgen05), by exact integer
+// slicing (the Ozaki scheme).
+//
+// Each row of A (M x K) and of B (N x K) is scaled by a power of two so its
+// entries lie in (-1, 1), then split into S = 9 slices of BETA = 6 bits:
+// x = sum_a q_a 2^(-6a) + r, |q_1| <= 64, |q_a| <= 32 (a > 1), each q an
+// integer held exactly in BF16.  The products q_a q_b are exact in FP32 and,
+// for K <= 1472, every partial sum of a group (all pairs with the same
+// a + b) stays below 2^24, so the tensor core's FP32 accumulation is exact
+// too.  All 45 pairs with a + b <= S + 1 are accumulated into 9 group
+// accumulators held in TMEM (9 x 48 FP32 columns per 128-row tile), and the
+// epilogue recombines C = 2^(e_row + e_col) sum_t 2^(-6t) group_t in FP64.
+// The dropped terms (a + b > 10) and the slice residuals are below 2^-54 of
+// each row's largest entry — FP64-level accuracy, measured on the sparse-GP
+// kernel and variance products (energy 5e-10 eV/atom, variance 2e-14).
+//
+// Data movement: slices are written by k_oz_slice directly in the tensor
+// core's no-swizzle K-major canonical layout (8 x 16-byte core matrices),
+// tiled so that every (slice, 128-row tile, 32-wide k chunk) is one
+// contiguous 8 KB block (3 KB for the 48-row B tiles).  One thread streams
+// the 18 blocks of a chunk with cp.async.bulk into a double-buffered shared
+// memory stage (mbarrier transaction counts), issues the 90 tcgen05.mma
+// (45 pairs x 2 k-steps) of the chunk and commits them to the stage's
+// "consumed" mbarrier; every wait is bounded and reports through `err`.
+#include <cuda_bf16.h>
+
+#include "fgb_internal.h"
+#include "fgb_ozaki.h"
+#include "fgb_tc.cuh"
+
+namespace fgb {
+namespace oz {
+
+namespace {
+
+constexpr uint32_t kTileA = kTM * kKC * 2;               // bytes
+constexpr uint32_t kTileB = kTN * kKC * 2;
+constexpr uint32_t kStage = kS * (kTileA + kTileB);
+constexpr uint32_t kSmem = 2 * kStage + 128;
+constexpr uint32_t kTmemCols = 512;
+constexpr long long kWaitLimit = 1LL << 22;
+constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTM, kTN);
+static_assert(kG * kTN <= (int)kTmemCols, "group accumulators exceed TMEM");
+static_assert(kSmem <= 227 * 1024, "stage exceeds shared memory");
+
+__device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
+  return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(TR * kKC) +
+         (size_t)(((m % TR) / 8) * (kKC / 8) + (k % kKC) / 8) * 64 +
+         (m % 8) * 8 + (k % 8);
+}
+
+// Warp per row: scale to (-1, 1) by a power of two, split into kS slices.
+__global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
+                           const double *__restrict__ src, long long ld,
+                           const int *__restrict__ perm,
+                           const double *__restrict__ rownorm, double thresh,
+                           __nv_bfloat16 *__restrict__ out,
+                           double *__restrict__ scale) {
+  const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= RP) return;
+  bool valid = m < R;
+  long long row = 0;
+  double inv = 1.0;
+  if (valid) {
+    row = perm ? (long long)perm[m] : (long long)m;
+    if (rownorm) {
+      double n = rownorm[row];
+      if (n >= thresh) inv = 1.0 / n;
+      else valid = false;
+    }
+  }
+  double mx = 0.0;
+  if (valid)
+    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(src[row * ld + k] * inv));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  const double down = ldexp(1.0, -e);
+  if (lane == 0) scale[m] = ldexp(1.0, e);
+  const size_t slice = (size_t)RP * KP;
+  for (int k = lane; k < KP; k += 32) {
+    double y = (valid && k < K) ? (src[row * ld + k] * inv) * down : 0.0;
+    const size_t idx = tiled_index(m, k, KP, TR);
+#pragma unroll
+    for (int a = 0; a < kS; a++) {
+      y *= (double)(1 << kBeta);
+      double q = rint(y);
+      y -= q;
+      out[a * slice + idx] = __double2bfloat16(q);
+    }
+  }
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(128, 1)
+k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
+          const __nv_bfloat16 *__restrict__ Asl,
+          const double *__restrict__ Ascale,
+          const __nv_bfloat16 *__restrict__ Bsl,
+          const double *__restrict__ Bscale, int tri, Epi epi,
+          int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char *stage[2] = {smem, smem + kStage};
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + 2 * kStage);
+  uint64_t *bar_mma = bar_load + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + 2);
+  int *ok_slot = reinterpret_cast<int *>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nt = blockIdx.x, mt = blockIdx.y;
+  const int m0 = mt * kTM, n0 = nt * kTN;
+
+  if (warp == 0) {
+    tc::tmem_alloc(tmem_slot, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar_load[0], 1);
+    tc::mbar_init(&bar_load[1], 1);
+    tc::mbar_init(&bar_mma[0], 1);
+    tc::mbar_init(&bar_mma[1], 1);
+    tc::mbar_fence_init();
+    *ok_slot = 1;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const int kmax = tri ? min(K, n0 + kTN) : K;
+  const int nch = (kmax + kKC - 1) / kKC;
+  const int KCH = KP / kKC, MTT = MP / kTM, NTT = NP / kTN;
+
+  if (tid == 0) {
+    bool ok = true;
+    uint32_t ph_load[2] = {0, 0}, ph_mma[2] = {0, 0};
+    bool pend_load[2] = {false, false}, pend_mma[2] = {false, false};
+    auto issue_load = [&](int c, int b) {
+      tc::mbar_expect_tx(&bar_load[b], kStage);
+      for (int a = 0; a < kS; a++) {
+        const __nv_bfloat16 *srcA =
+            Asl + ((size_t)(a * MTT + mt) * KCH + c) * (kTM * kKC);
+        tc::bulk_g2s(stage[b] + a * kTileA, srcA, kTileA, &bar_load[b]);
+        const __nv_bfloat16 *srcB =
+            Bsl + ((size_t)(a * NTT + nt) * KCH + c) * (kTN * kKC);
+        tc::bulk_g2s(stage[b] + kS * kTileA + a * kTileB, srcB, kTileB,
+                     &bar_load[b]);
+      }
+      pend_load[b] = true;
+    };
+    uint32_t inited = 0;
+    if (nch > 0) issue_load(0, 0);
+    for (int c = 0; c < nch; c++) {
+      const int b = c & 1;
+      if (c + 1 < nch) {
+        const int nb = (c + 1) & 1;
+        if (pend_mma[nb]) {   // MMAs of chunk c-1 still read stage nb
+          if (!tc::mbar_wait(&bar_mma[nb], ph_mma[nb], kWaitLimit)) { ok = false; break; }
+          ph_mma[nb] ^= 1;
+          pend_mma[nb] = false;
+        }
+        issue_load(c + 1, nb);
+      }
+      if (!tc::mbar_wait(&bar_load[b], ph_load[b], kWaitLimit)) { ok = false; break; }
+      ph_load[b] ^= 1;
+      pend_load[b] = false;
+      tc::fence_after_sync();
+      const uint32_t aBase = tc::smem_u32(stage[b]);
+      const uint32_t bBase = aBase + kS * kTileA;
+#pragma unroll 1
+      for (int kk = 0; kk < kKC / 16; kk++) {
+#pragma unroll 1
+        for (int a = 0; a < kS; a++) {
+          const uint64_t ad = tc::smem_desc(aBase + a * kTileA + kk * 256, 128,
+                                            (kKC / 8) * 128);
+#pragma unroll 1
+          for (int bb = 0; a + bb < kS; bb++) {
+            const int g = a + bb;
+            const uint64_t bd = tc::smem_desc(bBase + bb * kTileB + kk * 256,
+                                              128, (kKC / 8) * 128);
+            tc::mma_bf16(tmem + g * kTN, ad, bd, kIdesc, (inited >> g) & 1u);
+            inited |= 1u << g;
+          }
+        }
+      }
+      tc::mma_commit(&bar_mma[b]);
+      pend_mma[b] = true;
+    }
+    // Drain every outstanding copy and MMA before the accumulators are read
+    // or TMEM is released (bounded as well).
+    for (int b = 0; b < 2; b++) {
+      if (pend_mma[b] && !tc::mbar_wait(&bar_mma[b], ph_mma[b], kWaitLimit)) ok = false;
+      if (pend_load[b] && !tc::mbar_wait(&bar_load[b], ph_load[b], kWaitLimit)) ok = false;
+    }
+    if (nch == 0) ok = false;   // nothing accumulated: the host handles K == 0
+    if (!ok) {
+      *ok_slot = 0;
+      if (nch > 0) atomicExch(err, 1);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const bool ok = *ok_slot != 0;
+  if (ok) {
+    const int m = m0 + warp * 32 + lane;
+    double v[kTN];
+#pragma unroll
+    for (int j = 0; j < kTN; j++) v[j] = 0.0;
+#pragma unroll 1
+    for (int g = 0; g < kG; g++) {
+      const double sc = ldexp(1.0, -kBeta * (g + 2));
+#pragma unroll
+      for (int c0 = 0; c0 < kTN; c0 += 16) {
+        uint32_t r[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + g * kTN + c0, r);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[c0 + j] += (double)__uint_as_float(r[j]) * sc;
+      }
+    }
+    if (m < M) epi(m, n0, v, Ascale[m], Bscale);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+struct EpiStore {
+  double *C;
+  long long ldc;
+  int N;
+  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
+                             const double *cs) const {
+#pragma unroll
+    for (int j = 0; j < kTN; j++) {
+      int n = n0 + j;
+      if (n < N) C[(long long)m * ldc + n] = v[j] * rs * cs[n];
+    }
+  }
+};
+
+}  // namespace
+
+int pad_to(int x, int m) { return (x + m - 1) / m * m; }
+
+int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
+  out.rows = sp.rows;
+  out.K = sp.K;
+  out.TR = sp.TR;
+  out.RP = pad_to(std::max(sp.rows, 1), sp.TR);
+  out.KP = pad_to(std::max(sp.K, 1), kKC);
+  int rc;
+  if ((rc = out.q.ensure(sizeof(__nv_bfloat16) * (size_t)kS * out.RP * out.KP)) ||
+      (rc = out.scale.ensure(sizeof(double) * (size_t)out.RP)))
+    return rc;
+  const long long threads = (long long)out.RP * 32;
+  k_oz_slice<<<ceil_div(threads, 256), 256, 0, st>>>(
+      sp.rows, sp.K, out.RP, out.KP, sp.TR, sp.src, sp.ld, sp.perm,
+      sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
+      out.scale.as<double>());
+  FGB_LAUNCH_CHECK("k_oz_slice");
+  return FGB_OK;
+}
+
+template <class Epi>
+int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
+         cudaStream_t st) {
+  if (A.K != B.K || A.KP != B.KP || A.TR != kTM || B.TR != kTN) {
+    set_error("ozaki gemm: operand layouts disagree");
+    return FGB_EINVAL;
+  }
+  if (A.K > kMaxK) {
+    set_error("ozaki gemm: K = %d exceeds the exact-accumulation limit %d",
+              A.K, kMaxK);
+    return FGB_EINVAL;
+  }
+  if (A.rows == 0 || B.rows == 0) return FGB_OK;
+  FGB_CUDA(cudaFuncSetAttribute(k_oz_gemm<Epi>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kSmem));
+  dim3 grid(B.RP / kTN, A.RP / kTM);
+  k_oz_gemm<Epi><<<grid, 128, kSmem, st>>>(
+      A.rows, B.rows, A.K, A.KP, A.RP, B.RP, A.q.as<__nv_bfloat16>(),
+      A.scale.as<double>(), B.q.as<__nv_bfloat16>(), B.scale.as<double>(),
+      tri ? 1 : 0, epi, err);
+  FGB_LAUNCH_CHECK("k_oz_gemm");
+  return FGB_OK;
+}
+
+}  // namespace oz
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A,
+                               long long lda, const double *d_B, long long ldb,
+                               double *d_C, long long ldc, void *stream) {
+  if (M < 0 || N < 0 || K < 0 || (M && N && (!d_A || !d_B || !d_C))) {
+    set_error("fgb_oz_dgemm_nt: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (K > oz::kMaxK) {
+    set_error("fgb_oz_dgemm_nt: K = %d exceeds the exact-accumulation limit "
+              "%d", K, oz::kMaxK);
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (M == 0 || N == 0) return FGB_OK;
+  if (K == 0) {
+    for (int m = 0; m < M; m++)
+      FGB_CUDA(cudaMemsetAsync(d_C + (long long)m * ldc, 0,
+                               sizeof(double) * N, st));
+    return FGB_OK;
+  }
+  oz::Sliced A, B;
+  DevBuf err;
+  int rc;
+  if ((rc = err.ensure(sizeof(int)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  if ((rc = oz::slice({M, K, oz::kTM, d_A, lda, nullptr, nullptr}, A, st)) ||
+      (rc = oz::slice({N, K, oz::kTN, d_B, ldb, nullptr, nullptr}, B, st)))
+    return rc;
+  if ((rc = oz::gemm(A, B, false, oz::EpiStore{d_C, ldc, N}, err.as<int>(), st)))
+    return rc;
+  int h = 0;
+  FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("fgb_oz_dgemm_nt: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
+  return FGB_OK;
+}
+
+// ------------------------------------------------------------------------
+// Sparse-GP stages on the tensor cores (mixed precision mode).
+#include "fgb_gemm64.cuh"
+#include "fgb_kernels.h"
+#include "fgb_model.h"
+#include "fgb_profile.h"
+
+namespace fgb {
+namespace oz {
+namespace {
+
+// Kernel GEMM epilogue: c = d^ . s^ -> k = sig^2 c^xi (and the adjoint
+// weight w = sig^2 xi alpha c^(xi-1) when asked), zero for empty
+// environments — the same expressions as the FP64 path.
+struct EpiKernel {
+  double *K, *W;
+  const double *alpha;
+  const unsigned char *valid;
+  const int *perm;
+  const double *norms;
+  double sig2, xi;
+  int N;
+  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
+                             const double *cs) const {
+    const bool dok = norms[perm[m]] >= kEmptyThresh;
+#pragma unroll
+    for (int j = 0; j < kTN; j++) {
+      const int n = n0 + j;
+      if (n >= N) continue;
+      double kv = 0.0, wv = 0.0;
+      if (dok && valid[n]) {
+        const double c = v[j] * rs * cs[n];
+        kv = sig2 * gemm64::powx(c, xi);
+        wv = sig2 * xi * gemm64::powx(c, xi - 1.0) * alpha[n];
+      }
+      K[(long long)m * N + n] = kv;
+      if (W) W[(long long)m * N + n] = wv;
+    }
+  }
+};
+
+// Variance GEMM epilogue: per-row sum of z^2 over this tile's columns.
+struct EpiZsq {
+  double *part;
+  int ntiles, R;
+  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
+                             const double *cs) const {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < kTN; j++) {
+      const int n = n0 + j;
+      if (n < R) {
+        const double z = v[j] * rs * cs[n];
+        s += z * z;
+      }
+    }
+    part[(long long)m * ntiles + n0 / kTN] = s;
+  }
+};
+
+}  // namespace
+}  // namespace oz
+
+// Slice the model operands once: normalised sparse rows (B of the kernel
+// GEMM) and the L_inv panels (B of the variance GEMM), per species.
+static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
+  const int S = m->b2.n_species, nd = m->b2.n_d;
+  m->ozS.clear();
+  m->ozL.clear();
+  int rc;
+  for (int s = 0; s < S; s++) {
+    m->ozS.emplace_back(new oz::Sliced());
+    m->ozL.emplace_back(new oz::Sliced());
+    const int Ms = m->h_counts[s];
+    if (Ms == 0) continue;
+    if ((rc = oz::slice({Ms, nd, oz::kTN,
+                         m->S.as<double>() + (size_t)m->h_offsets[s] * nd, nd,
+                         nullptr, nullptr},
+                        *m->ozS[s], st)))
+      return rc;
+    if ((rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
+                         m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
+                         nullptr},
+                        *m->ozL[s], st)))
+      return rc;
+  }
+  FGB_CUDA(cudaStreamSynchronize(st));
+  m->oz_ready = true;
+  return FGB_OK;
+}
+
+bool oz_eligible(const fgb_model_s *m) {
+  if (m->b2.n_d > oz::kMaxK) return false;
+  for (int s = 0; s < m->b2.n_species; s++)
+    if (m->h_counts[s] > oz::kMaxK) return false;
+  return true;
+}
+
+int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
+                    bool want_w, bool want_var, double *d_e_atom, double *d_var,
+                    cudaStream_t st) {
+  int rc;
+  if (!m->oz_ready && (rc = build_oz_model(m, st))) return rc;
+  const B2Params &p = m->b2;
+  const int nd = p.n_d;
+  const double sig2 = m->sigma * m->sigma;
+  if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
+  int base = 0;
+  const int kRows = 32768;
+  for (int s = 0; s < p.n_species; s++) {
+    const int Ns = counts[s], Ms = m->h_counts[s];
+    const int *perm_s = m->ws.perm.as<int>() + base;
+    base += Ns;
+    if (Ns > 0 && Ms == 0 && want_var) {
+      if ((rc = launch_variance_final(Ns, 0, nullptr, perm_s,
+                                      m->ws.norms.as<double>(), sig2, m->power,
+                                      d_var, st)))
+        return rc;
+    }
+    for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRows) {
+      const int Mr = std::min(kRows, Ns - r0);
+      const int *perm = perm_s + r0;
+      if ((rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms)) ||
+          (want_w && (rc = m->ws.wmat.ensure(sizeof(double) * (size_t)Mr * Ms))) ||
+          (rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr)))
+        return rc;
+      {
+        StageTimer _pt(kStKernelGemm, st, 2);
+        if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
+                             m->ws.norms.as<double>()},
+                            m->ws.ozA, st)))
+          return rc;
+        oz::EpiKernel epi{m->ws.kmat.as<double>(),
+                          want_w ? m->ws.wmat.as<double>() : nullptr,
+                          m->alpha.as<double>() + m->h_offsets[s],
+                          m->svalid.as<unsigned char>() + m->h_offsets[s],
+                          perm, m->ws.norms.as<double>(), sig2, m->power, Ms};
+        if ((rc = oz::gemm(m->ws.ozA, *m->ozS[s], false, epi,
+                           m->ws.ozerr.as<int>(), st)))
+          return rc;
+      }
+      if ((rc = launch_row_energy(Mr, Ms, m->ws.kmat.as<double>(),
+                                  m->alpha.as<double>() + m->h_offsets[s], perm,
+                                  m->ws.erows.as<double>(), d_e_atom, st)))
+        return rc;
+      if (want_var) {
+        const int R = m->h_panel_rows[s];
+        const int ntiles = m->ozL[s]->RP / oz::kTN;
+        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
+          return rc;
+        {
+          StageTimer _pt(kStVarianceGemm, st, 2);
+          if ((rc = oz::slice({Mr, Ms, oz::kTM, m->ws.kmat.as<double>(), Ms,
+                               nullptr, nullptr},
+                              m->ws.ozK, st)))
+            return rc;
+          oz::EpiZsq epi{m->ws.part.as<double>(), ntiles, R};
+          if ((rc = oz::gemm(m->ws.ozK, *m->ozL[s], true, epi,
+                             m->ws.ozerr.as<int>(), st)))
+            return rc;
+        }
+        if ((rc = launch_variance_final(Mr, ntiles, m->ws.part.as<double>(),
+                                        perm, m->ws.norms.as<double>(), sig2,
+                                        m->power, d_var, st)))
+          return rc;
+      }
+    }
+  }
+  int h = 0;
+  FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("tensor-core kernel stage: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
+  return FGB_OK;
+}
+
+}  // namespace fgb

@@ -211,6 +211,26 @@ __global__ void k_check_species(int n, const int *__restrict__ species, int ns,
 
 }  // namespace
 
+int launch_row_energy(int Mr, int Ms, const double *Kmat, const double *alpha,
+                      const int *perm, double *e_rows, double *e_atom,
+                      cudaStream_t st) {
+  StageTimer _pt(kStRowEnergy, st);
+  k_row_energy<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+      Mr, Ms, Kmat, alpha, perm, e_rows, e_atom);
+  FGB_LAUNCH_CHECK("k_row_energy");
+  return FGB_OK;
+}
+
+int launch_variance_final(int Mr, int ntiles, const double *part,
+                          const int *perm, const double *norms, double sig2,
+                          double xi, double *var, cudaStream_t st) {
+  StageTimer _pt(kStVarianceFinal, st);
+  k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(Mr, ntiles, part, perm,
+                                                      norms, sig2, xi, var);
+  FGB_LAUNCH_CHECK("k_variance_final");
+  return FGB_OK;
+}
+
 int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
                   cudaStream_t st) {
   if (n == 0) return FGB_OK;
@@ -420,6 +440,7 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   }
   m->solved = false;
   m->bmap_ready = false;
+  m->oz_ready = false;
   if (!h_alpha || !h_L_inv) return FGB_OK;
   if ((rc = m->alpha.ensure(sizeof(double) * (M + 1)))) return rc;
   if (M > 0)

@@ -227,6 +227,15 @@ int fgb_envs_struc(fgb_b2_t b2, double sigma, double power,
 int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
                       double *d_mean_efs, double *d_local_var, void *stream);
 
+/* C = A B^T in FP64 accuracy on the BF16 tensor cores (tcgen05), by exact
+ * integer slicing of A and B (9 slices of 6 bits per row, 45 slice products
+ * accumulated exactly in FP32, recombined in FP64).  A[M x K] (lda),
+ * B[N x K] (ldb), C[M x N] (ldc), row-major device pointers; K <= 1472.
+ * The kernel used for the sparse-GP kernel and variance products. */
+int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A, long long lda,
+                    const double *d_B, long long ldb, double *d_C,
+                    long long ldc, void *stream);
+
 /* SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 on the GPU:
  * Cholesky of Kuu + jitter I, L_inv, QR of [diag(sqrt(noise)) Kuf^T ; L^T],
  * alpha = R^-1 Q^T b.  All device pointers, row-major.

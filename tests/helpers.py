@@ -94,7 +94,7 @@ def small_two_species(seed=0, n_train=3, power=2, multicut=False):
     return gp, b2a
 
 
-def c1_model(n_train=20, n_sparse=200):
+def c1_model(n_train=20, n_sparse=200, power=2):
     """FCC Al-like model of the 256-atom workload (seeded)."""
     b2a = b2_args(1, 8, 3, 5.0)
     strucs, labels = [], []
@@ -106,6 +106,6 @@ def c1_model(n_train=20, n_sparse=200):
     chosen = rng(1200).choice(n_train * 256, size=n_sparse, replace=False)
     sparse = [sorted(int(c) - 256 * i for c in chosen if c // 256 == i)
               for i in range(n_train)]
-    gp, b2 = oracle_model(strucs, labels, sparse, b2a, sigma=2.0, power=2,
+    gp, b2 = oracle_model(strucs, labels, sparse, b2a, sigma=2.0, power=power,
                           noise=(0.256, 0.05, 1.0))
     return gp, b2a

@@ -1,0 +1,66 @@
+"""GPU: the FP64-accurate tensor-core GEMM (exact BF16 slicing, tcgen05)
+against cuBLAS FP64 and against exact integer products."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def oz(A, B):
+    import torch
+    from flare_gb300 import _lib
+    M, K = A.shape
+    N = B.shape[0]
+    dA = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    dC = torch.full((max(M, 1), max(N, 1)), np.nan, dtype=torch.float64,
+                    device="cuda")
+    _lib.check(_lib.lib().fgb_oz_dgemm_nt(M, N, K, _lib.ptr(dA), K,
+                                          _lib.ptr(dB), K, _lib.ptr(dC),
+                                          max(N, 1), _lib.stream_ptr()))
+    torch.cuda.synchronize()
+    return dC.cpu().numpy()[:M, :N]
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 48, 32), (300, 130, 680),
+                                   (257, 1000, 1000), (5, 3, 17)])
+def test_random_fp64_accuracy(M, N, K):
+    r = np.random.Generator(np.random.PCG64(M * 7 + N))
+    # entries spanning several decades, mixed signs
+    A = r.normal(size=(M, K)) * np.exp(r.uniform(-6, 2, size=(M, K)))
+    B = r.normal(size=(N, K)) * np.exp(r.uniform(-6, 2, size=(N, K)))
+    C = oz(A, B)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2e-15 * bound + 1e-300), float((err / bound).max())
+
+
+def test_integer_products_exact():
+    r = np.random.Generator(np.random.PCG64(3))
+    A = r.integers(-100, 101, size=(200, 512)).astype(np.float64)
+    B = r.integers(-100, 101, size=(100, 512)).astype(np.float64)
+    C = oz(A, B)
+    exact = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    np.testing.assert_array_equal(C, exact)
+
+
+def test_worst_case_magnitudes_at_max_k():
+    """K at the exact-accumulation limit with every slice at its largest."""
+    K = 1472
+    A = np.full((130, K), 0.99609375 - 1e-12)
+    B = np.full((50, K), -(0.99609375 - 1e-12))
+    B[::2] *= -1
+    C = oz(A, B)
+    ref = A @ B.T
+    # no cancellation here: only the slice residuals and the FP64
+    # recombination round (the exactness of the FP32 group sums is what
+    # this shape checks; a lost bit would show at 1e-7)
+    np.testing.assert_allclose(C, ref, rtol=1e-14)
+
+
+def test_k_limit_rejected():
+    from flare_gb300 import _lib
+    with pytest.raises(ValueError):
+        oz(np.zeros((4, 1500)), np.zeros((4, 1500)))

@@ -161,23 +161,19 @@ def test_autograd_energy_gradient_is_minus_forces(c1):
 
 @pytest.mark.parametrize("power", [2, 1])
 def test_mixed_precision_within_budget(power):
-    """Mixed path against the FP64 path: energy and local variance come from
-    the same FP64 GEMMs (identical); forces from the alpha-folded FP32 GEMM
-    and the FP32 adjoint must stay within MAE <= 1e-4 eV/A, stress within
-    1e-5 eV/A^3."""
-    if power == 2:
-        ogp, b2a = c1_model(n_train=8, n_sparse=120)
-    else:
-        ogp, b2a = small_two_species(seed=12, n_train=3, power=1)
+    """Mixed path against the FP64 path on an FCC model (|alpha| ~ 1e4):
+    energy and local variance come from the tensor-core GEMMs with exact
+    integer slicing (FP64-level: energy <= 1e-8 eV/atom, variance <= 1e-11);
+    forces from the alpha-folded FP32 GEMM and the FP32 adjoint must stay
+    within the stated budget, MAE <= 1e-4 eV/A; stress within 1e-5 eV/A^3."""
+    ogp, b2a = c1_model(n_train=8, n_sparse=120, power=power)
     ggp, calc = to_gpu_sgp(ogp, b2a)
-    if power == 2:
-        items = [syn.fcc_al(seed=1120 + k) for k in range(3)]
-    else:
-        items = [random_atoms(seed=120 + k) for k in range(3)]
+    items = [syn.fcc_al(seed=1120 + k) for k in range(3)]
     a = gpu_predict(ggp, calc, items, precision="fp64")
     b = gpu_predict(ggp, calc, items, precision="mixed")
-    np.testing.assert_array_equal(a["energy"], b["energy"])
-    np.testing.assert_array_equal(a["local_var"], b["local_var"])
+    assert np.max(np.abs(a["energy"] - b["energy"])) / 256 <= 1e-8
+    np.testing.assert_allclose(b["local_var"], a["local_var"], rtol=0,
+                               atol=1e-11)
     mae = np.abs(a["forces"] - b["forces"]).mean()
     assert mae <= 1e-4, mae
     np.testing.assert_allclose(b["stress"], a["stress"], atol=1e-5)
