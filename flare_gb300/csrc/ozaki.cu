@@ -42,6 +42,8 @@ constexpr long long kWaitLimit = 1LL << 22;
 constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTM, kTN);
 static_assert(kG * kTN <= (int)kTmemCols, "group accumulators exceed TMEM");
 static_assert(kSmem <= 227 * 1024, "stage exceeds shared memory");
+static_assert(kS == 9 && kBeta == 6 && kTN % 16 == 0,
+              "the exact recombination assumes 9 slices of 6 bits");
 
 __device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
   return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(TR * kKC) +
@@ -50,6 +52,10 @@ __device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
 }
 
 // Warp per row: scale to (-1, 1) by a power of two, split into kS slices.
+// The scaled value y is taken as the integer X = rn(y 2^54) (exact for
+// |y| >= 2^-1 of the row's top binade, rounded at 2^-54 below that); the
+// 9 slices are the base-64 digits of X, each rounded to nearest, extracted
+// with 64-bit integer arithmetic: q_a = round(R / 2^(54-6a)), R -= q_a 2^(54-6a).
 __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
                            const double *__restrict__ src, long long ld,
                            const int *__restrict__ perm,
@@ -72,23 +78,24 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
   }
   double mx = 0.0;
   if (valid)
-    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(src[row * ld + k] * inv));
+    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(src[row * ld + k]));
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  mx *= inv;
   const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
-  const double down = ldexp(1.0, -e);
   if (lane == 0) scale[m] = ldexp(1.0, e);
+  const double to_int = inv * ldexp(1.0, 54 - e);
   const size_t slice = (size_t)RP * KP;
   for (int k = lane; k < KP; k += 32) {
-    double y = (valid && k < K) ? (src[row * ld + k] * inv) * down : 0.0;
+    long long X = (valid && k < K) ? __double2ll_rn(src[row * ld + k] * to_int) : 0;
     const size_t idx = tiled_index(m, k, KP, TR);
 #pragma unroll
-    for (int a = 0; a < kS; a++) {
-      y *= (double)(1 << kBeta);
-      double q = rint(y);
-      y -= q;
-      out[a * slice + idx] = __double2bfloat16(q);
+    for (int a = 1; a <= kS; a++) {
+      const int sh = 54 - kBeta * a;
+      long long q = sh > 0 ? (X + (1LL << (sh - 1))) >> sh : X;
+      X -= q << sh;
+      out[(a - 1) * slice + idx] = __float2bfloat16_rn((float)q);
     }
   }
 }
@@ -149,7 +156,6 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
       }
       pend_load[b] = true;
     };
-    uint32_t inited = 0;
     if (nch > 0) issue_load(0, 0);
     for (int c = 0; c < nch; c++) {
       const int b = c & 1;
@@ -167,20 +173,22 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
       pend_load[b] = false;
       tc::fence_after_sync();
       const uint32_t aBase = tc::smem_u32(stage[b]);
-      const uint32_t bBase = aBase + kS * kTileA;
-#pragma unroll 1
+      const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
+      const uint64_t bd0 = tc::smem_desc(aBase + kS * kTileA, 128,
+                                         (kKC / 8) * 128);
+      // descriptor start addresses are in 16-byte units in the low bits
+#pragma unroll
       for (int kk = 0; kk < kKC / 16; kk++) {
-#pragma unroll 1
+#pragma unroll
         for (int a = 0; a < kS; a++) {
-          const uint64_t ad = tc::smem_desc(aBase + a * kTileA + kk * 256, 128,
-                                            (kKC / 8) * 128);
-#pragma unroll 1
+          const uint64_t ad = ad0 + (uint64_t)((a * kTileA + kk * 256) >> 4);
+#pragma unroll
           for (int bb = 0; a + bb < kS; bb++) {
-            const int g = a + bb;
-            const uint64_t bd = tc::smem_desc(bBase + bb * kTileB + kk * 256,
-                                              128, (kKC / 8) * 128);
-            tc::mma_bf16(tmem + g * kTN, ad, bd, kIdesc, (inited >> g) & 1u);
-            inited |= 1u << g;
+            const uint64_t bd = bd0 + (uint64_t)((bb * kTileB + kk * 256) >> 4);
+            // the first product of each group (a == 0) in the first k-step
+            // initialises its accumulator
+            const uint32_t acc = (c != 0 || kk != 0 || a != 0) ? 1u : 0u;
+            tc::mma_bf16(tmem + (a + bb) * kTN, ad, bd, kIdesc, acc);
           }
         }
       }
@@ -204,23 +212,37 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   tc::fence_after_sync();
   const bool ok = *ok_slot != 0;
   if (ok) {
+    // Group sums are exact integers below 2^24; recombine them exactly in
+    // two 64-bit integers, hi = sum_{t=2..6} g_t 2^(6(6-t)) and
+    // lo = sum_{t=7..10} g_t 2^(6(10-t)), then C = hi 2^-36 + lo 2^-60.
     const int m = m0 + warp * 32 + lane;
-    double v[kTN];
-#pragma unroll
-    for (int j = 0; j < kTN; j++) v[j] = 0.0;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    double acc = 0.0;
 #pragma unroll 1
-    for (int g = 0; g < kG; g++) {
-      const double sc = ldexp(1.0, -kBeta * (g + 2));
+    for (int c0 = 0; c0 < kTN; c0 += 16) {
+      long long hi[16], lo[16];
 #pragma unroll
-      for (int c0 = 0; c0 < kTN; c0 += 16) {
+      for (int j = 0; j < 16; j++) { hi[j] = 0; lo[j] = 0; }
+#pragma unroll
+      for (int g = 0; g < kG; g++) {
         uint32_t r[16];
-        tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + g * kTN + c0, r);
+        tc::tmem_ld16(trow + g * kTN + c0, r);
         tc::tmem_ld_wait();
+        const int t = g + 2;
 #pragma unroll
-        for (int j = 0; j < 16; j++) v[c0 + j] += (double)__uint_as_float(r[j]) * sc;
+        for (int j = 0; j < 16; j++) {
+          const long long q = (long long)__float2int_rn(__uint_as_float(r[j]));
+          if (t <= 6) hi[j] += q << (6 * (6 - t));
+          else lo[j] += q << (6 * (10 - t));
+        }
       }
+      double v[16];
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        v[j] = fma((double)hi[j], 0x1p-36, (double)lo[j] * 0x1p-60);
+      if (m < M) acc = epi.chunk(m, n0 + c0, v, Ascale[m], Bscale, acc);
     }
-    if (m < M) epi(m, n0, v, Ascale[m], Bscale);
+    if (m < M) epi.finish(m, n0, acc);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -232,14 +254,16 @@ struct EpiStore {
   double *C;
   long long ldc;
   int N;
-  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
-                             const double *cs) const {
+  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
+                          const double *cs, double acc) const {
 #pragma unroll
-    for (int j = 0; j < kTN; j++) {
+    for (int j = 0; j < 16; j++) {
       int n = n0 + j;
       if (n < N) C[(long long)m * ldc + n] = v[j] * rs * cs[n];
     }
+    return acc;
   }
+  __device__ void finish(int, int, double) const {}
 };
 
 }  // namespace
@@ -357,41 +381,43 @@ struct EpiKernel {
   const double *norms;
   double sig2, xi;
   int N;
-  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
-                             const double *cs) const {
+  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
+                          const double *cs, double acc) const {
     const bool dok = norms[perm[m]] >= kEmptyThresh;
 #pragma unroll
-    for (int j = 0; j < kTN; j++) {
+    for (int j = 0; j < 16; j++) {
       const int n = n0 + j;
       if (n >= N) continue;
-      double kv = 0.0, wv = 0.0;
-      if (dok && valid[n]) {
-        const double c = v[j] * rs * cs[n];
-        kv = sig2 * gemm64::powx(c, xi);
-        wv = sig2 * xi * gemm64::powx(c, xi - 1.0) * alpha[n];
-      }
-      K[(long long)m * N + n] = kv;
-      if (W) W[(long long)m * N + n] = wv;
+      const bool ok = dok && valid[n];
+      const double c = v[j] * rs * cs[n];
+      K[(long long)m * N + n] = ok ? sig2 * gemm64::powx(c, xi) : 0.0;
+      if (W)
+        W[(long long)m * N + n] =
+            ok ? sig2 * xi * gemm64::powx(c, xi - 1.0) * alpha[n] : 0.0;
     }
+    return acc;
   }
+  __device__ void finish(int, int, double) const {}
 };
 
 // Variance GEMM epilogue: per-row sum of z^2 over this tile's columns.
 struct EpiZsq {
   double *part;
   int ntiles, R;
-  __device__ void operator()(int m, int n0, const double (&v)[kTN], double rs,
-                             const double *cs) const {
-    double s = 0.0;
+  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
+                          const double *cs, double acc) const {
 #pragma unroll
-    for (int j = 0; j < kTN; j++) {
+    for (int j = 0; j < 16; j++) {
       const int n = n0 + j;
       if (n < R) {
         const double z = v[j] * rs * cs[n];
-        s += z * z;
+        acc = fma(z, z, acc);
       }
     }
-    part[(long long)m * ntiles + n0 / kTN] = s;
+    return acc;
+  }
+  __device__ void finish(int m, int n0, double acc) const {
+    part[(long long)m * ntiles + n0 / kTN] = acc;
   }
 };
 
