@@ -36,12 +36,13 @@ namespace {
 constexpr uint32_t kTileA = kTM * kKC * 2;               // bytes
 constexpr uint32_t kTileB = kTN * kKC * 2;
 constexpr uint32_t kStage = kS * (kTileA + kTileB);
-constexpr uint32_t kSmem = 2 * kStage + 128;
+constexpr uint32_t kSmem = kStages * kStage + 256;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitLimit = 1LL << 22;
 constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTM, kTN);
 static_assert(kG * kTN <= (int)kTmemCols, "group accumulators exceed TMEM");
-static_assert(kSmem <= 227 * 1024, "stage exceeds shared memory");
+static_assert(kSmem <= 227 * 1024, "stages exceed shared memory");
+static_assert(kKC % 16 == 0, "a chunk is whole MMA k-steps");
 static_assert(kS == 9 && kBeta == 6 && kTN % 16 == 0,
               "the exact recombination assumes 9 slices of 6 bits");
 
@@ -109,10 +110,9 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
           const double *__restrict__ Bscale, int tri, Epi epi,
           int *__restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char *stage[2] = {smem, smem + kStage};
-  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + 2 * kStage);
-  uint64_t *bar_mma = bar_load + 2;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + 2);
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + kStages * kStage);
+  uint64_t *bar_mma = bar_load + kStages;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + kStages);
   int *ok_slot = reinterpret_cast<int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nt = blockIdx.x, mt = blockIdx.y;
@@ -123,10 +123,10 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    tc::mbar_init(&bar_load[0], 1);
-    tc::mbar_init(&bar_load[1], 1);
-    tc::mbar_init(&bar_mma[0], 1);
-    tc::mbar_init(&bar_mma[1], 1);
+    for (int b = 0; b < kStages; b++) {
+      tc::mbar_init(&bar_load[b], 1);
+      tc::mbar_init(&bar_mma[b], 1);
+    }
     tc::mbar_fence_init();
     *ok_slot = 1;
   }
@@ -140,39 +140,35 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   const int KCH = KP / kKC, MTT = MP / kTM, NTT = NP / kTN;
 
   if (tid == 0) {
+    // Ring of kStages stages.  Chunk c lives in stage c % kStages; its
+    // barriers complete once per use, so the parity for chunk c is
+    // (c / kStages) & 1.  MMAs of chunk c are issued as soon as its data has
+    // landed; only then does the thread wait for chunk c-1's MMAs, which
+    // frees that stage for chunk c + kStages - 1.  The tensor pipe always
+    // has the next chunk queued and kStages - 1 loads stay in flight.
     bool ok = true;
-    uint32_t ph_load[2] = {0, 0}, ph_mma[2] = {0, 0};
-    bool pend_load[2] = {false, false}, pend_mma[2] = {false, false};
-    auto issue_load = [&](int c, int b) {
+    int issued = 0;   // loads issued so far (chunks 0 .. issued-1)
+    auto issue_load = [&](int c) {
+      const int b = c % kStages;
+      unsigned char *st = smem + b * kStage;
       tc::mbar_expect_tx(&bar_load[b], kStage);
       for (int a = 0; a < kS; a++) {
         const __nv_bfloat16 *srcA =
             Asl + ((size_t)(a * MTT + mt) * KCH + c) * (kTM * kKC);
-        tc::bulk_g2s(stage[b] + a * kTileA, srcA, kTileA, &bar_load[b]);
+        tc::bulk_g2s(st + a * kTileA, srcA, kTileA, &bar_load[b]);
         const __nv_bfloat16 *srcB =
             Bsl + ((size_t)(a * NTT + nt) * KCH + c) * (kTN * kKC);
-        tc::bulk_g2s(stage[b] + kS * kTileA + a * kTileB, srcB, kTileB,
+        tc::bulk_g2s(st + kS * kTileA + a * kTileB, srcB, kTileB,
                      &bar_load[b]);
       }
-      pend_load[b] = true;
     };
-    if (nch > 0) issue_load(0, 0);
+    for (; issued < nch && issued < kStages - 1; issued++) issue_load(issued);
+    int mma_done = 0;   // chunks whose MMAs are known complete
     for (int c = 0; c < nch; c++) {
-      const int b = c & 1;
-      if (c + 1 < nch) {
-        const int nb = (c + 1) & 1;
-        if (pend_mma[nb]) {   // MMAs of chunk c-1 still read stage nb
-          if (!tc::mbar_wait(&bar_mma[nb], ph_mma[nb], kWaitLimit)) { ok = false; break; }
-          ph_mma[nb] ^= 1;
-          pend_mma[nb] = false;
-        }
-        issue_load(c + 1, nb);
-      }
-      if (!tc::mbar_wait(&bar_load[b], ph_load[b], kWaitLimit)) { ok = false; break; }
-      ph_load[b] ^= 1;
-      pend_load[b] = false;
+      const int b = c % kStages;
+      if (!tc::mbar_wait(&bar_load[b], (c / kStages) & 1, kWaitLimit)) { ok = false; break; }
       tc::fence_after_sync();
-      const uint32_t aBase = tc::smem_u32(stage[b]);
+      const uint32_t aBase = tc::smem_u32(smem + b * kStage);
       const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
       const uint64_t bd0 = tc::smem_desc(aBase + kS * kTileA, 128,
                                          (kKC / 8) * 128);
@@ -193,14 +189,24 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
         }
       }
       tc::mma_commit(&bar_mma[b]);
-      pend_mma[b] = true;
+      if (issued < nch) {
+        // the stage for chunk `issued` was last used by chunk issued-kStages
+        const int prev = issued - kStages;
+        if (prev >= 0) {
+          if (!tc::mbar_wait(&bar_mma[prev % kStages], (prev / kStages) & 1,
+                             kWaitLimit)) { ok = false; break; }
+          mma_done = prev + 1;
+        }
+        issue_load(issued);
+        issued++;
+      }
     }
-    // Drain every outstanding copy and MMA before the accumulators are read
-    // or TMEM is released (bounded as well).
-    for (int b = 0; b < 2; b++) {
-      if (pend_mma[b] && !tc::mbar_wait(&bar_mma[b], ph_mma[b], kWaitLimit)) ok = false;
-      if (pend_load[b] && !tc::mbar_wait(&bar_load[b], ph_load[b], kWaitLimit)) ok = false;
-    }
+    // Drain: every outstanding MMA (waiting on the last commit covers all
+    // earlier ones, but each barrier phase is consumed in order) and every
+    // issued load, bounded, before the accumulators are read or TMEM freed.
+    const int last = ok ? nch : 0;
+    for (int c = mma_done; c < last; c++)
+      if (!tc::mbar_wait(&bar_mma[c % kStages], (c / kStages) & 1, kWaitLimit)) { ok = false; break; }
     if (nch == 0) ok = false;   // nothing accumulated: the host handles K == 0
     if (!ok) {
       *ok_slot = 0;
