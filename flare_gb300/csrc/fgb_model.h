@@ -31,6 +31,7 @@ struct fgb_model_s {
   std::vector<double> h_desc, h_snorm, h_alpha;
   std::vector<int> h_panel_rows;
   std::vector<long long> h_panel_off;
+  std::vector<double> h_L_inv;   // host copy (replicas for serving workers)
   fgb::DevBuf S;        // normalised sparse descriptors, M x n_d (FP64)
   fgb::DevBuf Sraw;     // raw sparse descriptors, M x n_d (FP64)
   fgb::DevBuf snorm;    // sparse norms

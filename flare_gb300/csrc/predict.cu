@@ -447,6 +447,7 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
     FGB_CUDA(cudaMemcpy(m->alpha.p, h_alpha, sizeof(double) * M,
                         cudaMemcpyHostToDevice));
   m->h_alpha.assign(h_alpha, h_alpha + M);
+  m->h_L_inv.assign(h_L_inv, h_L_inv + (size_t)M * M);
   // L_inv panels: species s uses rows [c_s, c_s + R_s) and columns
   // [c_s, c_s + M_s); R_s = M_s when everything below the diagonal block is
   // exactly zero (the single-kernel case), else M - c_s.

@@ -200,6 +200,36 @@ int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
                      int precision, double *h_energy, double *h_forces,
                      double *h_stress, double *h_local_var, void *stream);
 
+/* ------------------------------------------------------------ serving
+ * Continuous batching over a solved model.  fgb_serve_start launches
+ * n_workers host threads; each owns a replica of the model (same weights,
+ * its own device workspace) and a CUDA stream.  Submitted structures queue
+ * in arrival order; a free worker takes the longest prefix of the queue
+ * whose device-memory footprint (atoms x the model's bytes per atom) fits
+ * what the budget has left, predicts it as one batch (fgb_predict_host),
+ * and hands each result back.  Batches of different workers run
+ * concurrently on the GPU.  A structure alone or in any batch gives the same
+ * bits (no float atomics, fixed reduction orders).  A request whose own
+ * footprint exceeds the budget is refused at submit (FGB_EINVAL). */
+typedef struct fgb_server_s *fgb_server_t;
+int fgb_serve_start(fgb_server_t *out, fgb_model_t model, int n_workers,
+                    long long memory_budget_bytes, int max_structures,
+                    double cutoff, int want, int precision);
+/* copies the inputs; returns the request id in *request_id */
+int fgb_serve_submit(fgb_server_t s, int n_atoms, const double *h_cell,
+                     const double *h_positions, const int *h_species,
+                     long long *request_id);
+/* *done = 1 when finished: results are copied out (any pointer may be NULL)
+ * and the request is released; *latency_ms = submit-to-completion time.
+ * A failed request returns its error status here. */
+int fgb_serve_poll(fgb_server_t s, long long request_id, int *done,
+                   double *h_energy, double *h_forces, double *h_stress,
+                   double *h_local_var, double *latency_ms);
+/* completed requests, batches run, bytes of the model's per-atom footprint */
+int fgb_serve_stats(fgb_server_t s, long long *completed, long long *batches,
+                    long long *bytes_per_atom);
+int fgb_serve_stop(fgb_server_t s);
+
 /* NormalizedDotProduct::envs_envs (normalized_dot_product.cpp:28-89) for
  * one species block in FP64: d_kern[n1 * n2] (row-major) =
  * sig2 * (d1.d2 / (norm1 norm2))^power, zero where either norm < 1e-8.
