@@ -46,6 +46,10 @@ def parse():
                     help="structures (1000 atoms each) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--workload", default="alloy1000",
+                    choices=["alloy1000", "fcc1m"],
+                    help="fcc1m: one 1,048,576-atom structure, E+F+virial, "
+                         "peak device memory (reported as a side record)")
     return ap.parse_args()
 
 
@@ -459,9 +463,7 @@ OZ_PRODUCTS = 45
 
 
 def oz_eligible(gp, b2, k_max=1472):
-    sd = gp.sparse_descriptors[0]
-    return (b2.n_descriptors <= k_max and gp.kernels[0].power in (1.0, 2.0)
-            and all(c <= k_max for c in sd.n_clusters_by_type))
+    return b2.n_descriptors <= k_max and gp.kernels[0].power in (1.0, 2.0)
 
 
 def bf16_peak():
@@ -516,11 +518,64 @@ def time_plain(L, _lib, model, structs, b2, c, torch):
             "sample": f"{len(times)} structure(s) after 1 warm-up, wall clock"}
 
 
+def run_fcc1m(args):
+    """One 1,048,576-atom FCC structure: energy, forces and virial through
+    the reverse-mode adjoint (mixed and FP64), device memory, and the
+    footprint the stored forward-mode gradients would need."""
+    import torch
+    import flare_gb300 as fg
+    from flare_gb300 import _lib
+    from flare_gb300 import workloads as wl
+    L = _lib.lib()
+    c = wl.FCC1M
+    t0 = time.time()
+    gp, b2, k = wl.build_fcc_model()
+    train_s = time.time() - t0
+    cell, sp, pos = wl.fcc_structure()
+    N = len(sp)
+    free0, total = torch.cuda.mem_get_info()
+    out = {}
+    for prec in ("mixed", "fp64"):
+        s = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        torch.cuda.synchronize()
+        times = []
+        for rep in range(max(1, args.steps)):
+            t1 = time.perf_counter()
+            r = gp.predict_batch([s], want=7, precision=prec)
+            times.append(time.perf_counter() - t1)
+        free1, _ = torch.cuda.mem_get_info()
+        out[prec] = {"seconds": float(np.median(times)),
+                     "atoms_per_s": N / float(np.median(times)),
+                     "energy_ev": float(r["energy"][0]),
+                     "stress_flare_order": [float(x) for x in r["stress"][0]],
+                     "device_bytes_in_use": int(total - free1),
+                     "device_bytes_added": int(free0 - free1)}
+    P = fg.Structure(cell, sp, pos, c["rc"], []).n_neighbors
+    nd = b2.n_descriptors
+    M = gp.n_sparse
+    print(json.dumps({
+        "workload": "fcc1m: 1,048,576-atom FCC (64^3 cells, a = 4.05, sigma "
+                    "0.08), B2 n_max 10 l_max 6 rc 5.0, 4000 sparse envs",
+        "n_atoms": N, "n_pairs": int(P), "train_setup_s": round(train_s, 1),
+        "adjoint": out,
+        "stored_forward_mode_bytes": {
+            "dB2_dr_3P_x_nd_fp64": 3 * int(P) * nd * 8,
+            "envs_struc_force_kernel_3P_x_M_fp64": 3 * int(P) * M * 8,
+            "device_total_bytes": int(total),
+            "fits": 3 * int(P) * nd * 8 < total},
+        "energy_difference_mixed_vs_fp64_ev_per_atom":
+            abs(out["mixed"]["energy_ev"] - out["fp64"]["energy_ev"]) / N,
+    }), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus if args.impl == "ours" else 0)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "fcc1m":
+        run_fcc1m(args)
         return
     run_ours(args, rank, world, local)
 

@@ -34,6 +34,12 @@ int launch_variance_final(int Mr, int ntiles, const double *part,
                           const int *perm, const double *norms, double sig2,
                           double xi, double *var, cudaStream_t st);
 
+// FP64 triangular variance GEMM (Z = K L^T, row sums of Z^2 per 64-column
+// tile), ntiles = ceil(R / 64).
+int launch_variance_fp64(int Mr, int R, int Ms, const double *Kmat,
+                         const double *Lp, double *part, int ntiles,
+                         cudaStream_t st);
+
 // Validate coded species in [0, n_species); returns FGB_EINVAL otherwise.
 int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
                   cudaStream_t st);

@@ -430,6 +430,15 @@ struct EpiZsq {
 }  // namespace
 }  // namespace oz
 
+// The kernel GEMM contracts over n_d; the variance GEMM over the species'
+// sparse count.  Either runs on the tensor cores when its K fits the
+// exact-accumulation limit (the variance GEMM falls back to FP64 otherwise).
+bool oz_eligible(const fgb_model_s *m) { return m->b2.n_d <= oz::kMaxK; }
+
+static bool oz_var_eligible(const fgb_model_s *m, int s) {
+  return m->h_counts[s] <= oz::kMaxK;
+}
+
 // Slice the model operands once: normalised sparse rows (B of the kernel
 // GEMM) and the L_inv panels (B of the variance GEMM), per species.
 static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
@@ -447,7 +456,8 @@ static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
                          nullptr, nullptr},
                         *m->ozS[s], st)))
       return rc;
-    if ((rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
+    if (oz_var_eligible(m, s) &&
+        (rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
                          m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
                          nullptr},
                         *m->ozL[s], st)))
@@ -458,12 +468,6 @@ static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
   return FGB_OK;
 }
 
-bool oz_eligible(const fgb_model_s *m) {
-  if (m->b2.n_d > oz::kMaxK) return false;
-  for (int s = 0; s < m->b2.n_species; s++)
-    if (m->h_counts[s] > oz::kMaxK) return false;
-  return true;
-}
 
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
@@ -513,7 +517,18 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                   m->alpha.as<double>() + m->h_offsets[s], perm,
                                   m->ws.erows.as<double>(), d_e_atom, st)))
         return rc;
-      if (want_var) {
+      if (want_var && !oz_var_eligible(m, s)) {
+        const int R = m->h_panel_rows[s];
+        const int ntiles = ceil_div(R, 64);
+        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)) ||
+            (rc = launch_variance_fp64(Mr, R, Ms, m->ws.kmat.as<double>(),
+                                       m->Lp.as<double>() + m->h_panel_off[s],
+                                       m->ws.part.as<double>(), ntiles, st)) ||
+            (rc = launch_variance_final(Mr, ntiles, m->ws.part.as<double>(),
+                                        perm, m->ws.norms.as<double>(), sig2,
+                                        m->power, d_var, st)))
+          return rc;
+      } else if (want_var) {
         const int R = m->h_panel_rows[s];
         const int ntiles = m->ozL[s]->RP / oz::kTN;
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))

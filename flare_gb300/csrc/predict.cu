@@ -231,6 +231,16 @@ int launch_variance_final(int Mr, int ntiles, const double *part,
   return FGB_OK;
 }
 
+int launch_variance_fp64(int Mr, int R, int Ms, const double *Kmat,
+                         const double *Lp, double *part, int ntiles,
+                         cudaStream_t st) {
+  StageTimer _pt(kStVarianceGemm, st);
+  dim3 g3(ntiles, ceil_div(Mr, BM));
+  k_variance_gemm<<<g3, GT, 0, st>>>(Mr, R, Ms, Kmat, Lp, part, ntiles);
+  FGB_LAUNCH_CHECK("k_variance_gemm");
+  return FGB_OK;
+}
+
 int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
                   cudaStream_t st) {
   if (n == 0) return FGB_OK;

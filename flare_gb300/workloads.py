@@ -76,3 +76,47 @@ def build_alloy_model(n_train=None, per_species=None, verbose=False):
             print(f"  trained structure {t}: M = {gp.n_sparse}", flush=True)
     gp.update_matrices_QR()
     return gp, b2, k
+
+
+# ``fcc1m``: 64x64x64 FCC cells (1,048,576 atoms, a = 4.05 A) with thermal
+# Gaussian displacements sigma = 0.08 A (seed 3000); B2 n_max = 10, l_max = 6,
+# rc = 5.0 A; model: 4,000 sparse environments from 16 seeded 256-atom FCC
+# structures at sigma = 0.08 (seeds 3001-3016), LJ energy and force labels.
+FCC1M = dict(n_cells=64, a=4.05, sigma_disp=0.08, seed=3000, rc=5.0, n_max=10,
+             l_max=6, sigma=2.0, power=2, n_train=16, train_seed0=3001,
+             n_sparse=4000, sparse_seed=3200, sigma_e_per_atom=1e-3,
+             sigma_f=0.05, sigma_s=1.0)
+
+
+def build_fcc_model(n_train=None, n_sparse=None):
+    """Train the large-structure model on the GPU (FP64)."""
+    import flare_gb300 as fg
+    c = FCC1M
+    n_train = n_train or c["n_train"]
+    n_sparse = n_sparse or c["n_sparse"]
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, c["rc"]], [],
+               [1, c["n_max"], c["l_max"]])
+    k = fg.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = fg.SparseGP([k], c["sigma_e_per_atom"] * 256, c["sigma_f"],
+                     c["sigma_s"])
+    r = syn.rng(c["sparse_seed"])
+    chosen = r.choice(n_train * 256, size=min(n_sparse, n_train * 256),
+                      replace=False)
+    for t in range(n_train):
+        cell, sp, pos = syn.fcc_al(n_cells=4, a=c["a"], sigma=c["sigma_disp"],
+                                   seed=c["train_seed0"] + t)
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, [0.4], [2.6], c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        atoms = sorted(int(q) - 256 * t for q in chosen if q // 256 == t)
+        gp.add_specific_environments(st, atoms)
+    gp.update_matrices_QR()
+    return gp, b2, k
+
+
+def fcc_structure(n_cells=None, seed=None):
+    c = FCC1M
+    return syn.fcc_al(n_cells=n_cells or c["n_cells"], a=c["a"],
+                      sigma=c["sigma_disp"], seed=seed or c["seed"])
