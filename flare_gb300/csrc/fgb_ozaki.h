@@ -31,6 +31,8 @@ struct Sliced {
 };
 
 int pad_to(int x, int m);
+// Size `out` for rows x K slices (no conversion).
+int prepare(int rows, int K, int TR, Sliced &out);
 int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st);
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,

@@ -9,19 +9,21 @@
 // a + b) stays below 2^24, so the tensor core's FP32 accumulation is exact
 // too.  All 45 pairs with a + b <= S + 1 are accumulated into 9 group
 // accumulators held in TMEM (9 x 48 FP32 columns per 128-row tile), and the
-// epilogue recombines C = 2^(e_row + e_col) sum_t 2^(-6t) group_t in FP64.
+// epilogue recombines C = 2^(e_row + e_col) sum_t 2^(-6t) group_t exactly in
+// 64-bit integers, rounding once to FP64.
 // The dropped terms (a + b > 10) and the slice residuals are below 2^-54 of
 // each row's largest entry — FP64-level accuracy, measured on the sparse-GP
 // kernel and variance products (energy 5e-10 eV/atom, variance 2e-14).
 //
 // Data movement: slices are written by k_oz_slice directly in the tensor
 // core's no-swizzle K-major canonical layout (8 x 16-byte core matrices),
-// tiled so that every (slice, 128-row tile, 32-wide k chunk) is one
-// contiguous 8 KB block (3 KB for the 48-row B tiles).  One thread streams
-// the 18 blocks of a chunk with cp.async.bulk into a double-buffered shared
-// memory stage (mbarrier transaction counts), issues the 90 tcgen05.mma
-// (45 pairs x 2 k-steps) of the chunk and commits them to the stage's
-// "consumed" mbarrier; every wait is bounded and reports through `err`.
+// tiled so that the 9 slices of every (128-row tile, 16-wide k chunk) are one
+// contiguous 36 KB block (13.5 KB for the 48-row B tiles).  One thread streams
+// each chunk with two cp.async.bulk copies into a 4-stage shared-memory
+// ring (mbarrier transaction counts), issues the chunk's 45 pair products as
+// 13 tcgen05.mma with the B slices stacked along N (mma_kstep) and commits
+// them to the stage's "consumed" mbarrier; every wait is bounded and reports
+// through `err`.
 #include <cuda_bf16.h>
 
 #include "fgb_internal.h"
@@ -39,17 +41,139 @@ constexpr uint32_t kStage = kS * (kTileA + kTileB);
 constexpr uint32_t kSmem = kStages * kStage + 256;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitLimit = 1LL << 22;
-constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTM, kTN);
 static_assert(kG * kTN <= (int)kTmemCols, "group accumulators exceed TMEM");
 static_assert(kSmem <= 227 * 1024, "stages exceed shared memory");
 static_assert(kKC % 16 == 0, "a chunk is whole MMA k-steps");
 static_assert(kS == 9 && kBeta == 6 && kTN % 16 == 0,
               "the exact recombination assumes 9 slices of 6 bits");
 
+// One tcgen05.mma covering the pairs (A, B0) .. (A, B0 + NB - 1).  The B
+// slices of a stage sit one after another in shared memory (each 48 rows of
+// 8-row core-matrix groups, 256 bytes apart), so NB consecutive slices are a
+// single N = 48 NB operand; their products belong to the consecutive groups
+// A + B0 .. A + B0 + NB - 1, whose accumulators are consecutive 48-column
+// blocks of TMEM.  An M = 128 MMA costs max(64, N / 2) cycles, so stacking
+// slices keeps every instruction at N >= 96 where the plan allows.
+template <int A, int B0, int NB>
+__device__ __forceinline__ void mma_span(uint32_t tmem, uint64_t ad0,
+                                         uint64_t bd0, bool first) {
+  static_assert(A >= 0 && B0 >= 0 && NB >= 1 && A + B0 + NB <= kS,
+                "span outside the 45 pairs with a + b <= kS + 1");
+  static_assert(NB * kTN <= 256, "an M = 128 MMA takes N <= 256");
+  // descriptor start addresses are in 16-byte units in the low bits
+  tc::mma_bf16(tmem + (uint32_t)((A + B0) * kTN),
+               ad0 + (uint64_t)((A * kTileA) >> 4),
+               bd0 + (uint64_t)((B0 * kTileB) >> 4),
+               tc::idesc_bf16_f32(kTM, NB * kTN),
+               (A == 0 && first) ? 0u : 1u);
+}
+
+// All 45 pairs of one 16-deep k-step as 13 MMAs.  A slice a pairs with B
+// slices 0 .. kS-1-a; each row below splits that range into spans of at most
+// five slices (N <= 240).  The two a = 0 spans together cover every group, so
+// with `first` set they initialise all nine accumulators.
+__device__ __forceinline__ void mma_kstep(uint32_t tmem, uint64_t ad0,
+                                          uint64_t bd0, bool first) {
+  mma_span<0, 0, 5>(tmem, ad0, bd0, first);
+  mma_span<0, 5, 4>(tmem, ad0, bd0, first);
+  mma_span<1, 0, 4>(tmem, ad0, bd0, first);
+  mma_span<1, 4, 4>(tmem, ad0, bd0, first);
+  mma_span<2, 0, 4>(tmem, ad0, bd0, first);
+  mma_span<2, 4, 3>(tmem, ad0, bd0, first);
+  mma_span<3, 0, 3>(tmem, ad0, bd0, first);
+  mma_span<3, 3, 3>(tmem, ad0, bd0, first);
+  mma_span<4, 0, 5>(tmem, ad0, bd0, first);
+  mma_span<5, 0, 4>(tmem, ad0, bd0, first);
+  mma_span<6, 0, 3>(tmem, ad0, bd0, first);
+  mma_span<7, 0, 2>(tmem, ad0, bd0, first);
+  mma_span<8, 0, 1>(tmem, ad0, bd0, first);
+}
+
+// Slice storage, chunk-major: the kS slices of one (row tile, 16-wide k chunk)
+// are one contiguous block (kS tiles of TR x 16 in the canonical layout), so a
+// pipeline stage is filled by a single bulk copy per operand.  Returns the
+// element index of (m, k) in slice 0; slice a sits a * TR * 16 further on.
 __device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
-  return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(TR * kKC) +
+  return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(kS * TR * kKC) +
          (size_t)(((m % TR) / 8) * (kKC / 8) + (k % kKC) / 8) * 64 +
          (m % 8) * 8 + (k % 8);
+}
+
+// ---------------------------------------------------------------------------
+// Integer helpers.  FP64 arithmetic runs at about 2 operations per clock per
+// SM on this GPU, so the slicing and recombination build and take apart
+// doubles with integer instructions; the results are the same doubles the
+// FP64 expressions give.
+
+// e for a power-of-two scale 2^e.
+__device__ __forceinline__ int pow2_exp(double s) {
+  return (int)((__double_as_longlong(s) >> 52) & 0x7FF) - 1023;
+}
+
+// x 2^sc as a double, exact, for an integer |x| < 2^53.
+__device__ __forceinline__ double exact_scaled(long long x, int sc) {
+  if (x == 0) return 0.0;
+  const unsigned long long a = x < 0 ? 0ULL - (unsigned long long)x
+                                     : (unsigned long long)x;
+  const int p = 63 - __clzll((long long)a);            // leading bit, <= 52
+  const int field = p + sc + 1023;
+  if (field < 1 || field > 2046) return ldexp((double)x, sc);  // not normal
+  unsigned long long bits = ((unsigned long long)field << 52) |
+                            ((a << (52 - p)) & 0xFFFFFFFFFFFFFULL);
+  if (x < 0) bits |= 1ULL << 63;
+  return __longlong_as_double(bits);
+}
+
+// rn(d 2^sh) as a 64-bit integer (nearest, ties to even, as __double2ll_rn
+// of the exactly scaled value), for |d 2^sh| < 2^62.
+__device__ __forceinline__ long long fixed_rn(double d, int sh) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
+  const int field = (int)((bits >> 52) & 0x7FF);
+  const int s = field - 1075 + sh;   // value = mant 2^s
+  if (field == 0 || s > 9) return __double2ll_rn(ldexp(d, sh));  // rare
+  const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+  unsigned long long q;
+  if (s >= 0) {
+    q = mant << s;
+  } else {
+    const int r = -s;
+    if (r > 53) {
+      q = 0;
+    } else {
+      q = mant >> r;
+      const unsigned long long rem = mant & ((1ULL << r) - 1);
+      const unsigned long long half = 1ULL << (r - 1);
+      q += (rem > half || (rem == half && (q & 1))) ? 1 : 0;
+    }
+  }
+  return (bits >> 63) ? -(long long)q : (long long)q;
+}
+
+// BF16 bits of a small integer (|q| <= 256, exact).
+__device__ __forceinline__ uint32_t bf16_bits(long long q) {
+  return __float_as_uint(__int2float_rn((int)q)) >> 16;
+}
+
+// The kS base-64 digits of X (|X| < 2^54) for 8 consecutive k, stored as
+// 16-byte rows of the canonical layout: slice a at out + a * stride.
+__device__ __forceinline__ void store_digits8(long long (&X)[8],
+                                              __nv_bfloat16 *out,
+                                              size_t stride) {
+#pragma unroll
+  for (int a = 1; a <= kS; a++) {
+    const int sh = 54 - kBeta * a;
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      long long q0 = sh > 0 ? (X[j] + (1LL << (sh - 1))) >> sh : X[j];
+      long long q1 = sh > 0 ? (X[j + 1] + (1LL << (sh - 1))) >> sh : X[j + 1];
+      X[j] -= q0 << sh;
+      X[j + 1] -= q1 << sh;
+      w[j / 2] = bf16_bits(q0) | (bf16_bits(q1) << 16);
+    }
+    *reinterpret_cast<uint4 *>(out + (size_t)(a - 1) * stride) =
+        make_uint4(w[0], w[1], w[2], w[3]);
+  }
 }
 
 // Warp per row: scale to (-1, 1) by a power of two, split into kS slices.
@@ -57,6 +181,8 @@ __device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
 // |y| >= 2^-1 of the row's top binade, rounded at 2^-54 below that); the
 // 9 slices are the base-64 digits of X, each rounded to nearest, extracted
 // with 64-bit integer arithmetic: q_a = round(R / 2^(54-6a)), R -= q_a 2^(54-6a).
+// Each lane converts 8 consecutive k and writes one 16-byte core-matrix row
+// per slice.
 __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
                            const double *__restrict__ src, long long ld,
                            const int *__restrict__ perm,
@@ -77,27 +203,31 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
       else valid = false;
     }
   }
-  double mx = 0.0;
+  // row max of |src| on the bit patterns (non-negative doubles order as
+  // integers)
+  unsigned long long mb = 0;
   if (valid)
-    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(src[row * ld + k]));
+    for (int k = lane; k < K; k += 32)
+      mb = max(mb, (unsigned long long)__double_as_longlong(src[row * ld + k]) &
+                       0x7FFFFFFFFFFFFFFFULL);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
-    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-  mx *= inv;
+    mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, off));
+  const double mx = __longlong_as_double((long long)mb) * inv;
   const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
   if (lane == 0) scale[m] = ldexp(1.0, e);
-  const double to_int = inv * ldexp(1.0, 54 - e);
-  const size_t slice = (size_t)RP * KP;
-  for (int k = lane; k < KP; k += 32) {
-    long long X = (valid && k < K) ? __double2ll_rn(src[row * ld + k] * to_int) : 0;
-    const size_t idx = tiled_index(m, k, KP, TR);
+  const size_t stride = (size_t)TR * kKC;
+  for (int k0 = lane * 8; k0 < KP; k0 += 256) {
+    long long X[8];
 #pragma unroll
-    for (int a = 1; a <= kS; a++) {
-      const int sh = 54 - kBeta * a;
-      long long q = sh > 0 ? (X + (1LL << (sh - 1))) >> sh : X;
-      X -= q << sh;
-      out[(a - 1) * slice + idx] = __float2bfloat16_rn((float)q);
+    for (int j = 0; j < 8; j++) {
+      const int k = k0 + j;
+      X[j] = (valid && k < K)
+                 ? fixed_rn(rownorm ? src[row * ld + k] * inv : src[row * ld + k],
+                            54 - e)
+                 : 0;
     }
+    store_digits8(X, out + tiled_index(m, k0, KP, TR), stride);
   }
 }
 
@@ -137,7 +267,7 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
 
   const int kmax = tri ? min(K, n0 + kTN) : K;
   const int nch = (kmax + kKC - 1) / kKC;
-  const int KCH = KP / kKC, MTT = MP / kTM, NTT = NP / kTN;
+  const int KCH = KP / kKC;
 
   if (tid == 0) {
     // Ring of kStages stages.  Chunk c lives in stage c % kStages; its
@@ -152,15 +282,11 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
       const int b = c % kStages;
       unsigned char *st = smem + b * kStage;
       tc::mbar_expect_tx(&bar_load[b], kStage);
-      for (int a = 0; a < kS; a++) {
-        const __nv_bfloat16 *srcA =
-            Asl + ((size_t)(a * MTT + mt) * KCH + c) * (kTM * kKC);
-        tc::bulk_g2s(st + a * kTileA, srcA, kTileA, &bar_load[b]);
-        const __nv_bfloat16 *srcB =
-            Bsl + ((size_t)(a * NTT + nt) * KCH + c) * (kTN * kKC);
-        tc::bulk_g2s(st + kS * kTileA + a * kTileB, srcB, kTileB,
-                     &bar_load[b]);
-      }
+      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + c) * (kS * kTM * kKC),
+                   kS * kTileA, &bar_load[b]);
+      tc::bulk_g2s(st + kS * kTileA,
+                   Bsl + ((size_t)nt * KCH + c) * (kS * kTN * kKC),
+                   kS * kTileB, &bar_load[b]);
     };
     for (; issued < nch && issued < kStages - 1; issued++) issue_load(issued);
     int mma_done = 0;   // chunks whose MMAs are known complete
@@ -172,22 +298,11 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
       const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
       const uint64_t bd0 = tc::smem_desc(aBase + kS * kTileA, 128,
                                          (kKC / 8) * 128);
-      // descriptor start addresses are in 16-byte units in the low bits
+      // k-steps of 16 are two core matrices (256 bytes) apart along K
 #pragma unroll
-      for (int kk = 0; kk < kKC / 16; kk++) {
-#pragma unroll
-        for (int a = 0; a < kS; a++) {
-          const uint64_t ad = ad0 + (uint64_t)((a * kTileA + kk * 256) >> 4);
-#pragma unroll
-          for (int bb = 0; a + bb < kS; bb++) {
-            const uint64_t bd = bd0 + (uint64_t)((bb * kTileB + kk * 256) >> 4);
-            // the first product of each group (a == 0) in the first k-step
-            // initialises its accumulator
-            const uint32_t acc = (c != 0 || kk != 0 || a != 0) ? 1u : 0u;
-            tc::mma_bf16(tmem + (a + bb) * kTN, ad, bd, kIdesc, acc);
-          }
-        }
-      }
+      for (int kk = 0; kk < kKC / 16; kk++)
+        mma_kstep(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
+                  bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
       tc::mma_commit(&bar_mma[b]);
       if (issued < nch) {
         // the stage for chunk `issued` was last used by chunk issued-kStages
@@ -220,8 +335,13 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   if (ok) {
     // Group sums are exact integers below 2^24; recombine them exactly in
     // two 64-bit integers, hi = sum_{t=2..6} g_t 2^(6(6-t)) and
-    // lo = sum_{t=7..10} g_t 2^(6(10-t)), then C = hi 2^-36 + lo 2^-60.
+    // lo = sum_{t=7..10} g_t 2^(6(10-t)), then C = (hi 2^-36 + lo 2^-60)
+    // 2^(e_row + e_col): two exact doubles built from the integers and one
+    // correctly rounded addition.  Rows past M (tile padding) still run the
+    // epilogue so that functors can write zero padding.
     const int m = m0 + warp * 32 + lane;
+    const bool row_ok = m < M;
+    const int er = pow2_exp(Ascale[m]);
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     double acc = 0.0;
 #pragma unroll 1
@@ -244,11 +364,13 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
       }
       double v[16];
 #pragma unroll
-      for (int j = 0; j < 16; j++)
-        v[j] = fma((double)hi[j], 0x1p-36, (double)lo[j] * 0x1p-60);
-      if (m < M) acc = epi.chunk(m, n0 + c0, v, Ascale[m], Bscale, acc);
+      for (int j = 0; j < 16; j++) {
+        const int e = er + pow2_exp(Bscale[n0 + c0 + j]);
+        v[j] = exact_scaled(hi[j], e - 36) + exact_scaled(lo[j], e - 60);
+      }
+      acc = epi.chunk(m, row_ok, n0 + c0, v, acc);
     }
-    if (m < M) epi.finish(m, n0, acc);
+    epi.finish(m, row_ok, n0, acc);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -256,36 +378,44 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
+// Plain product C = A B^T.
 struct EpiStore {
   double *C;
   long long ldc;
   int N;
-  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
-                          const double *cs, double acc) const {
+  __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
+                          double acc) const {
+    if (!row_ok) return acc;
 #pragma unroll
     for (int j = 0; j < 16; j++) {
       int n = n0 + j;
-      if (n < N) C[(long long)m * ldc + n] = v[j] * rs * cs[n];
+      if (n < N) C[(long long)m * ldc + n] = v[j];
     }
     return acc;
   }
-  __device__ void finish(int, int, double) const {}
+  __device__ void finish(int, bool, int, double) const {}
 };
 
 }  // namespace
 
 int pad_to(int x, int m) { return (x + m - 1) / m * m; }
 
-int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
-  out.rows = sp.rows;
-  out.K = sp.K;
-  out.TR = sp.TR;
-  out.RP = pad_to(std::max(sp.rows, 1), sp.TR);
-  out.KP = pad_to(std::max(sp.K, 1), kKC);
+int prepare(int rows, int K, int TR, Sliced &out) {
+  out.rows = rows;
+  out.K = K;
+  out.TR = TR;
+  out.RP = pad_to(std::max(rows, 1), TR);
+  out.KP = pad_to(std::max(K, 1), kKC);
   int rc;
   if ((rc = out.q.ensure(sizeof(__nv_bfloat16) * (size_t)kS * out.RP * out.KP)) ||
       (rc = out.scale.ensure(sizeof(double) * (size_t)out.RP)))
     return rc;
+  return FGB_OK;
+}
+
+int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
+  int rc;
+  if ((rc = prepare(sp.rows, sp.K, sp.TR, out))) return rc;
   const long long threads = (long long)out.RP * 32;
   k_oz_slice<<<ceil_div(threads, 256), 256, 0, st>>>(
       sp.rows, sp.K, out.RP, out.KP, sp.TR, sp.src, sp.ld, sp.perm,
@@ -376,56 +506,85 @@ namespace fgb {
 namespace oz {
 namespace {
 
-// Kernel GEMM epilogue: c = d^ . s^ -> k = sig^2 c^xi (and the adjoint
-// weight w = sig^2 xi alpha c^(xi-1) when asked), zero for empty
-// environments — the same expressions as the FP64 path.
+// Kernel GEMM epilogue: c = d^ . s^ -> k = sig^2 c^xi, zero for empty
+// environments and invalid sparse rows (the same expressions as the FP64
+// path).  Per row and tile it keeps sum_n alpha_n k_n (the energy partial,
+// finished in a fixed order by k_energy_final) and, for the variance GEMM,
+// writes k directly as exact BF16 slices (A operand layout, 128-row tiles,
+// K = N padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64
+// matrix is written only when the variance runs in FP64.
 struct EpiKernel {
-  double *K, *W;
+  double *Kd;                 // optional M x N FP64 kernel matrix
+  __nv_bfloat16 *Ksl;         // optional slices of K (variance A operand)
+  double *Kscale;             // their row scales (all 2^eK)
+  int KPv, eK;
+  double *epart;              // M x ntiles energy partials
+  int ntiles;
   const double *alpha;
   const unsigned char *valid;
   const int *perm;
   const double *norms;
   double sig2, xi;
   int N;
-  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
-                          const double *cs, double acc) const {
-    const bool dok = norms[perm[m]] >= kEmptyThresh;
+  __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
+                          double acc) const {
+    const bool dok = row_ok && norms[perm[m]] >= kEmptyThresh;
+    double k[16];
 #pragma unroll
     for (int j = 0; j < 16; j++) {
       const int n = n0 + j;
-      if (n >= N) continue;
-      const bool ok = dok && valid[n];
-      const double c = v[j] * rs * cs[n];
-      K[(long long)m * N + n] = ok ? sig2 * gemm64::powx(c, xi) : 0.0;
-      if (W)
-        W[(long long)m * N + n] =
-            ok ? sig2 * xi * gemm64::powx(c, xi - 1.0) * alpha[n] : 0.0;
+      const bool ok = dok && n < N && valid[n];
+      k[j] = ok ? sig2 * gemm64::powx(v[j], xi) : 0.0;
+      if (n < N && row_ok) acc = fma(alpha[n], k[j], acc);
+      if (Kd && n < N && row_ok) Kd[(long long)m * N + n] = k[j];
+    }
+    if (Ksl && n0 < KPv) {
+      // 16 columns = one k chunk of the variance operand: two core-matrix
+      // rows of 8
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        long long X[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], 54 - eK);
+        store_digits8(X, Ksl + tiled_index(m, n0 + 8 * h, KPv, kTM),
+                      (size_t)kTM * kKC);
+      }
     }
     return acc;
   }
-  __device__ void finish(int, int, double) const {}
+  __device__ void finish(int m, bool row_ok, int n0, double acc) const {
+    if (row_ok) epart[(long long)m * ntiles + n0 / kTN] = acc;
+    if (Ksl && n0 == 0) Kscale[m] = ldexp(1.0, eK);
+  }
 };
 
 // Variance GEMM epilogue: per-row sum of z^2 over this tile's columns.
 struct EpiZsq {
   double *part;
   int ntiles, R;
-  __device__ double chunk(int m, int n0, const double (&v)[16], double rs,
-                          const double *cs, double acc) const {
+  __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
+                          double acc) const {
+    if (!row_ok) return acc;
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const int n = n0 + j;
-      if (n < R) {
-        const double z = v[j] * rs * cs[n];
-        acc = fma(z, z, acc);
-      }
-    }
+    for (int j = 0; j < 16; j++)
+      if (n0 + j < R) acc = fma(v[j], v[j], acc);
     return acc;
   }
-  __device__ void finish(int m, int n0, double acc) const {
-    part[(long long)m * ntiles + n0 / kTN] = acc;
+  __device__ void finish(int m, bool row_ok, int n0, double acc) const {
+    if (row_ok) part[(long long)m * ntiles + n0 / kTN] = acc;
   }
 };
+
+// E_atom = sum of the row's energy partials, tiles in order.
+__global__ void k_energy_final(int M, int ntiles, const double *__restrict__ part,
+                               const int *__restrict__ perm,
+                               double *__restrict__ e_atom) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  double s = 0.0;
+  for (int t = 0; t < ntiles; t++) s += part[(long long)m * ntiles + t];
+  e_atom[perm[m]] = s;
+}
 
 }  // namespace
 }  // namespace oz
@@ -473,10 +632,16 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
                     cudaStream_t st) {
   int rc;
+  if (want_w) {
+    set_error("tensor-core kernel stage: adjoint weights are not produced");
+    return FGB_ENOTSUP;
+  }
   if (!m->oz_ready && (rc = build_oz_model(m, st))) return rc;
   const B2Params &p = m->b2;
   const int nd = p.n_d;
   const double sig2 = m->sigma * m->sigma;
+  // fixed scale of the sliced kernel matrix: |k| <= sig^2 < 2^eK
+  const int eK = std::ilogb(sig2) + 1;
   if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
   FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   int base = 0;
@@ -491,12 +656,16 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                       d_var, st)))
         return rc;
     }
+    const bool var_oz = want_var && oz_var_eligible(m, s);
+    const bool var_fp64 = want_var && !var_oz;
+    const int ktiles = Ms > 0 ? m->ozS[s]->RP / oz::kTN : 0;
     for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRows) {
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
-      if ((rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms)) ||
-          (want_w && (rc = m->ws.wmat.ensure(sizeof(double) * (size_t)Mr * Ms))) ||
-          (rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr)))
+      if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * ktiles)) ||
+          (var_fp64 &&
+           (rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms))) ||
+          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, m->ws.ozK))))
         return rc;
       {
         StageTimer _pt(kStKernelGemm, st, 2);
@@ -504,8 +673,11 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                              m->ws.norms.as<double>()},
                             m->ws.ozA, st)))
           return rc;
-        oz::EpiKernel epi{m->ws.kmat.as<double>(),
-                          want_w ? m->ws.wmat.as<double>() : nullptr,
+        oz::EpiKernel epi{var_fp64 ? m->ws.kmat.as<double>() : nullptr,
+                          var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
+                          var_oz ? m->ws.ozK.scale.as<double>() : nullptr,
+                          m->ws.ozK.KP, eK,
+                          m->ws.erows.as<double>(), ktiles,
                           m->alpha.as<double>() + m->h_offsets[s],
                           m->svalid.as<unsigned char>() + m->h_offsets[s],
                           perm, m->ws.norms.as<double>(), sig2, m->power, Ms};
@@ -513,11 +685,13 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                            m->ws.ozerr.as<int>(), st)))
           return rc;
       }
-      if ((rc = launch_row_energy(Mr, Ms, m->ws.kmat.as<double>(),
-                                  m->alpha.as<double>() + m->h_offsets[s], perm,
-                                  m->ws.erows.as<double>(), d_e_atom, st)))
-        return rc;
-      if (want_var && !oz_var_eligible(m, s)) {
+      {
+        StageTimer _pt(kStRowEnergy, st);
+        oz::k_energy_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
+            Mr, ktiles, m->ws.erows.as<double>(), perm, d_e_atom);
+        FGB_LAUNCH_CHECK("k_energy_final");
+      }
+      if (var_fp64) {
         const int R = m->h_panel_rows[s];
         const int ntiles = ceil_div(R, 64);
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)) ||
@@ -528,17 +702,13 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                         perm, m->ws.norms.as<double>(), sig2,
                                         m->power, d_var, st)))
           return rc;
-      } else if (want_var) {
+      } else if (var_oz) {
         const int R = m->h_panel_rows[s];
         const int ntiles = m->ozL[s]->RP / oz::kTN;
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
           return rc;
         {
-          StageTimer _pt(kStVarianceGemm, st, 2);
-          if ((rc = oz::slice({Mr, Ms, oz::kTM, m->ws.kmat.as<double>(), Ms,
-                               nullptr, nullptr},
-                              m->ws.ozK, st)))
-            return rc;
+          StageTimer _pt(kStVarianceGemm, st);
           oz::EpiZsq epi{m->ws.part.as<double>(), ntiles, R};
           if ((rc = oz::gemm(m->ws.ozK, *m->ozL[s], true, epi,
                              m->ws.ozerr.as<int>(), st)))

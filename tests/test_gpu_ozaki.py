@@ -64,3 +64,20 @@ def test_k_limit_rejected():
     from flare_gb300 import _lib
     with pytest.raises(ValueError):
         oz(np.zeros((4, 1500)), np.zeros((4, 1500)))
+
+
+@pytest.mark.parametrize("sa,sb", [(1e-150, 1e-150), (1e150, 1e-160),
+                                   (1e100, 1e100), (2.0 ** -1000, 2.0 ** 60)])
+def test_extreme_row_scales(sa, sb):
+    """Row scales far from 1: the power-of-two scalings and the integer
+    construction of the result doubles (including results near the bottom
+    of the normal range) stay FP64-accurate."""
+    r = np.random.Generator(np.random.PCG64(11))
+    A = r.normal(size=(140, 96)) * sa
+    B = r.normal(size=(60, 96)) * sb
+    C = oz(A, B)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2e-15 * bound + 1e-300), float((err / bound).max())
