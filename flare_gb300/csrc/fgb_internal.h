@@ -28,6 +28,12 @@ struct StrucGeom {
   int sweep;        // reference image sweep (structure.cpp:35)
   int atom0, natoms;
   int bin0;         // first global bin
+  // FP32 candidate prefilter: cell rows in FP32 and squared-distance bounds
+  // that bracket the FP64 test with a margin above the FP32 rounding error
+  float cell32[9];
+  float d2_out;     // FP32 d^2 above this: certainly outside the cutoff
+  float d2_in;      // FP32 d^2 below this (and above d2_zero): certainly inside
+  float d2_zero;    // FP32 d^2 at or below this: d may be 0, test in FP64
 };
 
 // Host-side cell algebra in the canonical operation order (no FMA).
@@ -59,6 +65,7 @@ struct fgb_nlist_s {
   fgb::DevBuf geom;          // StrucGeom[n_struc]
   fgb::DevBuf atom_struct;   // int[N]
   fgb::DevBuf wrapped;       // double[N*3]
+  fgb::DevBuf wrapped32;     // float4[N]: FP32 wrapped position, image flags
   fgb::DevBuf raw_bin;       // int[N*3]
   fgb::DevBuf home_bin;      // int[N]
   fgb::DevBuf bin_slot;      // int[N]

@@ -11,6 +11,18 @@
 // |s_a| <= sweep exactly as the reference's loop bounds, and each atom's
 // segment is finally ordered by (j, s1, s2, s3) — the reference's loop
 // order.  The result is the same set, the same order and the same bits.
+//
+// FP64 arithmetic is scarce on this GPU (about 2 operations per clock per
+// SM), so every candidate is first measured in FP32 from FP32 copies of the
+// wrapped positions and the cell.  A margin well above the FP32 rounding
+// error (set per structure in make_geom) sorts candidates into certainly
+// outside, certainly inside, or near the cutoff (or near zero distance);
+// only the last class is decided by the FP64 test in the count pass, and
+// only candidates not certainly outside are evaluated in FP64 in the fill
+// pass, whose FP64 test alone decides what is written.  The fill pass
+// checks that its FP64 decisions agree with the count pass.  One warp
+// serves one atom, a lane per bin image.
+#include <limits>
 #include <mutex>
 
 #include "fgb_internal.h"
@@ -28,7 +40,8 @@ __device__ __forceinline__ int floordiv(int a, int b) {
 __global__ void k_wrap_bin(int n, const double *__restrict__ pos,
                            const int *__restrict__ atom_struct,
                            const StrucGeom *__restrict__ geom,
-                           double *__restrict__ wrapped, int *__restrict__ raw,
+                           double *__restrict__ wrapped, float4 *__restrict__ w32,
+                           int *__restrict__ raw,
                            int *__restrict__ home, int *__restrict__ slot,
                            int *__restrict__ bin_count, int *__restrict__ flag) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,20 +67,26 @@ __global__ void k_wrap_bin(int n, const double *__restrict__ pos,
   for (int k = 0; k < 3; k++)
     u[k] = __dadd_rn(__dadd_rn(__dmul_rn(f[0], g.cd[k]), __dmul_rn(f[1], g.cd[3 + k])),
                      __dmul_rn(f[2], g.cd[6 + k]));
+  double w[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++)
-    wrapped[3 * a + k] =
-        __dadd_rn(__dadd_rn(__dmul_rn(u[0], g.cti[k]), __dmul_rn(u[1], g.cti[3 + k])),
-                  __dmul_rn(u[2], g.cti[6 + k]));
-  int hb[3];
+  for (int k = 0; k < 3; k++) {
+    w[k] = __dadd_rn(__dadd_rn(__dmul_rn(u[0], g.cti[k]), __dmul_rn(u[1], g.cti[3 + k])),
+                     __dmul_rn(u[2], g.cti[6 + k]));
+    wrapped[3 * a + k] = w[k];
+  }
+  int hb[3], top = 0;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     // f in [0, 1]; raw bin in [0, nb] (nb only when f rounded up to 1.0)
     int b = (int)floor(f[k] * (double)g.nb[k]);
     b = b < 0 ? 0 : (b > g.nb[k] ? g.nb[k] : b);
     raw[3 * a + k] = b;
+    if (b == g.nb[k]) top |= 1 << k;
     hb[k] = b == g.nb[k] ? 0 : b;
   }
+  // bad positions were replaced by 0 above; keep the FP32 copy finite too
+  w32[a] = make_float4(bad ? 0.f : (float)w[0], bad ? 0.f : (float)w[1],
+                       bad ? 0.f : (float)w[2], __int_as_float(top));
   if (bad) atomicExch(flag, 1);
   int hbin = g.bin0 + (hb[0] * g.nb[1] + hb[1]) * g.nb[2] + hb[2];
   home[a] = hbin;
@@ -83,104 +102,258 @@ __global__ void k_bin_fill(int n, const int *__restrict__ home,
   bin_atoms[bin_start[home[a]] + slot[a]] = a;
 }
 
-// Visit every candidate (j, s) of atom i in the bin-image block; calls
-// fn(j, s0, s1, s2, x, y, z, d) for each pair inside the cutoff.
+// Candidate classes of the FP32 prefilter.
+enum : int { kOut = 0, kIn = 1, kNear = 2 };
+
+// Visit this lane's share of atom i's candidates (j, s): the bin images
+// lane, lane + 32, ... of the search block.  fn(j, s0, s1, s2, cls) gets every
+// candidate that passes the reference's sweep filter and is not certainly
+// outside the cutoff by the FP32 distance.
 template <typename Fn>
-__device__ __forceinline__ void visit_pairs(int i, const StrucGeom &g,
-                                            const double *__restrict__ wrapped,
-                                            const int *__restrict__ raw,
-                                            const int *__restrict__ bin_start,
-                                            const int *__restrict__ bin_atoms,
-                                            double cutoff, Fn fn) {
-  const double wi0 = wrapped[3 * i], wi1 = wrapped[3 * i + 1],
-               wi2 = wrapped[3 * i + 2];
-  const int b0 = raw[3 * i], b1 = raw[3 * i + 1], b2 = raw[3 * i + 2];
-  for (int d0 = -g.kk[0]; d0 <= g.kk[0]; d0++) {
-    int t0 = b0 + d0, h0 = t0 - floordiv(t0, g.nb[0]) * g.nb[0],
-        q0 = floordiv(t0, g.nb[0]);
-    for (int d1 = -g.kk[1]; d1 <= g.kk[1]; d1++) {
-      int t1 = b1 + d1, h1 = t1 - floordiv(t1, g.nb[1]) * g.nb[1],
-          q1 = floordiv(t1, g.nb[1]);
-      for (int d2 = -g.kk[2]; d2 <= g.kk[2]; d2++) {
-        int t2 = b2 + d2, h2 = t2 - floordiv(t2, g.nb[2]) * g.nb[2],
-            q2 = floordiv(t2, g.nb[2]);
-        int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
-        int qb = bin_start[bin], qe = bin_start[bin + 1];
-        for (int q = qb; q < qe; q++) {
-          int j = bin_atoms[q];
-          // image shift relative to j's wrapped position
-          int s0 = q0 - (raw[3 * j] == g.nb[0] ? 1 : 0);
-          int s1 = q1 - (raw[3 * j + 1] == g.nb[1] ? 1 : 0);
-          int s2 = q2 - (raw[3 * j + 2] == g.nb[2] ? 1 : 0);
-          if (s0 < -g.sweep || s0 > g.sweep || s1 < -g.sweep ||
-              s1 > g.sweep || s2 < -g.sweep || s2 > g.sweep)
-            continue;
-          const double e0 = __dsub_rn(wrapped[3 * j], wi0);
-          const double e1 = __dsub_rn(wrapped[3 * j + 1], wi1);
-          const double e2 = __dsub_rn(wrapped[3 * j + 2], wi2);
-          const double f0 = (double)s0, f1 = (double)s1, f2 = (double)s2;
-          double x = __dadd_rn(__dadd_rn(__dadd_rn(e0, __dmul_rn(f0, g.cell[0])),
-                                         __dmul_rn(f1, g.cell[3])),
-                               __dmul_rn(f2, g.cell[6]));
-          double y = __dadd_rn(__dadd_rn(__dadd_rn(e1, __dmul_rn(f0, g.cell[1])),
-                                         __dmul_rn(f1, g.cell[4])),
-                               __dmul_rn(f2, g.cell[7]));
-          double z = __dadd_rn(__dadd_rn(__dadd_rn(e2, __dmul_rn(f0, g.cell[2])),
-                                         __dmul_rn(f1, g.cell[5])),
-                               __dmul_rn(f2, g.cell[8]));
-          double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)),
-                                          __dmul_rn(z, z)));
-          if (d < cutoff && d != 0.0) fn(j, s0, s1, s2, x, y, z, d);
-        }
-      }
+__device__ __forceinline__ void visit_lane(int lane, const StrucGeom &g,
+                                           float4 wi, int b0, int b1, int b2,
+                                           const float4 *__restrict__ w32,
+                                           const int *__restrict__ bin_start,
+                                           const int *__restrict__ bin_atoms,
+                                           Fn fn) {
+  const int n0 = 2 * g.kk[0] + 1, n1 = 2 * g.kk[1] + 1, n2 = 2 * g.kk[2] + 1;
+  const int nimg = n0 * n1 * n2;
+  for (int img = lane; img < nimg; img += 32) {
+    const int d0 = img / (n1 * n2) - g.kk[0];
+    const int d1 = (img / n2) % n1 - g.kk[1];
+    const int d2 = img % n2 - g.kk[2];
+    const int t0 = b0 + d0, t1 = b1 + d1, t2 = b2 + d2;
+    const int q0 = floordiv(t0, g.nb[0]), q1 = floordiv(t1, g.nb[1]),
+              q2 = floordiv(t2, g.nb[2]);
+    const int h0 = t0 - q0 * g.nb[0], h1 = t1 - q1 * g.nb[1],
+              h2 = t2 - q2 * g.nb[2];
+    const int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
+    const int qb = bin_start[bin], qe = bin_start[bin + 1];
+    for (int q = qb; q < qe; q++) {
+      const int j = bin_atoms[q];
+      const float4 wj = w32[j];
+      const int top = __float_as_int(wj.w);
+      // image shift relative to j's wrapped position
+      const int s0 = q0 - (top & 1), s1 = q1 - ((top >> 1) & 1),
+                s2 = q2 - ((top >> 2) & 1);
+      if (s0 < -g.sweep || s0 > g.sweep || s1 < -g.sweep || s1 > g.sweep ||
+          s2 < -g.sweep || s2 > g.sweep)
+        continue;
+      const float f0 = (float)s0, f1 = (float)s1, f2 = (float)s2;
+      const float x = (wj.x - wi.x) + f0 * g.cell32[0] + f1 * g.cell32[3] +
+                      f2 * g.cell32[6];
+      const float y = (wj.y - wi.y) + f0 * g.cell32[1] + f1 * g.cell32[4] +
+                      f2 * g.cell32[7];
+      const float z = (wj.z - wi.z) + f0 * g.cell32[2] + f1 * g.cell32[5] +
+                      f2 * g.cell32[8];
+      const float d2 = x * x + y * y + z * z;
+      if (d2 > g.d2_out) continue;
+      fn(j, s0, s1, s2, (d2 < g.d2_in && d2 > g.d2_zero) ? kIn : kNear);
     }
   }
 }
 
+// The reference's FP64 test for one candidate, in its operation order;
+// returns true (and x, y, z, d) for a pair inside the cutoff.
+__device__ __forceinline__ bool exact_pair(const StrucGeom &g,
+                                           const double *__restrict__ wrapped,
+                                           double wi0, double wi1, double wi2,
+                                           int j, int s0, int s1, int s2,
+                                           double cutoff, double &x, double &y,
+                                           double &z, double &d) {
+  const double e0 = __dsub_rn(wrapped[3 * j], wi0);
+  const double e1 = __dsub_rn(wrapped[3 * j + 1], wi1);
+  const double e2 = __dsub_rn(wrapped[3 * j + 2], wi2);
+  const double f0 = (double)s0, f1 = (double)s1, f2 = (double)s2;
+  x = __dadd_rn(__dadd_rn(__dadd_rn(e0, __dmul_rn(f0, g.cell[0])),
+                          __dmul_rn(f1, g.cell[3])),
+                __dmul_rn(f2, g.cell[6]));
+  y = __dadd_rn(__dadd_rn(__dadd_rn(e1, __dmul_rn(f0, g.cell[1])),
+                          __dmul_rn(f1, g.cell[4])),
+                __dmul_rn(f2, g.cell[7]));
+  z = __dadd_rn(__dadd_rn(__dadd_rn(e2, __dmul_rn(f0, g.cell[2])),
+                          __dmul_rn(f1, g.cell[5])),
+                __dmul_rn(f2, g.cell[8]));
+  d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)),
+                           __dmul_rn(z, z)));
+  return d < cutoff && d != 0.0;
+}
+
+// Warp per atom: number of pairs.  FP64 only for candidates near the cutoff
+// or near zero distance.
 __global__ void k_count(int n, const int *__restrict__ atom_struct,
                         const StrucGeom *__restrict__ geom,
                         const double *__restrict__ wrapped,
+                        const float4 *__restrict__ w32,
                         const int *__restrict__ raw,
                         const int *__restrict__ bin_start,
                         const int *__restrict__ bin_atoms, double cutoff,
                         int *__restrict__ counts) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
   const StrucGeom &g = geom[atom_struct[i]];
+  const double wi0 = wrapped[3 * i], wi1 = wrapped[3 * i + 1],
+               wi2 = wrapped[3 * i + 2];
   int c = 0;
-  visit_pairs(i, g, wrapped, raw, bin_start, bin_atoms, cutoff,
-              [&](int, int, int, int, double, double, double, double) { c++; });
-  counts[i] = c;
+  visit_lane(lane, g, w32[i], raw[3 * i], raw[3 * i + 1], raw[3 * i + 2], w32,
+             bin_start, bin_atoms, [&](int j, int s0, int s1, int s2, int cls) {
+               double x, y, z, d;
+               if (cls == kIn ||
+                   exact_pair(g, wrapped, wi0, wi1, wi2, j, s0, s1, s2, cutoff,
+                              x, y, z, d))
+                 c++;
+             });
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  if (lane == 0) counts[i] = c;
 }
 
-__global__ void k_fill(int n, const int *__restrict__ atom_struct,
-                       const StrucGeom *__restrict__ geom,
-                       const double *__restrict__ wrapped,
-                       const int *__restrict__ raw,
-                       const int *__restrict__ bin_start,
-                       const int *__restrict__ bin_atoms, double cutoff,
-                       const long long *__restrict__ offsets,
-                       unsigned long long *__restrict__ key,
-                       double4_16a *__restrict__ rel, int *__restrict__ flag) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// One lane's position in its candidate stream: bin images lane, lane + 32,
+// ... of the search block and the atoms of the current image's bin.
+struct LaneCursor {
+  int img, q, qe, q0, q1, q2;
+};
+
+__device__ __forceinline__ void cursor_seek(LaneCursor &c, const StrucGeom &g,
+                                            int b0, int b1, int b2,
+                                            const int *__restrict__ bin_start) {
+  const int n1 = 2 * g.kk[1] + 1, n2 = 2 * g.kk[2] + 1;
+  const int nimg = (2 * g.kk[0] + 1) * n1 * n2;
+  while (c.q >= c.qe && c.img < nimg) {
+    const int d0 = c.img / (n1 * n2) - g.kk[0];
+    const int d1 = (c.img / n2) % n1 - g.kk[1];
+    const int d2 = c.img % n2 - g.kk[2];
+    const int t0 = b0 + d0, t1 = b1 + d1, t2 = b2 + d2;
+    c.q0 = floordiv(t0, g.nb[0]);
+    c.q1 = floordiv(t1, g.nb[1]);
+    c.q2 = floordiv(t2, g.nb[2]);
+    const int h0 = t0 - c.q0 * g.nb[0], h1 = t1 - c.q1 * g.nb[1],
+              h2 = t2 - c.q2 * g.nb[2];
+    const int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
+    c.q = bin_start[bin];
+    c.qe = bin_start[bin + 1];
+    c.img += 32;
+  }
+}
+
+constexpr int kFillWarps = 4;   // warps (atoms) per block of k_fill
+constexpr int kQueue = 64;      // per-warp candidate queue
+
+// Warp per atom: write the pairs (key = local j, packed shift; FP64
+// relative vector and distance) into the atom's segment; the rank sort that
+// follows puts them in canonical order.  The lanes advance through their
+// candidate streams in lockstep; candidates that pass the FP32 filter are
+// compacted into a shared-memory queue and evaluated in FP64 32 at a time,
+// so the FP64 work runs on full warps.  flag[1] is set when the FP64
+// decisions disagree with the count pass or with a certain-inside class.
+__global__ void __launch_bounds__(32 * kFillWarps)
+k_fill(int n, const int *__restrict__ atom_struct,
+       const StrucGeom *__restrict__ geom, const double *__restrict__ wrapped,
+       const float4 *__restrict__ w32, const int *__restrict__ raw,
+       const int *__restrict__ bin_start, const int *__restrict__ bin_atoms,
+       double cutoff, const long long *__restrict__ offsets,
+       unsigned long long *__restrict__ key, double4_16a *__restrict__ rel,
+       int *__restrict__ flag) {
+  __shared__ int2 queue[kFillWarps][kQueue];
+  const int wib = threadIdx.x >> 5;
+  const int i = blockIdx.x * kFillWarps + wib;
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
+  int2 *qu = queue[wib];
   const StrucGeom &g = geom[atom_struct[i]];
-  long long p = offsets[i], pend = offsets[i + 1];
-  visit_pairs(i, g, wrapped, raw, bin_start, bin_atoms, cutoff,
-              [&](int j, int s0, int s1, int s2, double x, double y, double z,
-                  double d) {
-                if (p < pend) {
-                  unsigned long long jl = (unsigned long long)(j - g.atom0);
-                  key[p] = (jl << 24) |
-                           ((unsigned long long)(s0 + 128) << 16) |
-                           ((unsigned long long)(s1 + 128) << 8) |
-                           (unsigned long long)(s2 + 128);
-                  rel[p] = make_double4_16a(d, x, y, z);
-                } else {
-                  atomicExch(flag + 1, 1);
-                }
-                p++;
-              });
+  const double wi0 = wrapped[3 * i], wi1 = wrapped[3 * i + 1],
+               wi2 = wrapped[3 * i + 2];
+  const float4 wi = w32[i];
+  const int b0 = raw[3 * i], b1 = raw[3 * i + 1], b2 = raw[3 * i + 2];
+  const long long seg = offsets[i], seg_end = offsets[i + 1];
+  const unsigned lt = (1u << lane) - 1u;
+  LaneCursor c{lane, 0, 0, 0, 0, 0};
+  cursor_seek(c, g, b0, b1, b2, bin_start);
+  int queued = 0;            // warp-uniform
+  long long written = 0;     // warp-uniform
+  bool bad = false;
+  // evaluate queue entries [0, m) in FP64, one per lane, and write the pairs
+  auto drain = [&](int m) {
+    bool in = false, certain = false;
+    int j = 0, s0 = 0, s1 = 0, s2 = 0;
+    double x = 0, y = 0, z = 0, d = 0;
+    if (lane < m) {
+      const int2 e = qu[lane];
+      j = e.x;
+      s0 = ((e.y >> 16) & 0xFF) - 128;
+      s1 = ((e.y >> 8) & 0xFF) - 128;
+      s2 = (e.y & 0xFF) - 128;
+      certain = (e.y >> 24) & 1;
+      in = exact_pair(g, wrapped, wi0, wi1, wi2, j, s0, s1, s2, cutoff, x, y,
+                      z, d);
+      if (certain && !in) bad = true;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (in) {
+      const long long p = seg + written + __popc(bal & lt);
+      if (p < seg_end) {
+        const unsigned long long jl = (unsigned long long)(j - g.atom0);
+        key[p] = (jl << 24) | ((unsigned long long)(s0 + 128) << 16) |
+                 ((unsigned long long)(s1 + 128) << 8) |
+                 (unsigned long long)(s2 + 128);
+        rel[p] = make_double4_16a(d, x, y, z);
+      } else {
+        bad = true;
+      }
+    }
+    written += __popc(bal);
+  };
+  for (;;) {
+    const bool has = c.q < c.qe;
+    if (__ballot_sync(0xffffffffu, has) == 0u) break;
+    bool pass = false;
+    int packed = 0, j = 0;
+    if (has) {
+      j = bin_atoms[c.q];
+      const float4 wj = w32[j];
+      const int top = __float_as_int(wj.w);
+      const int s0 = c.q0 - (top & 1), s1 = c.q1 - ((top >> 1) & 1),
+                s2 = c.q2 - ((top >> 2) & 1);
+      if (s0 >= -g.sweep && s0 <= g.sweep && s1 >= -g.sweep &&
+          s1 <= g.sweep && s2 >= -g.sweep && s2 <= g.sweep) {
+        const float f0 = (float)s0, f1 = (float)s1, f2 = (float)s2;
+        const float x = (wj.x - wi.x) + f0 * g.cell32[0] + f1 * g.cell32[3] +
+                        f2 * g.cell32[6];
+        const float y = (wj.y - wi.y) + f0 * g.cell32[1] + f1 * g.cell32[4] +
+                        f2 * g.cell32[7];
+        const float z = (wj.z - wi.z) + f0 * g.cell32[2] + f1 * g.cell32[5] +
+                        f2 * g.cell32[8];
+        const float d2 = x * x + y * y + z * z;
+        if (d2 <= g.d2_out) {
+          pass = true;
+          const int certain = (d2 < g.d2_in && d2 > g.d2_zero) ? 1 : 0;
+          packed = (certain << 24) | ((s0 + 128) << 16) | ((s1 + 128) << 8) |
+                   (s2 + 128);
+        }
+      }
+      c.q++;
+      cursor_seek(c, g, b0, b1, b2, bin_start);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, pass);
+    if (pass) qu[queued + __popc(bal & lt)] = make_int2(j, packed);
+    queued += __popc(bal);
+    __syncwarp();
+    if (queued >= 32) {
+      drain(32);
+      __syncwarp();
+      // move the remainder (at most 31 entries) to the front
+      int2 rest = make_int2(0, 0);
+      if (lane < queued - 32) rest = qu[32 + lane];
+      __syncwarp();
+      if (lane < queued - 32) qu[lane] = rest;
+      queued -= 32;
+      __syncwarp();
+    }
+  }
+  if (queued > 0) drain(queued);
+  if (seg + written != seg_end) bad = true;
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(flag + 1, 1);
 }
 
 // Warp per atom: rank each key within the atom's segment (keys are unique),
@@ -209,31 +382,33 @@ __global__ void k_rank_scatter(int n, const int *__restrict__ atom_struct,
   }
 }
 
-// twin of pair p = (i -> j, s) is (j -> i, -s) in j's segment.
+// twin of pair p = (i -> j, s) is (j -> i, -s) in j's segment (binary
+// search of j's sorted segment); warp per atom, lane per pair.
 __global__ void k_twin(int n, const int *__restrict__ atom_struct,
                        const StrucGeom *__restrict__ geom,
                        const long long *__restrict__ offsets,
                        const int *__restrict__ nbr_j,
                        const int *__restrict__ nbr_shift,
                        long long *__restrict__ twin, int *__restrict__ flag) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (i >= n) return;
-  int atom0 = geom[atom_struct[i]].atom0;
-  for (long long p = offsets[i]; p < offsets[i + 1]; p++) {
-    int j = nbr_j[p];
-    int sh = nbr_shift[p];
-    int s0 = ((sh >> 16) & 0xFF) - 128, s1 = ((sh >> 8) & 0xFF) - 128,
-        s2 = (sh & 0xFF) - 128;
-    unsigned long long want = ((unsigned long long)(i - atom0) << 24) |
-                              ((unsigned long long)(-s0 + 128) << 16) |
-                              ((unsigned long long)(-s1 + 128) << 8) |
-                              (unsigned long long)(-s2 + 128);
+  const int atom0 = geom[atom_struct[i]].atom0;
+  for (long long p = offsets[i] + lane; p < offsets[i + 1]; p += 32) {
+    const int j = nbr_j[p];
+    const int sh = nbr_shift[p];
+    const int s0 = ((sh >> 16) & 0xFF) - 128, s1 = ((sh >> 8) & 0xFF) - 128,
+              s2 = (sh & 0xFF) - 128;
+    const unsigned long long want = ((unsigned long long)(i - atom0) << 24) |
+                                    ((unsigned long long)(-s0 + 128) << 16) |
+                                    ((unsigned long long)(-s1 + 128) << 8) |
+                                    (unsigned long long)(-s2 + 128);
     long long lo = offsets[j], hi = offsets[j + 1] - 1, found = -1;
     while (lo <= hi) {
-      long long mid = (lo + hi) >> 1;
-      int jj = nbr_j[mid];
-      unsigned long long km = ((unsigned long long)(jj - atom0) << 24) |
-                              (unsigned long long)nbr_shift[mid];
+      const long long mid = (lo + hi) >> 1;
+      const unsigned long long km =
+          ((unsigned long long)(nbr_j[mid] - atom0) << 24) |
+          (unsigned long long)nbr_shift[mid];
       if (km == want) { found = mid; break; }
       if (km < want) lo = mid + 1; else hi = mid - 1;
     }
@@ -302,6 +477,26 @@ static void make_geom(const double *cell, double cutoff, int atom0, int natoms,
   }
   for (int k = 0; k < 3; k++)
     g.kk[k] = (int)std::floor(rc * g.nb[k] / h[k]) + 1;
+  // FP32 prefilter bounds.  Every coordinate entering a candidate's FP32
+  // difference is at most (2 + sweep) * rowsum in magnitude; the FP32 result
+  // is within 5 * 2^-24 of that per component (operand rounding and four
+  // rounded operations).  eps takes 16 * 2^-24 of a larger bound, and the
+  // distance margin 4 eps + 1e-6 cutoff covers the error of the FP32 length
+  // as well: certain-outside and certain-inside classes can never disagree
+  // with the FP64 test, and the fill pass checks that they do not.
+  double rowsum = 0.0;
+  for (int k = 0; k < 3; k++)
+    rowsum += std::sqrt(v[k][0] * v[k][0] + v[k][1] * v[k][1] + v[k][2] * v[k][2]);
+  const double lam = (2.0 + 3.0 * g.sweep) * rowsum;
+  const double eps = 16.0 * 0x1p-24 * lam;
+  const double delta = 4.0 * eps + 1e-6 * cutoff;
+  for (int k = 0; k < 9; k++) g.cell32[k] = (float)cell[k];
+  const float inf = std::numeric_limits<float>::infinity();
+  g.d2_out = std::nextafter((float)((cutoff + delta) * (cutoff + delta)), inf);
+  g.d2_in = cutoff > delta
+                ? std::nextafter((float)((cutoff - delta) * (cutoff - delta)), 0.f)
+                : 0.f;
+  g.d2_zero = std::nextafter((float)(delta * delta), inf);
   g.atom0 = atom0;
   g.natoms = natoms;
   g.bin0 = bin0;
@@ -390,6 +585,7 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
   if ((rc = nl->geom.ensure(sizeof(StrucGeom) * n_struc)) ||
       (rc = nl->atom_struct.ensure(sizeof(int) * (N + 1))) ||
       (rc = nl->wrapped.ensure(sizeof(double) * 3 * (N + 1))) ||
+      (rc = nl->wrapped32.ensure(sizeof(float4) * (N + 1))) ||
       (rc = nl->raw_bin.ensure(sizeof(int) * 3 * (N + 1))) ||
       (rc = nl->home_bin.ensure(sizeof(int) * (N + 1))) ||
       (rc = nl->bin_slot.ensure(sizeof(int) * (N + 1))) ||
@@ -416,7 +612,8 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
   }
   k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(
       N, d_positions, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
-      nl->wrapped.as<double>(), nl->raw_bin.as<int>(), nl->home_bin.as<int>(),
+      nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+      nl->raw_bin.as<int>(), nl->home_bin.as<int>(),
       nl->bin_slot.as<int>(), nl->bin_count.as<int>(), nl->flag.as<int>());
   FGB_LAUNCH_CHECK("k_wrap_bin");
   if ((rc = scan_int_to_int(nl->bin_count.as<int>(), nl->bin_start.as<int>(),
@@ -427,9 +624,11 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
       N, nl->home_bin.as<int>(), nl->bin_slot.as<int>(),
       nl->bin_start.as<int>(), nl->bin_atoms.as<int>());
   FGB_LAUNCH_CHECK("k_bin_fill");
-  k_count<<<ceil_div(N, T), T, 0, st>>>(
+  const long long NW = (long long)N * 32;   // warp per atom
+  k_count<<<ceil_div(NW, T), T, 0, st>>>(
       N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
-      nl->wrapped.as<double>(), nl->raw_bin.as<int>(), nl->bin_start.as<int>(),
+      nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+      nl->raw_bin.as<int>(), nl->bin_start.as<int>(),
       nl->bin_atoms.as<int>(), cutoff, nl->counts.as<int>());
   FGB_LAUNCH_CHECK("k_count");
   // offsets[N] receives the total pair count
@@ -457,9 +656,10 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
       (rc = nl->nbr_twin.ensure(sizeof(long long) * (P + 1))))
     return rc;
   if (P > 0) {
-    k_fill<<<ceil_div(N, T), T, 0, st>>>(
+    k_fill<<<ceil_div(N, kFillWarps), 32 * kFillWarps, 0, st>>>(
         N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
-        nl->wrapped.as<double>(), nl->raw_bin.as<int>(),
+        nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+        nl->raw_bin.as<int>(),
         nl->bin_start.as<int>(), nl->bin_atoms.as<int>(), cutoff,
         nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
         nl->tmp_rel.as<double4_16a>(), nl->flag.as<int>());
@@ -470,7 +670,7 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
         nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(), nl->nbr_shift.as<int>(),
         nl->nbr_rel.as<double4_16a>());
     FGB_LAUNCH_CHECK("k_rank_scatter");
-    k_twin<<<ceil_div(N, T), T, 0, st>>>(
+    k_twin<<<ceil_div(NW, T), T, 0, st>>>(
         N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
         nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
         nl->nbr_shift.as<int>(), nl->nbr_twin.as<long long>(),
@@ -637,6 +837,7 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
   StrucGeom *d_geom = (StrucGeom *)take(sizeof(StrucGeom));
   int *atom_struct = (int *)take(sizeof(int) * (N + 1));
   double *wrapped = (double *)take(sizeof(double) * 3 * (N + 1));
+  float4 *w32 = (float4 *)take(sizeof(float4) * (N + 1));
   int *raw = (int *)take(sizeof(int) * 3 * (N + 1));
   int *home = (int *)take(sizeof(int) * (N + 1));
   int *slot = (int *)take(sizeof(int) * (N + 1));
@@ -663,17 +864,18 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
   }
   const int T = 128;
   k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(N, d_positions, atom_struct, d_geom,
-                                           wrapped, raw, home, slot, bin_count,
-                                           flag);
+                                           wrapped, w32, raw, home, slot,
+                                           bin_count, flag);
   FGB_LAUNCH_CHECK("k_wrap_bin");
   if ((rc = scan_int_to_int_raw(bin_count, bin_start, (int)nbins,
                                 bin_start + nbins, (int *)sums, st)))
     return rc;
   k_bin_fill<<<ceil_div(N, T), T, 0, st>>>(N, home, slot, bin_start, bin_atoms);
   FGB_LAUNCH_CHECK("k_bin_fill");
-  k_count<<<ceil_div(N, T), T, 0, st>>>(N, atom_struct, d_geom, wrapped, raw,
-                                        bin_start, bin_atoms, cutoff,
-                                        d_neighbor_count);
+  const long long NW = (long long)N * 32;   // warp per atom
+  k_count<<<ceil_div(NW, T), T, 0, st>>>(N, atom_struct, d_geom, wrapped, w32,
+                                         raw, bin_start, bin_atoms, cutoff,
+                                         d_neighbor_count);
   FGB_LAUNCH_CHECK("k_count");
   if ((rc = scan_int_to_ll_raw(d_neighbor_count, offsets, N, offsets + N, sums,
                                st)))
@@ -711,9 +913,9 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
   int *nbr_j = (int *)take(sizeof(int) * (P + 1));
   int *nbr_shift = (int *)take(sizeof(int) * (P + 1));
   double4_16a *nbr_rel = (double4_16a *)take(sizeof(double4_16a) * (P + 1));
-  k_fill<<<ceil_div(N, T), T, 0, st>>>(N, atom_struct, d_geom, wrapped, raw,
-                                       bin_start, bin_atoms, cutoff, offsets,
-                                       key, tmp_rel, flag);
+  k_fill<<<ceil_div(N, kFillWarps), 32 * kFillWarps, 0, st>>>(N, atom_struct, d_geom, wrapped, w32,
+                                        raw, bin_start, bin_atoms, cutoff,
+                                        offsets, key, tmp_rel, flag);
   FGB_LAUNCH_CHECK("k_fill");
   k_rank_scatter<<<ceil_div((long long)N * 32, T), T, 0, st>>>(
       N, atom_struct, d_geom, offsets, key, tmp_rel, nbr_j, nbr_shift, nbr_rel);
