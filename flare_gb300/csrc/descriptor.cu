@@ -12,6 +12,7 @@
 // -> per pair dE/dr_ij = sum_{n,lm} u[s_j][n][lm] d(g_n Y_lm)/dr_ij, with g
 // and Y recomputed instead of stored.  Forces and the virial are assembled by
 // owner-computes over each atom's pairs and their twins (no float atomics).
+#include "fgb_df.cuh"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 
@@ -49,24 +50,50 @@ __device__ T block_sum(T v, T *red) {
   return r;
 }
 
-// Shared memory: A[nA] | g[kChunk*nmax] | Y[kChunk*nh] | sp[kChunk] | red
+// acc += a b.  FP64: one fused multiply-add.  Double-float: the exact
+// product's high part enters a TwoSum with acc.hi and every low-order term
+// collects in acc.lo, renormalised once by the caller (finish).
+__device__ __forceinline__ void mac(double &acc, double a, double b) {
+  acc += a * b;
+}
+__device__ __forceinline__ void mac(df &acc, df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float pe = __fmaf_rn(a.hi, b.hi, -p);
+  pe = __fmaf_rn(a.hi, b.lo, pe);
+  pe = __fmaf_rn(a.lo, b.hi, pe);
+  float s, se;
+  two_sum(acc.hi, p, s, se);
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(se, pe));
+}
+__device__ __forceinline__ double finish(double a) { return a; }
+__device__ __forceinline__ df finish(df a) {
+  df r;
+  fast_two_sum(a.hi, a.lo, r.hi, r.lo);
+  return r;
+}
+
+// Shared memory: A[nA] | g[kChunk*nmax] | Y[kChunk*nh] | sp[kChunk] | red,
+// in the compute type T: double (FP64 path) or df (double-float, the
+// mixed-precision path; the pair geometry arrives in FP64 and is split).
+template <typename T>
 __global__ void __launch_bounds__(kChunk)
 k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, double *__restrict__ A_out,
              double *__restrict__ B2, double *__restrict__ norms) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int i = blockIdx.x;
   if (i >= n_atoms) return;
   const int nA = p.n_A, nh = p.n_harm, nm = p.n_max;
-  double *A = smem;
-  double *sg = A + nA;
-  double *sy = sg + kChunk * nm;
+  T *A = reinterpret_cast<T *>(smem_raw);
+  T *sg = A + nA;
+  T *sy = sg + kChunk * nm;
   int *ssp = (int *)(sy + kChunk * nh);
-  double *red = (double *)(ssp + kChunk);
+  T *red = (T *)(ssp + kChunk);
   const int t = threadIdx.x;
   const int si = species[i];
-  for (int e = t; e < nA; e += blockDim.x) A[e] = 0.0;
+  for (int e = t; e < nA; e += blockDim.x) A[e] = T(0);
   const long long b = offsets[i], e_ = offsets[i + 1];
   for (long long c0 = b; c0 < e_; c0 += kChunk) {
     long long pp = c0 + t;
@@ -77,9 +104,8 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       sj = species[j];
       double rc = p.cutoffs[si * kMaxSpecies + sj];
       if (r.x <= rc) {
-        double dg[kMaxNmax];
-        radial_eval<double>(p, r.x, rc, sg + t * nm, dg);
-        ylm_eval<double>(p.l_max, r.y, r.z, r.w, sy + t * nh, nullptr);
+        radial_eval<T>(p, T(r.x), T(rc), sg + t * nm, (T *)nullptr);
+        ylm_eval<T>(p.l_max, T(r.y), T(r.z), T(r.w), sy + t * nh, nullptr);
       } else {
         sj = -1;
       }
@@ -91,28 +117,30 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       int s = e / (nm * nh);
       int n = (e / nh) % nm;
       int lm = e % nh;
-      double acc = 0.0;
+      T acc = T(0);
       for (int q = 0; q < cnt; q++)
-        if (ssp[q] == s) acc += sg[q * nm + n] * sy[q * nh + lm];
-      A[e] += acc;
+        if (ssp[q] == s) mac(acc, sg[q * nm + n], sy[q * nh + lm]);
+      A[e] += finish(acc);
     }
     __syncthreads();
   }
   if (A_out)
-    for (int e = t; e < nA; e += blockDim.x) A_out[(long long)i * nA + e] = A[e];
+    for (int e = t; e < nA; e += blockDim.x)
+      A_out[(long long)i * nA + e] = to_double(A[e]);
   const int L1 = p.l_max + 1, nr = p.n_rad, nd = p.n_d;
-  double nrm = 0.0;
+  T nrm = T(0);
   for (int q = t; q < nd; q += blockDim.x) {
     int n1, n2, l;
     decode_b2(q, L1, nr, n1, n2, l);
-    const double *a1 = A + n1 * nh + l * l, *a2 = A + n2 * nh + l * l;
-    double v = 0.0;
-    for (int m = 0; m < 2 * l + 1; m++) v += a1[m] * a2[m];
-    B2[(long long)i * nd + q] = v;
-    nrm += v * v;
+    const T *a1 = A + n1 * nh + l * l, *a2 = A + n2 * nh + l * l;
+    T v = T(0);
+    for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[m], a2[m]);
+    v = finish(v);
+    B2[(long long)i * nd + q] = to_double(v);
+    mac(nrm, v, v);
   }
-  nrm = block_sum(nrm, red);
-  if (t == 0) norms[i] = sqrt(nrm);
+  nrm = block_sum(finish(nrm), red);
+  if (t == 0) norms[i] = to_double(sqrt(nrm));
 }
 
 // Shared memory: u[nA] | A[nA] (compute type T: double, or float in the
@@ -262,20 +290,29 @@ size_t b2_adjoint_smem(const B2Params &p) {
 
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
-                      double *d_norms, cudaStream_t st) {
+                      double *d_norms, cudaStream_t st, bool dfloat) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
-  size_t sm = b2_forward_smem(p);
+  size_t sm = b2_forward_smem(p);   // sizeof(df) == sizeof(double)
   if (sm > 200 * 1024) {
     set_error("B2 settings need %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  FGB_CUDA(cudaFuncSetAttribute(k_b2_forward,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sm));
-  k_b2_forward<<<N, kChunk, sm, st>>>(
-      p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-      nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
+  if (dfloat) {
+    FGB_CUDA(cudaFuncSetAttribute(k_b2_forward<df>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
+    k_b2_forward<df><<<N, kChunk, sm, st>>>(
+        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
+  } else {
+    FGB_CUDA(cudaFuncSetAttribute(k_b2_forward<double>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
+    k_b2_forward<double><<<N, kChunk, sm, st>>>(
+        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
+  }
   FGB_LAUNCH_CHECK("k_b2_forward");
   return FGB_OK;
 }

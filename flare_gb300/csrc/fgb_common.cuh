@@ -112,7 +112,10 @@ __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
   const int N = p.n_max;
   T r1 = T(p.r1);
   if (r < r1 || r > rc) {
-    for (int n = 0; n < N; n++) { g[n] = T(0); dg[n] = T(0); }
+    for (int n = 0; n < N; n++) {
+      g[n] = T(0);
+      if (dg) dg[n] = T(0);
+    }
     return;
   }
   T c = T(1) / (rc - r1);
@@ -128,7 +131,7 @@ __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
       b0 = b1; db0 = db1; b1 = b; db1 = db;
     }
     g[n] = b * fc;
-    dg[n] = db * fc + b * dfc;
+    if (dg) dg[n] = db * fc + b * dfc;   // dg may be null (values only)
   }
 }
 

@@ -6,9 +6,10 @@ namespace fgb {
 
 size_t b2_forward_smem(const B2Params &p);
 size_t b2_adjoint_smem(const B2Params &p);
+// dfloat: compute in double-float (mixed-precision path) instead of FP64
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
-                      double *d_norms, cudaStream_t st);
+                      double *d_norms, cudaStream_t st, bool dfloat = false);
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
                       const double *d_gB2, double3 *d_pair_grad,

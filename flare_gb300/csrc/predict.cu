@@ -542,9 +542,10 @@ static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   }
   {
     StageTimer _pt(kStB2Forward, st);
+    // mixed precision: the descriptor in double-float (about 46 bits)
     if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
                                 m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-                                st)))
+                                st, precision == FGB_PREC_MIXED)))
       return rc;
   }
   std::vector<int> counts;
