@@ -62,6 +62,7 @@ SIGNATURES = {
     "fgb_envs_struc": (_i, [_vp, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_predict_plain": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_oz_dgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
+    "fgb_oz_sgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
     "fgb_serve_start": (_i, [_pvp, _vp, _i, _ll, _i, _d, _i, _i]),
     "fgb_serve_submit": (_i, [_vp, _i, _vp, _vp, _vp, _pll]),
     "fgb_serve_poll": (_i, [_vp, _ll, _pi, _vp, _vp, _vp, _vp, _pd]),

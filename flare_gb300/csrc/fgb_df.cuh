@@ -128,6 +128,18 @@ __device__ __forceinline__ df df_from_double(double d) {
   return df(hi, sign ? -lo : lo);
 }
 
+// d with its mantissa cut to 24 bits (relative error below 2^-23); FP32
+// range only, FP64 conversion otherwise.
+__device__ __forceinline__ float trunc_float(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const int e = E - 1023;
+  if (E == 0 || e < -126 || e > 127) return __double2float_rn(d);
+  return __uint_as_float(((unsigned)(b >> 63) << 31) |
+                         ((unsigned)(e + 127) << 23) |
+                         (unsigned)((b & 0xFFFFFFFFFFFFFULL) >> 29));
+}
+
 // exact FP64 value of an FP32 number (normal or zero)
 __device__ __forceinline__ double f2d_exact(float f) {
   const unsigned u = __float_as_uint(f);
@@ -155,6 +167,8 @@ __device__ __forceinline__ df pow(df a, df b) {
 }  // namespace dfm
 using dfm::df;
 using dfm::to_double;
+using dfm::trunc_float;
+using dfm::f2d_exact;
 using dfm::two_sum;
 using dfm::fast_two_sum;
 __device__ __forceinline__ double to_double(double a) { return a; }

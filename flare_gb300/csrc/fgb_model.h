@@ -15,6 +15,7 @@ struct fgb_workspace {
   fgb::DevBuf b2f, yf;           // mixed path: FP32 normalised rows, D^ B
   fgb::DevBuf dB2, fdots, fdot, dots, kern;  // plain (stored-gradient) form
   fgb::oz::Sliced ozA, ozK;      // tensor-core path: sliced rows per call
+  fgb::oz::Sliced ozA4;          // FP32-level slices of the rows (force GEMM)
   fgb::DevBuf ozerr;
 };
 
@@ -41,6 +42,8 @@ struct fgb_model_s {
   fgb::DevBuf RinvT;    // R_inv^T (M x M, lower triangular) for SOR
   bool has_rinv = false;
   fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
+  // the folded matrices in FP32-level slices (tensor-core force GEMM)
+  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB;
   bool bmap_ready = false;
   // mixed path: sliced sparse set and L_inv panels per species (tensor cores)
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS, ozL;

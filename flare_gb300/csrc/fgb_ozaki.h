@@ -1,4 +1,4 @@
-// FP64-accurate tensor-core GEMM by exact BF16 slicing (see ozaki.cu).
+// FP64- and FP32-accurate tensor-core GEMMs by exact BF16 slicing (ozaki.cu).
 #pragma once
 #include "fgb_internal.h"
 
@@ -15,6 +15,11 @@ constexpr int kStages = 4;   // shared-memory pipeline depth
 // Largest K whose group sums stay below 2^24 (exact FP32 accumulation):
 // the biggest group (a + b = 10) sums to at most 11264 * K.
 constexpr int kMaxK = 1472;
+// FP32-level configuration (force GEMM of the mixed path): 4 slices, B tiles
+// of 128 rows; the biggest group (a + b = 5) sums to at most 6144 * K.
+constexpr int kSF32 = 4;
+constexpr int kTNF32 = 128;
+constexpr int kMaxKF32 = 2720;
 
 struct SliceSpec {
   int rows, K, TR;
@@ -25,18 +30,23 @@ struct SliceSpec {
 };
 
 struct Sliced {
-  int rows = 0, K = 0, TR = 0, RP = 0, KP = 0;
+  int rows = 0, K = 0, TR = 0, RP = 0, KP = 0, S = 0;
   DevBuf q;       // bf16 slices, tiled canonical layout
   DevBuf scale;   // per-row 2^e
 };
 
 int pad_to(int x, int m);
-// Size `out` for rows x K slices (no conversion).
-int prepare(int rows, int K, int TR, Sliced &out);
-int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st);
+// Size `out` for rows x K in S slices (no conversion).
+int prepare(int rows, int K, int TR, int S, Sliced &out);
+// Slice rows into S = kS (FP64-level) or kSF32 (FP32-level) digits.
+int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S = kS);
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
          cudaStream_t st);
+// Y (A.rows x B.rows, leading dimension ldy) = A B^T rounded to FP32, from
+// kSF32-slice operands (A tiles of kTM rows, B tiles of kTNF32 rows).
+int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
+             int *err, cudaStream_t st);
 
 }  // namespace oz
 }  // namespace fgb

@@ -10,12 +10,18 @@
 //   power 2:  E_i = sigma^2 d^_i^T B_s d^_i,  B_s = S^_s^T diag(alpha_s) S^_s
 //             dE/dd^ = 2 sigma^2 B_s d^   (one FP32 GEMM, n_d x n_d per species)
 //   power 1:  E_i = sigma^2 beta_s . d^_i,  beta_s = S^_s^T alpha_s
-// B_s / beta_s are built once per model in FP64 on the GPU and rounded to
-// FP32.  dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d|; the per-pair adjoint then
-// runs in FP32.  Other powers use the FP64 kernel, adjoint and variance GEMMs.
+// B_s / beta_s are built once per model in FP64 on the GPU; B_s is kept in
+// FP32-level exact slices for the tensor-core GEMM Y = D^ B_s (ozaki.cu, 4
+// slices, 10 pair products, exact accumulation; FP32 SIMT GEMM when n_d
+// exceeds that kernel's K limit) and beta_s in FP32.
+// dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d| in FP32; the per-pair adjoint
+// then runs in FP32.  Other powers use the FP64 kernel, adjoint and variance
+// GEMMs.
+#include "fgb_df.cuh"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 #include "fgb_model.h"
+#include "fgb_ozaki.h"
 #include "fgb_gemm64.cuh"
 #include "fgb_profile.h"
 
@@ -40,10 +46,11 @@ __global__ void k_scaled_transpose(int M, int nd, const double *__restrict__ S,
   STa[(long long)q * M + t] = valid[t] ? v * alpha[t] : 0.0;
 }
 
-// B = ST STa^T (nd x nd), written as FP32.
+// B = ST STa^T (nd x nd), written as FP32 and as FP64.
 __global__ void __launch_bounds__(GT)
 k_fold_gemm(int nd, int M, const double *__restrict__ ST,
-            const double *__restrict__ STa, float *__restrict__ B) {
+            const double *__restrict__ STa, float *__restrict__ B,
+            double *__restrict__ Bd) {
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   double acc[4][4];
   gemm_mainloop<true>(acc, m0, n0, nd, nd, M, ST, M, nullptr, STa, M);
@@ -55,7 +62,10 @@ k_fold_gemm(int nd, int M, const double *__restrict__ ST,
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       int n = n0 + tx + 16 * j;
-      if (n < nd) B[(long long)m * nd + n] = (float)acc[i][j];
+      if (n < nd) {
+        B[(long long)m * nd + n] = (float)acc[i][j];
+        Bd[(long long)m * nd + n] = acc[i][j];
+      }
     }
   }
 }
@@ -107,29 +117,32 @@ k_mapped_gemm(int Mr, int nd, const float *__restrict__ Dh,
 }
 
 // dE/dB2 rows from g = dE/dd^ (power 2: g = 2 sig2 Y; power 1: g = sig2 beta)
-// warp per row: q = d^ . g, dE/dB2 = (g - q d^) / |d|
+// warp per row: d^ = B2 / |d| in FP32 (mantissa cut, no FP64 arithmetic),
+// q = d^ . g, dE/dB2 = (g - q d^) / |d|.
 __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
                               const double *__restrict__ norms,
-                              const float *__restrict__ Dh,
+                              const double *__restrict__ B2,
                               const float *__restrict__ Y,
                               const float *__restrict__ beta, float scale,
                               double *__restrict__ gB2) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= Mr) return;
-  const float *d = Dh + (long long)warp * nd;
+  const int atom = perm[warp];
+  const double n = norms[atom];
+  const bool ok = n >= kEmptyThresh;
+  const float inv = ok ? __frcp_rn(trunc_float(n)) : 0.f;
+  const double *b = B2 + (long long)atom * nd;
   const float *y = Y ? Y + (long long)warp * nd : nullptr;
   float q = 0.f;
-  for (int k = lane; k < nd; k += 32) q += d[k] * (y ? y[k] : beta[k]);
+  for (int k = lane; k < nd; k += 32)
+    q = __fmaf_rn(trunc_float(b[k]) * inv, y ? y[k] : beta[k], q);
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
-  int atom = perm[warp];
-  double n = norms[atom];
-  double inv = n >= kEmptyThresh ? 1.0 / n : 0.0;
   for (int k = lane; k < nd; k += 32) {
-    float g = scale * (y ? y[k] : beta[k]);
-    float v = g - scale * q * d[k];
-    gB2[(long long)atom * nd + k] = (double)v * inv;
+    const float d = trunc_float(b[k]) * inv;
+    const float g = scale * (y ? y[k] : beta[k]);
+    gB2[(long long)atom * nd + k] = f2d_exact((g - scale * q * d) * inv);
   }
 }
 
@@ -143,15 +156,18 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
   int rc;
   if ((rc = m->Bmap.ensure(sizeof(float) * (per * S + 1)))) return rc;
   FGB_CUDA(cudaMemsetAsync(m->Bmap.p, 0, sizeof(float) * per * S, st));
-  DevBuf ST, STa;
+  DevBuf ST, STa, Bd;
+  m->ozB.clear();
   for (int s = 0; s < S; s++) {
+    m->ozB.emplace_back(new oz::Sliced());
     const int Ms = m->h_counts[s], c = m->h_offsets[s];
     if (Ms == 0) continue;
     const double *Ss = m->S.as<double>() + (size_t)c * nd;
     float *Bs = m->Bmap.as<float>() + per * s;
     if (quad) {
       if ((rc = ST.ensure(sizeof(double) * (size_t)Ms * nd)) ||
-          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)))
+          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)) ||
+          (rc = Bd.ensure(sizeof(double) * (size_t)nd * nd)))
         return rc;
       k_scaled_transpose<<<ceil_div((long long)Ms * nd, 256), 256, 0, st>>>(
           Ms, nd, Ss, m->alpha.as<double>() + c,
@@ -159,9 +175,15 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
       FGB_LAUNCH_CHECK("k_scaled_transpose");
       dim3 g(ceil_div(nd, BN), ceil_div(nd, BM));
       k_fold_gemm<<<g, GT, 0, st>>>(nd, Ms, ST.as<double>(), STa.as<double>(),
-                                    Bs);
+                                    Bs, Bd.as<double>());
       FGB_LAUNCH_CHECK("k_fold_gemm");
-      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa reused next species
+      // B_s is symmetric: its rows are the B operand of Y = D^ B_s
+      if (nd <= oz::kMaxKF32 &&
+          (rc = oz::slice({nd, nd, oz::kTNF32, Bd.as<double>(), nd, nullptr,
+                           nullptr},
+                          *m->ozB[s], st, oz::kSF32)))
+        return rc;
+      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa/Bd reused next species
     } else {
       k_fold_vec<<<ceil_div(nd, 128), 128, 0, st>>>(
           Ms, nd, Ss, m->alpha.as<double>() + c,
@@ -195,6 +217,10 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   const bool quad = m->power == 2.0;
   const float sig2 = (float)(m->sigma * m->sigma);
   const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
+  if (quad && nd <= oz::kMaxKF32) {
+    if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
+    FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
+  }
   int base = 0;
   for (int s = 0; s < p.n_species; s++) {
     const int Ns = counts[s];
@@ -202,28 +228,48 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
     base += Ns;
     if (Ns == 0 || m->h_counts[s] == 0) continue;   // gB2 stays zero
     const float *Bs = m->Bmap.as<float>() + per * s;
+    const bool tc_gemm = quad && nd <= oz::kMaxKF32;
     for (int r0 = 0; r0 < Ns; r0 += kRowChunkMixed) {
       const int Mr = std::min(kRowChunkMixed, Ns - r0);
       const int *perm = perm_s + r0;
-      if ((rc = m->ws.b2f.ensure(sizeof(float) * (size_t)Mr * nd)) ||
-          (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
+      if ((quad && (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd))) ||
+          (quad && !tc_gemm &&
+           (rc = m->ws.b2f.ensure(sizeof(float) * (size_t)Mr * nd))))
         return rc;
-      StageTimer _pt(kStMappedGemm, st, quad ? 3 : 2);
-      k_gather_dhat<<<ceil_div((long long)Mr * nd, 256), 256, 0, st>>>(
-          Mr, nd, perm, m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-          m->ws.b2f.as<float>());
-      FGB_LAUNCH_CHECK("k_gather_dhat");
-      if (quad) {
+      StageTimer _pt(kStMappedGemm, st, tc_gemm ? 3 : (quad ? 3 : 1));
+      if (tc_gemm) {
+        // Y = D^ B_s on the tensor cores (FP32-level exact slices)
+        if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
+                             m->ws.norms.as<double>()},
+                            m->ws.ozA4, st, oz::kSF32)) ||
+            (rc = oz::gemm_f32(m->ws.ozA4, *m->ozB[s], m->ws.yf.as<float>(),
+                               nd, m->ws.ozerr.as<int>(), st)))
+          return rc;
+      } else if (quad) {
+        k_gather_dhat<<<ceil_div((long long)Mr * nd, 256), 256, 0, st>>>(
+            Mr, nd, perm, m->ws.B2.as<double>(), m->ws.norms.as<double>(),
+            m->ws.b2f.as<float>());
+        FGB_LAUNCH_CHECK("k_gather_dhat");
         dim3 g(ceil_div(nd, BN), ceil_div(Mr, BM));
         k_mapped_gemm<<<g, GT, 0, st>>>(Mr, nd, m->ws.b2f.as<float>(), Bs,
                                         m->ws.yf.as<float>());
         FGB_LAUNCH_CHECK("k_mapped_gemm");
       }
       k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
-          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.b2f.as<float>(),
+          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
           quad ? m->ws.yf.as<float>() : nullptr, quad ? nullptr : Bs,
           quad ? 2.f * sig2 : sig2, d_gB2);
       FGB_LAUNCH_CHECK("k_mapped_grad");
+    }
+  }
+  if (quad && nd <= oz::kMaxKF32) {
+    int h = 0;
+    FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+    if (h) {
+      set_error("tensor-core force GEMM: a bounded device wait ran out");
+      return FGB_ETIMEOUT;
     }
   }
   return FGB_OK;

@@ -1,29 +1,30 @@
-// FP64-accurate GEMM on the BF16 tensor cores (tcgen05), by exact integer
-// slicing (the Ozaki scheme).
+// FP64-accurate (and FP32-accurate) GEMMs on the BF16 tensor cores
+// (tcgen05), by exact integer slicing (the Ozaki scheme).
 //
 // Each row of A (M x K) and of B (N x K) is scaled by a power of two so its
-// entries lie in (-1, 1), then split into S = 9 slices of BETA = 6 bits:
+// entries lie in (-1, 1), then split into S slices of BETA = 6 bits:
 // x = sum_a q_a 2^(-6a) + r, |q_1| <= 64, |q_a| <= 32 (a > 1), each q an
 // integer held exactly in BF16.  The products q_a q_b are exact in FP32 and,
-// for K <= 1472, every partial sum of a group (all pairs with the same
-// a + b) stays below 2^24, so the tensor core's FP32 accumulation is exact
-// too.  All 45 pairs with a + b <= S + 1 are accumulated into 9 group
-// accumulators held in TMEM (9 x 48 FP32 columns per 128-row tile), and the
-// epilogue recombines C = 2^(e_row + e_col) sum_t 2^(-6t) group_t exactly in
-// 64-bit integers, rounding once to FP64.
-// The dropped terms (a + b > 10) and the slice residuals are below 2^-54 of
-// each row's largest entry — FP64-level accuracy, measured on the sparse-GP
-// kernel and variance products (energy 5e-10 eV/atom, variance 2e-14).
+// for K up to the configuration's limit, every partial sum of a group (all
+// pairs with the same t = a + b) stays below 2^24, so the tensor core's FP32
+// accumulation is exact too.  The S (S + 1) / 2 pairs with a + b <= S + 1 are
+// accumulated into S group accumulators held in TMEM (S x TN FP32 columns
+// per 128-row tile), and the epilogue recombines
+// C = 2^(e_row + e_col) sum_t 2^(-6t) group_t exactly in 64-bit integers,
+// rounding once to FP64 or FP32.  The dropped terms (a + b > S + 1) and the
+// slice residuals are below 2^(-6S) of each row's largest entry.
+//   S = 9, TN = 48:  FP64-level (2^-54); kernel and variance products of the
+//                    sparse GP (energy 4e-12 eV/atom, std 4e-13 against FP64)
+//   S = 4, TN = 128: FP32-level (2^-24); the alpha-folded force GEMM
 //
 // Data movement: slices are written by k_oz_slice directly in the tensor
 // core's no-swizzle K-major canonical layout (8 x 16-byte core matrices),
-// tiled so that the 9 slices of every (128-row tile, 16-wide k chunk) are one
-// contiguous 36 KB block (13.5 KB for the 48-row B tiles).  One thread streams
-// each chunk with two cp.async.bulk copies into a 4-stage shared-memory
-// ring (mbarrier transaction counts), issues the chunk's 45 pair products as
-// 13 tcgen05.mma with the B slices stacked along N (mma_kstep) and commits
-// them to the stage's "consumed" mbarrier; every wait is bounded and reports
-// through `err`.
+// tiled so that the S slices of every (row tile, 16-wide k chunk) are one
+// contiguous block.  One thread streams each chunk with two cp.async.bulk
+// copies into a shared-memory ring (mbarrier transaction counts), issues the
+// chunk's pair products as tcgen05.mma with the B slices stacked along N
+// (mma_kstep) and commits them to the stage's "consumed" mbarrier; every
+// wait is bounded and reports through `err`.
 #include <cuda_bf16.h>
 
 #include "fgb_internal.h"
@@ -35,66 +36,99 @@ namespace oz {
 
 namespace {
 
-constexpr uint32_t kTileA = kTM * kKC * 2;               // bytes
-constexpr uint32_t kTileB = kTN * kKC * 2;
-constexpr uint32_t kStage = kS * (kTileA + kTileB);
-constexpr uint32_t kSmem = kStages * kStage + 256;
 constexpr uint32_t kTmemCols = 512;
 constexpr long long kWaitLimit = 1LL << 22;
-static_assert(kG * kTN <= (int)kTmemCols, "group accumulators exceed TMEM");
-static_assert(kSmem <= 227 * 1024, "stages exceed shared memory");
+
+// Largest per-k contribution to one group: sum over its pairs of
+// max|q_a| max|q_b| (64 for the first digit, 32 for the others).
+__host__ __device__ constexpr int max_group_weight(int S) {
+  int best = 0;
+  for (int t = 2; t <= S + 1; t++) {
+    int w = 0;
+    for (int a = 1; a <= S; a++) {
+      const int b = t - a;
+      if (b < 1 || b > S) continue;
+      w += (a == 1 ? 64 : 32) * (b == 1 ? 64 : 32);
+    }
+    best = w > best ? w : best;
+  }
+  return best;
+}
+
+// A tile configuration: S slices, TN columns of B per CTA, STAGES ring depth.
+template <int S_, int TN_, int STAGES_, int MAXK_>
+struct Cfg {
+  static constexpr int S = S_, TN = TN_, STAGES = STAGES_, MAXK = MAXK_;
+  static constexpr uint32_t TileA = kTM * kKC * 2;   // bytes per slice
+  static constexpr uint32_t TileB = TN * kKC * 2;
+  static constexpr uint32_t Stage = S * (TileA + TileB);
+  static constexpr uint32_t Smem = STAGES * Stage + 256;
+  // groups t = 2 .. TSPLIT go to the high integer, the rest to the low one
+  static constexpr int TSPLIT = S + 1 < 6 ? S + 1 : 6;
+  static constexpr bool HAS_LO = TSPLIT < S + 1;
+  static_assert(S * TN <= (int)kTmemCols, "group accumulators exceed TMEM");
+  static_assert(Smem <= 227 * 1024, "stages exceed shared memory");
+  static_assert(TN % 16 == 0 && TN <= 256, "MMA N");
+  static_assert((long long)MAXK * max_group_weight(S) < (1LL << 24),
+                "group sums must stay exact in FP32");
+};
+using CfgF64 = Cfg<kS, kTN, kStages, kMaxK>;
+using CfgF32 = Cfg<4, 128, 6, 2720>;
 static_assert(kKC % 16 == 0, "a chunk is whole MMA k-steps");
-static_assert(kS == 9 && kBeta == 6 && kTN % 16 == 0,
-              "the exact recombination assumes 9 slices of 6 bits");
+static_assert(kBeta == 6, "digits of 6 bits");
 
 // One tcgen05.mma covering the pairs (A, B0) .. (A, B0 + NB - 1).  The B
-// slices of a stage sit one after another in shared memory (each 48 rows of
+// slices of a stage sit one after another in shared memory (each TN rows of
 // 8-row core-matrix groups, 256 bytes apart), so NB consecutive slices are a
-// single N = 48 NB operand; their products belong to the consecutive groups
-// A + B0 .. A + B0 + NB - 1, whose accumulators are consecutive 48-column
+// single N = TN NB operand; their products belong to the consecutive groups
+// A + B0 .. A + B0 + NB - 1, whose accumulators are consecutive TN-column
 // blocks of TMEM.  An M = 128 MMA costs max(64, N / 2) cycles, so stacking
-// slices keeps every instruction at N >= 96 where the plan allows.
-template <int A, int B0, int NB>
+// slices keeps instructions wide.
+template <class C, int A, int B0, int NB>
 __device__ __forceinline__ void mma_span(uint32_t tmem, uint64_t ad0,
                                          uint64_t bd0, bool first) {
-  static_assert(A >= 0 && B0 >= 0 && NB >= 1 && A + B0 + NB <= kS,
-                "span outside the 45 pairs with a + b <= kS + 1");
-  static_assert(NB * kTN <= 256, "an M = 128 MMA takes N <= 256");
+  static_assert(A >= 0 && B0 >= 0 && NB >= 1 && A + B0 + NB <= C::S,
+                "span outside the pairs with a + b <= S + 1");
+  static_assert(NB * C::TN <= 256, "an M = 128 MMA takes N <= 256");
   // descriptor start addresses are in 16-byte units in the low bits
-  tc::mma_bf16(tmem + (uint32_t)((A + B0) * kTN),
-               ad0 + (uint64_t)((A * kTileA) >> 4),
-               bd0 + (uint64_t)((B0 * kTileB) >> 4),
-               tc::idesc_bf16_f32(kTM, NB * kTN),
+  tc::mma_bf16(tmem + (uint32_t)((A + B0) * C::TN),
+               ad0 + (uint64_t)((A * C::TileA) >> 4),
+               bd0 + (uint64_t)((B0 * C::TileB) >> 4),
+               tc::idesc_bf16_f32(kTM, NB * C::TN),
                (A == 0 && first) ? 0u : 1u);
 }
 
-// All 45 pairs of one 16-deep k-step as 13 MMAs.  A slice a pairs with B
-// slices 0 .. kS-1-a; each row below splits that range into spans of at most
-// five slices (N <= 240).  The two a = 0 spans together cover every group, so
-// with `first` set they initialise all nine accumulators.
+// All pairs of one 16-deep k-step.  A slice a pairs with B slices
+// 0 .. S-1-a, split into the fewest spans of at most 256 / TN slices, of
+// near-equal width (S = 9, TN = 48: 13 MMAs; S = 4, TN = 128: 6).  The a = 0
+// spans together cover every group, so with `first` set they initialise all
+// accumulators.
+template <class C, int A = 0, int B0 = 0>
 __device__ __forceinline__ void mma_kstep(uint32_t tmem, uint64_t ad0,
                                           uint64_t bd0, bool first) {
-  mma_span<0, 0, 5>(tmem, ad0, bd0, first);
-  mma_span<0, 5, 4>(tmem, ad0, bd0, first);
-  mma_span<1, 0, 4>(tmem, ad0, bd0, first);
-  mma_span<1, 4, 4>(tmem, ad0, bd0, first);
-  mma_span<2, 0, 4>(tmem, ad0, bd0, first);
-  mma_span<2, 4, 3>(tmem, ad0, bd0, first);
-  mma_span<3, 0, 3>(tmem, ad0, bd0, first);
-  mma_span<3, 3, 3>(tmem, ad0, bd0, first);
-  mma_span<4, 0, 5>(tmem, ad0, bd0, first);
-  mma_span<5, 0, 4>(tmem, ad0, bd0, first);
-  mma_span<6, 0, 3>(tmem, ad0, bd0, first);
-  mma_span<7, 0, 2>(tmem, ad0, bd0, first);
-  mma_span<8, 0, 1>(tmem, ad0, bd0, first);
+  if constexpr (A < C::S) {
+    constexpr int total = C::S - A;               // B slices for this A
+    constexpr int maxnb = 256 / C::TN;
+    constexpr int nspans = (total + maxnb - 1) / maxnb;
+    constexpr int width = (total + nspans - 1) / nspans;
+    constexpr int rem = total - B0;
+    if constexpr (rem > 0) {
+      constexpr int nb = rem < width ? rem : width;
+      mma_span<C, A, B0, nb>(tmem, ad0, bd0, first);
+      mma_kstep<C, A, B0 + nb>(tmem, ad0, bd0, first);
+    } else {
+      mma_kstep<C, A + 1, 0>(tmem, ad0, bd0, first);
+    }
+  }
 }
 
-// Slice storage, chunk-major: the kS slices of one (row tile, 16-wide k chunk)
-// are one contiguous block (kS tiles of TR x 16 in the canonical layout), so a
+// Slice storage, chunk-major: the S slices of one (row tile, 16-wide k chunk)
+// are one contiguous block (S tiles of TR x 16 in the canonical layout), so a
 // pipeline stage is filled by a single bulk copy per operand.  Returns the
 // element index of (m, k) in slice 0; slice a sits a * TR * 16 further on.
+template <int S>
 __device__ __forceinline__ size_t tiled_index(int m, int k, int KP, int TR) {
-  return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(kS * TR * kKC) +
+  return ((size_t)(m / TR) * (KP / kKC) + k / kKC) * (size_t)(S * TR * kKC) +
          (size_t)(((m % TR) / 8) * (kKC / 8) + (k % kKC) / 8) * 64 +
          (m % 8) * 8 + (k % 8);
 }
@@ -122,6 +156,14 @@ __device__ __forceinline__ double exact_scaled(long long x, int sc) {
                             ((a << (52 - p)) & 0xFFFFFFFFFFFFFULL);
   if (x < 0) bits |= 1ULL << 63;
   return __longlong_as_double(bits);
+}
+
+// x 2^sc rounded once to FP32.
+__device__ __forceinline__ float scaled_float(long long x, int sc) {
+  const float f = __ll2float_rn(x);
+  if (sc >= -126 && sc <= 127)
+    return __fmul_rn(f, __uint_as_float((unsigned)(sc + 127) << 23));
+  return ldexpf(f, sc);
 }
 
 // rn(d 2^sh) as a 64-bit integer (nearest, ties to even, as __double2ll_rn
@@ -154,14 +196,15 @@ __device__ __forceinline__ uint32_t bf16_bits(long long q) {
   return __float_as_uint(__int2float_rn((int)q)) >> 16;
 }
 
-// The kS base-64 digits of X (|X| < 2^54) for 8 consecutive k, stored as
+// The S base-64 digits of X (|X| < 2^(6S)) for 8 consecutive k, stored as
 // 16-byte rows of the canonical layout: slice a at out + a * stride.
+template <int S>
 __device__ __forceinline__ void store_digits8(long long (&X)[8],
                                               __nv_bfloat16 *out,
                                               size_t stride) {
 #pragma unroll
-  for (int a = 1; a <= kS; a++) {
-    const int sh = 54 - kBeta * a;
+  for (int a = 1; a <= S; a++) {
+    const int sh = kBeta * (S - a);
     uint32_t w[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
@@ -176,13 +219,14 @@ __device__ __forceinline__ void store_digits8(long long (&X)[8],
   }
 }
 
-// Warp per row: scale to (-1, 1) by a power of two, split into kS slices.
-// The scaled value y is taken as the integer X = rn(y 2^54) (exact for
-// |y| >= 2^-1 of the row's top binade, rounded at 2^-54 below that); the
-// 9 slices are the base-64 digits of X, each rounded to nearest, extracted
-// with 64-bit integer arithmetic: q_a = round(R / 2^(54-6a)), R -= q_a 2^(54-6a).
-// Each lane converts 8 consecutive k and writes one 16-byte core-matrix row
-// per slice.
+// Warp per row: scale to (-1, 1) by a power of two, split into S slices.
+// The scaled value y is taken as the integer X = rn(y 2^(6S)) (exact for
+// |y| >= 2^-1 of the row's top binade, rounded at 2^(-6S) below that); the
+// slices are the base-64 digits of X, each rounded to nearest, extracted
+// with 64-bit integer arithmetic: q_a = round(R / 2^(6(S-a))),
+// R -= q_a 2^(6(S-a)).  Each lane converts 8 consecutive k and writes one
+// 16-byte core-matrix row per slice.
+template <int S>
 __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
                            const double *__restrict__ src, long long ld,
                            const int *__restrict__ perm,
@@ -224,36 +268,37 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
       const int k = k0 + j;
       X[j] = (valid && k < K)
                  ? fixed_rn(rownorm ? src[row * ld + k] * inv : src[row * ld + k],
-                            54 - e)
+                            kBeta * S - e)
                  : 0;
     }
-    store_digits8(X, out + tiled_index(m, k0, KP, TR), stride);
+    store_digits8<S>(X, out + tiled_index<S>(m, k0, KP, TR), stride);
   }
 }
 
-template <class Epi>
+template <class C, class Epi>
 __global__ void __launch_bounds__(128, 1)
-k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
+k_oz_gemm(int M, int N, int K, int KP,
           const __nv_bfloat16 *__restrict__ Asl,
           const double *__restrict__ Ascale,
           const __nv_bfloat16 *__restrict__ Bsl,
           const double *__restrict__ Bscale, int tri, Epi epi,
           int *__restrict__ err) {
+  constexpr int S = C::S, TN = C::TN, NST = C::STAGES;
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + kStages * kStage);
-  uint64_t *bar_mma = bar_load + kStages;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + kStages);
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + NST * C::Stage);
+  uint64_t *bar_mma = bar_load + NST;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + NST);
   int *ok_slot = reinterpret_cast<int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nt = blockIdx.x, mt = blockIdx.y;
-  const int m0 = mt * kTM, n0 = nt * kTN;
+  const int m0 = mt * kTM, n0 = nt * TN;
 
   if (warp == 0) {
     tc::tmem_alloc(tmem_slot, kTmemCols);
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int b = 0; b < kStages; b++) {
+    for (int b = 0; b < NST; b++) {
       tc::mbar_init(&bar_load[b], 1);
       tc::mbar_init(&bar_mma[b], 1);
     }
@@ -265,50 +310,50 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  const int kmax = tri ? min(K, n0 + kTN) : K;
+  const int kmax = tri ? min(K, n0 + TN) : K;
   const int nch = (kmax + kKC - 1) / kKC;
   const int KCH = KP / kKC;
 
   if (tid == 0) {
-    // Ring of kStages stages.  Chunk c lives in stage c % kStages; its
-    // barriers complete once per use, so the parity for chunk c is
-    // (c / kStages) & 1.  MMAs of chunk c are issued as soon as its data has
-    // landed; only then does the thread wait for chunk c-1's MMAs, which
-    // frees that stage for chunk c + kStages - 1.  The tensor pipe always
-    // has the next chunk queued and kStages - 1 loads stay in flight.
+    // Ring of NST stages.  Chunk c lives in stage c % NST; its barriers
+    // complete once per use, so the parity for chunk c is (c / NST) & 1.
+    // MMAs of chunk c are issued as soon as its data has landed; only then
+    // does the thread wait for chunk c-1's MMAs, which frees that stage for
+    // chunk c + NST - 1.  The tensor pipe always has the next chunk queued
+    // and NST - 1 loads stay in flight.
     bool ok = true;
     int issued = 0;   // loads issued so far (chunks 0 .. issued-1)
     auto issue_load = [&](int c) {
-      const int b = c % kStages;
-      unsigned char *st = smem + b * kStage;
-      tc::mbar_expect_tx(&bar_load[b], kStage);
-      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + c) * (kS * kTM * kKC),
-                   kS * kTileA, &bar_load[b]);
-      tc::bulk_g2s(st + kS * kTileA,
-                   Bsl + ((size_t)nt * KCH + c) * (kS * kTN * kKC),
-                   kS * kTileB, &bar_load[b]);
+      const int b = c % NST;
+      unsigned char *st = smem + b * C::Stage;
+      tc::mbar_expect_tx(&bar_load[b], C::Stage);
+      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + c) * (S * kTM * kKC),
+                   S * C::TileA, &bar_load[b]);
+      tc::bulk_g2s(st + S * C::TileA,
+                   Bsl + ((size_t)nt * KCH + c) * (S * TN * kKC),
+                   S * C::TileB, &bar_load[b]);
     };
-    for (; issued < nch && issued < kStages - 1; issued++) issue_load(issued);
+    for (; issued < nch && issued < NST - 1; issued++) issue_load(issued);
     int mma_done = 0;   // chunks whose MMAs are known complete
     for (int c = 0; c < nch; c++) {
-      const int b = c % kStages;
-      if (!tc::mbar_wait(&bar_load[b], (c / kStages) & 1, kWaitLimit)) { ok = false; break; }
+      const int b = c % NST;
+      if (!tc::mbar_wait(&bar_load[b], (c / NST) & 1, kWaitLimit)) { ok = false; break; }
       tc::fence_after_sync();
-      const uint32_t aBase = tc::smem_u32(smem + b * kStage);
+      const uint32_t aBase = tc::smem_u32(smem + b * C::Stage);
       const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
-      const uint64_t bd0 = tc::smem_desc(aBase + kS * kTileA, 128,
+      const uint64_t bd0 = tc::smem_desc(aBase + S * C::TileA, 128,
                                          (kKC / 8) * 128);
       // k-steps of 16 are two core matrices (256 bytes) apart along K
 #pragma unroll
       for (int kk = 0; kk < kKC / 16; kk++)
-        mma_kstep(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
-                  bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
+        mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
+                     bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
       tc::mma_commit(&bar_mma[b]);
       if (issued < nch) {
-        // the stage for chunk `issued` was last used by chunk issued-kStages
-        const int prev = issued - kStages;
+        // the stage for chunk `issued` was last used by chunk issued-NST
+        const int prev = issued - NST;
         if (prev >= 0) {
-          if (!tc::mbar_wait(&bar_mma[prev % kStages], (prev / kStages) & 1,
+          if (!tc::mbar_wait(&bar_mma[prev % NST], (prev / NST) & 1,
                              kWaitLimit)) { ok = false; break; }
           mma_done = prev + 1;
         }
@@ -321,7 +366,7 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
     // issued load, bounded, before the accumulators are read or TMEM freed.
     const int last = ok ? nch : 0;
     for (int c = mma_done; c < last; c++)
-      if (!tc::mbar_wait(&bar_mma[c % kStages], (c / kStages) & 1, kWaitLimit)) { ok = false; break; }
+      if (!tc::mbar_wait(&bar_mma[c % NST], (c / NST) & 1, kWaitLimit)) { ok = false; break; }
     if (nch == 0) ok = false;   // nothing accumulated: the host handles K == 0
     if (!ok) {
       *ok_slot = 0;
@@ -334,43 +379,56 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   const bool ok = *ok_slot != 0;
   if (ok) {
     // Group sums are exact integers below 2^24; recombine them exactly in
-    // two 64-bit integers, hi = sum_{t=2..6} g_t 2^(6(6-t)) and
-    // lo = sum_{t=7..10} g_t 2^(6(10-t)), then C = (hi 2^-36 + lo 2^-60)
-    // 2^(e_row + e_col): two exact doubles built from the integers and one
-    // correctly rounded addition.  Rows past M (tile padding) still run the
-    // epilogue so that functors can write zero padding.
+    // 64-bit integers, hi = sum_{t <= TSPLIT} g_t 2^(6(TSPLIT-t)) and
+    // lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), so that
+    // C = (hi 2^(-6 TSPLIT) + lo 2^(-6(S+1))) 2^(e_row + e_col): exact
+    // doubles built from the integers and one correctly rounded addition
+    // (FP64 results), or one rounding of hi (FP32 results, no low part).
+    // Rows past M (tile padding) still run the epilogue so that functors can
+    // write zero padding.
     const int m = m0 + warp * 32 + lane;
     const bool row_ok = m < M;
     const int er = pow2_exp(Ascale[m]);
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     double acc = 0.0;
 #pragma unroll 1
-    for (int c0 = 0; c0 < kTN; c0 += 16) {
+    for (int c0 = 0; c0 < TN; c0 += 16) {
       long long hi[16], lo[16];
 #pragma unroll
       for (int j = 0; j < 16; j++) { hi[j] = 0; lo[j] = 0; }
 #pragma unroll
-      for (int g = 0; g < kG; g++) {
+      for (int g = 0; g < S; g++) {
         uint32_t r[16];
-        tc::tmem_ld16(trow + g * kTN + c0, r);
+        tc::tmem_ld16(trow + g * TN + c0, r);
         tc::tmem_ld_wait();
         const int t = g + 2;
 #pragma unroll
         for (int j = 0; j < 16; j++) {
           const long long q = (long long)__float2int_rn(__uint_as_float(r[j]));
-          if (t <= 6) hi[j] += q << (6 * (6 - t));
-          else lo[j] += q << (6 * (10 - t));
+          if (t <= C::TSPLIT) hi[j] += q << (6 * (C::TSPLIT - t));
+          else lo[j] += q << (6 * (S + 1 - t));
         }
       }
-      double v[16];
+      if constexpr (Epi::kFloat) {
+        static_assert(!C::HAS_LO, "FP32 results take configurations of at most 5 slices");
+        float v[16];
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int e = er + pow2_exp(Bscale[n0 + c0 + j]);
-        v[j] = exact_scaled(hi[j], e - 36) + exact_scaled(lo[j], e - 60);
+        for (int j = 0; j < 16; j++)
+          v[j] = scaled_float(hi[j], er + pow2_exp(Bscale[n0 + c0 + j]) -
+                                         6 * C::TSPLIT);
+        epi.chunk(m, row_ok, n0 + c0, v);
+      } else {
+        double v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int e = er + pow2_exp(Bscale[n0 + c0 + j]);
+          v[j] = exact_scaled(hi[j], e - 6 * C::TSPLIT);
+          if constexpr (C::HAS_LO) v[j] += exact_scaled(lo[j], e - 6 * (S + 1));
+        }
+        acc = epi.chunk(m, row_ok, n0 + c0, v, acc);
       }
-      acc = epi.chunk(m, row_ok, n0 + c0, v, acc);
     }
-    epi.finish(m, row_ok, n0, acc);
+    if constexpr (!Epi::kFloat) epi.finish(m, row_ok, n0, acc);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -378,8 +436,9 @@ k_oz_gemm(int M, int N, int K, int KP, int MP, int NP,
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
-// Plain product C = A B^T.
+// Plain product C = A B^T (FP64).
 struct EpiStore {
+  static constexpr bool kFloat = false;
   double *C;
   long long ldc;
   int N;
@@ -396,28 +455,46 @@ struct EpiStore {
   __device__ void finish(int, bool, int, double) const {}
 };
 
+// Plain product Y = A B^T rounded to FP32.
+struct EpiStoreF32 {
+  static constexpr bool kFloat = true;
+  float *Y;
+  long long ldy;
+  int N;
+  __device__ void chunk(int m, bool row_ok, int n0, const float (&v)[16]) const {
+    if (!row_ok) return;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      int n = n0 + j;
+      if (n < N) Y[(long long)m * ldy + n] = v[j];
+    }
+  }
+};
+
 }  // namespace
 
 int pad_to(int x, int m) { return (x + m - 1) / m * m; }
 
-int prepare(int rows, int K, int TR, Sliced &out) {
+int prepare(int rows, int K, int TR, int S, Sliced &out) {
   out.rows = rows;
   out.K = K;
   out.TR = TR;
+  out.S = S;
   out.RP = pad_to(std::max(rows, 1), TR);
   out.KP = pad_to(std::max(K, 1), kKC);
   int rc;
-  if ((rc = out.q.ensure(sizeof(__nv_bfloat16) * (size_t)kS * out.RP * out.KP)) ||
+  if ((rc = out.q.ensure(sizeof(__nv_bfloat16) * (size_t)S * out.RP * out.KP)) ||
       (rc = out.scale.ensure(sizeof(double) * (size_t)out.RP)))
     return rc;
   return FGB_OK;
 }
 
-int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
+template <int S>
+static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   int rc;
-  if ((rc = prepare(sp.rows, sp.K, sp.TR, out))) return rc;
+  if ((rc = prepare(sp.rows, sp.K, sp.TR, S, out))) return rc;
   const long long threads = (long long)out.RP * 32;
-  k_oz_slice<<<ceil_div(threads, 256), 256, 0, st>>>(
+  k_oz_slice<S><<<ceil_div(threads, 256), 256, 0, st>>>(
       sp.rows, sp.K, out.RP, out.KP, sp.TR, sp.src, sp.ld, sp.perm,
       sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
       out.scale.as<double>());
@@ -425,29 +502,47 @@ int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   return FGB_OK;
 }
 
-template <class Epi>
-int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
-         cudaStream_t st) {
-  if (A.K != B.K || A.KP != B.KP || A.TR != kTM || B.TR != kTN) {
+int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S) {
+  if (S == kS) return slice_s<kS>(sp, out, st);
+  if (S == kSF32) return slice_s<kSF32>(sp, out, st);
+  set_error("ozaki slice: unsupported slice count %d", S);
+  return FGB_EINVAL;
+}
+
+template <class C, class Epi>
+static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
+                  int *err, cudaStream_t st) {
+  if (A.K != B.K || A.KP != B.KP || A.TR != kTM || B.TR != C::TN ||
+      A.S != C::S || B.S != C::S) {
     set_error("ozaki gemm: operand layouts disagree");
     return FGB_EINVAL;
   }
-  if (A.K > kMaxK) {
+  if (A.K > C::MAXK) {
     set_error("ozaki gemm: K = %d exceeds the exact-accumulation limit %d",
-              A.K, kMaxK);
+              A.K, C::MAXK);
     return FGB_EINVAL;
   }
   if (A.rows == 0 || B.rows == 0) return FGB_OK;
-  FGB_CUDA(cudaFuncSetAttribute(k_oz_gemm<Epi>,
+  FGB_CUDA(cudaFuncSetAttribute(k_oz_gemm<C, Epi>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kSmem));
-  dim3 grid(B.RP / kTN, A.RP / kTM);
-  k_oz_gemm<Epi><<<grid, 128, kSmem, st>>>(
-      A.rows, B.rows, A.K, A.KP, A.RP, B.RP, A.q.as<__nv_bfloat16>(),
-      A.scale.as<double>(), B.q.as<__nv_bfloat16>(), B.scale.as<double>(),
-      tri ? 1 : 0, epi, err);
+                                (int)C::Smem));
+  dim3 grid(B.RP / C::TN, A.RP / kTM);
+  k_oz_gemm<C, Epi><<<grid, 128, C::Smem, st>>>(
+      A.rows, B.rows, A.K, A.KP, A.q.as<__nv_bfloat16>(), A.scale.as<double>(),
+      B.q.as<__nv_bfloat16>(), B.scale.as<double>(), tri ? 1 : 0, epi, err);
   FGB_LAUNCH_CHECK("k_oz_gemm");
   return FGB_OK;
+}
+
+template <class Epi>
+int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
+         cudaStream_t st) {
+  return gemm_c<CfgF64>(A, B, tri, epi, err, st);
+}
+
+int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
+             int *err, cudaStream_t st) {
+  return gemm_c<CfgF32>(A, B, false, EpiStoreF32{Y, ldy, B.rows}, err, st);
 }
 
 }  // namespace oz
@@ -495,6 +590,47 @@ extern "C" int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A,
   return FGB_OK;
 }
 
+extern "C" int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A,
+                               long long lda, const double *d_B, long long ldb,
+                               float *d_C, long long ldc, void *stream) {
+  if (M < 0 || N < 0 || K < 0 || (M && N && (!d_A || !d_B || !d_C))) {
+    set_error("fgb_oz_sgemm_nt: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (K > oz::kMaxKF32) {
+    set_error("fgb_oz_sgemm_nt: K = %d exceeds the exact-accumulation limit "
+              "%d", K, oz::kMaxKF32);
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (M == 0 || N == 0) return FGB_OK;
+  if (K == 0) {
+    for (int m = 0; m < M; m++)
+      FGB_CUDA(cudaMemsetAsync(d_C + (long long)m * ldc, 0, sizeof(float) * N,
+                               st));
+    return FGB_OK;
+  }
+  oz::Sliced A, B;
+  DevBuf err;
+  int rc;
+  if ((rc = err.ensure(sizeof(int)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  if ((rc = oz::slice({M, K, oz::kTM, d_A, lda, nullptr, nullptr}, A, st,
+                      oz::kSF32)) ||
+      (rc = oz::slice({N, K, oz::kTNF32, d_B, ldb, nullptr, nullptr}, B, st,
+                      oz::kSF32)))
+    return rc;
+  if ((rc = oz::gemm_f32(A, B, d_C, ldc, err.as<int>(), st))) return rc;
+  int h = 0;
+  FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("fgb_oz_sgemm_nt: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
+  return FGB_OK;
+}
+
 // ------------------------------------------------------------------------
 // Sparse-GP stages on the tensor cores (mixed precision mode).
 #include "fgb_gemm64.cuh"
@@ -514,6 +650,7 @@ namespace {
 // K = N padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64
 // matrix is written only when the variance runs in FP64.
 struct EpiKernel {
+  static constexpr bool kFloat = false;
   double *Kd;                 // optional M x N FP64 kernel matrix
   __nv_bfloat16 *Ksl;         // optional slices of K (variance A operand)
   double *Kscale;             // their row scales (all 2^eK)
@@ -546,7 +683,7 @@ struct EpiKernel {
         long long X[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], 54 - eK);
-        store_digits8(X, Ksl + tiled_index(m, n0 + 8 * h, KPv, kTM),
+        store_digits8<kS>(X, Ksl + tiled_index<kS>(m, n0 + 8 * h, KPv, kTM),
                       (size_t)kTM * kKC);
       }
     }
@@ -560,6 +697,7 @@ struct EpiKernel {
 
 // Variance GEMM epilogue: per-row sum of z^2 over this tile's columns.
 struct EpiZsq {
+  static constexpr bool kFloat = false;
   double *part;
   int ntiles, R;
   __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
@@ -665,7 +803,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * ktiles)) ||
           (var_fp64 &&
            (rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms))) ||
-          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, m->ws.ozK))))
+          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, oz::kS, m->ws.ozK))))
         return rc;
       {
         StageTimer _pt(kStKernelGemm, st, 2);

@@ -50,7 +50,9 @@ enum {
 /* prediction precision */
 enum {
   FGB_PREC_FP64 = 0,  /* FP64 adjoint path                                   */
-  FGB_PREC_MIXED = 1  /* FP64 descriptors/variance, FP32 tensor-core E and F */
+  FGB_PREC_MIXED = 1  /* double-float descriptors, FP64-accurate tensor-core
+                         kernel/variance GEMMs (exact slicing), FP32-level
+                         tensor-core force GEMM and FP32 adjoint            */
 };
 
 /* prediction outputs */
@@ -264,6 +266,14 @@ int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
  * The kernel used for the sparse-GP kernel and variance products. */
 int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A, long long lda,
                     const double *d_B, long long ldb, double *d_C,
+                    long long ldc, void *stream);
+
+/* C = A B^T in FP32 accuracy on the same tensor-core kernel with 4 slices
+ * (10 slice products, exact accumulation), FP64 inputs, FP32 output
+ * C[M x N] (ldc); K <= 2720.  The kernel used for the force GEMM of the
+ * mixed-precision path.  No reference counterpart (an internal product). */
+int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A, long long lda,
+                    const double *d_B, long long ldb, float *d_C,
                     long long ldc, void *stream);
 
 /* SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 on the GPU:

@@ -81,3 +81,54 @@ def test_extreme_row_scales(sa, sb):
         np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
     err = np.abs(C - ref)
     assert np.all(err <= 2e-15 * bound + 1e-300), float((err / bound).max())
+
+
+def oz32(A, B):
+    import torch
+    from flare_gb300 import _lib
+    M, K = A.shape
+    N = B.shape[0]
+    dA = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    dC = torch.full((max(M, 1), max(N, 1)), np.nan, dtype=torch.float32,
+                    device="cuda")
+    _lib.check(_lib.lib().fgb_oz_sgemm_nt(M, N, K, _lib.ptr(dA), K,
+                                          _lib.ptr(dB), K, _lib.ptr(dC),
+                                          max(N, 1), _lib.stream_ptr()))
+    torch.cuda.synchronize()
+    return dC.cpu().numpy()[:M, :N].astype(np.float64)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 16), (300, 200, 680),
+                                   (1000, 385, 385), (5, 3, 17)])
+def test_fp32_level_accuracy(M, N, K):
+    """4-slice configuration: the dropped digit products and slice residuals
+    are below 2^-24 of the row maxima, and the result is rounded once to
+    FP32."""
+    r = np.random.Generator(np.random.PCG64(M + 3 * N))
+    A = r.normal(size=(M, K)) * np.exp(r.uniform(-3, 1, size=(M, K)))
+    B = r.normal(size=(N, K)) * np.exp(r.uniform(-3, 1, size=(N, K)))
+    C = oz32(A, B)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2.0 ** -22 * bound + 2.0 ** -24 * np.abs(ref)), \
+        float((err / bound).max())
+
+
+def test_fp32_level_integer_products_exact():
+    """Integers of at most 24 bits in 4 digits: products exact, sums exact,
+    and small enough to be exact in FP32."""
+    r = np.random.Generator(np.random.PCG64(5))
+    A = r.integers(-1000, 1001, size=(130, 256)).astype(np.float64)
+    B = r.integers(-30, 31, size=(140, 256)).astype(np.float64)
+    C = oz32(A, B)
+    exact = (A.astype(np.int64) @ B.astype(np.int64).T).astype(np.float64)
+    assert np.abs(exact).max() < 2 ** 24
+    np.testing.assert_array_equal(C, exact)
+
+
+def test_fp32_level_k_limit_rejected():
+    with pytest.raises(ValueError):
+        oz32(np.zeros((4, 2736)), np.zeros((4, 2736)))

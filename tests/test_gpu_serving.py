@@ -40,10 +40,13 @@ def test_serving_same_alone_and_in_the_mix(precision):
     ids = [None] * len(reqs)
 
     def producer():
+        # a burst of 16 (queued while the workers run their first batches),
+        # then Poisson arrivals that land while other batches are on the GPU
         r = np.random.Generator(np.random.PCG64(7))
         for k, (cell, sp, pos) in enumerate(reqs):
             ids[k] = srv.submit(cell, sp, pos)
-            time.sleep(float(r.exponential(0.002)))   # Poisson arrivals
+            if k >= 16:
+                time.sleep(float(r.exponential(0.002)))
 
     t = threading.Thread(target=producer)
     t.start()
