@@ -12,6 +12,8 @@ constexpr int kTM = 128;     // A rows per tile (TMEM lanes)
 constexpr int kTN = 48;      // B rows per tile (columns per group)
 constexpr int kKC = 16;      // k per pipeline stage (one MMA k-step)
 constexpr int kStages = 4;   // shared-memory pipeline depth
+constexpr int kEpiWarps = 3; // epilogue warps per TMEM lane quarter (16 columns
+                             // each); partial sums per row: B tiles x kEpiWarps
 // Largest K whose group sums stay below 2^24 (exact FP32 accumulation):
 // the biggest group (a + b = 10) sums to at most 11264 * K.
 constexpr int kMaxK = 1472;

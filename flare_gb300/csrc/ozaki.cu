@@ -55,10 +55,14 @@ __host__ __device__ constexpr int max_group_weight(int S) {
   return best;
 }
 
-// A tile configuration: S slices, TN columns of B per CTA, STAGES ring depth.
-template <int S_, int TN_, int STAGES_, int MAXK_>
+// A tile configuration: S slices, TN columns of B per CTA, STAGES ring
+// depth, EW epilogue warps per TMEM lane quarter (each takes TN / EW columns).
+template <int S_, int TN_, int STAGES_, int MAXK_, int EW_>
 struct Cfg {
   static constexpr int S = S_, TN = TN_, STAGES = STAGES_, MAXK = MAXK_;
+  static constexpr int EW = EW_;
+  static constexpr int THREADS = 32 * (1 + 4 * EW);
+  static constexpr int WCOLS = TN / EW;   // columns per epilogue warp
   static constexpr uint32_t TileA = kTM * kKC * 2;   // bytes per slice
   static constexpr uint32_t TileB = TN * kKC * 2;
   static constexpr uint32_t Stage = S * (TileA + TileB);
@@ -71,9 +75,10 @@ struct Cfg {
   static_assert(TN % 16 == 0 && TN <= 256, "MMA N");
   static_assert((long long)MAXK * max_group_weight(S) < (1LL << 24),
                 "group sums must stay exact in FP32");
+  static_assert(TN % (16 * EW) == 0, "epilogue warps take whole 16-column chunks");
 };
-using CfgF64 = Cfg<kS, kTN, kStages, kMaxK>;
-using CfgF32 = Cfg<4, 128, 6, 2720>;
+using CfgF64 = Cfg<kS, kTN, kStages, kMaxK, kEpiWarps>;
+using CfgF32 = Cfg<kSF32, kTNF32, 6, kMaxKF32, 2>;
 static_assert(kKC % 16 == 0, "a chunk is whole MMA k-steps");
 static_assert(kBeta == 6, "digits of 6 bits");
 
@@ -275,23 +280,45 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
   }
 }
 
+// Persistent, warp-specialised GEMM: one CTA per SM walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... (B tiles fastest).
+//   warp 0, lane 0  streams chunks into the shared-memory ring and issues the
+//                   MMAs; the ring runs on across tile boundaries, so the next
+//                   tile's first chunks are already loaded when its MMAs may
+//                   start.
+//   warps 1..4 EW   the epilogue: warp w reads TMEM lanes 32 (w % 4) ...
+//                   (the hardware's lane quarter for that warp) and columns
+//                   [sub WCOLS, (sub + 1) WCOLS) with sub = (w - 1) / 4.
+//                   Phase 1 drains its part of the accumulator into registers
+//                   (exact integer recombination) and releases it
+//                   (acc_empty); phase 2 (the functor's arithmetic and
+//                   stores, latency-bound) then overlaps the next tile's MMAs,
+//                   with EW warps per quarter to hide its latency.
+// Barriers: load_full / load_empty per ring stage (transaction bytes; MMA
+// commit), acc_full (commit after a tile's last MMAs), acc_empty (one arrive
+// per epilogue warp).  Every wait is bounded; a producer that gives up sets
+// the CTA's abort flag, which the epilogue polls, waits (bounded) for its own
+// copies and MMAs in flight, and reports through `err`.  Energy and variance
+// partials are written per (tile, epilogue warp): NTt * EW slots per row.
 template <class C, class Epi>
-__global__ void __launch_bounds__(128, 1)
-k_oz_gemm(int M, int N, int K, int KP,
+__global__ void __launch_bounds__(C::THREADS, 1)
+k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
           const __nv_bfloat16 *__restrict__ Asl,
           const double *__restrict__ Ascale,
           const __nv_bfloat16 *__restrict__ Bsl,
           const double *__restrict__ Bscale, int tri, Epi epi,
           int *__restrict__ err) {
-  constexpr int S = C::S, TN = C::TN, NST = C::STAGES;
+  constexpr int S = C::S, TN = C::TN, NST = C::STAGES, NCH = C::WCOLS / 16;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + NST * C::Stage);
   uint64_t *bar_mma = bar_load + NST;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + NST);
-  int *ok_slot = reinterpret_cast<int *>(tmem_slot + 1);
+  uint64_t *acc_full = bar_mma + NST;
+  uint64_t *acc_empty = acc_full + 1;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nt = blockIdx.x, mt = blockIdx.y;
-  const int m0 = mt * kTM, n0 = nt * TN;
+  const int ntiles = MT * NTt;
+  const int KCH = KP / kKC;
 
   if (warp == 0) {
     tc::tmem_alloc(tmem_slot, kTmemCols);
@@ -302,133 +329,161 @@ k_oz_gemm(int M, int N, int K, int KP,
       tc::mbar_init(&bar_load[b], 1);
       tc::mbar_init(&bar_mma[b], 1);
     }
+    tc::mbar_init(acc_full, 1);
+    tc::mbar_init(acc_empty, 4 * C::EW);
     tc::mbar_fence_init();
-    *ok_slot = 1;
+    *abort_flag = 0;
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  const int kmax = tri ? min(K, n0 + TN) : K;
-  const int nch = (kmax + kKC - 1) / kKC;
-  const int KCH = KP / kKC;
+  // chunks of tile t (triangular B: columns n0 .. n0+TN-1 need k < n0 + TN)
+  auto tile_nch = [&](int t) {
+    const int n0 = (t % NTt) * TN;
+    const int kmax = tri ? min(K, n0 + TN) : K;
+    return (kmax + kKC - 1) / kKC;
+  };
 
-  if (tid == 0) {
-    // Ring of NST stages.  Chunk c lives in stage c % NST; its barriers
-    // complete once per use, so the parity for chunk c is (c / NST) & 1.
-    // MMAs of chunk c are issued as soon as its data has landed; only then
-    // does the thread wait for chunk c-1's MMAs, which frees that stage for
-    // chunk c + NST - 1.  The tensor pipe always has the next chunk queued
-    // and NST - 1 loads stay in flight.
+  if (warp == 0 && lane == 0) {
     bool ok = true;
-    int issued = 0;   // loads issued so far (chunks 0 .. issued-1)
-    auto issue_load = [&](int c) {
-      const int b = c % NST;
+    int lt = blockIdx.x, lc = 0;     // tile and chunk of the next load
+    long long nl = 0, nm = 0;        // loads issued, chunks consumed
+    auto issue_load = [&]() {
+      const int b = (int)(nl % NST);
       unsigned char *st = smem + b * C::Stage;
+      const int mt = lt / NTt, nt = lt % NTt;
       tc::mbar_expect_tx(&bar_load[b], C::Stage);
-      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + c) * (S * kTM * kKC),
+      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + lc) * (S * kTM * kKC),
                    S * C::TileA, &bar_load[b]);
       tc::bulk_g2s(st + S * C::TileA,
-                   Bsl + ((size_t)nt * KCH + c) * (S * TN * kKC),
+                   Bsl + ((size_t)nt * KCH + lc) * (S * TN * kKC),
                    S * C::TileB, &bar_load[b]);
+      nl++;
+      if (++lc == tile_nch(lt)) { lc = 0; lt += gridDim.x; }
     };
-    for (; issued < nch && issued < NST - 1; issued++) issue_load(issued);
-    int mma_done = 0;   // chunks whose MMAs are known complete
-    for (int c = 0; c < nch; c++) {
-      const int b = c % NST;
-      if (!tc::mbar_wait(&bar_load[b], (c / NST) & 1, kWaitLimit)) { ok = false; break; }
-      tc::fence_after_sync();
-      const uint32_t aBase = tc::smem_u32(smem + b * C::Stage);
-      const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
-      const uint64_t bd0 = tc::smem_desc(aBase + S * C::TileA, 128,
-                                         (kKC / 8) * 128);
-      // k-steps of 16 are two core matrices (256 bytes) apart along K
+    while (nl < NST - 1 && lt < ntiles) issue_load();
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, it++) {
+      const int nch = tile_nch(t);
+      if (it > 0) {
+        // the previous tile's accumulator must be drained by the epilogue
+        if (!tc::mbar_wait(acc_empty, (it - 1) & 1, kWaitLimit)) { ok = false; break; }
+        tc::fence_after_sync();
+      }
+      for (int c = 0; c < nch; c++) {
+        const int b = (int)(nm % NST);
+        if (!tc::mbar_wait(&bar_load[b], (uint32_t)((nm / NST) & 1), kWaitLimit)) { ok = false; break; }
+        tc::fence_after_sync();
+        const uint32_t aBase = tc::smem_u32(smem + b * C::Stage);
+        const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
+        const uint64_t bd0 = tc::smem_desc(aBase + S * C::TileA, 128,
+                                           (kKC / 8) * 128);
+        // k-steps of 16 are two core matrices (256 bytes) apart along K
 #pragma unroll
-      for (int kk = 0; kk < kKC / 16; kk++)
-        mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
-                     bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
-      tc::mma_commit(&bar_mma[b]);
-      if (issued < nch) {
-        // the stage for chunk `issued` was last used by chunk issued-NST
-        const int prev = issued - NST;
-        if (prev >= 0) {
-          if (!tc::mbar_wait(&bar_mma[prev % NST], (prev / NST) & 1,
+        for (int kk = 0; kk < kKC / 16; kk++)
+          mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
+                       bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
+        tc::mma_commit(&bar_mma[b]);
+        if (c == nch - 1) tc::mma_commit(acc_full);
+        nm++;
+        if (lt < ntiles) {
+          // load nl reuses the stage of chunk nl - NST, the chunk before the
+          // one just issued: wait for that chunk's MMAs (nothing to wait for
+          // before the ring has wrapped)
+          const long long prev = nl - NST;
+          if (prev >= 0 &&
+              !tc::mbar_wait(&bar_mma[prev % NST], (uint32_t)((prev / NST) & 1),
                              kWaitLimit)) { ok = false; break; }
-          mma_done = prev + 1;
+          issue_load();
         }
-        issue_load(issued);
-        issued++;
       }
     }
-    // Drain: every outstanding MMA (waiting on the last commit covers all
-    // earlier ones, but each barrier phase is consumed in order) and every
-    // issued load, bounded, before the accumulators are read or TMEM freed.
-    const int last = ok ? nch : 0;
-    for (int c = mma_done; c < last; c++)
-      if (!tc::mbar_wait(&bar_mma[c % NST], (c / NST) & 1, kWaitLimit)) { ok = false; break; }
-    if (nch == 0) ok = false;   // nothing accumulated: the host handles K == 0
     if (!ok) {
-      *ok_slot = 0;
-      if (nch > 0) atomicExch(err, 1);
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      // copies in flight land before the CTA may exit; MMAs finish before
+      // TMEM is freed (bounded waits)
+      for (long long g = nm; g < nl; g++)
+        tc::mbar_wait(&bar_load[g % NST], (uint32_t)((g / NST) & 1), kWaitLimit);
+      if (nm > 0)
+        tc::mbar_wait(&bar_mma[(nm - 1) % NST], (uint32_t)(((nm - 1) / NST) & 1),
+                      kWaitLimit);
     }
-  }
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const bool ok = *ok_slot != 0;
-  if (ok) {
-    // Group sums are exact integers below 2^24; recombine them exactly in
-    // 64-bit integers, hi = sum_{t <= TSPLIT} g_t 2^(6(TSPLIT-t)) and
-    // lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), so that
-    // C = (hi 2^(-6 TSPLIT) + lo 2^(-6(S+1))) 2^(e_row + e_col): exact
-    // doubles built from the integers and one correctly rounded addition
-    // (FP64 results), or one rounding of hi (FP32 results, no low part).
-    // Rows past M (tile padding) still run the epilogue so that functors can
-    // write zero padding.
-    const int m = m0 + warp * 32 + lane;
-    const bool row_ok = m < M;
-    const int er = pow2_exp(Ascale[m]);
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    double acc = 0.0;
-#pragma unroll 1
-    for (int c0 = 0; c0 < TN; c0 += 16) {
-      long long hi[16], lo[16];
+  } else if (warp >= 1) {
+    const int q = warp & 3;            // TMEM lane quarter of this warp
+    const int sub = (warp - 1) >> 2;   // its column range within the tile
+    const int c_lo = sub * C::WCOLS;
+    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+      bool got = false;
+      for (long long i = 0; i < kWaitLimit; i++) {
+        if (tc::mbar_try_wait(acc_full, it & 1)) { got = true; break; }
+        if (*abort_flag) break;
+      }
+      if (!got) {
+        if (!*abort_flag) atomicExch(err, 1);
+        break;
+      }
+      tc::fence_after_sync();
+      const int m0 = (t / NTt) * kTM, n0 = (t % NTt) * TN;
+      const int m = m0 + q * 32 + lane;
+      const bool row_ok = m < M;
+      const int er = pow2_exp(Ascale[m]);
+      // Phase 1.  Group sums are exact integers below 2^24; recombine them
+      // exactly in 64-bit integers, hi = sum_{t <= TSPLIT} g_t 2^(6(TSPLIT-t))
+      // and lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), so that
+      // C = (hi 2^(-6 TSPLIT) + lo 2^(-6(S+1))) 2^(e_row + e_col): exact
+      // doubles built from the integers and one correctly rounded addition
+      // (FP64 results), or one rounding of hi (FP32 results, no low part).
+      // Rows past M (tile padding) still run so that functors can write
+      // zero padding.
+      using V = typename Epi::Value;
+      V v[NCH][16];
 #pragma unroll
-      for (int j = 0; j < 16; j++) { hi[j] = 0; lo[j] = 0; }
+      for (int ch = 0; ch < NCH; ch++) {
+        long long hi[16], lo[16];
 #pragma unroll
-      for (int g = 0; g < S; g++) {
-        uint32_t r[16];
-        tc::tmem_ld16(trow + g * TN + c0, r);
-        tc::tmem_ld_wait();
-        const int t = g + 2;
+        for (int j = 0; j < 16; j++) { hi[j] = 0; lo[j] = 0; }
+#pragma unroll
+        for (int g = 0; g < S; g++) {
+          uint32_t r[16];
+          tc::tmem_ld16(trow + g * TN + c_lo + ch * 16, r);
+          tc::tmem_ld_wait();
+          const int tg = g + 2;
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const long long qv = (long long)__float2int_rn(__uint_as_float(r[j]));
+            if (tg <= C::TSPLIT) hi[j] += qv << (6 * (C::TSPLIT - tg));
+            else lo[j] += qv << (6 * (S + 1 - tg));
+          }
+        }
 #pragma unroll
         for (int j = 0; j < 16; j++) {
-          const long long q = (long long)__float2int_rn(__uint_as_float(r[j]));
-          if (t <= C::TSPLIT) hi[j] += q << (6 * (C::TSPLIT - t));
-          else lo[j] += q << (6 * (S + 1 - t));
+          const int e = er + pow2_exp(Bscale[n0 + c_lo + ch * 16 + j]);
+          if constexpr (Epi::kFloat) {
+            static_assert(!C::HAS_LO, "FP32 results take at most 5 slices");
+            v[ch][j] = scaled_float(hi[j], e - 6 * C::TSPLIT);
+          } else {
+            double x = exact_scaled(hi[j], e - 6 * C::TSPLIT);
+            if constexpr (C::HAS_LO) x += exact_scaled(lo[j], e - 6 * (S + 1));
+            v[ch][j] = x;
+          }
         }
       }
-      if constexpr (Epi::kFloat) {
-        static_assert(!C::HAS_LO, "FP32 results take configurations of at most 5 slices");
-        float v[16];
+      // the accumulator may now take the next tile
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(acc_empty);
+      // Phase 2
+      double acc = 0.0;
 #pragma unroll
-        for (int j = 0; j < 16; j++)
-          v[j] = scaled_float(hi[j], er + pow2_exp(Bscale[n0 + c0 + j]) -
-                                         6 * C::TSPLIT);
-        epi.chunk(m, row_ok, n0 + c0, v);
-      } else {
-        double v[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int e = er + pow2_exp(Bscale[n0 + c0 + j]);
-          v[j] = exact_scaled(hi[j], e - 6 * C::TSPLIT);
-          if constexpr (C::HAS_LO) v[j] += exact_scaled(lo[j], e - 6 * (S + 1));
-        }
-        acc = epi.chunk(m, row_ok, n0 + c0, v, acc);
-      }
+      for (int ch = 0; ch < NCH; ch++)
+        acc = epi.chunk(m, row_ok, n0 + c_lo + ch * 16, v[ch], acc);
+      epi.finish(m, row_ok, (t % NTt) * C::EW + sub, acc);
     }
-    if constexpr (!Epi::kFloat) epi.finish(m, row_ok, n0, acc);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -438,6 +493,7 @@ k_oz_gemm(int M, int N, int K, int KP,
 
 // Plain product C = A B^T (FP64).
 struct EpiStore {
+  using Value = double;
   static constexpr bool kFloat = false;
   double *C;
   long long ldc;
@@ -457,18 +513,22 @@ struct EpiStore {
 
 // Plain product Y = A B^T rounded to FP32.
 struct EpiStoreF32 {
+  using Value = float;
   static constexpr bool kFloat = true;
   float *Y;
   long long ldy;
   int N;
-  __device__ void chunk(int m, bool row_ok, int n0, const float (&v)[16]) const {
-    if (!row_ok) return;
+  __device__ double chunk(int m, bool row_ok, int n0, const float (&v)[16],
+                          double acc) const {
+    if (!row_ok) return acc;
 #pragma unroll
     for (int j = 0; j < 16; j++) {
       int n = n0 + j;
       if (n < N) Y[(long long)m * ldy + n] = v[j];
     }
+    return acc;
   }
+  __device__ void finish(int, bool, int, double) const {}
 };
 
 }  // namespace
@@ -526,10 +586,15 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
   FGB_CUDA(cudaFuncSetAttribute(k_oz_gemm<C, Epi>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)C::Smem));
-  dim3 grid(B.RP / C::TN, A.RP / kTM);
-  k_oz_gemm<C, Epi><<<grid, 128, C::Smem, st>>>(
-      A.rows, B.rows, A.K, A.KP, A.q.as<__nv_bfloat16>(), A.scale.as<double>(),
-      B.q.as<__nv_bfloat16>(), B.scale.as<double>(), tri ? 1 : 0, epi, err);
+  int dev = 0, sms = 0;
+  FGB_CUDA(cudaGetDevice(&dev));
+  FGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int MT = A.RP / kTM, NTt = B.RP / C::TN;
+  const int grid = std::max(1, std::min(MT * NTt, sms));
+  k_oz_gemm<C, Epi><<<grid, C::THREADS, C::Smem, st>>>(
+      A.rows, B.rows, A.K, A.KP, MT, NTt, A.q.as<__nv_bfloat16>(),
+      A.scale.as<double>(), B.q.as<__nv_bfloat16>(), B.scale.as<double>(),
+      tri ? 1 : 0, epi, err);
   FGB_LAUNCH_CHECK("k_oz_gemm");
   return FGB_OK;
 }
@@ -650,13 +715,14 @@ namespace {
 // K = N padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64
 // matrix is written only when the variance runs in FP64.
 struct EpiKernel {
+  using Value = double;
   static constexpr bool kFloat = false;
   double *Kd;                 // optional M x N FP64 kernel matrix
   __nv_bfloat16 *Ksl;         // optional slices of K (variance A operand)
   double *Kscale;             // their row scales (all 2^eK)
   int KPv, eK;
-  double *epart;              // M x ntiles energy partials
-  int ntiles;
+  double *epart;              // M x nslots energy partials
+  int nslots;                 // B tiles x epilogue warps per quarter
   const double *alpha;
   const unsigned char *valid;
   const int *perm;
@@ -689,17 +755,18 @@ struct EpiKernel {
     }
     return acc;
   }
-  __device__ void finish(int m, bool row_ok, int n0, double acc) const {
-    if (row_ok) epart[(long long)m * ntiles + n0 / kTN] = acc;
-    if (Ksl && n0 == 0) Kscale[m] = ldexp(1.0, eK);
+  __device__ void finish(int m, bool row_ok, int slot, double acc) const {
+    if (row_ok) epart[(long long)m * nslots + slot] = acc;
+    if (Ksl && slot == 0) Kscale[m] = ldexp(1.0, eK);
   }
 };
 
 // Variance GEMM epilogue: per-row sum of z^2 over this tile's columns.
 struct EpiZsq {
+  using Value = double;
   static constexpr bool kFloat = false;
   double *part;
-  int ntiles, R;
+  int nslots, R;   // slots: B tiles x epilogue warps per quarter
   __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
                           double acc) const {
     if (!row_ok) return acc;
@@ -708,8 +775,8 @@ struct EpiZsq {
       if (n0 + j < R) acc = fma(v[j], v[j], acc);
     return acc;
   }
-  __device__ void finish(int m, bool row_ok, int n0, double acc) const {
-    if (row_ok) part[(long long)m * ntiles + n0 / kTN] = acc;
+  __device__ void finish(int m, bool row_ok, int slot, double acc) const {
+    if (row_ok) part[(long long)m * nslots + slot] = acc;
   }
 };
 
@@ -796,7 +863,8 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
     }
     const bool var_oz = want_var && oz_var_eligible(m, s);
     const bool var_fp64 = want_var && !var_oz;
-    const int ktiles = Ms > 0 ? m->ozS[s]->RP / oz::kTN : 0;
+    // energy partial slots per row: B tiles x epilogue warps per quarter
+    const int ktiles = Ms > 0 ? m->ozS[s]->RP / oz::kTN * oz::kEpiWarps : 0;
     for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRows) {
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
@@ -842,7 +910,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
           return rc;
       } else if (var_oz) {
         const int R = m->h_panel_rows[s];
-        const int ntiles = m->ozL[s]->RP / oz::kTN;
+        const int ntiles = m->ozL[s]->RP / oz::kTN * oz::kEpiWarps;
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
           return rc;
         {
