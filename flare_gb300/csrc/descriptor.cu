@@ -76,7 +76,7 @@ __device__ __forceinline__ df finish(df a) {
 // Shared memory: A[nA] | g[kChunk*nmax] | Y[kChunk*nh] | sp[kChunk] | red,
 // in the compute type T: double (FP64 path) or df (double-float, the
 // mixed-precision path; the pair geometry arrives in FP64 and is split).
-template <typename T>
+template <typename T, int NC, int LC>
 __global__ void __launch_bounds__(kChunk)
 k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
@@ -85,7 +85,10 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int i = blockIdx.x;
   if (i >= n_atoms) return;
-  const int nA = p.n_A, nh = p.n_harm, nm = p.n_max;
+  // NC / LC > 0: n_max / l_max fixed at compile time
+  const int nh = LC > 0 ? (LC + 1) * (LC + 1) : p.n_harm;
+  const int nm = NC > 0 ? NC : p.n_max;
+  const int nA = p.n_species * nm * nh;
   T *A = reinterpret_cast<T *>(smem_raw);
   T *sg = A + nA;
   T *sy = sg + kChunk * nm;
@@ -104,8 +107,8 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       sj = species[j];
       double rc = p.cutoffs[si * kMaxSpecies + sj];
       if (r.x <= rc) {
-        radial_eval<T>(p, T(r.x), T(rc), sg + t * nm, (T *)nullptr);
-        ylm_eval<T>(p.l_max, T(r.y), T(r.z), T(r.w), sy + t * nh, nullptr);
+        radial_eval<T, NC>(p, T(r.x), T(rc), sg + t * nm, (T *)nullptr);
+        ylm_eval<T, LC>(p.l_max, T(r.y), T(r.z), T(r.w), sy + t * nh, nullptr);
       } else {
         sj = -1;
       }
@@ -127,7 +130,8 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   if (A_out)
     for (int e = t; e < nA; e += blockDim.x)
       A_out[(long long)i * nA + e] = to_double(A[e]);
-  const int L1 = p.l_max + 1, nr = p.n_rad, nd = p.n_d;
+  const int L1 = (LC > 0 ? LC : p.l_max) + 1, nr = p.n_species * nm,
+            nd = p.n_d;
   T nrm = T(0);
   for (int q = t; q < nd; q += blockDim.x) {
     int n1, n2, l;
@@ -145,24 +149,47 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
 
 // Shared memory: u[nA] | A[nA] (compute type T: double, or float in the
 // mixed-precision path)
-template <typename T>
-__global__ void __launch_bounds__(kChunk)
+// FP64 inputs in the compute type: FP32 takes the mantissa cut on the bit
+// pattern (integer instructions; an FP64 -> FP32 conversion runs on the FP64
+// pipe, which is scarce on this GPU).
+__device__ __forceinline__ double as_compute(double x, double) { return x; }
+__device__ __forceinline__ float as_compute(double x, float) {
+  return trunc_float(x);
+}
+__device__ __forceinline__ double3 pair_out(double x, double y, double z) {
+  return make_double3(x, y, z);
+}
+__device__ __forceinline__ double3 pair_out(float x, float y, float z) {
+  return make_double3(f2d_exact(x), f2d_exact(y), f2d_exact(z));
+}
+
+// Shared memory: u[nA] | A[nA] | w[nd] (the atom's dE/dB2 row, when it fits)
+template <typename T, int NC, int LC>
+__global__ void __launch_bounds__(kChunk, sizeof(T) == 4 ? 8 : 4)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
-             const double *__restrict__ gB2, double3 *__restrict__ pair_grad) {
+             const double *__restrict__ gB2, double3 *__restrict__ pair_grad,
+             int w_in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
   const int i = blockIdx.x;
   if (i >= n_atoms) return;
-  const int nA = p.n_A, nh = p.n_harm, nm = p.n_max, nr = p.n_rad,
-            L1 = p.l_max + 1, nd = p.n_d;
+  constexpr int NA = NC > 0 ? NC : kMaxNmax;
+  const int nh = LC > 0 ? (LC + 1) * (LC + 1) : p.n_harm;
+  const int nm = NC > 0 ? NC : p.n_max;
+  const int nA = p.n_species * nm * nh, nr = p.n_species * nm,
+            L1 = (LC > 0 ? LC : p.l_max) + 1, nd = p.n_d;
   T *u = smem;
   T *A = u + nA;
+  T *W = w_in_smem ? A + nA : nullptr;
   const int t = threadIdx.x;
-  for (int e = t; e < nA; e += blockDim.x) A[e] = T(A_in[(long long)i * nA + e]);
-  __syncthreads();
   const double *w = gB2 + (long long)i * nd;
+  for (int e = t; e < nA; e += blockDim.x)
+    A[e] = as_compute(A_in[(long long)i * nA + e], T(0));
+  if (W)
+    for (int q = t; q < nd; q += blockDim.x) W[q] = as_compute(w[q], T(0));
+  __syncthreads();
   for (int e = t; e < nA; e += blockDim.x) {
     int c = e / nh, lm = e % nh;
     int l = 0;
@@ -170,7 +197,8 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     T acc = T(0);
     for (int bb = 0; bb < nr; bb++) {
       int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
-      T wv = T(w[pair_index(lo, hi, nr) * L1 + l]);
+      const int wi = pair_index(lo, hi, nr) * L1 + l;
+      T wv = W ? W[wi] : as_compute(w[wi], T(0));
       T f = (bb == c) ? T(2) : T(1);
       acc += f * wv * A[bb * nh + lm];
     }
@@ -186,30 +214,38 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     double rc = p.cutoffs[si * kMaxSpecies + sj];
     double3 out = make_double3(0.0, 0.0, 0.0);
     if (r.x <= rc) {
-      T g[kMaxNmax], dg[kMaxNmax];
-      T Y[kMaxHarm], Yd[3 * kMaxHarm];
-      radial_eval<T>(p, T(r.x), T(rc), g, dg);
-      ylm_eval<T>(p.l_max, T(r.y), T(r.z), T(r.w), Y, Yd);
-      const T ir = T(1) / T(r.x);
-      const T ex = T(r.y) * ir, ey = T(r.z) * ir, ez = T(r.w) * ir;
+      // dE/dr = sum_{n,lm} u[n][lm] (dg_n/dr e Y_lm + g_n dY_lm/dr), the
+      // harmonics contracted as the recurrence produces them
+      T g[NA], dg[NA];
+      const T rx = as_compute(r.x, T(0)), ry = as_compute(r.y, T(0)),
+              rz = as_compute(r.z, T(0)), rw = as_compute(r.w, T(0));
+      radial_eval<T, NC>(p, rx, as_compute(rc, T(0)), g, dg);
       const T *us = u + sj * nm * nh;
-      T ox = T(0), oy = T(0), oz = T(0);
-      for (int n = 0; n < nm; n++) {
-        const T *un = us + n * nh;
-        T t1 = T(0), tx = T(0), ty = T(0), tz = T(0);
-        for (int lm = 0; lm < nh; lm++) {
-          T uv = un[lm];
-          t1 += uv * Y[lm];
-          tx += uv * Yd[3 * lm];
-          ty += uv * Yd[3 * lm + 1];
-          tz += uv * Yd[3 * lm + 2];
+      T t1[NA], tx[NA], ty[NA], tz[NA];
+#pragma unroll
+      for (int n = 0; n < nm; n++) { t1[n] = tx[n] = ty[n] = tz[n] = T(0); }
+      ylm_visit<T, LC, true>(p.l_max, ry, rz, rw,
+                             [&](int idx, T v, T gx, T gy, T gz) {
+#pragma unroll
+        for (int n = 0; n < nm; n++) {
+          const T uv = us[n * nh + idx];
+          t1[n] += uv * v;
+          tx[n] += uv * gx;
+          ty[n] += uv * gy;
+          tz[n] += uv * gz;
         }
-        T dgr = dg[n];
-        ox += dgr * ex * t1 + g[n] * tx;
-        oy += dgr * ey * t1 + g[n] * ty;
-        oz += dgr * ez * t1 + g[n] * tz;
+      });
+      const T ir = T(1) / rx;
+      const T ex = ry * ir, ey = rz * ir, ez = rw * ir;
+      T ox = T(0), oy = T(0), oz = T(0);
+#pragma unroll
+      for (int n = 0; n < nm; n++) {
+        const T dgr = dg[n];
+        ox += dgr * ex * t1[n] + g[n] * tx[n];
+        oy += dgr * ey * t1[n] + g[n] * ty[n];
+        oz += dgr * ez * t1[n] + g[n] * tz[n];
       }
-      out = make_double3((double)ox, (double)oy, (double)oz);
+      out = pair_out(ox, oy, oz);
     }
     pair_grad[pp] = out;
   }
@@ -288,6 +324,26 @@ size_t b2_adjoint_smem(const B2Params &p) {
   return sizeof(double) * 2 * (size_t)p.n_A;
 }
 
+// The descriptor sizes with compile-time specialisations (registers instead
+// of local memory for the per-pair basis values); others take the
+// runtime-sized kernels.
+template <template <typename, int, int> class K, typename T, typename F>
+static void dispatch_nl(const B2Params &p, F &&f) {
+  if (p.n_max == 8 && p.l_max == 4) f(K<T, 8, 4>{});
+  else if (p.n_max == 8 && p.l_max == 3) f(K<T, 8, 3>{});
+  else if (p.n_max == 10 && p.l_max == 6) f(K<T, 10, 6>{});
+  else f(K<T, 0, 0>{});
+}
+
+template <typename T, int NC, int LC>
+struct FwdK {
+  static constexpr auto fn = k_b2_forward<T, NC, LC>;
+};
+template <typename T, int NC, int LC>
+struct AdjK {
+  static constexpr auto fn = k_b2_adjoint<T, NC, LC>;
+};
+
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
                       double *d_norms, cudaStream_t st, bool dfloat) {
@@ -298,21 +354,19 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
     set_error("B2 settings need %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  if (dfloat) {
-    FGB_CUDA(cudaFuncSetAttribute(k_b2_forward<df>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
-    k_b2_forward<df><<<N, kChunk, sm, st>>>(
-        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
-  } else {
-    FGB_CUDA(cudaFuncSetAttribute(k_b2_forward<double>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
-    k_b2_forward<double><<<N, kChunk, sm, st>>>(
-        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_B2, d_norms);
-  }
+  cudaError_t e = cudaSuccess;
+  auto go = [&](auto k) {
+    auto fn = decltype(k)::fn;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
+    if (e != cudaSuccess) return;
+    fn<<<N, kChunk, sm, st>>>(p, N, nl->offsets.as<long long>(),
+                              nl->nbr_j.as<int>(), nl->nbr_rel.as<double4_16a>(),
+                              d_species, d_A, d_B2, d_norms);
+  };
+  if (dfloat) dispatch_nl<FwdK, df>(p, go);
+  else dispatch_nl<FwdK, double>(p, go);
+  FGB_CUDA(e);
   FGB_LAUNCH_CHECK("k_b2_forward");
   return FGB_OK;
 }
@@ -328,21 +382,23 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
     set_error("B2 adjoint needs %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  if (fp32) {
-    FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint<float>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
-    k_b2_adjoint<float><<<N, kChunk, sm, st>>>(
-        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
-  } else {
-    FGB_CUDA(cudaFuncSetAttribute(k_b2_adjoint<double>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
-    k_b2_adjoint<double><<<N, kChunk, sm, st>>>(
-        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad);
-  }
+  // the atom's dE/dB2 row in shared memory too, when it fits
+  const size_t wbytes = (fp32 ? sizeof(float) : sizeof(double)) * (size_t)p.n_d;
+  const int w_in_smem = sm + wbytes <= 96 * 1024 ? 1 : 0;
+  if (w_in_smem) sm += wbytes;
+  cudaError_t e = cudaSuccess;
+  auto go = [&](auto k) {
+    auto fn = decltype(k)::fn;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
+    if (e != cudaSuccess) return;
+    fn<<<N, kChunk, sm, st>>>(p, N, nl->offsets.as<long long>(),
+                              nl->nbr_j.as<int>(), nl->nbr_rel.as<double4_16a>(),
+                              d_species, d_A, d_gB2, d_pair_grad, w_in_smem);
+  };
+  if (fp32) dispatch_nl<AdjK, float>(p, go);
+  else dispatch_nl<AdjK, double>(p, go);
+  FGB_CUDA(e);
   FGB_LAUNCH_CHECK("k_b2_adjoint");
   return FGB_OK;
 }

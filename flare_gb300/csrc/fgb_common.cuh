@@ -48,20 +48,35 @@ struct B2Params {
 
 // Spherical-harmonic normalisation K_lm = sqrt((2l+1)/(4 pi) (l-m)!/(l+m)!),
 // times sqrt2 for m > 0, indexed [l * (kMaxL + 1) + m] (double-precision
-// values of the formula, evaluated once and written out).
+// values of the formula, evaluated once and written out), as FP64, as FP32
+// (nearest) and as the FP32 remainder K - (double)(float)K, so that FP32 and
+// double-float evaluations read their constants without conversions.
+#define FGB_YLM_NORM(X) \
+  X(0.28209479177387814) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 0 */ \
+  X(0.4886025119029199) X(0.48860251190292) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 1 */ \
+  X(0.6307831305050401) X(0.3641828101973597) X(0.18209140509867985) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 2 */ \
+  X(0.7463526651802308) X(0.3046971996429772) X(0.09635371475468515) X(0.03933623932844291) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 3 */ \
+  X(0.8462843753216345) X(0.2676186174229157) X(0.063078313050504) X(0.016858388283618388) X(0.005960340337611203) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 4 */ \
+  X(0.9356025796273888) X(0.2415715473043717) X(0.045652731285460234) X(0.009318824751147628) X(0.002196468058075176) X(0.0006945841871324552) X(0.0) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 5 */ \
+  X(1.0171072362820548) X(0.22195099524523101) X(0.03509353369580661) X(0.005848922282634434) X(0.0010678622237644956) X(0.00022766899107568565) X(6.57223766418388e-05) X(0.0) X(0.0) X(0.0) X(0.0)  /* l = 6 */ \
+  X(1.0925484305920792) X(0.20647224590289676) X(0.028097313806030647) X(0.003973560225074135) X(0.0005990367431114117) X(9.983945718523528e-05) X(1.958012847746254e-05) X(5.233009453691467e-06) X(0.0) X(0.0) X(0.0)  /* l = 7 */ \
+  X(1.1631066229203195) X(0.19385110382005324) X(0.023169638523677944) X(0.0028519853513317033) X(0.00036818972564450655) X(5.1058728265780266e-05) X(7.878532816214048e-06) X(1.4384167144950456e-06) X(3.596041786237614e-07) X(0.0) X(0.0)  /* l = 8 */ \
+  X(1.2296226898414837) X(0.1833013280774465) X(0.019539987227523183) X(0.0021319873940141734) X(0.00024140003633280337) X(2.8852822971932874e-05) X(3.7248834287122265e-06) X(5.376406125667451e-07) X(9.220460437034855e-08) X(2.1732833668965406e-08) X(0.0)  /* l = 9 */ \
+  X(1.2927207364566027) X(0.17431042854448453) X(0.016773028807119526) X(0.001644730792106853) X(0.0001661428994750111) X(1.7512999313514277e-05) X(1.958012847746254e-06) X(2.37443934928654e-07) X(3.231202683854524e-08) X(5.24170291336415e-09) X(1.1720804032140929e-09)  /* l = 10 */
+#define FGB_AS_F64(v) v,
+#define FGB_AS_F32(v) (float)(v),
+#define FGB_AS_F32_LO(v) (float)((v) - (double)(float)(v)),
 static __constant__ double c_ylm_norm[(kMaxL + 1) * (kMaxL + 1)] = {
-    0.28209479177387814, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 0
-    0.4886025119029199, 0.48860251190292, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 1
-    0.6307831305050401, 0.3641828101973597, 0.18209140509867985, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 2
-    0.7463526651802308, 0.3046971996429772, 0.09635371475468515, 0.03933623932844291, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 3
-    0.8462843753216345, 0.2676186174229157, 0.063078313050504, 0.016858388283618388, 0.005960340337611203, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 4
-    0.9356025796273888, 0.2415715473043717, 0.045652731285460234, 0.009318824751147628, 0.002196468058075176, 0.0006945841871324552, 0.0, 0.0, 0.0, 0.0, 0.0,  // l = 5
-    1.0171072362820548, 0.22195099524523101, 0.03509353369580661, 0.005848922282634434, 0.0010678622237644956, 0.00022766899107568565, 6.57223766418388e-05, 0.0, 0.0, 0.0, 0.0,  // l = 6
-    1.0925484305920792, 0.20647224590289676, 0.028097313806030647, 0.003973560225074135, 0.0005990367431114117, 9.983945718523528e-05, 1.958012847746254e-05, 5.233009453691467e-06, 0.0, 0.0, 0.0,  // l = 7
-    1.1631066229203195, 0.19385110382005324, 0.023169638523677944, 0.0028519853513317033, 0.00036818972564450655, 5.1058728265780266e-05, 7.878532816214048e-06, 1.4384167144950456e-06, 3.596041786237614e-07, 0.0, 0.0,  // l = 8
-    1.2296226898414837, 0.1833013280774465, 0.019539987227523183, 0.0021319873940141734, 0.00024140003633280337, 2.8852822971932874e-05, 3.7248834287122265e-06, 5.376406125667451e-07, 9.220460437034855e-08, 2.1732833668965406e-08, 0.0,  // l = 9
-    1.2927207364566027, 0.17431042854448453, 0.016773028807119526, 0.001644730792106853, 0.0001661428994750111, 1.7512999313514277e-05, 1.958012847746254e-06, 2.37443934928654e-07, 3.231202683854524e-08, 5.24170291336415e-09, 1.1720804032140929e-09,  // l = 10
-};
+    FGB_YLM_NORM(FGB_AS_F64)};
+static __constant__ float c_ylm_norm_f[(kMaxL + 1) * (kMaxL + 1)] = {
+    FGB_YLM_NORM(FGB_AS_F32)};
+static __constant__ float c_ylm_norm_lo[(kMaxL + 1) * (kMaxL + 1)] = {
+    FGB_YLM_NORM(FGB_AS_F32_LO)};
+
+// K_lm in the compute type T (FP64 and FP32 here; the double-float type
+// adds its overload in fgb_df.cuh).
+__device__ __forceinline__ void ylm_norm(int i, double &k) { k = c_ylm_norm[i]; }
+__device__ __forceinline__ void ylm_norm(int i, float &k) { k = c_ylm_norm_f[i]; }
 
 // ------------------------------------------------------------ cutoff
 // cutoffs.cpp:7-85.  Returns value and derivative w.r.t. r.
@@ -103,15 +118,18 @@ __device__ __forceinline__ void cutoff_eval(const B2Params &p, T r, T rc,
 
 // Chebyshev radial basis on x = (r - r1)/(rc - r1) (radial.cpp:138-169)
 // times the cutoff (radial.cpp:344-379).  Writes g[n] and dg/dr[n]
-// (radial derivative; Cartesian derivatives are dg/dr * x_k / r).
-template <typename T>
+// (radial derivative; Cartesian derivatives are dg/dr * x_k / r); dg may be
+// null.  NC > 0 fixes n_max at compile time (loops unrolled, arrays of the
+// caller kept in registers); NC = 0 reads it from p.
+template <typename T, int NC = 0>
 __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
                                             T *g, T *dg) {
   T fc, dfc;
   cutoff_eval<T>(p, r, rc, fc, dfc);
-  const int N = p.n_max;
+  const int N = NC > 0 ? NC : p.n_max;
   T r1 = T(p.r1);
   if (r < r1 || r > rc) {
+#pragma unroll
     for (int n = 0; n < N; n++) {
       g[n] = T(0);
       if (dg) dg[n] = T(0);
@@ -121,6 +139,7 @@ __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
   T c = T(1) / (rc - r1);
   T x = (r - r1) * c;
   T b0 = T(1), db0 = T(0), b1 = x, db1 = c;
+#pragma unroll
   for (int n = 0; n < N; n++) {
     T b, db;
     if (n == 0) { b = b0; db = db0; }
@@ -137,67 +156,96 @@ __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
 
 // Real spherical harmonics, l-major and m = -l..l (the y_grad.cpp:667
 // convention), by the associated-Legendre recurrence on the unit vector.
-// If Yd != nullptr, also writes the Cartesian gradient: Yd[3*idx + k].
-template <typename T>
-__device__ __forceinline__ void ylm_eval(int L, T x, T y, T z, T *Y, T *Yd) {
+// Calls fn(idx, Y, Gx, Gy, Gz) once per harmonic (idx = l*l + l + m, visited
+// m = L..0, l = m..L) with the Cartesian gradient when Grad (zeros
+// otherwise).  LC > 0 fixes l_max at compile time (loops unrolled, the
+// recurrence state kept in registers); LC = 0 takes Lrt.
+template <typename T, int LC, bool Grad, typename Fn>
+__device__ __forceinline__ void ylm_visit(int Lrt, T x, T y, T z, Fn &&fn) {
+  constexpr int LA = LC > 0 ? LC : kMaxL;
+  const int L = LC > 0 ? LC : Lrt;
   T r = sqrt(x * x + y * y + z * z);
   T ir = T(1) / r;
   T ux = x * ir, uy = y * ir, uz = z * ir;
-  T C[kMaxL + 1], S[kMaxL + 1];
+  T C[LA + 1], S[LA + 1];
   C[0] = T(1); S[0] = T(0);
+#pragma unroll
   for (int m = 1; m <= L; m++) {
     C[m] = ux * C[m - 1] - uy * S[m - 1];
     S[m] = ux * S[m - 1] + uy * C[m - 1];
   }
-  T qnext[kMaxL + 2];   // Q_l^{m+1}, indexed by l
-  T qcur[kMaxL + 2];
+  T qnext[LA + 2];   // Q_l^{m+1}, indexed by l
+  T qcur[LA + 2];
+#pragma unroll
   for (int l = 0; l <= L + 1; l++) qnext[l] = T(0);
   // (2m-1)!! for m = L
   T dfact = T(1);
+#pragma unroll
   for (int k = 1; k <= L; k++) dfact *= T(2 * k - 1);
+#pragma unroll
   for (int m = L; m >= 0; m--) {
     if (m < L) dfact /= T(2 * m + 1);       // (2m-1)!!
+#pragma unroll
     for (int l = 0; l <= L; l++) qcur[l] = T(0);
     qcur[m] = dfact;
     if (m + 1 <= L) qcur[m + 1] = T(2 * m + 1) * uz * dfact;
+#pragma unroll
     for (int l = m + 2; l <= L; l++)
       qcur[l] = (T(2 * l - 1) * uz * qcur[l - 1] - T(l + m - 1) * qcur[l - 2]) /
                 T(l - m);
+#pragma unroll
     for (int l = m; l <= L; l++) {
-      T K = T(c_ylm_norm[l * (kMaxL + 1) + m]);
+      T K;
+      ylm_norm(l * (kMaxL + 1) + m, K);
       T qv = qcur[l], qd = qnext[l];
       if (m == 0) {
-        int idx = l * l + l;
-        Y[idx] = K * qv;
-        if (Yd) {
+        const int idx = l * l + l;
+        if (Grad) {
           T G2 = K * qd;
           T ug = uz * G2;
-          Yd[3 * idx + 0] = (-ux * ug) * ir;
-          Yd[3 * idx + 1] = (-uy * ug) * ir;
-          Yd[3 * idx + 2] = (G2 - uz * ug) * ir;
+          fn(idx, K * qv, (-ux * ug) * ir, (-uy * ug) * ir, (G2 - uz * ug) * ir);
+        } else {
+          fn(idx, K * qv, T(0), T(0), T(0));
         }
       } else {
-        int ip = l * l + l + m, in = l * l + l - m;
-        Y[ip] = K * qv * C[m];
-        Y[in] = K * qv * S[m];
-        if (Yd) {
+        const int ip = l * l + l + m, in = l * l + l - m;
+        if (Grad) {
           T a = K * qv * T(m);
           // +m: G = K (Q m C_{m-1}, -Q m S_{m-1}, Q' C_m)
           T G0 = a * C[m - 1], G1 = -a * S[m - 1], G2 = K * qd * C[m];
           T ug = ux * G0 + uy * G1 + uz * G2;
-          Yd[3 * ip + 0] = (G0 - ux * ug) * ir;
-          Yd[3 * ip + 1] = (G1 - uy * ug) * ir;
-          Yd[3 * ip + 2] = (G2 - uz * ug) * ir;
+          fn(ip, K * qv * C[m], (G0 - ux * ug) * ir, (G1 - uy * ug) * ir,
+             (G2 - uz * ug) * ir);
           // -m: G = K (Q m S_{m-1}, Q m C_{m-1}, Q' S_m)
           G0 = a * S[m - 1]; G1 = a * C[m - 1]; G2 = K * qd * S[m];
           ug = ux * G0 + uy * G1 + uz * G2;
-          Yd[3 * in + 0] = (G0 - ux * ug) * ir;
-          Yd[3 * in + 1] = (G1 - uy * ug) * ir;
-          Yd[3 * in + 2] = (G2 - uz * ug) * ir;
+          fn(in, K * qv * S[m], (G0 - ux * ug) * ir, (G1 - uy * ug) * ir,
+             (G2 - uz * ug) * ir);
+        } else {
+          fn(ip, K * qv * C[m], T(0), T(0), T(0));
+          fn(in, K * qv * S[m], T(0), T(0), T(0));
         }
       }
     }
+#pragma unroll
     for (int l = 0; l <= L; l++) qnext[l] = qcur[l];
+  }
+}
+
+// The harmonics into Y[] (and, if Yd != nullptr, the Cartesian gradient
+// into Yd[3*idx + k]).
+template <typename T, int LC = 0>
+__device__ __forceinline__ void ylm_eval(int L, T x, T y, T z, T *Y, T *Yd) {
+  if (Yd) {
+    ylm_visit<T, LC, true>(L, x, y, z, [&](int idx, T v, T gx, T gy, T gz) {
+      Y[idx] = v;
+      Yd[3 * idx] = gx;
+      Yd[3 * idx + 1] = gy;
+      Yd[3 * idx + 2] = gz;
+    });
+  } else {
+    ylm_visit<T, LC, false>(L, x, y, z,
+                            [&](int idx, T v, T, T, T) { Y[idx] = v; });
   }
 }
 

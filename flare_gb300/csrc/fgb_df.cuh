@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "fgb_common.cuh"
+
 namespace fgb {
 // The type and its functions live in a nested namespace: argument-dependent
 // lookup finds sqrt(df) and the operators from anywhere, while unqualified
@@ -108,14 +110,18 @@ __device__ __forceinline__ df sqrt(df a) {
 // hi = d with its mantissa cut to 24 bits (exact), lo = the remaining 29
 // bits rounded to FP32; |d - (hi + lo)| <= 2^-47 |d|.  Zero, subnormal and
 // out-of-FP32-range inputs go through the FP64 conversion instead.
+// Out of line so that the compiler cannot if-convert it into the common
+// path: its FP64 instructions would then run on every call.
+static __device__ __noinline__ df df_from_double_rare(double d) {
+  const float h = __double2float_rn(d);
+  return df(h, __double2float_rn(d - (double)h));
+}
+
 __device__ __forceinline__ df df_from_double(double d) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const int E = (int)((b >> 52) & 0x7FF);
   const int e = E - 1023;
-  if (E == 0 || e < -100 || e > 100) {
-    const float h = __double2float_rn(d);
-    return df(h, __double2float_rn(d - (double)h));
-  }
+  if (E == 0 || e < -100 || e > 100) return df_from_double_rare(d);
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const unsigned long long m = b & 0xFFFFFFFFFFFFFULL;
   const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) |
@@ -130,32 +136,42 @@ __device__ __forceinline__ df df_from_double(double d) {
 
 // d with its mantissa cut to 24 bits (relative error below 2^-23); FP32
 // range only, FP64 conversion otherwise.
+static __device__ __noinline__ float trunc_float_rare(double d) {
+  return __double2float_rn(d);
+}
+
 __device__ __forceinline__ float trunc_float(double d) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const int E = (int)((b >> 52) & 0x7FF);
   const int e = E - 1023;
-  if (E == 0 || e < -126 || e > 127) return __double2float_rn(d);
+  if (E == 0 || e < -126 || e > 127) return trunc_float_rare(d);
   return __uint_as_float(((unsigned)(b >> 63) << 31) |
                          ((unsigned)(e + 127) << 23) |
                          (unsigned)((b & 0xFFFFFFFFFFFFFULL) >> 29));
 }
 
-// exact FP64 value of an FP32 number (normal or zero)
+// FP64 value of an FP32 number, on the bit patterns: exact for normal
+// numbers, infinities and NaNs; FP32 subnormals become signed zeros.
 __device__ __forceinline__ double f2d_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned E = (u >> 23) & 0xFF;
-  if (E == 0 || E == 255) return (double)f;
-  const unsigned long long bits =
-      ((unsigned long long)(u >> 31) << 63) |
-      ((unsigned long long)(E - 127 + 1023) << 52) |
-      ((unsigned long long)(u & 0x7FFFFF) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned long long field =
+      E == 0 ? 0ULL : (E == 255 ? 2047ULL : (unsigned long long)(E - 127 + 1023));
+  const unsigned long long mant =
+      E == 0 ? 0ULL : (unsigned long long)(u & 0x7FFFFF) << 29;
+  return __longlong_as_double((long long)(sign | (field << 52) | mant));
 }
 
 // hi + lo rounded once to FP64
 __device__ __forceinline__ double to_double(df a) {
   return f2d_exact(a.hi) + f2d_exact(a.lo);
 }
+// K_lm as a double-float from the FP32 tables (no conversion)
+__device__ __forceinline__ void ylm_norm(int i, df &k) {
+  k = df(c_ylm_norm_f[i], c_ylm_norm_lo[i]);
+}
+
 // Rare-path functions (cutoffs other than quadratic and hard): evaluated in
 // FP64 and split back.
 __device__ __forceinline__ df cos(df a) { return df_from_double(::cos(to_double(a))); }
