@@ -14,8 +14,9 @@ constexpr int kKC = 16;      // k per pipeline stage (one MMA k-step)
 constexpr int kStages = 4;   // shared-memory pipeline depth
 constexpr int kEpiWarps = 3; // epilogue warps per TMEM lane quarter (16 columns
                              // each); partial sums per row: B tiles x kEpiWarps
-// Largest K whose group sums stay below 2^24 (exact FP32 accumulation):
-// the biggest group (a + b = 10) sums to at most 11264 * K.
+// K segment: the largest K whose group sums stay below 2^24 (exact FP32
+// accumulation in TMEM); the biggest group (a + b = 10) sums to at most
+// 11264 * K.  Longer K runs in segments summed in 64-bit integers.
 constexpr int kMaxK = 1472;
 // FP32-level configuration (force GEMM of the mixed path): 4 slices, B tiles
 // of 128 rows; the biggest group (a + b = 5) sums to at most 6144 * K.

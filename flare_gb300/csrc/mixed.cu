@@ -3,17 +3,15 @@
 // Energy and local variance need FP64-level accuracy: the sparse-set sum and
 // sigma^2 - |L_inv k|^2 cancel too many digits for any 24-bit arithmetic.
 // They come from the kernel GEMM and the variance GEMM run on the BF16 tensor
-// cores with exact integer slicing (ozaki.cu, FP64-accurate) when n_d and the
-// per-species sparse counts fit its exact-accumulation limit, else from the
-// FP64 GEMMs.  The forces, which only need 1e-4 eV/A, use the alpha-weighted
-// sum folded into the sparse set before the GEMM:
+// cores with exact integer slicing (ozaki.cu, FP64-accurate).  The forces,
+// which only need 1e-4 eV/A, use the alpha-weighted sum folded into the
+// sparse set before the GEMM:
 //   power 2:  E_i = sigma^2 d^_i^T B_s d^_i,  B_s = S^_s^T diag(alpha_s) S^_s
-//             dE/dd^ = 2 sigma^2 B_s d^   (one FP32 GEMM, n_d x n_d per species)
+//             dE/dd^ = 2 sigma^2 B_s d^   (one GEMM, n_d x n_d per species)
 //   power 1:  E_i = sigma^2 beta_s . d^_i,  beta_s = S^_s^T alpha_s
 // B_s / beta_s are built once per model in FP64 on the GPU; B_s is kept in
 // FP32-level exact slices for the tensor-core GEMM Y = D^ B_s (ozaki.cu, 4
-// slices, 10 pair products, exact accumulation; FP32 SIMT GEMM when n_d
-// exceeds that kernel's K limit) and beta_s in FP32.
+// slices, 10 pair products, exact accumulation) and beta_s in FP32.
 // dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d| in FP32; the per-pair adjoint
 // then runs in FP32.  Other powers use the FP64 kernel, adjoint and variance
 // GEMMs.
@@ -26,7 +24,6 @@
 #include "fgb_profile.h"
 
 namespace fgb {
-bool oz_eligible(const fgb_model_s *m);
 namespace {
 using namespace gemm64;
 
@@ -81,39 +78,6 @@ __global__ void k_fold_vec(int M, int nd, const double *__restrict__ S,
   for (int t = 0; t < M; t++)
     if (valid[t]) acc += alpha[t] * S[(long long)t * nd + q];
   beta[q] = (float)acc;
-}
-
-// FP32 normalised descriptor rows of one species chunk (gathered)
-__global__ void k_gather_dhat(int Mr, int nd, const int *__restrict__ perm,
-                              const double *__restrict__ B2,
-                              const double *__restrict__ norms,
-                              float *__restrict__ out) {
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)Mr * nd) return;
-  int m = (int)(idx / nd), q = (int)(idx % nd);
-  int atom = perm[m];
-  double n = norms[atom];
-  out[idx] = n >= kEmptyThresh ? (float)(B2[(long long)atom * nd + q] / n) : 0.f;
-}
-
-// Y = Dh B (FP32): rows Mr, cols nd, K = nd (B symmetric, row-major)
-__global__ void __launch_bounds__(GT)
-k_mapped_gemm(int Mr, int nd, const float *__restrict__ Dh,
-              const float *__restrict__ B, float *__restrict__ Y) {
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  float acc[4][4];
-  gemm_mainloop_t<float, true>(acc, m0, n0, Mr, nd, nd, Dh, nd, nullptr, B, nd);
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    int m = m0 + ty + 16 * i;
-    if (m >= Mr) continue;
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      int n = n0 + tx + 16 * j;
-      if (n < nd) Y[(long long)m * nd + n] = acc[i][j];
-    }
-  }
 }
 
 // dE/dB2 rows from g = dE/dd^ (power 2: g = 2 sig2 Y; power 1: g = sig2 beta)
@@ -178,8 +142,7 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
                                     Bs, Bd.as<double>());
       FGB_LAUNCH_CHECK("k_fold_gemm");
       // B_s is symmetric: its rows are the B operand of Y = D^ B_s
-      if (nd <= oz::kMaxKF32 &&
-          (rc = oz::slice({nd, nd, oz::kTNF32, Bd.as<double>(), nd, nullptr,
+      if ((rc = oz::slice({nd, nd, oz::kTNF32, Bd.as<double>(), nd, nullptr,
                            nullptr},
                           *m->ozB[s], st, oz::kSF32)))
         return rc;
@@ -201,12 +164,12 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        double *d_gB2, double *d_var, cudaStream_t st) {
   const bool foldable = m->power == 2.0 || m->power == 1.0;
   int rc;
-  if (foldable && oz_eligible(m)) {
+  if (foldable) {
     // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact
     // integer slicing (ozaki.cu).
     rc = kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st);
   } else {
-    // FP64 GEMMs; the FP64 adjoint GEMM only when the power cannot be folded.
+    // powers other than 1 and 2: the FP64 kernel, adjoint and variance GEMMs
     rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
                            d_e_atom, d_gB2, d_var, st);
   }
@@ -217,7 +180,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   const bool quad = m->power == 2.0;
   const float sig2 = (float)(m->sigma * m->sigma);
   const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
-  if (quad && nd <= oz::kMaxKF32) {
+  if (quad) {
     if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
     FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   }
@@ -228,16 +191,13 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
     base += Ns;
     if (Ns == 0 || m->h_counts[s] == 0) continue;   // gB2 stays zero
     const float *Bs = m->Bmap.as<float>() + per * s;
-    const bool tc_gemm = quad && nd <= oz::kMaxKF32;
     for (int r0 = 0; r0 < Ns; r0 += kRowChunkMixed) {
       const int Mr = std::min(kRowChunkMixed, Ns - r0);
       const int *perm = perm_s + r0;
-      if ((quad && (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd))) ||
-          (quad && !tc_gemm &&
-           (rc = m->ws.b2f.ensure(sizeof(float) * (size_t)Mr * nd))))
+      if (quad && (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
         return rc;
-      StageTimer _pt(kStMappedGemm, st, tc_gemm ? 3 : (quad ? 3 : 1));
-      if (tc_gemm) {
+      StageTimer _pt(kStMappedGemm, st, quad ? 3 : 1);
+      if (quad) {
         // Y = D^ B_s on the tensor cores (FP32-level exact slices)
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
@@ -245,15 +205,6 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
             (rc = oz::gemm_f32(m->ws.ozA4, *m->ozB[s], m->ws.yf.as<float>(),
                                nd, m->ws.ozerr.as<int>(), st)))
           return rc;
-      } else if (quad) {
-        k_gather_dhat<<<ceil_div((long long)Mr * nd, 256), 256, 0, st>>>(
-            Mr, nd, perm, m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-            m->ws.b2f.as<float>());
-        FGB_LAUNCH_CHECK("k_gather_dhat");
-        dim3 g(ceil_div(nd, BN), ceil_div(Mr, BM));
-        k_mapped_gemm<<<g, GT, 0, st>>>(Mr, nd, m->ws.b2f.as<float>(), Bs,
-                                        m->ws.yf.as<float>());
-        FGB_LAUNCH_CHECK("k_mapped_gemm");
       }
       k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
           Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
@@ -262,7 +213,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
       FGB_LAUNCH_CHECK("k_mapped_grad");
     }
   }
-  if (quad && nd <= oz::kMaxKF32) {
+  if (quad) {
     int h = 0;
     FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
                              cudaMemcpyDeviceToHost, st));

@@ -63,6 +63,9 @@ struct Cfg {
   static constexpr int EW = EW_;
   static constexpr int THREADS = 32 * (1 + 4 * EW);
   static constexpr int WCOLS = TN / EW;   // columns per epilogue warp
+  // K segment: chunks accumulated in TMEM before the epilogue adds the exact
+  // group sums into its 64-bit registers (any K, exact)
+  static constexpr int SEGC = MAXK / kKC;
   static constexpr uint32_t TileA = kTM * kKC * 2;   // bytes per slice
   static constexpr uint32_t TileB = TN * kKC * 2;
   static constexpr uint32_t Stage = S * (TileA + TileB);
@@ -149,14 +152,20 @@ __device__ __forceinline__ int pow2_exp(double s) {
   return (int)((__double_as_longlong(s) >> 52) & 0x7FF) - 1023;
 }
 
-// x 2^sc as a double, exact, for an integer |x| < 2^53.
+// Out of line so that its FP64 instructions stay off the common path.
+static __device__ __noinline__ double scaled_rare(long long x, int sc) {
+  return ldexp((double)x, sc);
+}
+
+// x 2^sc as a double: exact for |x| < 2^53 and a normal result (the common
+// case), else rounded once.
 __device__ __forceinline__ double exact_scaled(long long x, int sc) {
   if (x == 0) return 0.0;
   const unsigned long long a = x < 0 ? 0ULL - (unsigned long long)x
                                      : (unsigned long long)x;
-  const int p = 63 - __clzll((long long)a);            // leading bit, <= 52
+  const int p = 63 - __clzll((long long)a);            // leading bit
   const int field = p + sc + 1023;
-  if (field < 1 || field > 2046) return ldexp((double)x, sc);  // not normal
+  if (p > 52 || field < 1 || field > 2046) return scaled_rare(x, sc);
   unsigned long long bits = ((unsigned long long)field << 52) |
                             ((a << (52 - p)) & 0xFFFFFFFFFFFFFULL);
   if (x < 0) bits |= 1ULL << 63;
@@ -364,15 +373,16 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
       if (++lc == tile_nch(lt)) { lc = 0; lt += gridDim.x; }
     };
     while (nl < NST - 1 && lt < ntiles) issue_load();
-    int it = 0;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, it++) {
+    int sg = 0;   // K segments accumulated so far (acc_full phases)
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
       const int nch = tile_nch(t);
-      if (it > 0) {
-        // the previous tile's accumulator must be drained by the epilogue
-        if (!tc::mbar_wait(acc_empty, (it - 1) & 1, kWaitLimit)) { ok = false; break; }
-        tc::fence_after_sync();
-      }
       for (int c = 0; c < nch; c++) {
+        const bool seg_first = c % C::SEGC == 0;
+        if (seg_first && sg > 0) {
+          // the previous segment's accumulator must be drained first
+          if (!tc::mbar_wait(acc_empty, (sg - 1) & 1, kWaitLimit)) { ok = false; break; }
+          tc::fence_after_sync();
+        }
         const int b = (int)(nm % NST);
         if (!tc::mbar_wait(&bar_load[b], (uint32_t)((nm / NST) & 1), kWaitLimit)) { ok = false; break; }
         tc::fence_after_sync();
@@ -384,9 +394,12 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
 #pragma unroll
         for (int kk = 0; kk < kKC / 16; kk++)
           mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
-                       bd0 + (uint64_t)((kk * 256) >> 4), c == 0 && kk == 0);
+                       bd0 + (uint64_t)((kk * 256) >> 4), seg_first && kk == 0);
         tc::mma_commit(&bar_mma[b]);
-        if (c == nch - 1) tc::mma_commit(acc_full);
+        if (c == nch - 1 || (c + 1) % C::SEGC == 0) {
+          tc::mma_commit(acc_full);
+          sg++;
+        }
         nm++;
         if (lt < ntiles) {
           // load nl reuses the stage of chunk nl - NST, the chunk before the
@@ -416,67 +429,81 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
     const int sub = (warp - 1) >> 2;   // its column range within the tile
     const int c_lo = sub * C::WCOLS;
     const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16);
-    int it = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
-      bool got = false;
-      for (long long i = 0; i < kWaitLimit; i++) {
-        if (tc::mbar_try_wait(acc_full, it & 1)) { got = true; break; }
-        if (*abort_flag) break;
-      }
-      if (!got) {
-        if (!*abort_flag) atomicExch(err, 1);
-        break;
-      }
-      tc::fence_after_sync();
+    int sg = 0;   // K segments drained so far
+    bool alive = true;
+    for (int t = blockIdx.x; t < ntiles && alive; t += gridDim.x) {
       const int m0 = (t / NTt) * kTM, n0 = (t % NTt) * TN;
       const int m = m0 + q * 32 + lane;
       const bool row_ok = m < M;
-      const int er = pow2_exp(Ascale[m]);
-      // Phase 1.  Group sums are exact integers below 2^24; recombine them
-      // exactly in 64-bit integers, hi = sum_{t <= TSPLIT} g_t 2^(6(TSPLIT-t))
-      // and lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), so that
+      const int nseg = (tile_nch(t) + C::SEGC - 1) / C::SEGC;
+      // Phase 1, per K segment.  Group sums are exact integers below 2^24;
+      // add them exactly into 64-bit integers, hi = sum_{t <= TSPLIT} g_t
+      // 2^(6(TSPLIT-t)) and lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), and
+      // release the accumulator after each segment.
+      long long hi[NCH][16], lo[NCH][16];
+#pragma unroll
+      for (int ch = 0; ch < NCH; ch++)
+#pragma unroll
+        for (int j = 0; j < 16; j++) { hi[ch][j] = 0; lo[ch][j] = 0; }
+      for (int seg = 0; seg < nseg; seg++, sg++) {
+        bool got = false;
+        for (long long i = 0; i < kWaitLimit; i++) {
+          if (tc::mbar_try_wait(acc_full, sg & 1)) { got = true; break; }
+          if (*abort_flag) break;
+        }
+        if (!got) {
+          if (!*abort_flag) atomicExch(err, 1);
+          alive = false;
+          break;
+        }
+        tc::fence_after_sync();
+#pragma unroll
+        for (int ch = 0; ch < NCH; ch++) {
+#pragma unroll
+          for (int g = 0; g < S; g++) {
+            uint32_t r[16];
+            tc::tmem_ld16(trow + g * TN + c_lo + ch * 16, r);
+            tc::tmem_ld_wait();
+            const int tg = g + 2;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              const long long qv =
+                  (long long)__float2int_rn(__uint_as_float(r[j]));
+              if (tg <= C::TSPLIT) hi[ch][j] += qv << (6 * (C::TSPLIT - tg));
+              else lo[ch][j] += qv << (6 * (S + 1 - tg));
+            }
+          }
+        }
+        // the accumulator may now take the next segment or tile
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(acc_empty);
+      }
+      if (!alive) break;
       // C = (hi 2^(-6 TSPLIT) + lo 2^(-6(S+1))) 2^(e_row + e_col): exact
       // doubles built from the integers and one correctly rounded addition
       // (FP64 results), or one rounding of hi (FP32 results, no low part).
       // Rows past M (tile padding) still run so that functors can write
       // zero padding.
+      const int er = pow2_exp(Ascale[m]);
       using V = typename Epi::Value;
       V v[NCH][16];
 #pragma unroll
       for (int ch = 0; ch < NCH; ch++) {
-        long long hi[16], lo[16];
-#pragma unroll
-        for (int j = 0; j < 16; j++) { hi[j] = 0; lo[j] = 0; }
-#pragma unroll
-        for (int g = 0; g < S; g++) {
-          uint32_t r[16];
-          tc::tmem_ld16(trow + g * TN + c_lo + ch * 16, r);
-          tc::tmem_ld_wait();
-          const int tg = g + 2;
-#pragma unroll
-          for (int j = 0; j < 16; j++) {
-            const long long qv = (long long)__float2int_rn(__uint_as_float(r[j]));
-            if (tg <= C::TSPLIT) hi[j] += qv << (6 * (C::TSPLIT - tg));
-            else lo[j] += qv << (6 * (S + 1 - tg));
-          }
-        }
 #pragma unroll
         for (int j = 0; j < 16; j++) {
           const int e = er + pow2_exp(Bscale[n0 + c_lo + ch * 16 + j]);
           if constexpr (Epi::kFloat) {
             static_assert(!C::HAS_LO, "FP32 results take at most 5 slices");
-            v[ch][j] = scaled_float(hi[j], e - 6 * C::TSPLIT);
+            v[ch][j] = scaled_float(hi[ch][j], e - 6 * C::TSPLIT);
           } else {
-            double x = exact_scaled(hi[j], e - 6 * C::TSPLIT);
-            if constexpr (C::HAS_LO) x += exact_scaled(lo[j], e - 6 * (S + 1));
+            double x = exact_scaled(hi[ch][j], e - 6 * C::TSPLIT);
+            if constexpr (C::HAS_LO)
+              x += exact_scaled(lo[ch][j], e - 6 * (S + 1));
             v[ch][j] = x;
           }
         }
       }
-      // the accumulator may now take the next tile
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(acc_empty);
       // Phase 2
       double acc = 0.0;
 #pragma unroll
@@ -577,11 +604,6 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
     set_error("ozaki gemm: operand layouts disagree");
     return FGB_EINVAL;
   }
-  if (A.K > C::MAXK) {
-    set_error("ozaki gemm: K = %d exceeds the exact-accumulation limit %d",
-              A.K, C::MAXK);
-    return FGB_EINVAL;
-  }
   if (A.rows == 0 || B.rows == 0) return FGB_OK;
   FGB_CUDA(cudaFuncSetAttribute(k_oz_gemm<C, Epi>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -622,11 +644,6 @@ extern "C" int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A,
     set_error("fgb_oz_dgemm_nt: invalid arguments");
     return FGB_EINVAL;
   }
-  if (K > oz::kMaxK) {
-    set_error("fgb_oz_dgemm_nt: K = %d exceeds the exact-accumulation limit "
-              "%d", K, oz::kMaxK);
-    return FGB_EINVAL;
-  }
   cudaStream_t st = (cudaStream_t)stream;
   if (M == 0 || N == 0) return FGB_OK;
   if (K == 0) {
@@ -660,11 +677,6 @@ extern "C" int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A,
                                float *d_C, long long ldc, void *stream) {
   if (M < 0 || N < 0 || K < 0 || (M && N && (!d_A || !d_B || !d_C))) {
     set_error("fgb_oz_sgemm_nt: invalid arguments");
-    return FGB_EINVAL;
-  }
-  if (K > oz::kMaxKF32) {
-    set_error("fgb_oz_sgemm_nt: K = %d exceeds the exact-accumulation limit "
-              "%d", K, oz::kMaxKF32);
     return FGB_EINVAL;
   }
   cudaStream_t st = (cudaStream_t)stream;
@@ -794,14 +806,6 @@ __global__ void k_energy_final(int M, int ntiles, const double *__restrict__ par
 }  // namespace
 }  // namespace oz
 
-// The kernel GEMM contracts over n_d; the variance GEMM over the species'
-// sparse count.  Either runs on the tensor cores when its K fits the
-// exact-accumulation limit (the variance GEMM falls back to FP64 otherwise).
-bool oz_eligible(const fgb_model_s *m) { return m->b2.n_d <= oz::kMaxK; }
-
-static bool oz_var_eligible(const fgb_model_s *m, int s) {
-  return m->h_counts[s] <= oz::kMaxK;
-}
 
 // Slice the model operands once: normalised sparse rows (B of the kernel
 // GEMM) and the L_inv panels (B of the variance GEMM), per species.
@@ -820,8 +824,7 @@ static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
                          nullptr, nullptr},
                         *m->ozS[s], st)))
       return rc;
-    if (oz_var_eligible(m, s) &&
-        (rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
+    if ((rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
                          m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
                          nullptr},
                         *m->ozL[s], st)))
@@ -861,16 +864,13 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                       d_var, st)))
         return rc;
     }
-    const bool var_oz = want_var && oz_var_eligible(m, s);
-    const bool var_fp64 = want_var && !var_oz;
+    const bool var_oz = want_var;
     // energy partial slots per row: B tiles x epilogue warps per quarter
     const int ktiles = Ms > 0 ? m->ozS[s]->RP / oz::kTN * oz::kEpiWarps : 0;
     for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRows) {
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
       if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * ktiles)) ||
-          (var_fp64 &&
-           (rc = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * Ms))) ||
           (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, oz::kS, m->ws.ozK))))
         return rc;
       {
@@ -879,7 +879,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                              m->ws.norms.as<double>()},
                             m->ws.ozA, st)))
           return rc;
-        oz::EpiKernel epi{var_fp64 ? m->ws.kmat.as<double>() : nullptr,
+        oz::EpiKernel epi{nullptr,
                           var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
                           var_oz ? m->ws.ozK.scale.as<double>() : nullptr,
                           m->ws.ozK.KP, eK,
@@ -897,18 +897,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
             Mr, ktiles, m->ws.erows.as<double>(), perm, d_e_atom);
         FGB_LAUNCH_CHECK("k_energy_final");
       }
-      if (var_fp64) {
-        const int R = m->h_panel_rows[s];
-        const int ntiles = ceil_div(R, 64);
-        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)) ||
-            (rc = launch_variance_fp64(Mr, R, Ms, m->ws.kmat.as<double>(),
-                                       m->Lp.as<double>() + m->h_panel_off[s],
-                                       m->ws.part.as<double>(), ntiles, st)) ||
-            (rc = launch_variance_final(Mr, ntiles, m->ws.part.as<double>(),
-                                        perm, m->ws.norms.as<double>(), sig2,
-                                        m->power, d_var, st)))
-          return rc;
-      } else if (var_oz) {
+      if (var_oz) {
         const int R = m->h_panel_rows[s];
         const int ntiles = m->ozL[s]->RP / oz::kTN * oz::kEpiWarps;
         if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))

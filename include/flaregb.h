@@ -261,16 +261,17 @@ int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
 
 /* C = A B^T in FP64 accuracy on the BF16 tensor cores (tcgen05), by exact
  * integer slicing of A and B (9 slices of 6 bits per row, 45 slice products
- * accumulated exactly in FP32, recombined in FP64).  A[M x K] (lda),
- * B[N x K] (ldb), C[M x N] (ldc), row-major device pointers; K <= 1472.
- * The kernel used for the sparse-GP kernel and variance products. */
+ * accumulated exactly in FP32 over K segments of at most 1472, summed and
+ * recombined in 64-bit integers, rounded once to FP64).  A[M x K] (lda),
+ * B[N x K] (ldb), C[M x N] (ldc), row-major device pointers.  The kernel
+ * used for the sparse-GP kernel and variance products. */
 int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A, long long lda,
                     const double *d_B, long long ldb, double *d_C,
                     long long ldc, void *stream);
 
 /* C = A B^T in FP32 accuracy on the same tensor-core kernel with 4 slices
  * (10 slice products, exact accumulation), FP64 inputs, FP32 output
- * C[M x N] (ldc); K <= 2720.  The kernel used for the force GEMM of the
+ * C[M x N] (ldc).  The kernel used for the force GEMM of the
  * mixed-precision path.  No reference counterpart (an internal product). */
 int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A, long long lda,
                     const double *d_B, long long ldb, float *d_C,

@@ -60,10 +60,29 @@ def test_worst_case_magnitudes_at_max_k():
     np.testing.assert_allclose(C, ref, rtol=1e-14)
 
 
-def test_k_limit_rejected():
-    from flare_gb300 import _lib
-    with pytest.raises(ValueError):
-        oz(np.zeros((4, 1500)), np.zeros((4, 1500)))
+@pytest.mark.parametrize("K", [1473, 3000, 4000])
+def test_k_segments(K):
+    """K beyond one exact-accumulation segment (1472): the kernel restarts
+    the TMEM accumulators per segment and adds the exact group sums in
+    64-bit integers, so the bound is unchanged."""
+    r = np.random.Generator(np.random.PCG64(K))
+    A = r.normal(size=(150, K)) * np.exp(r.uniform(-4, 1, size=(150, K)))
+    B = r.normal(size=(70, K)) * np.exp(r.uniform(-4, 1, size=(70, K)))
+    C = oz(A, B)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2e-15 * bound + 1e-300), float((err / bound).max())
+
+
+def test_worst_case_magnitudes_two_segments():
+    """Every slice at its largest over three segments (2 x 1472 + 56)."""
+    K = 3000
+    A = np.full((130, K), 0.99609375 - 1e-12)
+    B = np.full((50, K), -(0.99609375 - 1e-12))
+    B[::2] *= -1
+    np.testing.assert_allclose(oz(A, B), A @ B.T, rtol=1e-14)
 
 
 @pytest.mark.parametrize("sa,sb", [(1e-150, 1e-150), (1e150, 1e-160),
@@ -129,6 +148,15 @@ def test_fp32_level_integer_products_exact():
     np.testing.assert_array_equal(C, exact)
 
 
-def test_fp32_level_k_limit_rejected():
-    with pytest.raises(ValueError):
-        oz32(np.zeros((4, 2736)), np.zeros((4, 2736)))
+def test_fp32_level_k_segments():
+    """FP32-level configuration past its segment length (2720)."""
+    r = np.random.Generator(np.random.PCG64(77))
+    K = 6000
+    A = r.normal(size=(140, K))
+    B = r.normal(size=(130, K))
+    C = oz32(A, B)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2.0 ** -22 * bound + 2.0 ** -24 * np.abs(ref))
