@@ -46,8 +46,10 @@ def parse():
                     help="structures (1000 atoms each) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--replicas", type=int, default=0,
+                    help="md workload: number of replicas (default 256)")
     ap.add_argument("--workload", default="alloy1000",
-                    choices=["alloy1000", "fcc1m"],
+                    choices=["alloy1000", "fcc1m", "md"],
                     help="fcc1m: one 1,048,576-atom structure, E+F+virial, "
                          "peak device memory (reported as a side record)")
     return ap.parse_args()
@@ -583,6 +585,75 @@ def run_fcc1m(args):
     }), flush=True)
 
 
+def run_md(args):
+    """Uncertainty-aware MD ensemble (md3): replicas advanced together by
+    velocity Verlet with forces and local std every step; then the sparse
+    set grows by the most uncertain environments and is re-solved in FP64."""
+    import torch
+    from flare_gb300 import workloads as wl
+    from flare_gb300.md import Ensemble
+    c = wl.MD3
+    R = args.replicas or c["n_replicas"]
+    t0 = time.time()
+    reps = wl.md_replicas(R)           # spawned workers, before CUDA work
+    gen_s = time.time() - t0
+    t0 = time.time()
+    gp, b2, k = wl.build_md_model()
+    train_s = time.time() - t0
+    ens = Ensemble(gp, [b2], reps, c["masses"], temperature=c["temperature"],
+                   seed=c["velocity_seed0"], precision=args.precision)
+    N = R * c["n_atoms"]
+    s0 = ens.state()
+    ens.step(max(args.warmup, 1), dt=c["dt"], std_threshold=c["std_threshold"])
+    e0 = ens.state()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_md.csv"))
+    os.makedirs(os.path.dirname(clocks.path), exist_ok=True)
+    with clocks:
+        ev0.record()
+        ens.step(args.steps, dt=c["dt"], std_threshold=c["std_threshold"])
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    s1 = ens.state()
+    flagged = int(s1["flagged"].sum() - e0["flagged"].sum())
+    drift = (s1["energy"] + s1["kinetic"]) - (e0["energy"] + e0["kinetic"])
+    grow = ens.grow_sparse_set(c["n_grow"])
+    torch.cuda.synchronize()
+    ev0.record()
+    ens.step(1, dt=c["dt"], std_threshold=c["std_threshold"])
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_after = ev0.elapsed_time(ev1)
+    print(json.dumps({
+        "metric": "MD ensemble atom-steps/s (forces + local std every step)",
+        "value": N * args.steps / (ms * 1e-3), "unit": "atom-steps/s",
+        "ms_per_step": ms / args.steps, "steps": args.steps,
+        "warmup": max(args.warmup, 1), "precision": args.precision,
+        "config": {"workload": "md3: %d replicas x 2000 atoms, 3 species "
+                               "(0.5/0.3/0.2, 27/58/1 amu), 1200 K, dt 1 fs, "
+                               "B2 [3,8,4] rc 5.5 (n_d 1500), %d sparse envs"
+                               % (R, grow["sparse_before"]),
+                   "replicas": R, "atoms": N},
+        "projected_1000_steps_s": ms / args.steps,
+        "flagged_atom_steps_per_step": flagged / args.steps,
+        "flag_threshold_std_over_sigma": c["std_threshold"],
+        "max_std_over_sigma": float(s1["max_std"].max()),
+        "temperature_K": {"start": float(s0["temperature"].mean()),
+                          "end": float(s1["temperature"].mean())},
+        "total_energy_drift_ev_per_atom": {
+            "mean": float(np.mean(drift) / c["n_atoms"]),
+            "max_abs": float(np.max(np.abs(drift)) / c["n_atoms"])},
+        "sparse_update": grow,
+        "ms_per_step_after_update": ms_after,
+        "setup_s": {"train_fp64": round(train_s, 1),
+                    "replica_generation": round(gen_s, 1)},
+        "clocks": clocks.summary(),
+    }), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_setup(args.gpus if args.impl == "ours" else 0)
@@ -591,6 +662,9 @@ def main():
         return
     if args.workload == "fcc1m":
         run_fcc1m(args)
+        return
+    if args.workload == "md":
+        run_md(args)
         return
     run_ours(args, rank, world, local)
 

@@ -63,6 +63,11 @@ SIGNATURES = {
     "fgb_predict_plain": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_oz_dgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
     "fgb_oz_sgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
+    "fgb_md_create": (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _d, _i]),
+    "fgb_md_destroy": (_i, [_vp]),
+    "fgb_md_set_model": (_i, [_vp, _vp]),
+    "fgb_md_step": (_i, [_vp, _i, _d, _d, _vp]),
+    "fgb_md_read": (_i, [_vp] + [_vp] * 8 + [_vp]),
     "fgb_serve_start": (_i, [_pvp, _vp, _i, _ll, _i, _d, _i, _i]),
     "fgb_serve_submit": (_i, [_vp, _i, _vp, _vp, _vp, _pll]),
     "fgb_serve_poll": (_i, [_vp, _ll, _pi, _vp, _vp, _vp, _vp, _pd]),

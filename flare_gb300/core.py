@@ -532,9 +532,10 @@ class _Training:
                 blk[:, n_energy + n_force:] = \
                     esk[:, 1 + 3 * n_atoms:1 + 3 * n_atoms + n_stress]
                 if n_force:
-                    for a, at in enumerate(atoms):
-                        blk[:, n_energy + 3 * a:n_energy + 3 * a + 3] = \
-                            esk[:, 1 + 3 * at:1 + 3 * at + 3]
+                    ats = np.asarray(atoms, np.int64)
+                    cols = (1 + 3 * ats[:, None] +
+                            np.arange(3)[None, :]).reshape(-1)
+                    blk[:, n_energy:n_energy + cols.size] = esk[:, cols]
             old = self.Kuf_kernels[i]
             if old.shape != (n_sparse, self.n_labels):
                 old = np.zeros((n_sparse, self.n_labels))
@@ -561,9 +562,9 @@ class _Training:
         self.alpha = None
         self._model = None
 
-    def add_specific_environments(self, structure, atoms):
-        """sparse_gp.cpp:141-189."""
-        self.initialize_sparse_descriptors(structure)
+    def _specific_by_kernel(self, structure, atoms):
+        """Per kernel and species, the cluster indices of ``atoms``
+        (sparse_gp.cpp:148-168); records them in sparse_indices."""
         atoms = [int(a) for a in atoms]
         by_kernel = []
         for i in range(self.n_kernels):
@@ -577,7 +578,42 @@ class _Training:
                     ind.extend(kk for a2 in atoms if a1 == a2)
                 by_type.append(ind)
             by_kernel.append(by_type)
-        self._add_clusters(structure, by_kernel)
+        return by_kernel
+
+    def add_specific_environments(self, structure, atoms):
+        """sparse_gp.cpp:141-189."""
+        self.initialize_sparse_descriptors(structure)
+        self._add_clusters(structure,
+                           self._specific_by_kernel(structure, atoms))
+
+    def add_environments_batch(self, items):
+        """``add_specific_environments`` for several ``(structure, atoms)``
+        at once: the same Kuu, Kuf and sparse set as the calls in sequence,
+        with the new rows computed in one pass over the training structures
+        (one envs_struc per training structure instead of one per call)."""
+        items = [(s, a) for s, a in items if len(a)]
+        if not items:
+            return
+        for s, _ in items:
+            self.initialize_sparse_descriptors(s)
+        picks = [self._specific_by_kernel(s, a) for s, a in items]
+        clusters = []
+        for i in range(self.n_kernels):
+            dv0 = items[0][0].descriptors[i]
+            cd = ClusterDescriptor(dv0.n_types, dv0.n_descriptors)
+            for (s, _), bk in zip(items, picks):
+                cd.add_clusters_by_type(s.descriptors[i], bk[i])
+            clusters.append(cd)
+        self._update_Kuu(clusters)
+        self._update_Kuf(clusters)
+        self._stack_Kuu()
+        self._stack_Kuf()
+        for i in range(self.n_kernels):
+            for (s, _), bk in zip(items, picks):
+                self.sparse_descriptors[i].add_clusters_by_type(
+                    s.descriptors[i], bk[i])
+        self.alpha = None
+        self._model = None
 
     def add_all_environments(self, structure):
         """sparse_gp.cpp:307-341."""
@@ -706,12 +742,16 @@ class _Training:
                         km[u + n3:u + n3 + n4, lc] = esk[n2:n2 + n4, 0]
                         cc += 1
                     if nf_j:
-                        for at in self.training_atom_indices[j]:
-                            km[u:u + n3, lc + cc:lc + cc + 3] = \
-                                old[n1:n1 + n3, lc + cc:lc + cc + 3]
-                            km[u + n3:u + n3 + n4, lc + cc:lc + cc + 3] = \
-                                esk[n2:n2 + n4, 1 + 3 * at:1 + 3 * at + 3]
-                            cc += 3
+                        ats = np.asarray(self.training_atom_indices[j],
+                                         np.int64)
+                        cols = (1 + 3 * ats[:, None] +
+                                np.arange(3)[None, :]).reshape(-1)
+                        w = cols.size
+                        km[u:u + n3, lc + cc:lc + cc + w] = \
+                            old[n1:n1 + n3, lc + cc:lc + cc + w]
+                        km[u + n3:u + n3 + n4, lc + cc:lc + cc + w] = \
+                            esk[n2:n2 + n4, cols]
+                        cc += w
                     if ns_j:
                         km[u:u + n3, lc + cc:lc + cc + 6] = \
                             old[n1:n1 + n3, lc + cc:lc + cc + 6]

@@ -53,6 +53,14 @@ struct fgb_model_s {
   fgb_io io;
 };
 
+// One batched prediction on device positions (predict.cu): the body of
+// fgb_predict, also driven by the MD ensemble.
+int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
+                 const double *h_cells, const double *d_positions,
+                 const int *d_species, double cutoff, int want, int precision,
+                 double *d_energy, double *d_forces, double *d_stress,
+                 double *d_local_var, cudaStream_t st);
+
 namespace fgb {
 int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
                       bool want_grad, bool want_var, double *d_e_atom,

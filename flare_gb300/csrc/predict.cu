@@ -486,7 +486,7 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
 }
 
 // ------------------------------------------------------------- predict
-static int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
+int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
                         const double *h_cells, const double *d_positions,
                         const int *d_species, double cutoff, int want,
                         int precision, double *d_energy, double *d_forces,

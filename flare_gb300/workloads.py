@@ -120,3 +120,68 @@ def fcc_structure(n_cells=None, seed=None):
     c = FCC1M
     return syn.fcc_al(n_cells=n_cells or c["n_cells"], a=c["a"],
                       sigma=c["sigma_disp"], seed=seed or c["seed"])
+
+
+# ``md3``: an ensemble of 2,000-atom 3-species cubic cells at
+# 0.06 atoms/A^3 (species fractions 0.5/0.3/0.2, masses 27/58/1 amu), filled
+# by random sequential addition with a 1.8 A minimum distance (replica r:
+# seed 5000 + r), Maxwell-Boltzmann velocities at 1,200 K (seed 5500 + r),
+# velocity Verlet dt = 1 fs; atoms flagged when their local std (divided by
+# sigma, as the reference calculator reports it) exceeds 0.05.
+# Model: B2 chebyshev/quadratic [3, 8, 4], rc 5.5 A (n_d = 1,500);
+# NormalizedDotProduct sigma 2, power 2; 8,000 sparse environments = every
+# atom of 4 training cells (seeds 5600-5603) labelled by truncated LJ energies
+# and forces (eps 0.4/0.25/0.1 eV, sigma 1.8/1.7/1.5 A, Lorentz-Berthelot
+# mixing: the 1.8 A minimum distance of the cells sits at or beyond sigma, so
+# the replicas start near the potential's repulsive edge instead of high up
+# its wall); noise sigma_E 1e-3 eV/atom, sigma_F 0.05 eV/A.  The sparse set then
+# grows by the 256 most uncertain environments of the ensemble and is
+# re-solved in FP64.
+MD3 = dict(n_atoms=2000, density=0.06, fractions=(0.5, 0.3, 0.2), dmin=1.8,
+           masses=(27.0, 58.0, 1.0), temperature=1200.0, dt=1.0,
+           std_threshold=0.05, n_replicas=256, replica_seed0=5000,
+           velocity_seed0=5500, rc=5.5, n_max=8, l_max=4, sigma=2.0, power=2,
+           n_train=4, train_seed0=5600, eps=(0.4, 0.25, 0.1),
+           lj_sigma=(1.8, 1.7, 1.5), sigma_e_per_atom=1e-3, sigma_f=0.05,
+           sigma_s=1.0, n_grow=256)
+
+
+def md_cell(seed):
+    c = MD3
+    return syn.rsa_alloy(c["n_atoms"], density=c["density"],
+                         fractions=c["fractions"], dmin=c["dmin"], seed=seed)
+
+
+def md_replicas(n, processes=8):
+    """Replica cells ``md_cell(replica_seed0 + r)``, r < n, generated by a
+    pool of spawned processes (safe after CUDA is initialised)."""
+    import multiprocessing as mp
+    seeds = [MD3["replica_seed0"] + r for r in range(n)]
+    if n <= 4 or processes <= 1:
+        return [md_cell(s) for s in seeds]
+    with mp.get_context("spawn").Pool(min(processes, n)) as pool:
+        return pool.map(md_cell, seeds)
+
+
+def build_md_model(n_train=None):
+    """Train the 3-species ensemble model on the GPU (FP64); every atom of
+    the training cells is a sparse environment."""
+    import flare_gb300 as fg
+    c = MD3
+    n_train = n_train or c["n_train"]
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, c["rc"]], [],
+               [3, c["n_max"], c["l_max"]])
+    k = fg.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = fg.SparseGP([k], c["sigma_e_per_atom"] * c["n_atoms"], c["sigma_f"],
+                     c["sigma_s"])
+    for t in range(n_train):
+        cell, sp, pos = md_cell(c["train_seed0"] + t)
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, c["eps"], c["lj_sigma"],
+                                    c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(st, list(range(len(sp))))
+    gp.update_matrices_QR()
+    return gp, b2, k

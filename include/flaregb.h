@@ -202,6 +202,37 @@ int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
                      int precision, double *h_energy, double *h_forces,
                      double *h_stress, double *h_local_var, void *stream);
 
+/* --------------------------------------------------- MD ensemble
+ * Uncertainty-aware molecular dynamics on the device: R replicas of N atoms
+ * (own cells and species, packed replica by replica) advanced together by
+ * velocity Verlet with the model's forces, every replica predicted in one
+ * batched call per step (precision as in fgb_predict).  No counterpart in
+ * flare_pp: the reference's OTF learner (flare/learners/otf.py:507-521)
+ * drives an ASE integrator on the host and calls SGP_Calculator once per
+ * structure per step.  Units: A, A/fs, amu, eV; dt in fs.  After each step
+ * the local std of every atom, sign(v) sqrt|v| / |sigma| (calculator.py:121),
+ * is compared with std_threshold and counted per replica.  The ensemble
+ * shares the model's device workspace: do not predict with the same model
+ * handle concurrently. */
+typedef struct fgb_md_s *fgb_md_t;
+int fgb_md_create(fgb_md_t *out, fgb_model_t model, int n_replicas,
+                  int n_atoms, const double *h_cells, const double *h_positions,
+                  const double *h_velocities, const int *h_species,
+                  const double *h_masses, double cutoff, int precision);
+int fgb_md_destroy(fgb_md_t md);
+/* Switch to another (re-solved) model with the same species; forces are
+ * recomputed at the next step. */
+int fgb_md_set_model(fgb_md_t md, fgb_model_t model);
+int fgb_md_step(fgb_md_t md, int n_steps, double dt, double std_threshold,
+                void *stream);
+/* Current state to host buffers (any may be NULL): positions, velocities,
+ * forces [R*N*3], local variances [R*N], potential and kinetic energies
+ * [R], largest std [R], flagged atom-steps since creation [R]. */
+int fgb_md_read(fgb_md_t md, double *h_positions, double *h_velocities,
+                double *h_forces, double *h_local_var, double *h_energy,
+                double *h_kinetic, double *h_max_std, long long *h_flagged,
+                void *stream);
+
 /* ------------------------------------------------------------ serving
  * Continuous batching over a solved model.  fgb_serve_start launches
  * n_workers host threads; each owns a replica of the model (same weights,

@@ -111,3 +111,41 @@ def test_plain_form_matches_fused_path():
     np.testing.assert_allclose(mean[-6:], fused["stress"][0], atol=1e-10)
     np.testing.assert_allclose(var.cpu().numpy(), fused["local_var"],
                                atol=1e-12)
+
+
+def test_batched_environment_addition_matches_sequential():
+    """add_environments_batch gives the Kuu, Kuf, sparse set and weights of
+    the same add_specific_environments calls made one by one."""
+    import flare_gb300 as fg
+    S = 2
+    b2a = b2_args(S, 3, 2, 5.0)
+    gb2 = fg.B2(*b2a[:5])
+    gps = [fg.SparseGP([fg.NormalizedDotProduct(1.5, 2)], 0.3, 0.2, 0.4)
+           for _ in range(2)]
+    strucs = []
+    for t in range(3):
+        cell, sp, pos = random_atoms(seed=70 + t)
+        E, F, St = lj_labels(cell, sp, pos, S)
+        st = fg.Structure(cell, sp, pos, 5.0, [gb2])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        st.stresses = St
+        strucs.append(st)
+    for gp in gps:
+        for st in strucs[:2]:
+            gp.add_training_structure(st)
+            gp.add_specific_environments(st, [0, 3])
+    picks = [(strucs[0], [1, 5]), (strucs[2], [2, 4, 6]), (strucs[1], [7])]
+    for st, atoms in picks:
+        gps[0].add_specific_environments(st, atoms)
+    gps[1].add_environments_batch(picks)
+    for gp in gps:
+        gp.update_matrices_QR()
+    a, b = gps
+    assert a.n_sparse == b.n_sparse
+    np.testing.assert_allclose(b.Kuu, a.Kuu, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(b.Kuf, a.Kuf, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(b.alpha, a.alpha, rtol=1e-9, atol=1e-9)
+    for s in range(S):
+        np.testing.assert_array_equal(b.sparse_descriptors[0].descriptors[s],
+                                      a.sparse_descriptors[0].descriptors[s])
