@@ -46,10 +46,12 @@ def parse():
                     help="structures (1000 atoms each) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--requests", type=int, default=0,
+                    help="serve workload: number of requests (default 4096)")
     ap.add_argument("--replicas", type=int, default=0,
                     help="md workload: number of replicas (default 256)")
     ap.add_argument("--workload", default="alloy1000",
-                    choices=["alloy1000", "fcc1m", "md"],
+                    choices=["alloy1000", "fcc1m", "md", "serve"],
                     help="fcc1m: one 1,048,576-atom structure, E+F+virial, "
                          "peak device memory (reported as a side record)")
     return ap.parse_args()
@@ -585,6 +587,86 @@ def run_fcc1m(args):
     }), flush=True)
 
 
+def run_serve(args):
+    """Serving stream (serve3): requests of 32-4096 atoms and 1-3 species
+    through the continuous-batching server; first all at once (saturation
+    throughput), then Poisson arrivals at 0.25-4x that rate, each with
+    throughput and p50/p99 latency (submit to result, server clock)."""
+    import threading
+    import torch
+    from flare_gb300 import workloads as wl
+    from flare_gb300.serving import Server
+    c = wl.SERVE3
+    n_req = args.requests or c["n_requests"]
+    t0 = time.time()
+    reqs = wl.serve_requests(n_req)          # spawned workers
+    gen_s = time.time() - t0
+    t0 = time.time()
+    gp, b2, k = wl.build_serve_model()
+    train_s = time.time() - t0
+    atoms = np.array([len(r[1]) for r in reqs])
+    srv = Server(gp, b2, c["rc"], n_workers=2, memory_budget_gb=16.0,
+                 max_structures=64, precision=args.precision)
+    for q in range(min(8, n_req)):            # warm-up: model set-up, kernels
+        srv.result(srv.submit(*reqs[q]))
+
+    def run(times):
+        """Submit request q at times[q] (s from start); wait for all."""
+        ids = [None] * n_req
+        start = time.perf_counter()
+
+        def producer():
+            for q in range(n_req):
+                while True:
+                    dt = times[q] - (time.perf_counter() - start)
+                    if dt <= 0:
+                        break
+                    time.sleep(min(dt, 2e-4) if dt > 2e-4 else 0)
+                ids[q] = srv.submit(*reqs[q])
+        b0 = srv.stats()["batches"]
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        lat = np.array([srv.result(i)["latency_ms"] for i in ids])
+        span = time.perf_counter() - start
+        return {"requests": n_req, "seconds": span,
+                "atoms_per_s": float(atoms.sum() / span),
+                "requests_per_s": n_req / span,
+                "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)),
+                "batches": srv.stats()["batches"] - b0}
+
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with Clocks(os.path.join(ROOT, "gpurun_out", "clocks_serve.csv")) as clocks:
+        sat = run(np.zeros(n_req))
+        lam = sat["requests_per_s"]
+        sweep = []
+        rng_ = np.random.Generator(np.random.PCG64(4500))
+        for f in (0.25, 0.5, 1.0, 2.0, 4.0):
+            gaps = rng_.exponential(1.0 / (f * lam), size=n_req)
+            r = run(np.cumsum(gaps) - gaps[0])
+            r["offered_rate_x_saturation"] = f
+            sweep.append(r)
+    srv.close()
+    print(json.dumps({
+        "metric": "serving atoms/s (E+F+stress+local std per request) with "
+                  "p50/p99 latency",
+        "value": sat["atoms_per_s"], "unit": "atoms/s",
+        "precision": args.precision,
+        "config": {"workload": "serve3: %d requests, 32-4096 atoms "
+                               "(log-uniform), 1-3 species, density "
+                               "0.05-0.09; B2 [3,8,4] rc 5.5 (n_d 1500), "
+                               "1000 sparse envs per species; 2 workers, "
+                               "<= 64 structures per batch" % n_req,
+                   "atoms_total": int(atoms.sum()),
+                   "atoms_mean": float(atoms.mean())},
+        "saturation": sat, "poisson_sweep": sweep,
+        "setup_s": {"train_fp64": round(train_s, 1),
+                    "request_generation": round(gen_s, 1)},
+        "clocks": clocks.summary(),
+    }), flush=True)
+
+
 def run_md(args):
     """Uncertainty-aware MD ensemble (md3): replicas advanced together by
     velocity Verlet with forces and local std every step; then the sparse
@@ -665,6 +747,9 @@ def main():
         return
     if args.workload == "md":
         run_md(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
     run_ours(args, rank, world, local)
 

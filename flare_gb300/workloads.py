@@ -185,3 +185,70 @@ def build_md_model(n_train=None):
         gp.add_specific_environments(st, list(range(len(sp))))
     gp.update_matrices_QR()
     return gp, b2, k
+
+
+# ``serve3``: prediction requests of uneven size and species mix.
+# Request q (seed 4000 + q): N = floor(exp(U[ln 32, ln 4096])) atoms, a
+# uniformly drawn number (1-3) of the 3 species with fractions uniform on the
+# simplex, density U[0.05, 0.09] atoms/A^3, random sequential addition with a
+# 1.8 A minimum distance.  Model: the alloy1000 descriptor and kernel
+# settings with 3 species (B2 [3, 8, 4], rc 5.5 A, n_d 1,500), 1,000 sparse
+# environments per species drawn (seed 4300) from 10 training cells of 1,000
+# atoms (seeds 4200-4209, species 1/3 each, density 0.06) with the md3 LJ
+# labels.
+SERVE3 = dict(n_requests=4096, seed0=4000, n_min=32, n_max_atoms=4096,
+              density=(0.05, 0.09), dmin=1.8, rc=5.5, n_max=8, l_max=4,
+              sigma=2.0, power=2, n_train=10, train_atoms=1000,
+              train_seed0=4200, sparse_per_species=1000, sparse_seed=4300,
+              sigma_e_per_atom=1e-3, sigma_f=0.05, sigma_s=1.0)
+
+
+def serve_request(q):
+    """Request q of the serving stream: (cell, species, positions)."""
+    c = SERVE3
+    r = syn.rng(c["seed0"] + q)
+    n = int(np.floor(np.exp(r.uniform(np.log(c["n_min"]),
+                                      np.log(c["n_max_atoms"])))))
+    k = int(r.integers(1, 4))
+    present = r.choice(3, size=k, replace=False)
+    fr = np.zeros(3)
+    fr[present] = r.dirichlet(np.ones(k))
+    dens = float(r.uniform(*c["density"]))
+    return syn.rsa_alloy(n, density=dens, fractions=fr, dmin=c["dmin"],
+                         seed=c["seed0"] + 100000 + q)
+
+
+def serve_requests(n, processes=16):
+    """The first n requests, generated by spawned worker processes."""
+    import multiprocessing as mp
+    if n <= 8 or processes <= 1:
+        return [serve_request(q) for q in range(n)]
+    with mp.get_context("spawn").Pool(processes) as pool:
+        return pool.map(serve_request, range(n), chunksize=16)
+
+
+def build_serve_model():
+    """Train the 3-species serving model on the GPU (FP64)."""
+    import flare_gb300 as fg
+    c, m = SERVE3, MD3
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, c["rc"]], [],
+               [3, c["n_max"], c["l_max"]])
+    k = fg.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = fg.SparseGP([k], c["sigma_e_per_atom"] * c["train_atoms"],
+                     c["sigma_f"], c["sigma_s"])
+    data = [syn.rsa_alloy(c["train_atoms"], density=0.06,
+                          fractions=(1 / 3, 1 / 3, 1 / 3), dmin=c["dmin"],
+                          seed=c["train_seed0"] + t)
+            for t in range(c["n_train"])]
+    sparse = alloy_sparse_choice(c["n_train"], [d[1] for d in data],
+                                 c["sparse_per_species"], c["sparse_seed"])
+    for t, (cell, sp, pos) in enumerate(data):
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, m["eps"], m["lj_sigma"],
+                                    c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(st, sparse[t])
+    gp.update_matrices_QR()
+    return gp, b2, k
