@@ -700,8 +700,18 @@ def run_md(args):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     s1 = ens.state()
+    stats = ens.stats()
     flagged = int(s1["flagged"].sum() - e0["flagged"].sum())
     drift = (s1["energy"] + s1["kinetic"]) - (e0["energy"] + e0["kinetic"])
+    # the same number of steps without graph replay (full, checked steps)
+    ens.set_graphs(False)
+    torch.cuda.synchronize()
+    ev0.record()
+    ens.step(args.steps, dt=c["dt"], std_threshold=c["std_threshold"])
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_full = ev0.elapsed_time(ev1)
+    ens.set_graphs(True)
     grow = ens.grow_sparse_set(c["n_grow"])
     torch.cuda.synchronize()
     ev0.record()
@@ -720,6 +730,9 @@ def run_md(args):
                                % (R, grow["sparse_before"]),
                    "replicas": R, "atoms": N},
         "projected_1000_steps_s": ms / args.steps,
+        "graph_replay": {"ms_per_step_replayed": ms / args.steps,
+                         "ms_per_step_full": ms_full / args.steps,
+                         "counters_timed_region": stats},
         "flagged_atom_steps_per_step": flagged / args.steps,
         "flag_threshold_std_over_sigma": c["std_threshold"],
         "max_std_over_sigma": float(s1["max_std"].max()),

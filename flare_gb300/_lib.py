@@ -67,6 +67,8 @@ SIGNATURES = {
     "fgb_md_destroy": (_i, [_vp]),
     "fgb_md_set_model": (_i, [_vp, _vp]),
     "fgb_md_step": (_i, [_vp, _i, _d, _d, _vp]),
+    "fgb_md_set_graphs": (_i, [_vp, _i, _d]),
+    "fgb_md_stats": (_i, [_vp, _vp]),
     "fgb_md_read": (_i, [_vp] + [_vp] * 8 + [_vp]),
     "fgb_serve_start": (_i, [_pvp, _vp, _i, _ll, _i, _d, _i, _i]),
     "fgb_serve_submit": (_i, [_vp, _i, _vp, _vp, _vp, _pll]),

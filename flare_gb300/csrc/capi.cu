@@ -1,5 +1,6 @@
 // C-ABI plumbing for libflaregb: error state, device buffers, host cell
 // algebra, deterministic scans, B2 settings.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -26,9 +27,14 @@ int cuda_status(cudaError_t e, const char *where) {
   return FGB_ECUDA;
 }
 
+static std::atomic<unsigned long long> g_allocations{0};
+
+unsigned long long devbuf_allocations() { return g_allocations.load(); }
+
 int DevBuf::ensure(size_t n) {
   if (n == 0) n = 16;
   if (n <= bytes) return FGB_OK;
+  g_allocations.fetch_add(1);
   release();
   cudaError_t e = cudaMalloc(&p, n);
   if (e != cudaSuccess) {

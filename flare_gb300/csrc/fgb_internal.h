@@ -18,6 +18,10 @@ struct DevBuf {
   template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+// Device allocations made by DevBuf::ensure so far (process-wide): a graph
+// captured while this number changed may refer to freed buffers.
+unsigned long long devbuf_allocations();
+
 // Per-structure geometry for the cell-list build (device copy).
 struct StrucGeom {
   double cell[9];
@@ -54,11 +58,25 @@ int scan_int_to_ll_raw(const int *d_in, long long *d_out, int n,
 
 }  // namespace fgb
 
+struct fgb_nlist_s;
+namespace fgb {
+// Per-pair buffers for at least `cap` pairs (neighbors.cu).
+int nlist_reserve(fgb_nlist_s *nl, long long cap);
+// The list of the last full build's structures (same atoms, cells, bins) at
+// new positions, with no host synchronisation and no allocation: pairs go
+// into the capacity reserved by nlist_reserve; more pairs than that set
+// flag[3] and truncate every list at the capacity (the caller discards the
+// result).  Flags are cleared first and left on the device for the caller.
+int nlist_rebuild_fixed(fgb_nlist_s *nl, const double *d_positions,
+                        double cutoff, long long cap, cudaStream_t st);
+}  // namespace fgb
+
 struct fgb_nlist_s {
   int n_struc = 0;
   int n_atoms = 0;
   long long n_pairs = 0;
   int max_neighbors = 0;
+  long long n_bins = 0;       // bins of the last full build
   std::vector<int> h_atom_offsets;
   std::vector<double> h_cells;
   std::vector<double> h_volume;
@@ -80,7 +98,9 @@ struct fgb_nlist_s {
   fgb::DevBuf nbr_shift;     // int[P]  packed (s0+128)<<16|(s1+128)<<8|(s2+128)
   fgb::DevBuf nbr_rel;       // double4_16a[P] (d, x, y, z)
   fgb::DevBuf nbr_twin;      // long long[P] index of (j -> i, -s)
-  fgb::DevBuf flag;          // int[4] device error flags
+  fgb::DevBuf flag;          // int[4] device error flags: non-finite
+                             // positions, fill or twin inconsistency, pair
+                             // capacity exceeded (fixed rebuild)
   fgb::DevBuf scan_tmp;
   fgb::DevBuf scalars;       // long long[4]
 };

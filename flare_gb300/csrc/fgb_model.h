@@ -51,26 +51,50 @@ struct fgb_model_s {
   fgb_nlist_s nl;
   fgb_workspace ws;
   fgb_io io;
+  std::vector<int> last_species_counts;   // atoms per species, last full call
 };
 
+namespace fgb {
+// A prediction repeated on the atoms, species and cells of the model's last
+// full call at new positions (a molecular-dynamics step).  The geometry, the
+// species permutation and the workspace of that call are reused, the
+// neighbour list is rebuilt into a reserved pair capacity, and nothing is
+// read back, synchronised or allocated: the launches can be captured in a
+// CUDA graph.  Error flags stay on the device for the caller: nl.flag (and
+// flag[3] = pair capacity exceeded) and ws.ozerr (bounded tensor-core
+// waits), which the caller clears before the call.
+struct FixedPlan {
+  long long pair_cap = 0;
+  std::vector<int> counts;   // atoms per species (last_species_counts)
+};
+}  // namespace fgb
+
+// A model with the same weights and its own device workspace (predict.cu);
+// nullptr with rc set on failure.
+fgb_model_s *model_replicate(const fgb_model_s *src, int &rc);
+
 // One batched prediction on device positions (predict.cu): the body of
-// fgb_predict, also driven by the MD ensemble.
+// fgb_predict, also driven by the MD ensemble (with `fixed` for the steps
+// it replays).
 int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
                  const double *h_cells, const double *d_positions,
                  const int *d_species, double cutoff, int want, int precision,
                  double *d_energy, double *d_forces, double *d_stress,
-                 double *d_local_var, cudaStream_t st);
+                 double *d_local_var, cudaStream_t st,
+                 const fgb::FixedPlan *fixed = nullptr);
 
 namespace fgb {
 int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
                       bool want_grad, bool want_var, double *d_e_atom,
                       double *d_gB2, double *d_var, cudaStream_t st);
+// `fixed`: neither clear nor read ws.ozerr (the caller does both)
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
-                    cudaStream_t st);
+                    cudaStream_t st, bool fixed = false);
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
-                       double *d_gB2, double *d_var, cudaStream_t st);
+                       double *d_gB2, double *d_var, cudaStream_t st,
+                       bool fixed = false);
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st);
 int envs_struc_impl(const B2Params &p, double sigma, double power,

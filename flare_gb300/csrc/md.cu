@@ -12,6 +12,19 @@
 // with a threshold and counted per replica; kinetic energies are summed per
 // replica.  Reductions run in a fixed order and counters are integers: a
 // replica's trajectory is the same alone and in the ensemble.
+//
+// Replayed steps.  Atoms, species and cells do not change between steps, so
+// after one full step the step is captured once as a CUDA graph (the
+// prediction in its fixed form: neighbour list rebuilt into a reserved pair
+// capacity, species permutation and geometry reused, no host
+// synchronisation) and replayed.  Device error flags of every replayed
+// step are ORed into a status word read once per chunk of steps; a chunk
+// that overflowed the pair capacity or raised any flag is rolled back to a
+// snapshot taken before it and redone with full, checked steps, after which
+// the capacity is re-planned and the step captured again.  Replayed and
+// full steps run the same kernels on the same data: the trajectories are
+// identical.  The ensemble predicts with a private replica of the model, so
+// the buffers a captured graph refers to belong to it alone.
 #include "fgb_internal.h"
 #include "fgb_model.h"
 
@@ -77,13 +90,29 @@ __global__ void k_observe(int N, const int *__restrict__ species,
   }
 }
 
+// Sticky status of replayed steps: bit 0 neighbour-list flags (non-finite
+// positions, fill or twin inconsistency), bit 1 pair capacity exceeded,
+// bit 2 a bounded tensor-core wait ran out.
+__global__ void k_collect(const int *__restrict__ nl_flag,
+                          const int *__restrict__ ozerr,
+                          int *__restrict__ status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int s = 0;
+  if (nl_flag[0] | nl_flag[1] | nl_flag[2]) s |= 1;
+  if (nl_flag[3]) s |= 2;
+  if (ozerr[0]) s |= 4;
+  if (s) atomicOr(status, s);
+}
+
+constexpr int kChunk = 50;   // replayed steps per status read
+
 }  // namespace
 }  // namespace fgb
 
 using namespace fgb;
 
 struct fgb_md_s {
-  fgb_model_s *model = nullptr;
+  fgb_model_s *model = nullptr;    // private replica of the caller's model
   int R = 0, N = 0;
   double cutoff = 0.0;
   int precision = FGB_PREC_MIXED;
@@ -92,17 +121,43 @@ struct fgb_md_s {
   DevBuf pos, vel, force, species, mass, inv_mass, energy, var, flagged,
       kinetic, max_std;
   bool have_forces = false;
+  // replayed steps
+  bool graphs = true;
+  double pair_margin = 0.25;       // capacity = pairs of the last full step x (1 + margin) + 4096
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double g_dt = 0.0, g_thresh = 0.0;
+  unsigned long long g_allocs = 0;  // allocation count when captured
+  FixedPlan plan;
+  bool planned = false;
+  DevBuf status, s_pos, s_vel, s_force, s_energy, s_var, s_flagged, s_kinetic,
+      s_max_std;
+  long long n_replayed = 0, n_full = 0, n_captures = 0, n_rollbacks = 0;
+
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+  ~fgb_md_s() {
+    drop_graph();
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    delete model;
+  }
 };
 
-static int md_forces(fgb_md_s *md, cudaStream_t st) {
+// Forces, energies and variances at the current positions: the full,
+// checked prediction, or (plan given) the fixed one.
+static int md_forces(fgb_md_s *md, cudaStream_t st,
+                     const FixedPlan *plan = nullptr) {
   const int want = FGB_WANT_ENERGY | FGB_WANT_FORCES | FGB_WANT_LOCAL_VAR;
   int rc = predict_impl(md->model, md->R, md->h_offsets.data(),
                         md->h_cells.data(), md->pos.as<double>(),
                         md->species.as<int>(), md->cutoff, want,
                         md->precision, md->energy.as<double>(),
                         md->force.as<double>(), nullptr, md->var.as<double>(),
-                        st);
+                        st, plan);
   if (rc) return rc;
+  if (!plan) md->planned = false;   // a full build may have moved buffers
   md->have_forces = true;
   return FGB_OK;
 }
@@ -149,7 +204,11 @@ extern "C" int fgb_md_create(fgb_md_t *out, fgb_model_t model, int n_replicas,
       return FGB_EINVAL;
     }
   auto *md = new fgb_md_s();
-  md->model = model;
+  int rc = FGB_OK;
+  if (!(md->model = model_replicate(model, rc))) {
+    delete md;
+    return rc;
+  }
   md->R = n_replicas;
   md->N = n_atoms;
   md->cutoff = cutoff;
@@ -159,7 +218,6 @@ extern "C" int fgb_md_create(fgb_md_t *out, fgb_model_t model, int n_replicas,
   md->h_cells.assign(h_cells, h_cells + 9 * (size_t)n_replicas);
   std::vector<double> inv(S);
   for (int s = 0; s < S; s++) inv[s] = 1.0 / h_masses[s];
-  int rc;
   if ((rc = md->pos.ensure(sizeof(double) * 3 * NT)) ||
       (rc = md->vel.ensure(sizeof(double) * 3 * NT)) ||
       (rc = md->force.ensure(sizeof(double) * 3 * NT)) ||
@@ -170,7 +228,8 @@ extern "C" int fgb_md_create(fgb_md_t *out, fgb_model_t model, int n_replicas,
       (rc = md->var.ensure(sizeof(double) * NT)) ||
       (rc = md->flagged.ensure(sizeof(long long) * n_replicas)) ||
       (rc = md->kinetic.ensure(sizeof(double) * n_replicas)) ||
-      (rc = md->max_std.ensure(sizeof(double) * n_replicas))) {
+      (rc = md->max_std.ensure(sizeof(double) * n_replicas)) ||
+      (rc = md->status.ensure(sizeof(int)))) {
     delete md;
     return rc;
   }
@@ -204,8 +263,156 @@ extern "C" int fgb_md_set_model(fgb_md_t md, fgb_model_t model) {
     set_error("fgb_md_set_model: invalid arguments");
     return FGB_EINVAL;
   }
-  md->model = model;
+  int rc = FGB_OK;
+  fgb_model_s *rep = model_replicate(model, rc);
+  if (!rep) return rc;
+  md->drop_graph();
+  delete md->model;
+  md->model = rep;
+  md->planned = false;
   md->have_forces = false;   // recomputed at the next step
+  return FGB_OK;
+}
+
+extern "C" int fgb_md_set_graphs(fgb_md_t md, int enable, double pair_margin) {
+  if (!md || !(pair_margin > -0.5) || !(pair_margin <= 16.0)) {
+    set_error("fgb_md_set_graphs: invalid arguments");
+    return FGB_EINVAL;
+  }
+  md->graphs = enable != 0;
+  md->pair_margin = pair_margin;
+  md->planned = false;
+  md->drop_graph();
+  return FGB_OK;
+}
+
+extern "C" int fgb_md_stats(fgb_md_t md, long long *out4) {
+  if (!md || !out4) {
+    set_error("fgb_md_stats: invalid arguments");
+    return FGB_EINVAL;
+  }
+  out4[0] = md->n_replayed;
+  out4[1] = md->n_full;
+  out4[2] = md->n_captures;
+  out4[3] = md->n_rollbacks;
+  return FGB_OK;
+}
+
+// One velocity-Verlet step; `plan` selects the fixed prediction (then the
+// step's device flags are collected into md->status).
+static int md_step_once(fgb_md_s *md, double dt, double thresh,
+                        cudaStream_t st, const FixedPlan *plan) {
+  const long long n3 = 3LL * md->R * md->N;
+  const int T = 256;
+  int rc;
+  if (plan)
+    FGB_CUDA(cudaMemsetAsync(md->model->ws.ozerr.p, 0, sizeof(int), st));
+  k_vv<<<ceil_div(n3, T), T, 0, st>>>(n3, md->species.as<int>(),
+                                      md->inv_mass.as<double>(), 0.5 * dt, dt,
+                                      md->force.as<double>(),
+                                      md->vel.as<double>(),
+                                      md->pos.as<double>());
+  FGB_LAUNCH_CHECK("k_vv");
+  if ((rc = md_forces(md, st, plan))) return rc;
+  if (plan) {
+    k_collect<<<1, 32, 0, st>>>(md->model->nl.flag.as<int>(),
+                                md->model->ws.ozerr.as<int>(),
+                                md->status.as<int>());
+    FGB_LAUNCH_CHECK("k_collect");
+  }
+  k_vv<<<ceil_div(n3, T), T, 0, st>>>(n3, md->species.as<int>(),
+                                      md->inv_mass.as<double>(), 0.5 * dt, 0.0,
+                                      md->force.as<double>(),
+                                      md->vel.as<double>(), nullptr);
+  FGB_LAUNCH_CHECK("k_vv");
+  return md_observe(md, thresh, st);
+}
+
+// Pair capacity and buffers for fixed steps, from the last full step.
+static int md_plan(fgb_md_s *md) {
+  fgb_model_s *m = md->model;
+  const long long P = m->nl.n_pairs;
+  long long cap = (long long)std::ceil((double)P * (1.0 + md->pair_margin));
+  if (md->pair_margin >= 0.0) cap += 4096;
+  cap = std::max(cap, 1LL);
+  int rc;
+  if ((rc = nlist_reserve(&m->nl, cap)) ||
+      (rc = m->ws.pair_grad.ensure(sizeof(double3) * (cap + 1))) ||
+      (rc = m->ws.ozerr.ensure(sizeof(int))))
+    return rc;
+  const long long NT = (long long)md->R * md->N;
+  const struct { DevBuf *b; size_t n; } snaps[] = {
+      {&md->s_pos, sizeof(double) * 3 * NT},
+      {&md->s_vel, sizeof(double) * 3 * NT},
+      {&md->s_force, sizeof(double) * 3 * NT},
+      {&md->s_energy, sizeof(double) * md->R},
+      {&md->s_var, sizeof(double) * NT},
+      {&md->s_flagged, sizeof(long long) * md->R},
+      {&md->s_kinetic, sizeof(double) * md->R},
+      {&md->s_max_std, sizeof(double) * md->R}};
+  for (const auto &q : snaps)
+    if ((rc = q.b->ensure(q.n))) return rc;
+  md->plan.pair_cap = cap;
+  md->plan.counts = m->last_species_counts;
+  md->planned = true;
+  md->drop_graph();
+  return FGB_OK;
+}
+
+// Capture one fixed step on the ensemble's own stream.
+static int md_capture(fgb_md_s *md, double dt, double thresh) {
+  if (!md->cap_stream)
+    FGB_CUDA(cudaStreamCreateWithFlags(&md->cap_stream, cudaStreamNonBlocking));
+  md->drop_graph();
+  for (int attempt = 0; attempt < 2; attempt++) {
+    const unsigned long long a0 = devbuf_allocations();
+    FGB_CUDA(cudaStreamBeginCapture(md->cap_stream,
+                                    cudaStreamCaptureModeRelaxed));
+    const int rc = md_step_once(md, dt, thresh, md->cap_stream, &md->plan);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(md->cap_stream, &g);
+    if (rc || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      if (rc) return rc;
+      return cuda_status(e, "fgb_md_step: graph capture");
+    }
+    if (devbuf_allocations() != a0) {   // a buffer moved while recording
+      cudaGraphDestroy(g);
+      continue;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&md->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      md->exec = nullptr;
+      return cuda_status(ei, "fgb_md_step: graph instantiation");
+    }
+    md->g_dt = dt;
+    md->g_thresh = thresh;
+    md->g_allocs = a0;
+    md->n_captures++;
+    return FGB_OK;
+  }
+  set_error("fgb_md_step: buffers kept growing during graph capture");
+  return FGB_ECUDA;
+}
+
+// Copies between the state and its snapshot (to_snap: state -> snapshot).
+static int md_snapshot(fgb_md_s *md, bool to_snap, cudaStream_t st) {
+  const long long NT = (long long)md->R * md->N;
+  const struct { DevBuf *a, *b; size_t n; } pairs[] = {
+      {&md->pos, &md->s_pos, sizeof(double) * 3 * NT},
+      {&md->vel, &md->s_vel, sizeof(double) * 3 * NT},
+      {&md->force, &md->s_force, sizeof(double) * 3 * NT},
+      {&md->energy, &md->s_energy, sizeof(double) * md->R},
+      {&md->var, &md->s_var, sizeof(double) * NT},
+      {&md->flagged, &md->s_flagged, sizeof(long long) * md->R},
+      {&md->kinetic, &md->s_kinetic, sizeof(double) * md->R},
+      {&md->max_std, &md->s_max_std, sizeof(double) * md->R}};
+  for (const auto &q : pairs)
+    FGB_CUDA(cudaMemcpyAsync(to_snap ? q.b->p : q.a->p,
+                             to_snap ? q.a->p : q.b->p, q.n,
+                             cudaMemcpyDeviceToDevice, st));
   return FGB_OK;
 }
 
@@ -216,24 +423,42 @@ extern "C" int fgb_md_step(fgb_md_t md, int n_steps, double dt,
     return FGB_EINVAL;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  const long long n3 = 3LL * md->R * md->N;
-  const int T = 256;
   int rc;
   if (!md->have_forces && (rc = md_forces(md, st))) return rc;
-  for (int k = 0; k < n_steps; k++) {
-    k_vv<<<ceil_div(n3, T), T, 0, st>>>(n3, md->species.as<int>(),
-                                        md->inv_mass.as<double>(), 0.5 * dt,
-                                        dt, md->force.as<double>(),
-                                        md->vel.as<double>(),
-                                        md->pos.as<double>());
-    FGB_LAUNCH_CHECK("k_vv");
-    if ((rc = md_forces(md, st))) return rc;
-    k_vv<<<ceil_div(n3, T), T, 0, st>>>(n3, md->species.as<int>(),
-                                        md->inv_mass.as<double>(), 0.5 * dt,
-                                        0.0, md->force.as<double>(),
-                                        md->vel.as<double>(), nullptr);
-    FGB_LAUNCH_CHECK("k_vv");
-    if ((rc = md_observe(md, std_threshold, st))) return rc;
+  int k = 0;
+  while (k < n_steps) {
+    if (!md->graphs) {
+      if ((rc = md_step_once(md, dt, std_threshold, st, nullptr))) return rc;
+      md->n_full++;
+      k++;
+      continue;
+    }
+    if (!md->planned && (rc = md_plan(md))) return rc;
+    if (!md->exec || md->g_dt != dt || md->g_thresh != std_threshold ||
+        md->g_allocs != devbuf_allocations())
+      if ((rc = md_capture(md, dt, std_threshold))) return rc;
+    const int c = std::min(kChunk, n_steps - k);
+    if ((rc = md_snapshot(md, true, st))) return rc;
+    FGB_CUDA(cudaMemsetAsync(md->status.p, 0, sizeof(int), st));
+    for (int q = 0; q < c; q++) FGB_CUDA(cudaGraphLaunch(md->exec, st));
+    int h = 0;
+    FGB_CUDA(cudaMemcpyAsync(&h, md->status.p, sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+    if (h == 0) {
+      md->n_replayed += c;
+      k += c;
+      continue;
+    }
+    // redo the chunk with full, checked steps from the snapshot
+    md->n_rollbacks++;
+    if ((rc = md_snapshot(md, false, st))) return rc;
+    for (int q = 0; q < c; q++) {
+      if ((rc = md_step_once(md, dt, std_threshold, st, nullptr))) return rc;
+      md->n_full++;
+    }
+    k += c;
+    if ((rc = md_plan(md))) return rc;   // capacity from the latest pairs
   }
   return FGB_OK;
 }

@@ -161,20 +161,28 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
 
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
-                       double *d_gB2, double *d_var, cudaStream_t st) {
+                       double *d_gB2, double *d_var, cudaStream_t st,
+                       bool fixed) {
   const bool foldable = m->power == 2.0 || m->power == 1.0;
   int rc;
   if (foldable) {
     // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact
     // integer slicing (ozaki.cu).
-    rc = kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st);
+    rc = kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st,
+                         fixed);
   } else {
     // powers other than 1 and 2: the FP64 kernel, adjoint and variance GEMMs
     rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
                            d_e_atom, d_gB2, d_var, st);
   }
   if (rc || !want_grad || !foldable) return rc;
-  if (!m->bmap_ready && (rc = build_fold(m, st))) return rc;
+  if (!m->bmap_ready) {
+    if (fixed) {
+      set_error("mixed force stage: folded matrices not built before a fixed call");
+      return FGB_EINVAL;
+    }
+    if ((rc = build_fold(m, st))) return rc;
+  }
   const B2Params &p = m->b2;
   const int nd = p.n_d;
   const bool quad = m->power == 2.0;
@@ -182,7 +190,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
   if (quad) {
     if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
-    FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
+    if (!fixed) FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   }
   int base = 0;
   for (int s = 0; s < p.n_species; s++) {
@@ -213,7 +221,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
       FGB_LAUNCH_CHECK("k_mapped_grad");
     }
   }
-  if (quad) {
+  if (quad && !fixed) {
     int h = 0;
     FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
                              cudaMemcpyDeviceToHost, st));

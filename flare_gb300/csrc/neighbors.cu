@@ -444,6 +444,20 @@ __global__ void k_export(int n, const long long *__restrict__ offsets,
   }
 }
 
+// Fixed rebuilds: segments past the reserved capacity are cut at it (so
+// every later kernel stays inside the buffers) and flag[3] records it.
+__global__ void k_clamp_offsets(int n, long long cap,
+                                long long *__restrict__ offsets,
+                                int *__restrict__ flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  const long long o = offsets[i];
+  if (o > cap) {
+    offsets[i] = cap;
+    if (i == n) atomicExch(flag + 3, 1);
+  }
+}
+
 }  // namespace
 
 // Host geometry set-up for one structure: bins and search widths.
@@ -648,6 +662,7 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
     return FGB_EINVAL;
   }
   nl->n_pairs = P;
+  nl->n_bins = nbins;
   if ((rc = nl->tmp_key.ensure(sizeof(unsigned long long) * (P + 1))) ||
       (rc = nl->tmp_rel.ensure(sizeof(double4_16a) * (P + 1))) ||
       (rc = nl->nbr_j.ensure(sizeof(int) * (P + 1))) ||
@@ -693,6 +708,83 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
   nl->max_neighbors = mx;
   return FGB_OK;
 }
+
+namespace fgb {
+
+int nlist_reserve(fgb_nlist_s *nl, long long cap) {
+  int rc;
+  if ((rc = nl->tmp_key.ensure(sizeof(unsigned long long) * (cap + 1))) ||
+      (rc = nl->tmp_rel.ensure(sizeof(double4_16a) * (cap + 1))) ||
+      (rc = nl->nbr_j.ensure(sizeof(int) * (cap + 1))) ||
+      (rc = nl->nbr_shift.ensure(sizeof(int) * (cap + 1))) ||
+      (rc = nl->nbr_rel.ensure(sizeof(double4_16a) * (cap + 1))) ||
+      (rc = nl->nbr_twin.ensure(sizeof(long long) * (cap + 1))))
+    return rc;
+  return FGB_OK;
+}
+
+int nlist_rebuild_fixed(fgb_nlist_s *nl, const double *d_positions,
+                        double cutoff, long long cap, cudaStream_t st) {
+  const int N = nl->n_atoms;
+  const long long nbins = nl->n_bins;
+  const int T = 128;
+  int rc;
+  FGB_CUDA(cudaMemsetAsync(nl->bin_count.p, 0, sizeof(int) * (nbins + 1), st));
+  FGB_CUDA(cudaMemsetAsync(nl->flag.p, 0, sizeof(int) * 4, st));
+  if (N == 0) return FGB_OK;
+  k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(
+      N, d_positions, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+      nl->raw_bin.as<int>(), nl->home_bin.as<int>(), nl->bin_slot.as<int>(),
+      nl->bin_count.as<int>(), nl->flag.as<int>());
+  FGB_LAUNCH_CHECK("k_wrap_bin");
+  if ((rc = scan_int_to_int(nl->bin_count.as<int>(), nl->bin_start.as<int>(),
+                            (int)nbins, nl->bin_start.as<int>() + nbins,
+                            nl->scan_tmp, st)))
+    return rc;
+  k_bin_fill<<<ceil_div(N, T), T, 0, st>>>(
+      N, nl->home_bin.as<int>(), nl->bin_slot.as<int>(),
+      nl->bin_start.as<int>(), nl->bin_atoms.as<int>());
+  FGB_LAUNCH_CHECK("k_bin_fill");
+  const long long NW = (long long)N * 32;
+  k_count<<<ceil_div(NW, T), T, 0, st>>>(
+      N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+      nl->raw_bin.as<int>(), nl->bin_start.as<int>(), nl->bin_atoms.as<int>(),
+      cutoff, nl->counts.as<int>());
+  FGB_LAUNCH_CHECK("k_count");
+  if ((rc = scan_int_to_ll(nl->counts.as<int>(), nl->offsets.as<long long>(),
+                           N, nl->offsets.as<long long>() + N, nl->scan_tmp,
+                           st)))
+    return rc;
+  k_clamp_offsets<<<ceil_div(N + 1, T), T, 0, st>>>(
+      N, cap, nl->offsets.as<long long>(), nl->flag.as<int>());
+  FGB_LAUNCH_CHECK("k_clamp_offsets");
+  k_fill<<<ceil_div(N, kFillWarps), 32 * kFillWarps, 0, st>>>(
+      N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+      nl->raw_bin.as<int>(), nl->bin_start.as<int>(), nl->bin_atoms.as<int>(),
+      cutoff, nl->offsets.as<long long>(),
+      nl->tmp_key.as<unsigned long long>(), nl->tmp_rel.as<double4_16a>(),
+      nl->flag.as<int>());
+  FGB_LAUNCH_CHECK("k_fill");
+  k_rank_scatter<<<ceil_div(NW, T), T, 0, st>>>(
+      N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
+      nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(),
+      nl->nbr_shift.as<int>(), nl->nbr_rel.as<double4_16a>());
+  FGB_LAUNCH_CHECK("k_rank_scatter");
+  k_twin<<<ceil_div(NW, T), T, 0, st>>>(
+      N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+      nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+      nl->nbr_shift.as<int>(), nl->nbr_twin.as<long long>(),
+      nl->flag.as<int>());
+  FGB_LAUNCH_CHECK("k_twin");
+  nl->n_pairs = cap;   // an upper bound; the device offsets hold the count
+  return FGB_OK;
+}
+
+}  // namespace fgb
 
 extern "C" int fgb_nlist_size(fgb_nlist_t nl, long long *n_pairs,
                               int *n_atoms) {

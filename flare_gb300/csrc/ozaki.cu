@@ -838,20 +838,26 @@ static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
 
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool fixed) {
   int rc;
   if (want_w) {
     set_error("tensor-core kernel stage: adjoint weights are not produced");
     return FGB_ENOTSUP;
   }
-  if (!m->oz_ready && (rc = build_oz_model(m, st))) return rc;
+  if (!m->oz_ready) {
+    if (fixed) {
+      set_error("tensor-core kernel stage: operands not sliced before a fixed call");
+      return FGB_EINVAL;
+    }
+    if ((rc = build_oz_model(m, st))) return rc;
+  }
   const B2Params &p = m->b2;
   const int nd = p.n_d;
   const double sig2 = m->sigma * m->sigma;
   // fixed scale of the sliced kernel matrix: |k| <= sig^2 < 2^eK
   const int eK = std::ilogb(sig2) + 1;
   if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
-  FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
+  if (!fixed) FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   int base = 0;
   const int kRows = 32768;
   for (int s = 0; s < p.n_species; s++) {
@@ -916,6 +922,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       }
     }
   }
+  if (fixed) return FGB_OK;
   int h = 0;
   FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
                            cudaMemcpyDeviceToHost, st));

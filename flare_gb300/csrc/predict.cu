@@ -485,13 +485,36 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   return FGB_OK;
 }
 
+// A model with the same weights and its own device workspace.
+fgb_model_s *model_replicate(const fgb_model_s *src, int &rc) {
+  fgb_model_s *m = new fgb_model_s();
+  m->b2 = src->b2;
+  m->sigma = src->sigma;
+  m->power = src->power;
+  rc = fgb_model_set(m, src->h_counts.data(), src->h_desc.data(),
+                     src->solved ? src->h_alpha.data() : nullptr,
+                     src->solved ? src->h_L_inv.data() : nullptr);
+  if (rc) { delete m; return nullptr; }
+  if (src->has_rinv) {
+    if ((rc = m->RinvT.ensure(src->RinvT.bytes))) { delete m; return nullptr; }
+    cudaError_t e = cudaMemcpy(m->RinvT.p, src->RinvT.p, src->RinvT.bytes,
+                               cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+      rc = cuda_status(e, "model_replicate");
+      delete m;
+      return nullptr;
+    }
+    m->has_rinv = true;
+  }
+  return m;
+}
+
 // ------------------------------------------------------------- predict
 int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
-                        const double *h_cells, const double *d_positions,
-                        const int *d_species, double cutoff, int want,
-                        int precision, double *d_energy, double *d_forces,
-                        double *d_stress, double *d_local_var,
-                        cudaStream_t st) {
+                 const double *h_cells, const double *d_positions,
+                 const int *d_species, double cutoff, int want, int precision,
+                 double *d_energy, double *d_forces, double *d_stress,
+                 double *d_local_var, cudaStream_t st, const FixedPlan *fixed) {
   if (!m->solved) {
     set_error("L_inv must be up to date to make predictions. Please call "
               "update_matrices_QR and try again.");
@@ -502,16 +525,26 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     return FGB_EINVAL;
   }
   int rc;
+  if (fixed && (m->nl.n_struc != n_struc || m->nl.n_atoms !=
+                    h_atom_offsets[n_struc] ||
+                (int)fixed->counts.size() != m->b2.n_species)) {
+    set_error("fgb_predict: fixed call on a different batch than the last");
+    return FGB_EINVAL;
+  }
   {
     StageTimer _pt(kStNeighbors, st, 11);
-    if ((rc = fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
-                              d_positions, cutoff, st)))
-      return rc;
+    rc = fixed ? nlist_rebuild_fixed(&m->nl, d_positions, cutoff,
+                                     fixed->pair_cap, st)
+               : fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
+                                 d_positions, cutoff, st);
+    if (rc) return rc;
   }
   const B2Params &p = m->b2;
   const int N = m->nl.n_atoms;
   const long long P = m->nl.n_pairs;
-  if ((rc = check_species(d_species, N, p.n_species, m->ws.flag, st))) return rc;
+  if (!fixed &&
+      (rc = check_species(d_species, N, p.n_species, m->ws.flag, st)))
+    return rc;
   const bool want_e = want & FGB_WANT_ENERGY, want_f = want & FGB_WANT_FORCES,
              want_s = want & FGB_WANT_STRESS, want_v = want & FGB_WANT_LOCAL_VAR;
   const bool want_grad = want_f || want_s;
@@ -529,11 +562,14 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
        (rc = m->ws.forces.ensure(sizeof(double) * (3 * (size_t)N + 1))) ||
        (rc = m->ws.virial.ensure(sizeof(double) * (6 * (size_t)N + 1)))))
     return rc;
-  FGB_CUDA(cudaMemcpyAsync(m->ws.volume.p, m->nl.h_volume.data(),
-                           sizeof(double) * n_struc, cudaMemcpyHostToDevice, st));
-  FGB_CUDA(cudaMemcpyAsync(m->ws.atom_off.p, h_atom_offsets,
-                           sizeof(int) * (n_struc + 1), cudaMemcpyHostToDevice,
-                           st));
+  if (!fixed) {   // a fixed call keeps the last call's (same cells, atoms)
+    FGB_CUDA(cudaMemcpyAsync(m->ws.volume.p, m->nl.h_volume.data(),
+                             sizeof(double) * n_struc, cudaMemcpyHostToDevice,
+                             st));
+    FGB_CUDA(cudaMemcpyAsync(m->ws.atom_off.p, h_atom_offsets,
+                             sizeof(int) * (n_struc + 1),
+                             cudaMemcpyHostToDevice, st));
+  }
   if (N > 0) {
     FGB_CUDA(cudaMemsetAsync(m->ws.e_atom.p, 0, sizeof(double) * N, st));
     FGB_CUDA(cudaMemsetAsync(m->ws.var.p, 0, sizeof(double) * N, st));
@@ -549,15 +585,18 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       return rc;
   }
   std::vector<int> counts;
-  {
+  if (fixed) {
+    counts = fixed->counts;
+  } else {
     StageTimer _pt(kStSpeciesPerm, st, 2 + 5 * p.n_species);
     if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
+    m->last_species_counts = counts;
   }
   if (precision == FGB_PREC_MIXED) {
     if ((rc = kernel_stage_mixed(m, N, counts, want_grad, want_v,
                                  m->ws.e_atom.as<double>(),
                                  m->ws.gB2.as<double>(), m->ws.var.as<double>(),
-                                 st)))
+                                 st, fixed != nullptr)))
       return rc;
   } else {
     if ((rc = kernel_stage_fp64(m, N, counts, want_grad, want_v,

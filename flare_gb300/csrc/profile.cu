@@ -65,6 +65,12 @@ StageTimer::StageTimer(int stage, cudaStream_t st, int launches)
     : stage_(stage), launches_(launches), st_(st) {
   Prof &p = prof();
   if (!p.on) return;
+  // launches captured into a graph are not timed (their events would be
+  // graph dependencies, not timestamps)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st_, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone)
+    return;
   std::lock_guard<std::mutex> g(p.mu);
   a_ = get_event(p);
   cudaEventRecord((cudaEvent_t)a_, st_);

@@ -64,21 +64,6 @@ struct fgb_server_s {
   bool stop = false;
 };
 
-static fgb_model_s *replicate(const fgb_model_s *src, int &rc) {
-  fgb_model_s *m = new fgb_model_s();
-  m->b2 = src->b2;
-  m->sigma = src->sigma;
-  m->power = src->power;
-  rc = fgb_model_set(m, src->h_counts.data(), src->h_desc.data(),
-                     src->h_alpha.data(), src->h_L_inv.data());
-  if (rc) { delete m; return nullptr; }
-  if (src->has_rinv) {
-    m->RinvT.ensure(src->RinvT.bytes);
-    cudaMemcpy(m->RinvT.p, src->RinvT.p, src->RinvT.bytes, cudaMemcpyDeviceToDevice);
-    m->has_rinv = true;
-  }
-  return m;
-}
 
 static void worker_loop(fgb_server_s *s, int w) {
   cudaSetDevice(s->device);
@@ -181,7 +166,7 @@ extern "C" int fgb_serve_start(fgb_server_t *out, fgb_model_t model,
   s->precision = precision;
   for (int w = 0; w < n_workers; w++) {
     int rc = FGB_OK;
-    fgb_model_s *m = replicate(model, rc);
+    fgb_model_s *m = model_replicate(model, rc);
     if (!m) {
       for (auto *r : s->replicas) delete r;
       delete s;

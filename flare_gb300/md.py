@@ -41,7 +41,7 @@ class Ensemble:
 
     def __init__(self, sgp, descriptor_calculators, replicas, masses,
                  temperature=None, velocities=None, seed=0, cutoff=None,
-                 precision="mixed"):
+                 precision="mixed", graphs=True, pair_margin=0.25):
         if not replicas:
             raise ValueError("no replicas")
         n = len(replicas[0][1])
@@ -80,6 +80,7 @@ class Ensemble:
                                   self.cutoff, self._prec), "Ensemble")
         self.h = h
         self.steps_done = 0
+        self.set_graphs(graphs, pair_margin)
 
     def __del__(self):
         if getattr(self, "h", None) is not None and _lib._lib is not None:
@@ -93,6 +94,19 @@ class Ensemble:
                                 float(std_threshold), _lib.stream_ptr()),
               "Ensemble.step")
         self.steps_done += n_steps
+
+    def set_graphs(self, enable=True, pair_margin=0.25):
+        """Replay CUDA-graph-captured steps (``enable``) with a pair
+        capacity of the last full step's pairs x (1 + ``pair_margin``)."""
+        check(lib().fgb_md_set_graphs(self.h, int(bool(enable)),
+                                      float(pair_margin)), "Ensemble")
+
+    def stats(self):
+        """Replayed steps, full steps, graph captures, rolled-back chunks."""
+        out = np.zeros(4, np.int64)
+        check(lib().fgb_md_stats(self.h, ptr(out)), "Ensemble.stats")
+        return dict(zip(("replayed", "full", "captures", "rollbacks"),
+                        (int(x) for x in out)))
 
     def state(self):
         NT = self.R * self.N
@@ -147,7 +161,7 @@ class Ensemble:
         self.sgp.update_matrices_QR()
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        # switch the ensemble to the new model before the old one is freed
+        # the ensemble copies the new model's weights into its own replica
         new = self.sgp._device_model(self.calcs)
         check(lib().fgb_md_set_model(self.h, new.h), "Ensemble")
         self._model = new

@@ -212,8 +212,15 @@ int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
  * structure per step.  Units: A, A/fs, amu, eV; dt in fs.  After each step
  * the local std of every atom, sign(v) sqrt|v| / |sigma| (calculator.py:121),
  * is compared with std_threshold and counted per replica.  The ensemble
- * shares the model's device workspace: do not predict with the same model
- * handle concurrently. */
+ * predicts with its own replica of the model (weights copied at creation
+ * and at fgb_md_set_model), so the model handle stays free for other use.
+ *
+ * Steps after the first are captured once as a CUDA graph and replayed
+ * (neighbour list rebuilt into a reserved pair capacity, no host
+ * synchronisation inside a step); device error flags are read once per
+ * chunk of up to 50 steps, and a chunk that exceeded the capacity or
+ * raised a flag is rolled back and redone with full, checked steps.
+ * Replayed and full steps give identical trajectories. */
 typedef struct fgb_md_s *fgb_md_t;
 int fgb_md_create(fgb_md_t *out, fgb_model_t model, int n_replicas,
                   int n_atoms, const double *h_cells, const double *h_positions,
@@ -225,6 +232,13 @@ int fgb_md_destroy(fgb_md_t md);
 int fgb_md_set_model(fgb_md_t md, fgb_model_t model);
 int fgb_md_step(fgb_md_t md, int n_steps, double dt, double std_threshold,
                 void *stream);
+/* Replayed steps on (enable != 0, the default) or off; pair capacity of a
+ * replayed step = pairs of the last full step x (1 + pair_margin), plus
+ * 4096 when pair_margin >= 0 (default 0.25; -0.5 < pair_margin <= 16). */
+int fgb_md_set_graphs(fgb_md_t md, int enable, double pair_margin);
+/* Counters since creation: replayed steps, full steps, graph captures,
+ * rolled-back chunks. */
+int fgb_md_stats(fgb_md_t md, long long *out4);
 /* Current state to host buffers (any may be NULL): positions, velocities,
  * forces [R*N*3], local variances [R*N], potential and kinetic energies
  * [R], largest std [R], flagged atom-steps since creation [R]. */

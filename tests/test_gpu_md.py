@@ -134,3 +134,56 @@ def test_grow_sparse_set_lowers_uncertainty():
     assert np.all(after < before), (before, after)
     ens.step(2)                                  # continues with the new model
     assert np.all(np.isfinite(ens.state()["positions"]))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_replayed_steps_equal_full_steps(precision):
+    """Graph-replayed steps (fixed neighbour rebuild, no host sync) give the
+    same trajectory, bit for bit, as full checked steps; a change of dt or
+    threshold recaptures."""
+    from flare_gb300.md import Ensemble, maxwell_boltzmann
+    gp, b2 = gpu_model()
+    reps = replicas(3)
+    vel = np.concatenate([maxwell_boltzmann(sp, MASSES, 900.0, 70 + r)
+                          for r, (_, sp, _) in enumerate(reps)])
+    g = Ensemble(gp, [b2], reps, MASSES, velocities=vel, precision=precision)
+    f = Ensemble(gp, [b2], reps, MASSES, velocities=vel, precision=precision,
+                 graphs=False)
+    for n, dt, th in ((61, 1.0, 0.05), (7, 0.5, 0.05), (5, 0.5, 0.01)):
+        g.step(n, dt=dt, std_threshold=th)
+        f.step(n, dt=dt, std_threshold=th)
+    a, b = g.state(), f.state()
+    for k in ("positions", "velocities", "forces", "local_var", "energy",
+              "kinetic", "max_std", "flagged"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    sg, sf = g.stats(), f.stats()
+    assert sg["replayed"] > 0 and sg["captures"] >= 3, sg
+    assert sf == {"replayed": 0, "full": 73, "captures": 0, "rollbacks": 0}
+    assert sg["replayed"] + sg["full"] == 73
+
+
+def test_pair_capacity_overflow_rolls_back():
+    """A pair capacity below the current pair count: every replayed chunk
+    overflows, is rolled back to its snapshot and redone with full steps;
+    the trajectory is unchanged."""
+    from flare_gb300.md import Ensemble, maxwell_boltzmann
+    gp, b2 = gpu_model()
+    reps = replicas(2)
+    vel = np.concatenate([maxwell_boltzmann(sp, MASSES, 600.0, 80 + r)
+                          for r, (_, sp, _) in enumerate(reps)])
+    g = Ensemble(gp, [b2], reps, MASSES, velocities=vel, pair_margin=-0.2)
+    f = Ensemble(gp, [b2], reps, MASSES, velocities=vel, graphs=False)
+    g.step(12, std_threshold=0.02)
+    f.step(12, std_threshold=0.02)
+    a, b = g.state(), f.state()
+    for k in ("positions", "velocities", "forces", "local_var", "flagged"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    s = g.stats()
+    assert s["rollbacks"] >= 1 and s["replayed"] == 0 and s["full"] == 12, s
+    # a normal margin afterwards replays again
+    g.set_graphs(True, 0.25)
+    f.step(10)
+    g.step(10)
+    np.testing.assert_array_equal(g.state()["positions"],
+                                  f.state()["positions"])
+    assert g.stats()["replayed"] == 10
