@@ -450,6 +450,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": gpu_launches,
         "errors_vs_fp64": errors,
         "clocks": clocks.summary(local),
+        "autotune": autotune_table(),
     }
     if rank == 0 and not args.no_plain:
         result["fp64_plain"] = time_plain(L, _lib, model, structs[:2], b2, c,
@@ -667,6 +668,14 @@ def run_serve(args):
     }), flush=True)
 
 
+def autotune_table():
+    """Tile shapes the autotuner chose for the sliced GEMMs (per shape:
+    operation, rows bucket, columns, depth, choice, ms per candidate)."""
+    from flare_gb300 import autotune
+    return [{**e, "ms": [round(x, 4) for x in e["ms"]]}
+            for e in autotune.table()]
+
+
 def run_md(args):
     """Uncertainty-aware MD ensemble (md3): replicas advanced together by
     velocity Verlet with forces and local std every step; then the sparse
@@ -743,6 +752,7 @@ def run_md(args):
             "max_abs": float(np.max(np.abs(drift)) / c["n_atoms"])},
         "sparse_update": grow,
         "ms_per_step_after_update": ms_after,
+        "autotune": autotune_table(),
         "setup_s": {"train_fp64": round(train_s, 1),
                     "replica_generation": round(gen_s, 1)},
         "clocks": clocks.summary(),

@@ -69,6 +69,11 @@ SIGNATURES = {
     "fgb_md_step": (_i, [_vp, _i, _d, _d, _vp]),
     "fgb_md_set_graphs": (_i, [_vp, _i, _d]),
     "fgb_md_stats": (_i, [_vp, _vp]),
+    "fgb_tune_set_mode": (_i, [_i]),
+    "fgb_tune_force": (_i, [_i, _i]),
+    "fgb_tune_clear": (_i, []),
+    "fgb_tune_count": (_i, []),
+    "fgb_tune_entry": (_i, [_i, _vp, _vp]),
     "fgb_md_read": (_i, [_vp] + [_vp] * 8 + [_vp]),
     "fgb_serve_start": (_i, [_pvp, _vp, _i, _ll, _i, _d, _i, _i]),
     "fgb_serve_submit": (_i, [_vp, _i, _vp, _vp, _vp, _pll]),

@@ -42,12 +42,17 @@ struct fgb_model_s {
   fgb::DevBuf RinvT;    // R_inv^T (M x M, lower triangular) for SOR
   bool has_rinv = false;
   fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
-  // the folded matrices in FP32-level slices (tensor-core force GEMM)
-  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB;
+  fgb::DevBuf Bfold;    // the folded matrices in FP64 (power 2), per species
+  // the folded matrices in FP32-level slices (tensor-core force GEMM), one
+  // set per B tile height of the autotuner's candidates
+  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB[fgb::oz::kF32Sets];
+  bool ozB_ready[fgb::oz::kF32Sets] = {};
   bool bmap_ready = false;
-  // mixed path: sliced sparse set and L_inv panels per species (tensor cores)
-  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS, ozL;
-  bool oz_ready = false;
+  // mixed path: sliced sparse set and L_inv panels per species (tensor
+  // cores), one set per B tile width of the autotuner's candidates
+  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS[fgb::oz::kF64Variants],
+      ozL[fgb::oz::kF64Variants];
+  bool oz_ready[fgb::oz::kF64Variants] = {};
   fgb_nlist_s nl;
   fgb_workspace ws;
   fgb_io io;

@@ -9,7 +9,7 @@ constexpr int kS = 9;        // slices per operand
 constexpr int kBeta = 6;     // bits per slice
 constexpr int kG = kS;       // groups a + b = 2 .. kS + 1
 constexpr int kTM = 128;     // A rows per tile (TMEM lanes)
-constexpr int kTN = 48;      // B rows per tile (columns per group)
+constexpr int kTN = 48;      // B rows per tile (columns per group), default
 constexpr int kKC = 16;      // k per pipeline stage (one MMA k-step)
 constexpr int kStages = 4;   // shared-memory pipeline depth
 constexpr int kEpiWarps = 3; // epilogue warps per TMEM lane quarter (16 columns
@@ -23,6 +23,21 @@ constexpr int kMaxK = 1472;
 constexpr int kSF32 = 4;
 constexpr int kTNF32 = 128;
 constexpr int kMaxKF32 = 2720;
+
+// Tile shapes the autotuner chooses from (fgb_tune.h).  FP64 level: B tiles
+// of kTNF64v[v] rows, one 16-column chunk per epilogue warp, so row partial
+// sums land in the same 16-column slots whatever the tile.  FP32 level: B
+// tiles of kTNF32v[v] rows drained by kEWF32v[v] epilogue warps per TMEM
+// lane quarter.  All candidates give the same results bit for bit.
+constexpr int kF64Variants = 2;
+constexpr int kTNF64v[kF64Variants] = {48, 32};
+constexpr int kF32Variants = 3;
+constexpr int kTNF32v[kF32Variants] = {128, 128, 64};
+constexpr int kEWF32v[kF32Variants] = {2, 4, 2};
+// B operand slice sets of the FP32 level (one per distinct tile height)
+constexpr int kF32Sets = 2;
+constexpr int kTNF32set[kF32Sets] = {128, 64};
+constexpr int f32_set(int v) { return kTNF32v[v] == 128 ? 0 : 1; }
 
 struct SliceSpec {
   int rows, K, TR;
@@ -43,13 +58,16 @@ int pad_to(int x, int m);
 int prepare(int rows, int K, int TR, int S, Sliced &out);
 // Slice rows into S = kS (FP64-level) or kSF32 (FP32-level) digits.
 int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S = kS);
+// FP64-level product of kS-slice operands; the tile shape follows B.TR
+// (one of kTNF64v).
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
          cudaStream_t st);
 // Y (A.rows x B.rows, leading dimension ldy) = A B^T rounded to FP32, from
-// kSF32-slice operands (A tiles of kTM rows, B tiles of kTNF32 rows).
+// kSF32-slice operands (A tiles of kTM rows, B tiles of 128 or 64 rows;
+// `ew` epilogue warps per lane quarter, 2 or 4 for 128-row tiles).
 int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
-             int *err, cudaStream_t st);
+             int *err, cudaStream_t st, int ew = 2);
 
 }  // namespace oz
 }  // namespace fgb

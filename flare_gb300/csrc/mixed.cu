@@ -22,6 +22,7 @@
 #include "fgb_ozaki.h"
 #include "fgb_gemm64.cuh"
 #include "fgb_profile.h"
+#include "fgb_tune.h"
 
 namespace fgb {
 namespace {
@@ -112,6 +113,25 @@ __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
 
 }  // namespace
 
+// FP32-level slices of the folded matrices for B tiles of set `set`.
+static int build_fold_slices(fgb_model_s *m, int set, cudaStream_t st) {
+  const int nd = m->b2.n_d, S = m->b2.n_species;
+  m->ozB[set].clear();
+  int rc;
+  for (int s = 0; s < S; s++) {
+    m->ozB[set].emplace_back(new oz::Sliced());
+    if (m->h_counts[s] == 0) continue;
+    // B_s is symmetric: its rows are the B operand of Y = D^ B_s
+    if ((rc = oz::slice({nd, nd, oz::kTNF32set[set],
+                         m->Bfold.as<double>() + (size_t)s * nd * nd, nd,
+                         nullptr, nullptr},
+                        *m->ozB[set][s], st, oz::kSF32)))
+      return rc;
+  }
+  m->ozB_ready[set] = true;
+  return FGB_OK;
+}
+
 static int build_fold(fgb_model_s *m, cudaStream_t st) {
   const B2Params &p = m->b2;
   const int nd = p.n_d, S = p.n_species;
@@ -120,18 +140,20 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
   int rc;
   if ((rc = m->Bmap.ensure(sizeof(float) * (per * S + 1)))) return rc;
   FGB_CUDA(cudaMemsetAsync(m->Bmap.p, 0, sizeof(float) * per * S, st));
-  DevBuf ST, STa, Bd;
-  m->ozB.clear();
+  if (quad) {
+    if ((rc = m->Bfold.ensure(sizeof(double) * (per * S + 1)))) return rc;
+    FGB_CUDA(cudaMemsetAsync(m->Bfold.p, 0, sizeof(double) * per * S, st));
+  }
+  DevBuf ST, STa;
+  for (bool &r : m->ozB_ready) r = false;
   for (int s = 0; s < S; s++) {
-    m->ozB.emplace_back(new oz::Sliced());
     const int Ms = m->h_counts[s], c = m->h_offsets[s];
     if (Ms == 0) continue;
     const double *Ss = m->S.as<double>() + (size_t)c * nd;
     float *Bs = m->Bmap.as<float>() + per * s;
     if (quad) {
       if ((rc = ST.ensure(sizeof(double) * (size_t)Ms * nd)) ||
-          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)) ||
-          (rc = Bd.ensure(sizeof(double) * (size_t)nd * nd)))
+          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)))
         return rc;
       k_scaled_transpose<<<ceil_div((long long)Ms * nd, 256), 256, 0, st>>>(
           Ms, nd, Ss, m->alpha.as<double>() + c,
@@ -139,14 +161,9 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
       FGB_LAUNCH_CHECK("k_scaled_transpose");
       dim3 g(ceil_div(nd, BN), ceil_div(nd, BM));
       k_fold_gemm<<<g, GT, 0, st>>>(nd, Ms, ST.as<double>(), STa.as<double>(),
-                                    Bs, Bd.as<double>());
+                                    Bs, m->Bfold.as<double>() + per * s);
       FGB_LAUNCH_CHECK("k_fold_gemm");
-      // B_s is symmetric: its rows are the B operand of Y = D^ B_s
-      if ((rc = oz::slice({nd, nd, oz::kTNF32, Bd.as<double>(), nd, nullptr,
-                           nullptr},
-                          *m->ozB[s], st, oz::kSF32)))
-        return rc;
-      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa/Bd reused next species
+      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa reused next species
     } else {
       k_fold_vec<<<ceil_div(nd, 128), 128, 0, st>>>(
           Ms, nd, Ss, m->alpha.as<double>() + c,
@@ -154,6 +171,7 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
       FGB_LAUNCH_CHECK("k_fold_vec");
     }
   }
+  if (quad && (rc = build_fold_slices(m, 0, st))) return rc;
   FGB_CUDA(cudaStreamSynchronize(st));
   m->bmap_ready = true;
   return FGB_OK;
@@ -209,9 +227,26 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
         // Y = D^ B_s on the tensor cores (FP32-level exact slices)
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
-                            m->ws.ozA4, st, oz::kSF32)) ||
-            (rc = oz::gemm_f32(m->ws.ozA4, *m->ozB[s], m->ws.yf.as<float>(),
-                               nd, m->ws.ozerr.as<int>(), st)))
+                            m->ws.ozA4, st, oz::kSF32)))
+          return rc;
+        auto usable = [m](int v) { return m->ozB_ready[oz::f32_set(v)]; };
+        auto launch = [&](int v) -> int {
+          const int set = oz::f32_set(v);
+          int r;
+          if (!m->ozB_ready[set]) {
+            if (fixed) {
+              set_error("mixed force stage: tile variant not prepared");
+              return FGB_EINVAL;
+            }
+            if ((r = build_fold_slices(m, set, st))) return r;
+          }
+          return oz::gemm_f32(m->ws.ozA4, *m->ozB[set][s],
+                              m->ws.yf.as<float>(), nd, m->ws.ozerr.as<int>(),
+                              st, oz::kEWF32v[v]);
+        };
+        int v = 0;
+        if ((rc = tune::run(tune::kOpForceGemm, Mr, nd, nd, oz::kF32Variants,
+                            launch, usable, st, fixed, &v)))
           return rc;
       }
       k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(

@@ -80,8 +80,19 @@ struct Cfg {
                 "group sums must stay exact in FP32");
   static_assert(TN % (16 * EW) == 0, "epilogue warps take whole 16-column chunks");
 };
-using CfgF64 = Cfg<kS, kTN, kStages, kMaxK, kEpiWarps>;
-using CfgF32 = Cfg<kSF32, kTNF32, 6, kMaxKF32, 2>;
+using CfgF64 = Cfg<kS, 48, kStages, kMaxK, 3>;
+using CfgF64n = Cfg<kS, 32, kStages, kMaxK, 2>;
+using CfgF32 = Cfg<kSF32, 128, 6, kMaxKF32, 2>;
+using CfgF32w = Cfg<kSF32, 128, 6, kMaxKF32, 4>;
+using CfgF32n = Cfg<kSF32, 64, 8, kMaxKF32, 2>;
+static_assert(CfgF64::TN == kTNF64v[0] && CfgF64n::TN == kTNF64v[1] &&
+                  CfgF64::WCOLS == 16 && CfgF64n::WCOLS == 16,
+              "FP64-level candidates: one 16-column chunk per epilogue warp");
+static_assert(CfgF64::TN == kTN && CfgF64::EW == kEpiWarps, "default shape");
+static_assert(CfgF32::TN == kTNF32v[0] && CfgF32::EW == kEWF32v[0] &&
+                  CfgF32w::TN == kTNF32v[1] && CfgF32w::EW == kEWF32v[1] &&
+                  CfgF32n::TN == kTNF32v[2] && CfgF32n::EW == kEWF32v[2],
+              "FP32-level candidates");
 static_assert(kKC % 16 == 0, "a chunk is whole MMA k-steps");
 static_assert(kBeta == 6, "digits of 6 bits");
 
@@ -624,12 +635,16 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
          cudaStream_t st) {
+  if (B.TR == CfgF64n::TN) return gemm_c<CfgF64n>(A, B, tri, epi, err, st);
   return gemm_c<CfgF64>(A, B, tri, epi, err, st);
 }
 
 int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
-             int *err, cudaStream_t st) {
-  return gemm_c<CfgF32>(A, B, false, EpiStoreF32{Y, ldy, B.rows}, err, st);
+             int *err, cudaStream_t st, int ew) {
+  const EpiStoreF32 epi{Y, ldy, B.rows};
+  if (B.TR == CfgF32n::TN) return gemm_c<CfgF32n>(A, B, false, epi, err, st);
+  if (ew == CfgF32w::EW) return gemm_c<CfgF32w>(A, B, false, epi, err, st);
+  return gemm_c<CfgF32>(A, B, false, epi, err, st);
 }
 
 }  // namespace oz
@@ -714,6 +729,7 @@ extern "C" int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A,
 #include "fgb_kernels.h"
 #include "fgb_model.h"
 #include "fgb_profile.h"
+#include "fgb_tune.h"
 
 namespace fgb {
 namespace oz {
@@ -807,31 +823,31 @@ __global__ void k_energy_final(int M, int ntiles, const double *__restrict__ par
 }  // namespace oz
 
 
-// Slice the model operands once: normalised sparse rows (B of the kernel
-// GEMM) and the L_inv panels (B of the variance GEMM), per species.
-static int build_oz_model(fgb_model_s *m, cudaStream_t st) {
-  const int S = m->b2.n_species, nd = m->b2.n_d;
-  m->ozS.clear();
-  m->ozL.clear();
+// Slice the model operands for B tiles of variant v: normalised sparse rows
+// (B of the kernel GEMM) and the L_inv panels (B of the variance GEMM), per
+// species.  Done once per variant, the first time the variant runs.
+static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
+  const int S = m->b2.n_species, nd = m->b2.n_d, TN = oz::kTNF64v[v];
+  m->ozS[v].clear();
+  m->ozL[v].clear();
   int rc;
   for (int s = 0; s < S; s++) {
-    m->ozS.emplace_back(new oz::Sliced());
-    m->ozL.emplace_back(new oz::Sliced());
+    m->ozS[v].emplace_back(new oz::Sliced());
+    m->ozL[v].emplace_back(new oz::Sliced());
     const int Ms = m->h_counts[s];
     if (Ms == 0) continue;
-    if ((rc = oz::slice({Ms, nd, oz::kTN,
+    if ((rc = oz::slice({Ms, nd, TN,
                          m->S.as<double>() + (size_t)m->h_offsets[s] * nd, nd,
                          nullptr, nullptr},
-                        *m->ozS[s], st)))
+                        *m->ozS[v][s], st)))
       return rc;
-    if ((rc = oz::slice({m->h_panel_rows[s], Ms, oz::kTN,
+    if ((rc = oz::slice({m->h_panel_rows[s], Ms, TN,
                          m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
                          nullptr},
-                        *m->ozL[s], st)))
+                        *m->ozL[v][s], st)))
       return rc;
   }
-  FGB_CUDA(cudaStreamSynchronize(st));
-  m->oz_ready = true;
+  m->oz_ready[v] = true;
   return FGB_OK;
 }
 
@@ -844,13 +860,23 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
     set_error("tensor-core kernel stage: adjoint weights are not produced");
     return FGB_ENOTSUP;
   }
-  if (!m->oz_ready) {
+  if (!m->oz_ready[0]) {
     if (fixed) {
       set_error("tensor-core kernel stage: operands not sliced before a fixed call");
       return FGB_EINVAL;
     }
-    if ((rc = build_oz_model(m, st))) return rc;
+    if ((rc = build_oz_model(m, 0, st))) return rc;
   }
+  // variant v usable without preparation; prepare it (not in fixed calls)
+  auto usable = [m](int v) { return m->oz_ready[v]; };
+  auto prepare_variant = [&](int v) -> int {
+    if (m->oz_ready[v]) return FGB_OK;
+    if (fixed) {
+      set_error("tensor-core kernel stage: tile variant not prepared");
+      return FGB_EINVAL;
+    }
+    return build_oz_model(m, v, st);
+  };
   const B2Params &p = m->b2;
   const int nd = p.n_d;
   const double sig2 = m->sigma * m->sigma;
@@ -871,52 +897,75 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
         return rc;
     }
     const bool var_oz = want_var;
-    // energy partial slots per row: B tiles x epilogue warps per quarter
-    const int ktiles = Ms > 0 ? m->ozS[s]->RP / oz::kTN * oz::kEpiWarps : 0;
+    // row partial sums: one slot per 16 columns, for the widest padding
+    auto slots = [](int n) {
+      int w = 0;
+      for (int v = 0; v < oz::kF64Variants; v++)
+        w = std::max(w, oz::pad_to(n, oz::kTNF64v[v]) / 16);
+      return w;
+    };
+    const int R = m->h_panel_rows[s];
+    const int kslots = Ms > 0 ? slots(Ms) : 0;
+    const int vslots = Ms > 0 ? slots(R) : 0;
     for (int r0 = 0; r0 < Ns && Ms > 0; r0 += kRows) {
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
-      if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * ktiles)) ||
+      if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * kslots)) ||
           (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, oz::kS, m->ws.ozK))))
         return rc;
+      int vk = 0;
       {
         StageTimer _pt(kStKernelGemm, st, 2);
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
                             m->ws.ozA, st)))
           return rc;
-        oz::EpiKernel epi{nullptr,
-                          var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
-                          var_oz ? m->ws.ozK.scale.as<double>() : nullptr,
-                          m->ws.ozK.KP, eK,
-                          m->ws.erows.as<double>(), ktiles,
-                          m->alpha.as<double>() + m->h_offsets[s],
-                          m->svalid.as<unsigned char>() + m->h_offsets[s],
-                          perm, m->ws.norms.as<double>(), sig2, m->power, Ms};
-        if ((rc = oz::gemm(m->ws.ozA, *m->ozS[s], false, epi,
-                           m->ws.ozerr.as<int>(), st)))
+        auto launch = [&](int v) -> int {
+          int r;
+          if ((r = prepare_variant(v))) return r;
+          const oz::Sliced &B = *m->ozS[v][s];
+          oz::EpiKernel epi{nullptr,
+                            var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
+                            var_oz ? m->ws.ozK.scale.as<double>() : nullptr,
+                            m->ws.ozK.KP, eK,
+                            m->ws.erows.as<double>(), B.RP / 16,
+                            m->alpha.as<double>() + m->h_offsets[s],
+                            m->svalid.as<unsigned char>() + m->h_offsets[s],
+                            perm, m->ws.norms.as<double>(), sig2, m->power, Ms};
+          return oz::gemm(m->ws.ozA, B, false, epi, m->ws.ozerr.as<int>(), st);
+        };
+        if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::kF64Variants,
+                            launch, usable, st, fixed, &vk)))
           return rc;
       }
       {
         StageTimer _pt(kStRowEnergy, st);
         oz::k_energy_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
-            Mr, ktiles, m->ws.erows.as<double>(), perm, d_e_atom);
+            Mr, m->ozS[vk][s]->RP / 16, m->ws.erows.as<double>(), perm,
+            d_e_atom);
         FGB_LAUNCH_CHECK("k_energy_final");
       }
       if (var_oz) {
-        const int R = m->h_panel_rows[s];
-        const int ntiles = m->ozL[s]->RP / oz::kTN * oz::kEpiWarps;
-        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * ntiles)))
+        if ((rc = m->ws.part.ensure(sizeof(double) * (size_t)Mr * vslots)))
           return rc;
+        int vv = 0;
         {
           StageTimer _pt(kStVarianceGemm, st);
-          oz::EpiZsq epi{m->ws.part.as<double>(), ntiles, R};
-          if ((rc = oz::gemm(m->ws.ozK, *m->ozL[s], true, epi,
-                             m->ws.ozerr.as<int>(), st)))
+          auto launch = [&](int v) -> int {
+            int r;
+            if ((r = prepare_variant(v))) return r;
+            const oz::Sliced &B = *m->ozL[v][s];
+            oz::EpiZsq epi{m->ws.part.as<double>(), B.RP / 16, R};
+            return oz::gemm(m->ws.ozK, B, true, epi, m->ws.ozerr.as<int>(), st);
+          };
+          if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms,
+                              oz::kF64Variants, launch, usable, st, fixed,
+                              &vv)))
             return rc;
         }
-        if ((rc = launch_variance_final(Mr, ntiles, m->ws.part.as<double>(),
-                                        perm, m->ws.norms.as<double>(), sig2,
+        if ((rc = launch_variance_final(Mr, m->ozL[vv][s]->RP / 16,
+                                        m->ws.part.as<double>(), perm,
+                                        m->ws.norms.as<double>(), sig2,
                                         m->power, d_var, st)))
           return rc;
       }

@@ -450,7 +450,8 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   }
   m->solved = false;
   m->bmap_ready = false;
-  m->oz_ready = false;
+  for (bool &r : m->oz_ready) r = false;
+  for (bool &r : m->ozB_ready) r = false;
   if (!h_alpha || !h_L_inv) return FGB_OK;
   if ((rc = m->alpha.ensure(sizeof(double) * (M + 1)))) return rc;
   if (M > 0)

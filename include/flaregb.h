@@ -247,6 +247,33 @@ int fgb_md_read(fgb_md_t md, double *h_positions, double *h_velocities,
                 double *h_kinetic, double *h_max_std, long long *h_flagged,
                 void *stream);
 
+/* ------------------------------------------------------------ autotuner
+ * Tile shapes of the sliced tensor-core GEMMs (kernel, variance and force
+ * GEMMs of the mixed path) are chosen per problem shape: at the first call
+ * with a new (operation, rows rounded up to a power of two, columns, depth)
+ * every candidate shape is timed with CUDA events and the fastest is kept
+ * (process-wide; appended to the file named by FGB_TUNE_CACHE when that is
+ * set, and read from it at start).  All candidates give identical results.
+ * FGB_AUTOTUNE=0 in the environment starts with tuning off.  No counterpart
+ * in flare_pp (CPU code with fixed loops). */
+enum {
+  FGB_TUNE_KERNEL_GEMM = 0,     /* candidates: B tiles of 48, 32 rows      */
+  FGB_TUNE_VARIANCE_GEMM = 1,   /* candidates: B tiles of 48, 32 rows      */
+  FGB_TUNE_FORCE_GEMM = 2       /* candidates: 128 rows x 2 epilogue warps,
+                                   128 x 4, 64 x 2                          */
+};
+/* 1: tune at first use (default); 0: always the first candidate. */
+int fgb_tune_set_mode(int mode);
+/* Force candidate `candidate` for operation `op` (-1: back to tuning). */
+int fgb_tune_force(int op, int candidate);
+/* Forget every tuned shape. */
+int fgb_tune_clear(void);
+/* Tuned shapes so far, and entry i: key5 = {op, rows bucket, columns,
+ * depth, chosen candidate}, ms4 = best timed launch per candidate (0 for
+ * entries read from the cache file). */
+int fgb_tune_count(void);
+int fgb_tune_entry(int i, int *key5, double *ms4);
+
 /* ------------------------------------------------------------ serving
  * Continuous batching over a solved model.  fgb_serve_start launches
  * n_workers host threads; each owns a replica of the model (same weights,
