@@ -38,6 +38,12 @@ struct StrucGeom {
   float d2_out;     // FP32 d^2 above this: certainly outside the cutoff
   float d2_in;      // FP32 d^2 below this (and above d2_zero): certainly inside
   float d2_zero;    // FP32 d^2 at or below this: d may be 0, test in FP64
+  // Integer division without the FP64/conversion pipe: n / d = (n m) >> 32
+  // with m = floor(2^32 / d) + 1, exact for n, d < 2^16 and for n < 2^24,
+  // d < 2^8 (the image counts and bins here are within both).
+  unsigned long long m_nb[3];    // for nb[k]
+  unsigned long long m_n1, m_n2; // for 2 kk[1] + 1 and 2 kk[2] + 1
+  int wrap_c[3];    // floordiv(t, nb) = (t + wrap_c nb) / nb - wrap_c, t > -kk
 };
 
 // Host-side cell algebra in the canonical operation order (no FMA).
@@ -60,6 +66,12 @@ int scan_int_to_ll_raw(const int *d_in, long long *d_out, int n,
 
 struct fgb_nlist_s;
 namespace fgb {
+// fgb_nlist_build on a stream; with `check` false the fill and twin
+// consistency flags (flag[1], flag[2]) are left on the device for the
+// caller, so the build synchronises once (the pair count).
+int nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
+                const double *h_cells, const double *d_positions,
+                double cutoff, cudaStream_t st, bool check);
 // Per-pair buffers for at least `cap` pairs (neighbors.cu).
 int nlist_reserve(fgb_nlist_s *nl, long long cap);
 // The list of the last full build's structures (same atoms, cells, bins) at
@@ -75,7 +87,6 @@ struct fgb_nlist_s {
   int n_struc = 0;
   int n_atoms = 0;
   long long n_pairs = 0;
-  int max_neighbors = 0;
   long long n_bins = 0;       // bins of the last full build
   std::vector<int> h_atom_offsets;
   std::vector<double> h_cells;

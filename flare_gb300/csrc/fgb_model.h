@@ -92,7 +92,8 @@ namespace fgb {
 int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
                       bool want_grad, bool want_var, double *d_e_atom,
                       double *d_gB2, double *d_var, cudaStream_t st);
-// `fixed`: neither clear nor read ws.ozerr (the caller does both)
+// Bounded tensor-core waits report into ws.ozerr, which the caller clears
+// before and reads after; `fixed`: prepare nothing (operands must be ready).
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
                     cudaStream_t st, bool fixed = false);

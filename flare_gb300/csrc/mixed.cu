@@ -206,10 +206,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   const bool quad = m->power == 2.0;
   const float sig2 = (float)(m->sigma * m->sigma);
   const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
-  if (quad) {
-    if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
-    if (!fixed) FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
-  }
+  if (quad && (rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
   int base = 0;
   for (int s = 0; s < p.n_species; s++) {
     const int Ns = counts[s];
@@ -254,16 +251,6 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
           quad ? m->ws.yf.as<float>() : nullptr, quad ? nullptr : Bs,
           quad ? 2.f * sig2 : sig2, d_gB2);
       FGB_LAUNCH_CHECK("k_mapped_grad");
-    }
-  }
-  if (quad && !fixed) {
-    int h = 0;
-    FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
-                             cudaMemcpyDeviceToHost, st));
-    FGB_CUDA(cudaStreamSynchronize(st));
-    if (h) {
-      set_error("tensor-core force GEMM: a bounded device wait ran out");
-      return FGB_ETIMEOUT;
     }
   }
   return FGB_OK;

@@ -31,9 +31,35 @@ namespace fgb {
 
 namespace {
 
-__device__ __forceinline__ int floordiv(int a, int b) {
-  int q = a / b;
-  return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+// Integer-to-float conversions and divisions by run-time divisors go
+// through the FP64/conversion pipe, which this GPU runs at a small fraction
+// of the integer and FP32 rates; the candidate loops use the forms below.
+
+// n / d for the multiplier m = floor(2^32 / d) + 1 (see StrucGeom).
+__device__ __forceinline__ int udiv(int n, unsigned long long m) {
+  return (int)(((unsigned long long)(unsigned)n * m) >> 32);
+}
+
+// floor(t / nb[k]) for t > -kk[k] - 1
+__device__ __forceinline__ int floordiv_k(const StrucGeom &g, int k, int t) {
+  return udiv(t + g.wrap_c[k] * g.nb[k], g.m_nb[k]) - g.wrap_c[k];
+}
+
+// (float)s for |s| < 2^22, exactly, with one FP32 subtraction: the bits of
+// 1.5 * 2^23 + s minus 1.5 * 2^23.
+__device__ __forceinline__ float small_int_to_float(int s) {
+  return __fsub_rn(__int_as_float(0x4B400000 + s), 12582912.0f);
+}
+
+// Search-block image img -> offsets (d0, d1, d2) in [-kk, kk]^3.
+__device__ __forceinline__ void image_offsets(const StrucGeom &g, int img,
+                                              int &d0, int &d1, int &d2) {
+  const int n1 = 2 * g.kk[1] + 1, n2 = 2 * g.kk[2] + 1;
+  const int q = udiv(img, g.m_n2);     // img / n2
+  const int p = udiv(q, g.m_n1);       // img / (n1 n2)
+  d2 = img - q * n2 - g.kk[2];
+  d1 = q - p * n1 - g.kk[1];
+  d0 = p - g.kk[0];
 }
 
 // frac = (p * ct) * cdi ; f = frac - floor(frac); w = (f * cd) * cti
@@ -119,12 +145,11 @@ __device__ __forceinline__ void visit_lane(int lane, const StrucGeom &g,
   const int n0 = 2 * g.kk[0] + 1, n1 = 2 * g.kk[1] + 1, n2 = 2 * g.kk[2] + 1;
   const int nimg = n0 * n1 * n2;
   for (int img = lane; img < nimg; img += 32) {
-    const int d0 = img / (n1 * n2) - g.kk[0];
-    const int d1 = (img / n2) % n1 - g.kk[1];
-    const int d2 = img % n2 - g.kk[2];
+    int d0, d1, d2;
+    image_offsets(g, img, d0, d1, d2);
     const int t0 = b0 + d0, t1 = b1 + d1, t2 = b2 + d2;
-    const int q0 = floordiv(t0, g.nb[0]), q1 = floordiv(t1, g.nb[1]),
-              q2 = floordiv(t2, g.nb[2]);
+    const int q0 = floordiv_k(g, 0, t0), q1 = floordiv_k(g, 1, t1),
+              q2 = floordiv_k(g, 2, t2);
     const int h0 = t0 - q0 * g.nb[0], h1 = t1 - q1 * g.nb[1],
               h2 = t2 - q2 * g.nb[2];
     const int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
@@ -139,7 +164,8 @@ __device__ __forceinline__ void visit_lane(int lane, const StrucGeom &g,
       if (s0 < -g.sweep || s0 > g.sweep || s1 < -g.sweep || s1 > g.sweep ||
           s2 < -g.sweep || s2 > g.sweep)
         continue;
-      const float f0 = (float)s0, f1 = (float)s1, f2 = (float)s2;
+      const float f0 = small_int_to_float(s0), f1 = small_int_to_float(s1),
+                  f2 = small_int_to_float(s2);
       const float x = (wj.x - wi.x) + f0 * g.cell32[0] + f1 * g.cell32[3] +
                       f2 * g.cell32[6];
       const float y = (wj.y - wi.y) + f0 * g.cell32[1] + f1 * g.cell32[4] +
@@ -221,13 +247,12 @@ __device__ __forceinline__ void cursor_seek(LaneCursor &c, const StrucGeom &g,
   const int n1 = 2 * g.kk[1] + 1, n2 = 2 * g.kk[2] + 1;
   const int nimg = (2 * g.kk[0] + 1) * n1 * n2;
   while (c.q >= c.qe && c.img < nimg) {
-    const int d0 = c.img / (n1 * n2) - g.kk[0];
-    const int d1 = (c.img / n2) % n1 - g.kk[1];
-    const int d2 = c.img % n2 - g.kk[2];
+    int d0, d1, d2;
+    image_offsets(g, c.img, d0, d1, d2);
     const int t0 = b0 + d0, t1 = b1 + d1, t2 = b2 + d2;
-    c.q0 = floordiv(t0, g.nb[0]);
-    c.q1 = floordiv(t1, g.nb[1]);
-    c.q2 = floordiv(t2, g.nb[2]);
+    c.q0 = floordiv_k(g, 0, t0);
+    c.q1 = floordiv_k(g, 1, t1);
+    c.q2 = floordiv_k(g, 2, t2);
     const int h0 = t0 - c.q0 * g.nb[0], h1 = t1 - c.q1 * g.nb[1],
               h2 = t2 - c.q2 * g.nb[2];
     const int bin = g.bin0 + (h0 * g.nb[1] + h1) * g.nb[2] + h2;
@@ -317,7 +342,8 @@ k_fill(int n, const int *__restrict__ atom_struct,
                 s2 = c.q2 - ((top >> 2) & 1);
       if (s0 >= -g.sweep && s0 <= g.sweep && s1 >= -g.sweep &&
           s1 <= g.sweep && s2 >= -g.sweep && s2 <= g.sweep) {
-        const float f0 = (float)s0, f1 = (float)s1, f2 = (float)s2;
+        const float f0 = small_int_to_float(s0),
+                    f1 = small_int_to_float(s1), f2 = small_int_to_float(s2);
         const float x = (wj.x - wi.x) + f0 * g.cell32[0] + f1 * g.cell32[3] +
                         f2 * g.cell32[6];
         const float y = (wj.y - wi.y) + f0 * g.cell32[1] + f1 * g.cell32[4] +
@@ -491,6 +517,17 @@ static void make_geom(const double *cell, double cutoff, int atom0, int natoms,
   }
   for (int k = 0; k < 3; k++)
     g.kk[k] = (int)std::floor(rc * g.nb[k] / h[k]) + 1;
+  // multipliers of the device's integer divisions (nb <= 1024, kk <= 127
+  // are checked by the callers before any launch)
+  auto magic = [](int d) {
+    return d > 0 ? (1ULL << 32) / (unsigned long long)d + 1ULL : 0ULL;
+  };
+  for (int k = 0; k < 3; k++) {
+    g.m_nb[k] = magic(g.nb[k]);
+    g.wrap_c[k] = g.kk[k] / g.nb[k] + 1;   // wrap_c nb > kk
+  }
+  g.m_n1 = magic(2 * g.kk[1] + 1);
+  g.m_n2 = magic(2 * g.kk[2] + 1);
   // FP32 prefilter bounds.  Every coordinate entering a candidate's FP32
   // difference is at most (2 + sweep) * rowsum in magnitude; the FP32 result
   // is within 5 * 2^-24 of that per component (operand rounding and four
@@ -535,6 +572,13 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
                                const int *h_atom_offsets, const double *h_cells,
                                const double *d_positions, double cutoff,
                                void *stream) {
+  return nlist_build(nl, n_struc, h_atom_offsets, h_cells, d_positions,
+                     cutoff, (cudaStream_t)stream, true);
+}
+
+int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
+                     const double *h_cells, const double *d_positions,
+                     double cutoff, cudaStream_t st, bool check) {
   if (!nl || n_struc <= 0 || !h_atom_offsets || !h_cells) {
     set_error("fgb_nlist_build: invalid arguments");
     return FGB_EINVAL;
@@ -543,7 +587,6 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
     set_error("fgb_nlist_build: cutoff must be positive and finite");
     return FGB_EINVAL;
   }
-  cudaStream_t st = (cudaStream_t)stream;
   const int N = h_atom_offsets[n_struc];
   if (h_atom_offsets[0] != 0 || N < 0) {
     set_error("fgb_nlist_build: atom offsets must start at 0");
@@ -692,10 +735,8 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
         nl->flag.as<int>());
     FGB_LAUNCH_CHECK("k_twin");
   }
+  if (!check) return FGB_OK;   // the caller reads flag[1], flag[2] later
   FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
-                           cudaMemcpyDeviceToHost, st));
-  std::vector<int> hc(N);
-  FGB_CUDA(cudaMemcpyAsync(hc.data(), nl->counts.p, sizeof(int) * N,
                            cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
   if (hflag[1] || hflag[2]) {
@@ -703,9 +744,6 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
               hflag[1], hflag[2]);
     return FGB_ECUDA;
   }
-  int mx = 0;
-  for (int i = 0; i < N; i++) mx = std::max(mx, hc[i]);
-  nl->max_neighbors = mx;
   return FGB_OK;
 }
 

@@ -883,7 +883,6 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
   // fixed scale of the sliced kernel matrix: |k| <= sig^2 < 2^eK
   const int eK = std::ilogb(sig2) + 1;
   if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
-  if (!fixed) FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   int base = 0;
   const int kRows = 32768;
   for (int s = 0; s < p.n_species; s++) {
@@ -970,15 +969,6 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
           return rc;
       }
     }
-  }
-  if (fixed) return FGB_OK;
-  int h = 0;
-  FGB_CUDA(cudaMemcpyAsync(&h, m->ws.ozerr.p, sizeof(int),
-                           cudaMemcpyDeviceToHost, st));
-  FGB_CUDA(cudaStreamSynchronize(st));
-  if (h) {
-    set_error("tensor-core kernel stage: a bounded device wait ran out");
-    return FGB_ETIMEOUT;
   }
   return FGB_OK;
 }

@@ -196,11 +196,16 @@ __global__ void k_species_flags(int n, const int *__restrict__ species, int s,
   if (i < n) flags[i] = species[i] == s ? 1 : 0;
 }
 
+// totals[q] = atoms of species q < s (already counted on the stream)
 __global__ void k_species_scatter(int n, const int *__restrict__ species, int s,
-                                  const int *__restrict__ pos, int base,
+                                  const int *__restrict__ pos,
+                                  const int *__restrict__ totals,
                                   int *__restrict__ perm) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && species[i] == s) perm[base + pos[i]] = i;
+  if (i >= n || species[i] != s) return;
+  int base = 0;
+  for (int q = 0; q < s; q++) base += totals[q];
+  perm[base + pos[i]] = i;
 }
 
 __global__ void k_check_species(int n, const int *__restrict__ species, int ns,
@@ -261,6 +266,8 @@ int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
 }
 
 // Species permutation: perm = atoms of species 0 (ascending), then 1, ...
+// The species range check and every species count come back to the host in
+// one read (a single synchronisation).
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st) {
   const int S = m->b2.n_species;
@@ -269,26 +276,33 @@ int species_permutation(fgb_model_s *m, const int *d_species, int N,
   if ((rc = m->ws.perm.ensure(sizeof(int) * (N + 1))) ||
       (rc = m->ws.flags.ensure(sizeof(int) * (N + 1))) ||
       (rc = m->ws.pos.ensure(sizeof(int) * (N + 1))) ||
-      (rc = m->ws.scal.ensure(sizeof(int) * (S + 1))))
+      (rc = m->ws.scal.ensure(sizeof(int) * (S + 2))))
     return rc;
-  std::vector<int> h(S);
+  if (N == 0) return FGB_OK;
+  int *tot = m->ws.scal.as<int>();   // [0, S): counts; [S]: range flag
+  FGB_CUDA(cudaMemsetAsync(tot + S, 0, sizeof(int), st));
+  k_check_species<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, S, tot + S);
+  FGB_LAUNCH_CHECK("k_check_species");
   for (int s = 0; s < S; s++) {
     k_species_flags<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, s,
                                                       m->ws.flags.as<int>());
     FGB_LAUNCH_CHECK("k_species_flags");
     if ((rc = scan_int_to_int(m->ws.flags.as<int>(), m->ws.pos.as<int>(), N,
-                              m->ws.scal.as<int>() + s, m->ws.scan_tmp, st)))
+                              tot + s, m->ws.scan_tmp, st)))
       return rc;
-    FGB_CUDA(cudaMemcpyAsync(&h[s], m->ws.scal.as<int>() + s, sizeof(int),
-                             cudaMemcpyDeviceToHost, st));
-    FGB_CUDA(cudaStreamSynchronize(st));
-    int base = 0;
-    for (int q = 0; q < s; q++) base += h[q];
     k_species_scatter<<<ceil_div(N, 256), 256, 0, st>>>(
-        N, d_species, s, m->ws.pos.as<int>(), base, m->ws.perm.as<int>());
+        N, d_species, s, m->ws.pos.as<int>(), tot, m->ws.perm.as<int>());
     FGB_LAUNCH_CHECK("k_species_scatter");
   }
-  counts = h;
+  std::vector<int> h(S + 1);
+  FGB_CUDA(cudaMemcpyAsync(h.data(), tot, sizeof(int) * (S + 1),
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h[S]) {
+    set_error("species must lie in [0, %d)", S);
+    return FGB_EINVAL;
+  }
+  counts.assign(h.begin(), h.begin() + S);
   return FGB_OK;
 }
 
@@ -536,16 +550,19 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     StageTimer _pt(kStNeighbors, st, 11);
     rc = fixed ? nlist_rebuild_fixed(&m->nl, d_positions, cutoff,
                                      fixed->pair_cap, st)
-               : fgb_nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
-                                 d_positions, cutoff, st);
+               : nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
+                             d_positions, cutoff, st, false);
     if (rc) return rc;
   }
   const B2Params &p = m->b2;
   const int N = m->nl.n_atoms;
   const long long P = m->nl.n_pairs;
-  if (!fixed &&
-      (rc = check_species(d_species, N, p.n_species, m->ws.flag, st)))
-    return rc;
+  const bool mixed = precision == FGB_PREC_MIXED;
+  // the bounded tensor-core waits report into ws.ozerr, read at the end (a
+  // fixed call's caller clears and reads it)
+  if ((rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
+  if (!fixed && mixed)
+    FGB_CUDA(cudaMemsetAsync(m->ws.ozerr.p, 0, sizeof(int), st));
   const bool want_e = want & FGB_WANT_ENERGY, want_f = want & FGB_WANT_FORCES,
              want_s = want & FGB_WANT_STRESS, want_v = want & FGB_WANT_LOCAL_VAR;
   const bool want_grad = want_f || want_s;
@@ -638,6 +655,24 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (want_v && d_local_var && N > 0)
     FGB_CUDA(cudaMemcpyAsync(d_local_var, m->ws.var.p, sizeof(double) * N,
                              cudaMemcpyDeviceToDevice, st));
+  if (fixed) return FGB_OK;
+  // deferred checks: neighbour-list consistency, tensor-core waits
+  int h[5] = {0, 0, 0, 0, 0};
+  FGB_CUDA(cudaMemcpyAsync(h, m->nl.flag.p, sizeof(int) * 4,
+                           cudaMemcpyDeviceToHost, st));
+  if (mixed)
+    FGB_CUDA(cudaMemcpyAsync(h + 4, m->ws.ozerr.p, sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h[1] || h[2]) {
+    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
+              h[1], h[2]);
+    return FGB_ECUDA;
+  }
+  if (h[4]) {
+    set_error("tensor-core stage: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
   return FGB_OK;
 }
 
