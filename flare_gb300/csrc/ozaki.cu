@@ -61,7 +61,8 @@ template <int S_, int TN_, int STAGES_, int MAXK_, int EW_>
 struct Cfg {
   static constexpr int S = S_, TN = TN_, STAGES = STAGES_, MAXK = MAXK_;
   static constexpr int EW = EW_;
-  static constexpr int THREADS = 32 * (1 + 4 * EW);
+  static constexpr int THREADS = 32 * (2 + 4 * EW);
+  static constexpr int MMA_WARP = 1 + 4 * EW;   // after the epilogue warps
   static constexpr int WCOLS = TN / EW;   // columns per epilogue warp
   // K segment: chunks accumulated in TMEM before the epilogue adds the exact
   // group sums into its 64-bit registers (any K, exact)
@@ -300,12 +301,42 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
   }
 }
 
+// n / d for 32-bit n and d >= 1 without the FP64/conversion pipe (which
+// run-time integer division uses, and which this GPU runs slowly): m =
+// floor((2^64 - 1) / d) + 1, q = high 64 bits of n m (exact: the excess
+// n (m - 2^64/d) / 2^64 < 2^-32 stays below 1/d).
+struct FastDiv {
+  unsigned d;
+  unsigned long long m;
+};
+inline FastDiv make_fastdiv(int d) {
+  return {(unsigned)d, d > 1 ? ~0ULL / (unsigned long long)d + 1ULL : 0ULL};
+}
+__device__ __forceinline__ int fdiv(int n, FastDiv f) {
+  return f.d == 1 ? n : (int)__umul64hi((unsigned long long)(unsigned)n, f.m);
+}
+
+// Wait for a phase, giving up when `abort_flag` is raised or after
+// kWaitLimit polls: 0 done, 1 aborted elsewhere, 2 timed out.
+__device__ __forceinline__ int wait_or_abort(uint64_t *bar, uint32_t phase,
+                                             volatile int *abort_flag) {
+  for (long long i = 0; i < kWaitLimit; i++) {
+    if (tc::mbar_try_wait(bar, phase)) return 0;
+    if (*abort_flag) return 1;
+  }
+  return 2;
+}
+
 // Persistent, warp-specialised GEMM: one CTA per SM walks the tiles
 // blockIdx.x, blockIdx.x + gridDim.x, ... (B tiles fastest).
-//   warp 0, lane 0  streams chunks into the shared-memory ring and issues the
-//                   MMAs; the ring runs on across tile boundaries, so the next
-//                   tile's first chunks are already loaded when its MMAs may
-//                   start.
+//   warp 0, lane 0  streams chunks into the shared-memory ring: a stage is
+//                   refilled as soon as the MMAs that read it complete; the
+//                   ring runs on across tile boundaries.
+//   last warp, lane 0  issues the MMAs of each chunk as soon as its copies
+//                   land (so the tensor pipe never waits on the copy issue),
+//                   commits the stage back to the loader and, after a tile's
+//                   (or K segment's) last chunk, the accumulator to the
+//                   epilogue.
 //   warps 1..4 EW   the epilogue: warp w reads TMEM lanes 32 (w % 4) ...
 //                   (the hardware's lane quarter for that warp) and columns
 //                   [sub WCOLS, (sub + 1) WCOLS) with sub = (w - 1) / 4.
@@ -316,13 +347,14 @@ __global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
 //                   with EW warps per quarter to hide its latency.
 // Barriers: load_full / load_empty per ring stage (transaction bytes; MMA
 // commit), acc_full (commit after a tile's last MMAs), acc_empty (one arrive
-// per epilogue warp).  Every wait is bounded; a producer that gives up sets
-// the CTA's abort flag, which the epilogue polls, waits (bounded) for its own
-// copies and MMAs in flight, and reports through `err`.  Energy and variance
-// partials are written per (tile, epilogue warp): NTt * EW slots per row.
+// per epilogue warp).  Every wait is bounded; a thread that gives up raises
+// the CTA's abort flag, which every other wait polls; the copies and MMAs
+// in flight are waited for (bounded) before TMEM is freed and the CTA
+// exits, and `err` reports it.  Energy and variance partials are written
+// per (tile, epilogue warp): NTt * EW slots per row.
 template <class C, class Epi>
 __global__ void __launch_bounds__(C::THREADS, 1)
-k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
+k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
           const __nv_bfloat16 *__restrict__ Asl,
           const double *__restrict__ Ascale,
           const __nv_bfloat16 *__restrict__ Bsl,
@@ -336,6 +368,8 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
   uint64_t *acc_empty = acc_full + 1;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  long long *issued = reinterpret_cast<long long *>(tmem_slot + 2);
+  long long *consumed = issued + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntiles = MT * NTt;
   const int KCH = KP / kKC;
@@ -353,89 +387,107 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
     tc::mbar_init(acc_empty, 4 * C::EW);
     tc::mbar_fence_init();
     *abort_flag = 0;
+    *issued = 0;
+    *consumed = 0;
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  // chunks of tile t (triangular B: columns n0 .. n0+TN-1 need k < n0 + TN)
-  auto tile_nch = [&](int t) {
-    const int n0 = (t % NTt) * TN;
+  // row and column tile of tile t; chunks of a tile (triangular B: columns
+  // n0 .. n0+TN-1 need k < n0 + TN)
+  auto tile_rc = [&](int t, int &mt, int &nt) {
+    mt = fdiv(t, divNT);
+    nt = t - mt * NTt;
+  };
+  auto tile_nch = [&](int nt) {
+    const int n0 = nt * TN;
     const int kmax = tri ? min(K, n0 + TN) : K;
     return (kmax + kKC - 1) / kKC;
   };
-
-  if (warp == 0 && lane == 0) {
-    bool ok = true;
-    int lt = blockIdx.x, lc = 0;     // tile and chunk of the next load
-    long long nl = 0, nm = 0;        // loads issued, chunks consumed
-    auto issue_load = [&]() {
-      const int b = (int)(nl % NST);
-      unsigned char *st = smem + b * C::Stage;
-      const int mt = lt / NTt, nt = lt % NTt;
-      tc::mbar_expect_tx(&bar_load[b], C::Stage);
-      tc::bulk_g2s(st, Asl + ((size_t)mt * KCH + lc) * (S * kTM * kKC),
-                   S * C::TileA, &bar_load[b]);
-      tc::bulk_g2s(st + S * C::TileA,
-                   Bsl + ((size_t)nt * KCH + lc) * (S * TN * kKC),
-                   S * C::TileB, &bar_load[b]);
-      nl++;
-      if (++lc == tile_nch(lt)) { lc = 0; lt += gridDim.x; }
-    };
-    while (nl < NST - 1 && lt < ntiles) issue_load();
-    int sg = 0;   // K segments accumulated so far (acc_full phases)
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      const int nch = tile_nch(t);
-      for (int c = 0; c < nch; c++) {
-        const bool seg_first = c % C::SEGC == 0;
-        if (seg_first && sg > 0) {
-          // the previous segment's accumulator must be drained first
-          if (!tc::mbar_wait(acc_empty, (sg - 1) & 1, kWaitLimit)) { ok = false; break; }
-          tc::fence_after_sync();
-        }
-        const int b = (int)(nm % NST);
-        if (!tc::mbar_wait(&bar_load[b], (uint32_t)((nm / NST) & 1), kWaitLimit)) { ok = false; break; }
-        tc::fence_after_sync();
-        const uint32_t aBase = tc::smem_u32(smem + b * C::Stage);
-        const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
-        const uint64_t bd0 = tc::smem_desc(aBase + S * C::TileA, 128,
-                                           (kKC / 8) * 128);
-        // k-steps of 16 are two core matrices (256 bytes) apart along K
-#pragma unroll
-        for (int kk = 0; kk < kKC / 16; kk++)
-          mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
-                       bd0 + (uint64_t)((kk * 256) >> 4), seg_first && kk == 0);
-        tc::mma_commit(&bar_mma[b]);
-        if (c == nch - 1 || (c + 1) % C::SEGC == 0) {
-          tc::mma_commit(acc_full);
-          sg++;
-        }
-        nm++;
-        if (lt < ntiles) {
-          // load nl reuses the stage of chunk nl - NST, the chunk before the
-          // one just issued: wait for that chunk's MMAs (nothing to wait for
-          // before the ring has wrapped)
-          const long long prev = nl - NST;
-          if (prev >= 0 &&
-              !tc::mbar_wait(&bar_mma[prev % NST], (uint32_t)((prev / NST) & 1),
-                             kWaitLimit)) { ok = false; break; }
-          issue_load();
-        }
-      }
-    }
-    if (!ok) {
+  auto give_up = [&](int why) {   // why: 1 aborted elsewhere, 2 timed out
+    if (why == 2) {
       *abort_flag = 1;
       atomicExch(err, 1);
-      // copies in flight land before the CTA may exit; MMAs finish before
-      // TMEM is freed (bounded waits)
-      for (long long g = nm; g < nl; g++)
-        tc::mbar_wait(&bar_load[g % NST], (uint32_t)((g / NST) & 1), kWaitLimit);
-      if (nm > 0)
-        tc::mbar_wait(&bar_mma[(nm - 1) % NST], (uint32_t)(((nm - 1) / NST) & 1),
+    }
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      long long g = 0;   // chunks issued
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int mt, nt;
+        tile_rc(t, mt, nt);
+        const int nch = tile_nch(nt);
+        const __nv_bfloat16 *a = Asl + (size_t)mt * KCH * (S * kTM * kKC);
+        const __nv_bfloat16 *bsrc = Bsl + (size_t)nt * KCH * (S * TN * kKC);
+        for (int c = 0; c < nch; c++, g++) {
+          const int b = (int)(g % NST);
+          if (g >= NST) {
+            // stage b last held chunk g - NST: its MMAs must be done
+            const int w = wait_or_abort(&bar_mma[b],
+                                        (uint32_t)(((g / NST) - 1) & 1),
+                                        abort_flag);
+            if (w) { give_up(w); ok = false; break; }
+          }
+          unsigned char *st = smem + b * C::Stage;
+          tc::mbar_expect_tx(&bar_load[b], C::Stage);
+          tc::bulk_g2s(st, a + (size_t)c * (S * kTM * kKC), S * C::TileA,
+                       &bar_load[b]);
+          tc::bulk_g2s(st + S * C::TileA, bsrc + (size_t)c * (S * TN * kKC),
+                       S * C::TileB, &bar_load[b]);
+        }
+      }
+      *issued = g;
+    }
+  } else if (warp == C::MMA_WARP) {
+    if (lane == 0) {
+      long long g = 0;   // chunks consumed
+      int sg = 0;        // K segments accumulated so far (acc_full phases)
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int mt, nt;
+        tile_rc(t, mt, nt);
+        const int nch = tile_nch(nt);
+        for (int c = 0; c < nch; c++) {
+          const bool seg_first = c % C::SEGC == 0;
+          if (seg_first && sg > 0) {
+            // the previous segment's accumulator must be drained first
+            const int w = wait_or_abort(acc_empty, (sg - 1) & 1, abort_flag);
+            if (w) { give_up(w); ok = false; break; }
+            tc::fence_after_sync();
+          }
+          const int b = (int)(g % NST);
+          const int w = wait_or_abort(&bar_load[b], (uint32_t)((g / NST) & 1),
+                                      abort_flag);
+          if (w) { give_up(w); ok = false; break; }
+          tc::fence_after_sync();
+          const uint32_t aBase = tc::smem_u32(smem + b * C::Stage);
+          const uint64_t ad0 = tc::smem_desc(aBase, 128, (kKC / 8) * 128);
+          const uint64_t bd0 = tc::smem_desc(aBase + S * C::TileA, 128,
+                                             (kKC / 8) * 128);
+          // k-steps of 16 are two core matrices (256 bytes) apart along K
+#pragma unroll
+          for (int kk = 0; kk < kKC / 16; kk++)
+            mma_kstep<C>(tmem, ad0 + (uint64_t)((kk * 256) >> 4),
+                         bd0 + (uint64_t)((kk * 256) >> 4),
+                         seg_first && kk == 0);
+          tc::mma_commit(&bar_mma[b]);
+          if (c == nch - 1 || (c + 1) % C::SEGC == 0) {
+            tc::mma_commit(acc_full);
+            sg++;
+          }
+          g++;
+        }
+      }
+      *consumed = g;
+      if (!ok && g > 0)   // MMAs finish before TMEM is freed (bounded)
+        tc::mbar_wait(&bar_mma[(g - 1) % NST], (uint32_t)(((g - 1) / NST) & 1),
                       kWaitLimit);
     }
-  } else if (warp >= 1) {
+  } else {
     const int q = warp & 3;            // TMEM lane quarter of this warp
     const int sub = (warp - 1) >> 2;   // its column range within the tile
     const int c_lo = sub * C::WCOLS;
@@ -443,10 +495,12 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
     int sg = 0;   // K segments drained so far
     bool alive = true;
     for (int t = blockIdx.x; t < ntiles && alive; t += gridDim.x) {
-      const int m0 = (t / NTt) * kTM, n0 = (t % NTt) * TN;
+      int mt, nt;
+      tile_rc(t, mt, nt);
+      const int m0 = mt * kTM, n0 = nt * TN;
       const int m = m0 + q * 32 + lane;
       const bool row_ok = m < M;
-      const int nseg = (tile_nch(t) + C::SEGC - 1) / C::SEGC;
+      const int nseg = (tile_nch(nt) + C::SEGC - 1) / C::SEGC;
       // Phase 1, per K segment.  Group sums are exact integers below 2^24;
       // add them exactly into 64-bit integers, hi = sum_{t <= TSPLIT} g_t
       // 2^(6(TSPLIT-t)) and lo = sum_{t > TSPLIT} g_t 2^(6(S+1-t)), and
@@ -457,13 +511,9 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
 #pragma unroll
         for (int j = 0; j < 16; j++) { hi[ch][j] = 0; lo[ch][j] = 0; }
       for (int seg = 0; seg < nseg; seg++, sg++) {
-        bool got = false;
-        for (long long i = 0; i < kWaitLimit; i++) {
-          if (tc::mbar_try_wait(acc_full, sg & 1)) { got = true; break; }
-          if (*abort_flag) break;
-        }
-        if (!got) {
-          if (!*abort_flag) atomicExch(err, 1);
+        const int w = wait_or_abort(acc_full, sg & 1, abort_flag);
+        if (w) {
+          give_up(w);
           alive = false;
           break;
         }
@@ -520,12 +570,18 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt,
 #pragma unroll
       for (int ch = 0; ch < NCH; ch++)
         acc = epi.chunk(m, row_ok, n0 + c_lo + ch * 16, v[ch], acc);
-      epi.finish(m, row_ok, (t % NTt) * C::EW + sub, acc);
+      epi.finish(m, row_ok, nt * C::EW + sub, acc);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
+  if (tid == 0 && *abort_flag) {
+    // copies issued but never consumed land before the CTA exits (bounded)
+    for (long long g = *consumed; g < *issued; g++)
+      tc::mbar_wait(&bar_load[g % NST], (uint32_t)((g / NST) & 1), kWaitLimit);
+  }
+  __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
@@ -625,7 +681,8 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
   const int MT = A.RP / kTM, NTt = B.RP / C::TN;
   const int grid = std::max(1, std::min(MT * NTt, sms));
   k_oz_gemm<C, Epi><<<grid, C::THREADS, C::Smem, st>>>(
-      A.rows, B.rows, A.K, A.KP, MT, NTt, A.q.as<__nv_bfloat16>(),
+      A.rows, B.rows, A.K, A.KP, MT, NTt, make_fastdiv(NTt),
+      A.q.as<__nv_bfloat16>(),
       A.scale.as<double>(), B.q.as<__nv_bfloat16>(), B.scale.as<double>(),
       tri ? 1 : 0, epi, err);
   FGB_LAUNCH_CHECK("k_oz_gemm");
