@@ -184,12 +184,32 @@ __device__ __forceinline__ double exact_scaled(long long x, int sc) {
   return __longlong_as_double(bits);
 }
 
-// x 2^sc rounded once to FP32.
+static __device__ __noinline__ float scaled_float_rare(long long x, int sc) {
+  return ldexpf(__ll2float_rn(x), sc);
+}
+
+// x 2^sc rounded once to FP32 (nearest, ties to even: the value of
+// __ll2float_rn(x) scaled exactly), built with integer instructions.
 __device__ __forceinline__ float scaled_float(long long x, int sc) {
-  const float f = __ll2float_rn(x);
-  if (sc >= -126 && sc <= 127)
-    return __fmul_rn(f, __uint_as_float((unsigned)(sc + 127) << 23));
-  return ldexpf(f, sc);
+  if (x == 0) return 0.f;
+  const unsigned long long a = x < 0 ? 0ULL - (unsigned long long)x
+                                     : (unsigned long long)x;
+  const int p = 63 - __clzll((long long)a);            // leading bit
+  unsigned long long q;
+  int lead = p;                                        // weight of q's top bit
+  if (p > 23) {
+    const int r = p - 23;
+    q = a >> r;
+    const unsigned long long rem = a & ((1ULL << r) - 1), half = 1ULL << (r - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    if (q == (1ULL << 24)) { q >>= 1; lead++; }
+  } else {
+    q = a << (23 - p);
+  }
+  const int field = lead + sc + 127;
+  if (field < 1 || field > 254) return scaled_float_rare(x, sc);
+  return __uint_as_float((x < 0 ? 0x80000000u : 0u) | ((unsigned)field << 23) |
+                         ((unsigned)q & 0x7FFFFFu));
 }
 
 // rn(d 2^sh) as a 64-bit integer (nearest, ties to even, as __double2ll_rn
@@ -217,9 +237,14 @@ __device__ __forceinline__ long long fixed_rn(double d, int sh) {
   return (bits >> 63) ? -(long long)q : (long long)q;
 }
 
-// BF16 bits of a small integer (|q| <= 256, exact).
+// BF16 bits of a small integer (|q| <= 256, exact): the float of q from the
+// bits of 1.5 * 2^23 + q minus 1.5 * 2^23 (one FP32 subtraction; an
+// integer-to-float conversion would run on the FP64/conversion pipe, which
+// this GPU runs slowly and which the tensor-core epilogue must leave free).
 __device__ __forceinline__ uint32_t bf16_bits(long long q) {
-  return __float_as_uint(__int2float_rn((int)q)) >> 16;
+  return __float_as_uint(
+             __fsub_rn(__int_as_float(0x4B400000 + (int)q), 12582912.0f)) >>
+         16;
 }
 
 // The S base-64 digits of X (|X| < 2^(6S)) for 8 consecutive k, stored as
