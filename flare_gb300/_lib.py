@@ -69,6 +69,12 @@ SIGNATURES = {
     "fgb_md_step": (_i, [_vp, _i, _d, _d, _vp]),
     "fgb_md_set_graphs": (_i, [_vp, _i, _d]),
     "fgb_md_stats": (_i, [_vp, _vp]),
+    "fgb_model_mapping": (_i, [_vp, _vp, _vp]),
+    "fgb_qr_thin_q": (_i, [_i, _i, _vp, _vp, _vp]),
+    "fgb_mapped_create": (_i, [_pvp, _vp, _i, _i, _vp, _vp]),
+    "fgb_mapped_destroy": (_i, [_vp]),
+    "fgb_mapped_predict": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp,
+                                _vp, _vp, _vp, _vp, _vp]),
     "fgb_tune_set_mode": (_i, [_i]),
     "fgb_tune_force": (_i, [_i, _i]),
     "fgb_tune_clear": (_i, []),

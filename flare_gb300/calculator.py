@@ -115,6 +115,22 @@ class SGP_Calculator(Calculator):
             full[:, 0] = _signed_sqrt(v) / np.abs(self.gp_model.hyps[0])
             self.results["stds"] = full
 
+    def build_map(self, filename="lmp.flare", contributor="user",
+                  map_uncertainty=False):
+        """calculator.py:169-185: the LAMMPS potential file and the files of
+        its uncertainty compute (variance map, or L_inv and sparse
+        descriptors)."""
+        self.gp_model.sparse_gp.write_mapping_coefficients(filename,
+                                                           contributor, 0)
+        if map_uncertainty:
+            self.gp_model.write_varmap_coefficients(f"map_unc_{filename}",
+                                                    contributor, 0)
+        else:
+            self.gp_model.sparse_gp.write_L_inverse(f"L_inv_{filename}",
+                                                    contributor)
+            self.gp_model.sparse_gp.write_sparse_descriptors(
+                f"sparse_desc_{filename}", contributor)
+
     def get_uncertainties(self, atoms):
         return self.get_property("stds", atoms)
 

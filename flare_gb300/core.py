@@ -975,6 +975,31 @@ class SparseGP(_Training):
             "predict_DTC needs self_kernel_struc "
             "(normalized_dot_product.cpp:451-586), which is not built")
 
+    # -------------------------------------------------- mapped models
+    def write_mapping_coefficients(self, file_name, contributor,
+                                   kernel_index=0):
+        """lmp.flare coefficients (sparse_gp.cpp:1199-1264); flare_gb300.mapped."""
+        from . import mapped
+        return mapped.write_mapping_coefficients(self, file_name, contributor,
+                                                 kernel_index)
+
+    def write_varmap_coefficients(self, file_name, contributor,
+                                  kernel_index=0):
+        """Power-1 variance map (sparse_gp.cpp:1266-1335)."""
+        from . import mapped
+        return mapped.write_varmap_coefficients(self, file_name, contributor,
+                                                kernel_index)
+
+    def write_L_inverse(self, file_name, contributor):
+        """L_inv blocks for compute flare/std/atom (sparse_gp.cpp:1337-1391)."""
+        from . import mapped
+        mapped.write_L_inverse(self, file_name, contributor)
+
+    def write_sparse_descriptors(self, file_name, contributor):
+        """Sparse descriptors for compute flare/std/atom (sparse_gp.cpp:1393-1466)."""
+        from . import mapped
+        mapped.write_sparse_descriptors(self, file_name, contributor)
+
     def compute_cluster_uncertainties(self, structure):
         """sparse_gp.cpp:94-139 (species-sorted variances)."""
         r = self.predict_batch([structure], _lib.FGB_WANT_LOCAL_VAR)

@@ -103,6 +103,10 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool fixed = false);
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st);
+// The same on any workspace: perm = atoms of species 0 (ascending), then
+// 1, ...; one host synchronisation (counts and the species range check).
+int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
+                        std::vector<int> &counts, cudaStream_t st);
 int envs_struc_impl(const B2Params &p, double sigma, double power,
                     const int *h_counts, const double *d_sparse,
                     fgb_nlist_s *nl, const int *d_species, double *d_kern,

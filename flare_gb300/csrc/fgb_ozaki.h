@@ -63,6 +63,11 @@ int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S = kS);
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
          cudaStream_t st);
+// C (A.rows x B.rows, leading dimension ldc) = A B^T in FP64 from kS-slice
+// operands (A tiles of kTM rows, B tiles of kTN rows): exact integer sums,
+// one rounding.
+int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
+               int *err, cudaStream_t st);
 // Y (A.rows x B.rows, leading dimension ldy) = A B^T rounded to FP32, from
 // kSF32-slice operands (A tiles of kTM rows, B tiles of 128 or 64 rows;
 // `ew` epilogue warps per lane quarter, 2 or 4 for 128-row tiles).

@@ -68,6 +68,19 @@ k_fold_gemm(int nd, int M, const double *__restrict__ ST,
   }
 }
 
+// beta = S^T (alpha * valid), FP64 output
+__global__ void k_fold_vec64(int M, int nd, const double *__restrict__ S,
+                             const double *__restrict__ alpha,
+                             const unsigned char *__restrict__ valid,
+                             double *__restrict__ beta) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nd) return;
+  double acc = 0.0;
+  for (int t = 0; t < M; t++)
+    if (valid[t]) acc += alpha[t] * S[(long long)t * nd + q];
+  beta[q] = acc;
+}
+
 // beta = S^T (alpha * valid), FP32 output
 __global__ void k_fold_vec(int M, int nd, const double *__restrict__ S,
                            const double *__restrict__ alpha,
@@ -257,3 +270,64 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
 }
 
 }  // namespace fgb
+
+using namespace fgb;
+
+// Mapping coefficients of a solved power-1 or power-2 model
+// (normalized_dot_product.cpp:653-767): per species s,
+//   power 2: sigma^2 sum_t alpha_t s^_t s^_t^T   (n_d x n_d, row-major)
+//   power 1: sigma^2 sum_t alpha_t s^_t          (n_d)
+// over the valid sparse environments of the species (s^ = s / |s|), in
+// FP64 on the device.
+extern "C" int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream) {
+  if (!m || !h_beta || (m->power != 1.0 && m->power != 2.0)) {
+    set_error("fgb_model_mapping: invalid arguments (power 1 or 2 models)");
+    return FGB_EINVAL;
+  }
+  if (!m->solved) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int S = m->b2.n_species, nd = m->b2.n_d;
+  const bool quad = m->power == 2.0;
+  const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
+  const double sig2 = m->sigma * m->sigma;
+  DevBuf out, ST, STa, Bf;
+  int rc;
+  if ((rc = out.ensure(sizeof(double) * per * S)) ||
+      (quad && (rc = Bf.ensure(sizeof(float) * per))))
+    return rc;
+  FGB_CUDA(cudaMemsetAsync(out.p, 0, sizeof(double) * per * S, st));
+  for (int s = 0; s < S; s++) {
+    const int Ms = m->h_counts[s], c = m->h_offsets[s];
+    if (Ms == 0) continue;
+    const double *Ss = m->S.as<double>() + (size_t)c * nd;
+    double *dst = out.as<double>() + per * s;
+    if (quad) {
+      if ((rc = ST.ensure(sizeof(double) * (size_t)Ms * nd)) ||
+          (rc = STa.ensure(sizeof(double) * (size_t)Ms * nd)))
+        return rc;
+      k_scaled_transpose<<<ceil_div((long long)Ms * nd, 256), 256, 0, st>>>(
+          Ms, nd, Ss, m->alpha.as<double>() + c,
+          m->svalid.as<unsigned char>() + c, ST.as<double>(), STa.as<double>());
+      FGB_LAUNCH_CHECK("k_scaled_transpose");
+      dim3 g(ceil_div(nd, BN), ceil_div(nd, BM));
+      k_fold_gemm<<<g, GT, 0, st>>>(nd, Ms, ST.as<double>(), STa.as<double>(),
+                                    Bf.as<float>(), dst);
+      FGB_LAUNCH_CHECK("k_fold_gemm");
+      FGB_CUDA(cudaStreamSynchronize(st));   // ST/STa reused next species
+    } else {
+      k_fold_vec64<<<ceil_div(nd, 128), 128, 0, st>>>(
+          Ms, nd, Ss, m->alpha.as<double>() + c,
+          m->svalid.as<unsigned char>() + c, dst);
+      FGB_LAUNCH_CHECK("k_fold_vec64");
+    }
+  }
+  FGB_CUDA(cudaMemcpyAsync(h_beta, out.p, sizeof(double) * per * S,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  for (size_t i = 0; i < per * S; i++) h_beta[i] *= sig2;
+  return FGB_OK;
+}

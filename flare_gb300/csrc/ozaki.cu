@@ -721,6 +721,11 @@ int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
   return gemm_c<CfgF64>(A, B, tri, epi, err, st);
 }
 
+int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
+               int *err, cudaStream_t st) {
+  return gemm(A, B, false, EpiStore{C, ldc, B.rows}, err, st);
+}
+
 int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
              int *err, cudaStream_t st, int ew) {
   const EpiStoreF32 epi{Y, ldy, B.rows};

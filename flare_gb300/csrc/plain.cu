@@ -685,3 +685,50 @@ done:
   if (blas) cublasDestroy(blas);
   return rc;
 }
+
+// Thin Q of a Householder QR (cuSOLVER geqrf + orgqr): A and Q column-major
+// rows x cols (rows >= cols).  The varmap coefficients of a power-1 model
+// (normalized_dot_product.cpp:769-830) are the leading rows of such a Q.
+extern "C" int fgb_qr_thin_q(int rows, int cols, const double *d_A,
+                             double *d_Q, void *stream) {
+  if (rows <= 0 || cols <= 0 || rows < cols || !d_A || !d_Q) {
+    set_error("fgb_qr_thin_q: invalid arguments (rows >= cols > 0)");
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = FGB_OK;
+  cusolverDnHandle_t sol = nullptr;
+  DevBuf tau, work, info;
+  int lwork = 0, lw2 = 0, hinfo = 0;
+  if ((rc = tau.ensure(sizeof(double) * (size_t)cols)) ||
+      (rc = info.ensure(sizeof(int))))
+    return rc;
+  FGB_SOLVER(cusolverDnCreate(&sol), "cusolverDnCreate");
+  FGB_SOLVER(cusolverDnSetStream(sol, st), "cusolverDnSetStream");
+  FGB_SOLVER(cudaMemcpyAsync(d_Q, d_A, sizeof(double) * (size_t)rows * cols,
+                             cudaMemcpyDeviceToDevice, st), "copy A");
+  FGB_SOLVER(cusolverDnDgeqrf_bufferSize(sol, rows, cols, d_Q, rows, &lwork),
+             "geqrf_bufferSize");
+  FGB_SOLVER(cusolverDnDorgqr_bufferSize(sol, rows, cols, cols, d_Q, rows,
+                                         tau.as<double>(), &lw2),
+             "orgqr_bufferSize");
+  lwork = std::max(lwork, lw2);
+  if ((rc = work.ensure(sizeof(double) * ((size_t)lwork + 1)))) goto done;
+  FGB_SOLVER(cusolverDnDgeqrf(sol, rows, cols, d_Q, rows, tau.as<double>(),
+                              work.as<double>(), lwork, info.as<int>()),
+             "geqrf");
+  FGB_SOLVER(cusolverDnDorgqr(sol, rows, cols, cols, d_Q, rows,
+                              tau.as<double>(), work.as<double>(), lwork,
+                              info.as<int>()),
+             "orgqr");
+  FGB_SOLVER(cudaMemcpyAsync(&hinfo, info.p, sizeof(int),
+                             cudaMemcpyDeviceToHost, st), "info");
+  FGB_SOLVER(cudaStreamSynchronize(st), "sync");
+  if (hinfo != 0) {
+    set_error("fgb_qr_thin_q: QR failed (info %d)", hinfo);
+    rc = FGB_ECUDA;
+  }
+done:
+  if (sol) cusolverDnDestroy(sol);
+  return rc;
+}

@@ -270,28 +270,32 @@ int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
 // one read (a single synchronisation).
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st) {
-  const int S = m->b2.n_species;
+  return species_permutation(m->b2.n_species, m->ws, d_species, N, counts, st);
+}
+
+int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
+                        std::vector<int> &counts, cudaStream_t st) {
   counts.assign(S, 0);
   int rc;
-  if ((rc = m->ws.perm.ensure(sizeof(int) * (N + 1))) ||
-      (rc = m->ws.flags.ensure(sizeof(int) * (N + 1))) ||
-      (rc = m->ws.pos.ensure(sizeof(int) * (N + 1))) ||
-      (rc = m->ws.scal.ensure(sizeof(int) * (S + 2))))
+  if ((rc = ws.perm.ensure(sizeof(int) * (N + 1))) ||
+      (rc = ws.flags.ensure(sizeof(int) * (N + 1))) ||
+      (rc = ws.pos.ensure(sizeof(int) * (N + 1))) ||
+      (rc = ws.scal.ensure(sizeof(int) * (S + 2))))
     return rc;
   if (N == 0) return FGB_OK;
-  int *tot = m->ws.scal.as<int>();   // [0, S): counts; [S]: range flag
+  int *tot = ws.scal.as<int>();   // [0, S): counts; [S]: range flag
   FGB_CUDA(cudaMemsetAsync(tot + S, 0, sizeof(int), st));
   k_check_species<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, S, tot + S);
   FGB_LAUNCH_CHECK("k_check_species");
   for (int s = 0; s < S; s++) {
     k_species_flags<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, s,
-                                                      m->ws.flags.as<int>());
+                                                      ws.flags.as<int>());
     FGB_LAUNCH_CHECK("k_species_flags");
-    if ((rc = scan_int_to_int(m->ws.flags.as<int>(), m->ws.pos.as<int>(), N,
-                              tot + s, m->ws.scan_tmp, st)))
+    if ((rc = scan_int_to_int(ws.flags.as<int>(), ws.pos.as<int>(), N,
+                              tot + s, ws.scan_tmp, st)))
       return rc;
     k_species_scatter<<<ceil_div(N, 256), 256, 0, st>>>(
-        N, d_species, s, m->ws.pos.as<int>(), tot, m->ws.perm.as<int>());
+        N, d_species, s, ws.pos.as<int>(), tot, ws.perm.as<int>());
     FGB_LAUNCH_CHECK("k_species_scatter");
   }
   std::vector<int> h(S + 1);

@@ -147,6 +147,20 @@ class SGP_Wrapper:
         if update_qr:
             sgp.update_matrices_QR()
 
+    def write_mapping_coefficients(self, filename, contributor, kernel_idx):
+        """flare/bffs/sgp/sparse_gp.py:429-430."""
+        self.sparse_gp.write_mapping_coefficients(filename, contributor,
+                                                  kernel_idx)
+
+    def write_varmap_coefficients(self, filename, contributor, kernel_idx):
+        """flare/bffs/sgp/sparse_gp.py:432-495: the variance map of the
+        power-1 model with this sparse set, sigma and jitter (which is all
+        it depends on; the reference rebuilds and retrains that model)."""
+        assert len(self.sparse_gp.kernels) == 1 and kernel_idx == 0, \
+            "Not support multiple kernels"
+        return self.sparse_gp.write_varmap_coefficients(filename, contributor,
+                                                        kernel_idx)
+
     def _numbers(self, coded):
         inv = {v: k for k, v in self.species_map.items()}
         return [int(inv[s]) for s in coded]

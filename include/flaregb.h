@@ -247,6 +247,43 @@ int fgb_md_read(fgb_md_t md, double *h_positions, double *h_velocities,
                 double *h_kinetic, double *h_max_std, long long *h_flagged,
                 void *stream);
 
+/* ------------------------------------------------------- mapped models
+ * The mapping coefficients of a solved power-1 or power-2 model
+ * (SparseGP::write_mapping_coefficients, sparse_gp.cpp:1199-1264, with
+ * compute_map_coeff_pow1/pow2, normalized_dot_product.cpp:653-767): per
+ * species sigma^2 sum_t alpha_t s^_t s^_t^T (power 2; n_d x n_d row-major,
+ * symmetric) or sigma^2 sum_t alpha_t s^_t (power 1; n_d), FP64. */
+int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream);
+
+/* Thin Q (rows x cols, column-major) of the Householder QR of A (rows x
+ * cols, column-major, rows >= cols), device buffers; the varmap
+ * coefficients (normalized_dot_product.cpp:769-830) are its leading rows. */
+int fgb_qr_thin_q(int rows, int cols, const double *d_A, double *d_Q,
+                  void *stream);
+
+/* Evaluation from mapping coefficients, the model a LAMMPS run loads from
+ * an lmp.flare file (pair_flare.cpp:68-175, lammps_descriptor.cpp:250-326):
+ * E_i = B2.beta_s B2/|B2|^2 (power 2) or beta_s.B2/|B2| (power 1) for the
+ * NormalizedDotProduct kernel (normalized != 0; the DotProduct forms
+ * without the norms), zero where |B2|^2 < 1e-8, forces and stresses by the
+ * reverse-mode adjoint.  h_beta as returned by fgb_model_mapping.  An
+ * optional variance map h_varmap (n_species x n_d x n_d row-major Q_s, the
+ * map_unc file of compute flare/std/atom, compute_flare_std_atom.cpp:
+ * 179-193) gives v_i = 1 - |Q_s^T B2/|B2||^2 per atom (FGB_WANT_LOCAL_VAR;
+ * the std is sign(v) sqrt|v|).  Outputs as in fgb_predict, plus per-atom
+ * energies (any output may be NULL). */
+typedef struct fgb_mapped_s *fgb_mapped_t;
+int fgb_mapped_create(fgb_mapped_t *out, fgb_b2_t b2, int power,
+                      int normalized, const double *h_beta,
+                      const double *h_varmap);
+int fgb_mapped_destroy(fgb_mapped_t m);
+int fgb_mapped_predict(fgb_mapped_t m, int n_struc, const int *h_atom_offsets,
+                       const double *h_cells, const double *d_positions,
+                       const int *d_species, double cutoff, int want,
+                       double *d_energy, double *d_forces, double *d_stress,
+                       double *d_atom_energy, double *d_local_var,
+                       void *stream);
+
 /* ------------------------------------------------------------ autotuner
  * Tile shapes of the sliced tensor-core GEMMs (kernel, variance and force
  * GEMMs of the mixed path) are chosen per problem shape: at the first call

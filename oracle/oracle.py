@@ -695,3 +695,117 @@ def calculator_results(structure, variance_type, sigma,
         full[:, 0] = stds / abs(sigma)
         res["stds"] = full
     return res
+
+
+# ------------------------------------------------------------ mapped models
+def mapping_coefficients(sgp, kernel_index=0):
+    """NormalizedDotProduct::compute_map_coeff_pow1 / _pow2
+    (normalized_dot_product.cpp:653-767): per species, over its non-empty
+    sparse environments j in order, beta += sig2 p_k alpha_j (power 1) or
+    beta(k<=l) += (k == l ? 1 : 2) sig2 p_k p_l alpha_j (power 2),
+    p = s_j / |s_j|; the upper triangle row by row."""
+    k = sgp.kernels[kernel_index]
+    cd = sgp.sparse_descriptors[kernel_index]
+    sig2 = k.sigma ** 2
+    p = cd.n_descriptors
+    alpha_ind = sum(sgp.sparse_descriptors[i].n_clusters
+                    for i in range(kernel_index))
+    if k.power == 1:
+        out = np.zeros((cd.n_types, p))
+    else:
+        iu = np.triu_indices(p)
+        fac = np.where(iu[0] == iu[1], 1.0, 2.0)
+        out = np.zeros((cd.n_types, len(iu[0])))
+    for s in range(cd.n_types):
+        c = cd.cumulative_type_count[s]
+        for j in range(cd.n_clusters_by_type[s]):
+            nrm = cd.descriptor_norms[s][j]
+            if nrm < 1e-8:
+                continue
+            a = sgp.alpha[alpha_ind + c + j]
+            pv = cd.descriptors[s][j] / nrm
+            if k.power == 1:
+                out[s] += sig2 * pv * a
+            else:
+                out[s] += fac * (sig2 * pv[iu[0]] * pv[iu[1]] * a)
+    return out
+
+
+def varmap_coefficients(sgp, kernel_index=0):
+    """NormalizedDotProduct::compute_varmap_coefficients
+    (normalized_dot_product.cpp:769-830): Householder QR (LAPACK, standing in
+    for Eigen's HouseholderQR) of [S^T; sqrt(jitter)/sigma I] per species;
+    coefficient (i, j) = Q(i, j) for j < n_s, row-major p x p."""
+    k = sgp.kernels[kernel_index]
+    cd = sgp.sparse_descriptors[kernel_index]
+    p = cd.n_descriptors
+    jr = math.sqrt(sgp.Kuu_jitter)
+    out = np.zeros((cd.n_types, p * p))
+    for s in range(cd.n_types):
+        n = cd.n_clusters_by_type[s]
+        if n == 0:
+            continue
+        pi = np.array(cd.descriptors[s], dtype=np.float64)
+        for i in range(n):
+            if cd.descriptor_norms[s][i] >= 1e-8:
+                pi[i] = pi[i] / cd.descriptor_norms[s][i]
+        A = np.vstack([pi.T, jr * np.eye(n) / k.sigma])
+        Q, _ = np.linalg.qr(A, mode="reduced")
+        blk = np.zeros((p, p))
+        w = min(n, p)
+        blk[:, :w] = Q[:p, :w]
+        out[s] = blk.reshape(-1)
+    return out
+
+
+def write_mapping_text(coeffs, power, descriptor_settings, radial_basis,
+                       cutoff_function, cutoffs, contributor, date):
+    """SparseGP::write_mapping_coefficients (sparse_gp.cpp:1199-1264) with
+    NormalizedDotProduct::write_info (:832-835) and B2::write_to_file
+    (b2.cpp:52-74), statement by statement."""
+    o = ["DATE: ", date, " ", "CONTRIBUTOR: ", contributor, "\n"]
+    o += ["%.0f" % power, " NormalizedDotProduct\n"]
+    S, N, L = descriptor_settings
+    o += [radial_basis, "\n", "%d %d %d " % (S, N, L), "%d" % coeffs.shape[1],
+          "\n", cutoff_function, "\n"]
+    for i in range(S):
+        for j in range(S):
+            o += ["%.2f" % cutoffs[i][j], " "]
+    o += ["\n"]
+    count = 0
+    for i in range(coeffs.shape[0]):
+        if count != 0:
+            o += ["\n"]
+        for j in range(coeffs.shape[1]):
+            v = coeffs[i, j]
+            o += ["  " if v > 0 else " ", "%.16e" % v]
+            count += 1
+            if count == 5:
+                count = 0
+                o += ["\n"]
+    return "".join(o)
+
+
+def mapped_energy_and_w(B2, beta, power, normalized=True):
+    """compute_energy_and_u (lammps_descriptor.cpp:250-275): the local
+    energy and w = dE/dB2 from one B2 vector and the species' beta (matrix
+    for power 2, vector for power 1)."""
+    n2 = float(B2 @ B2)
+    if normalized:
+        if power == 1:
+            nrm = n2 ** 0.5
+            e = float(B2 @ beta) / nrm
+            w = beta / nrm - e * B2 / n2
+        else:
+            bp = beta @ B2
+            e = float(B2 @ bp) / n2
+            w = 2 * (bp - e * B2) / n2
+    else:
+        if power == 1:
+            w = beta.copy()
+            e = float(B2 @ w)
+        else:
+            bp = beta @ B2
+            e = float(B2 @ bp)
+            w = 2 * bp
+    return e, w
