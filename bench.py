@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--replicas", type=int, default=0,
                     help="md workload: number of replicas (default 256)")
     ap.add_argument("--workload", default="alloy1000",
-                    choices=["alloy1000", "fcc1m", "md", "serve"],
+                    choices=["alloy1000", "fcc1m", "md", "serve", "mapped"],
                     help="fcc1m: one 1,048,576-atom structure, E+F+virial, "
                          "peak device memory (reported as a side record)")
     return ap.parse_args()
@@ -676,6 +676,111 @@ def autotune_table():
             for e in autotune.table()]
 
 
+def run_mapped(args):
+    """Evaluation from mapping coefficients (the LAMMPS pair style's model):
+    the alloy1000 power-2 model written to an lmp.flare file and read back,
+    energies + forces + stresses of 32 structures per call, device-resident
+    inputs, against the same model's sparse-GP prediction (E+F+S, FP64)."""
+    import tempfile
+    import torch
+    from flare_gb300 import _lib
+    from flare_gb300 import workloads as wl
+    from flare_gb300.mapped import MappedPotential
+    L = _lib.lib()
+    c = wl.ALLOY
+    gp, b2, k = wl.build_alloy_model()
+    model = gp._device_model([b2])
+    with tempfile.TemporaryDirectory() as td:
+        t0 = time.time()
+        path = os.path.join(td, "lmp.flare")
+        gp.write_mapping_coefficients(path, "bench", 0)
+        write_s = time.time() - t0
+        size = os.path.getsize(path)
+        pot = MappedPotential(path)
+    B = args.batch
+    structs = [wl.alloy_structure(c["test_seed0"] + i) for i in range(B)]
+    offsets = np.zeros(B + 1, dtype=np.int32)
+    for i, s_ in enumerate(structs):
+        offsets[i + 1] = offsets[i] + len(s_[1])
+    cells = np.ascontiguousarray(np.stack([s_[0].reshape(-1) for s_ in structs]))
+    pos = np.ascontiguousarray(np.concatenate([s_[2] for s_ in structs]))
+    sp = np.ascontiguousarray(np.concatenate([s_[1] for s_ in structs]).astype(np.int32))
+    N = int(offsets[-1])
+    dev = torch.device("cuda", 0)
+    d_pos = torch.from_numpy(pos).to(dev)
+    d_sp = torch.from_numpy(sp).to(dev)
+    out = {k_: torch.zeros(n, dtype=torch.float64, device=dev)
+           for k_, n in (("e", B), ("f", 3 * N), ("s", 6 * B), ("a", N),
+                         ("e2", B), ("f2", 3 * N), ("s2", 6 * B), ("v", N))}
+    sptr = _lib.stream_ptr(torch.cuda.current_stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    mprec = {"fp64": _lib.FGB_PREC_FP64, "mixed": _lib.FGB_PREC_MIXED}
+
+    def mapped_step(precision=args.precision):
+        _lib.check(L.fgb_mapped_predict(
+            pot.h, B, _lib.ptr(offsets), _lib.ptr(cells), _lib.ptr(d_pos),
+            _lib.ptr(d_sp), c["rc"], 0x7, _lib.ptr(out["e"]), _lib.ptr(out["f"]),
+            _lib.ptr(out["s"]), _lib.ptr(out["a"]), None, mprec[precision],
+            sptr))
+
+    def gp_step(prec):
+        _lib.check(L.fgb_predict(model.h, B, _lib.ptr(offsets), _lib.ptr(cells),
+                                 _lib.ptr(d_pos), _lib.ptr(d_sp), c["rc"], 0x7,
+                                 prec, _lib.ptr(out["e2"]), _lib.ptr(out["f2"]),
+                                 _lib.ptr(out["s2"]), None, sptr))
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        per = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            per.append(e0.elapsed_time(e1))
+        return float(np.median(per))
+
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_mapped.csv"))
+    os.makedirs(os.path.dirname(clocks.path), exist_ok=True)
+    with clocks:
+        ms_map = timed(mapped_step)
+    other = "fp64" if args.precision == "mixed" else "mixed"
+    ms_map_other = timed(lambda: mapped_step(other))
+    ms_gp64 = timed(lambda: gp_step(_lib.FGB_PREC_FP64))
+    ms_gpmx = timed(lambda: gp_step(_lib.FGB_PREC_MIXED))
+    mapped_step()
+    gp_step(_lib.FGB_PREC_FP64)
+    torch.cuda.synchronize()
+    e_err = float((out["e"] - out["e2"]).abs().max()) / 1000
+    f_err = float((out["f"] - out["f2"]).abs().max())
+    f_mae = float((out["f"] - out["f2"]).abs().mean())
+    print(json.dumps({
+        "metric": "mapped evaluation atoms/s (E+F+S from lmp.flare coefficients)",
+        "value": N / (ms_map * 1e-3), "unit": "atoms/s",
+        "ms_per_step": ms_map, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "precision": args.precision,
+        "dtype": "f64 (exact-slicing tensor-core Y = B2 beta)" if args.precision == "fp64"
+                 else "f64+df+f32 (double-float descriptor, FP32 adjoint, FP64-level Y)",
+        "other_precision_ms_per_step": {other: ms_map_other},
+        "config": {"workload": "alloy1000 power-2 model mapped: %d structures x "
+                               "1000 atoms, B2 [2,8,4] rc 5.5 (n_d 680)" % B,
+                   "atoms_per_step": N, "l2": "flushed between steps"},
+        "coefficient_file": {"bytes": size, "write_s": round(write_s, 2)},
+        "same_model_sparse_gp_ms_per_step": {"fp64": ms_gp64, "mixed": ms_gpmx,
+                                             "want": "E+F+S"},
+        "mapped_vs_fp64_gp": {"energy_ev_per_atom_max": e_err,
+                              "force_max_ev_per_a": f_err,
+                              "force_mae_ev_per_a": f_mae},
+        "clocks": clocks.summary(),
+    }), flush=True)
+
+
 def run_md(args):
     """Uncertainty-aware MD ensemble (md3): replicas advanced together by
     velocity Verlet with forces and local std every step; then the sparse
@@ -773,6 +878,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "mapped":
+        run_mapped(args)
         return
     run_ours(args, rank, world, local)
 

@@ -74,7 +74,7 @@ SIGNATURES = {
     "fgb_mapped_create": (_i, [_pvp, _vp, _i, _i, _vp, _vp]),
     "fgb_mapped_destroy": (_i, [_vp]),
     "fgb_mapped_predict": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _vp,
-                                _vp, _vp, _vp, _vp, _vp]),
+                                _vp, _vp, _vp, _vp, _i, _vp]),
     "fgb_tune_set_mode": (_i, [_i]),
     "fgb_tune_force": (_i, [_i, _i]),
     "fgb_tune_clear": (_i, []),

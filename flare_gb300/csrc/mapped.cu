@@ -135,7 +135,6 @@ struct fgb_mapped_s {
   DevBuf beta;                                        // FP64, per species
   std::vector<std::unique_ptr<oz::Sliced>> ozBeta;    // power 2: beta_s rows
   std::vector<std::unique_ptr<oz::Sliced>> ozQ;       // variance map: Q_s^T rows
-  std::vector<int> zero_species;                      // species with beta_s = 0
   fgb_nlist_s nl;
   fgb_workspace ws;
 };
@@ -236,8 +235,15 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
                                   int want, double *d_energy,
                                   double *d_forces, double *d_stress,
                                   double *d_atom_energy, double *d_local_var,
-                                  void *stream) {
+                                  int precision, void *stream) {
   if (!m) { set_error("fgb_mapped_predict: null handle"); return FGB_EINVAL; }
+  if (precision != FGB_PREC_FP64 && precision != FGB_PREC_MIXED) {
+    set_error("fgb_mapped_predict: unknown precision %d", precision);
+    return FGB_EINVAL;
+  }
+  // mixed: the descriptor in double-float and the adjoint in FP32, as in
+  // the prediction pipeline; Y = B2 beta stays FP64-level (exact slicing)
+  const bool mixed = precision == FGB_PREC_MIXED;
   if ((want & FGB_WANT_LOCAL_VAR) && !m->has_var) {
     set_error("fgb_mapped_predict: no variance map loaded");
     return FGB_EINVAL;
@@ -279,7 +285,7 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   }
   if ((rc = launch_b2_forward(p, &m->nl, d_species, ws.A.as<double>(),
                               ws.B2.as<double>(), ws.norms.as<double>(), st,
-                              false)))
+                              mixed)))
     return rc;
   std::vector<int> counts;
   if ((rc = species_permutation(S, ws, d_species, N, counts, st))) return rc;
@@ -329,7 +335,7 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   if (want_grad) {
     if ((rc = launch_b2_adjoint(p, &m->nl, d_species, ws.A.as<double>(),
                                 ws.gB2.as<double>(), ws.pair_grad.as<double3>(),
-                                st, false)) ||
+                                st, mixed)) ||
         (rc = launch_forces(&m->nl, ws.pair_grad.as<double3>(),
                             ws.forces.as<double>(), ws.virial.as<double>(),
                             st)))

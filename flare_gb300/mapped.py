@@ -408,9 +408,12 @@ class MappedPotential:
             _lib._lib.fgb_mapped_destroy(self.h)
             self.h = None
 
-    def predict(self, structures, std=False):
+    def predict(self, structures, std=False, precision="fp64"):
         """dict: energy [S], forces [N, 3], stress [S, 6] (flare order),
-        atom_energies [N]; with ``std`` the mapped local std [N]."""
+        atom_energies [N]; with ``std`` the mapped local std [N].
+        ``precision`` "mixed": descriptor in double-float and adjoint in
+        FP32 (the prediction pipeline's mixed mode)."""
+        prec = {"fp64": _lib.FGB_PREC_FP64, "mixed": _lib.FGB_PREC_MIXED}[precision]
         if std and not self.has_std:
             raise ValueError("no variance map loaded")
         want = 0x7 | (0x8 if std else 0)
@@ -420,7 +423,7 @@ class MappedPotential:
                 self.h, S, ptr(offsets), ptr(cells), ptr(d_pos), ptr(d_sp),
                 self.cutoff, want, ptr(out["energy"]), ptr(out["forces"]),
                 ptr(out["stress"]), ptr(out["atom_energies"]),
-                ptr(out["local_var"]), stream_ptr()), "MappedPotential")
+                ptr(out["local_var"]), prec, stream_ptr()), "MappedPotential")
 
         r, _ = _run(go, structures)
         if std:

@@ -271,7 +271,9 @@ int fgb_qr_thin_q(int rows, int cols, const double *d_A, double *d_Q,
  * map_unc file of compute flare/std/atom, compute_flare_std_atom.cpp:
  * 179-193) gives v_i = 1 - |Q_s^T B2/|B2||^2 per atom (FGB_WANT_LOCAL_VAR;
  * the std is sign(v) sqrt|v|).  Outputs as in fgb_predict, plus per-atom
- * energies (any output may be NULL). */
+ * energies (any output may be NULL); precision FGB_PREC_FP64, or
+ * FGB_PREC_MIXED (descriptor in double-float, adjoint in FP32, the beta
+ * product still FP64-level). */
 typedef struct fgb_mapped_s *fgb_mapped_t;
 int fgb_mapped_create(fgb_mapped_t *out, fgb_b2_t b2, int power,
                       int normalized, const double *h_beta,
@@ -282,7 +284,7 @@ int fgb_mapped_predict(fgb_mapped_t m, int n_struc, const int *h_atom_offsets,
                        const int *d_species, double cutoff, int want,
                        double *d_energy, double *d_forces, double *d_stress,
                        double *d_atom_energy, double *d_local_var,
-                       void *stream);
+                       int precision, void *stream);
 
 /* ------------------------------------------------------------ autotuner
  * Tile shapes of the sliced tensor-core GEMMs (kernel, variance and force
