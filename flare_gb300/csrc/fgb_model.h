@@ -1,8 +1,8 @@
 // Device-resident sparse-GP model and its prediction workspace.
 #pragma once
-#include <vector>
-
+#include <functional>
 #include <memory>
+#include <vector>
 
 #include "fgb_internal.h"
 #include "fgb_ozaki.h"
@@ -15,7 +15,6 @@ struct fgb_workspace {
   fgb::DevBuf b2f, yf;           // mixed path: FP32 normalised rows, D^ B
   fgb::DevBuf dB2, fdots, fdot, dots, kern;  // plain (stored-gradient) form
   fgb::oz::Sliced ozA, ozK;      // tensor-core path: sliced rows per call
-  fgb::oz::Sliced ozA4;          // FP32-level slices of the rows (force GEMM)
   fgb::DevBuf ozerr;
 };
 
@@ -94,9 +93,14 @@ int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
                       double *d_gB2, double *d_var, cudaStream_t st);
 // Bounded tensor-core waits report into ws.ozerr, which the caller clears
 // before and reads after; `fixed`: prepare nothing (operands must be ready).
+// `after_chunk(s, Mr, perm)` runs after each row chunk's kernel and
+// variance GEMMs, with the chunk's rows still sliced in ws.ozA (the force
+// stage of the mixed path).
+using ChunkHook = std::function<int(int, int, const int *)>;
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
-                    cudaStream_t st, bool fixed = false);
+                    cudaStream_t st, bool fixed = false,
+                    const ChunkHook *after_chunk = nullptr);
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
                        double *d_gB2, double *d_var, cudaStream_t st,

@@ -58,6 +58,7 @@ int pad_to(int x, int m);
 int prepare(int rows, int K, int TR, int S, Sliced &out);
 // Slice rows into S = kS (FP64-level) or kSF32 (FP32-level) digits.
 int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S = kS);
+
 // FP64-level product of kS-slice operands; the tile shape follows B.TR
 // (one of kTNF64v).
 template <class Epi>
@@ -70,7 +71,8 @@ int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
                int *err, cudaStream_t st);
 // Y (A.rows x B.rows, leading dimension ldy) = A B^T rounded to FP32, from
 // kSF32-slice operands (A tiles of kTM rows, B tiles of 128 or 64 rows;
-// `ew` epilogue warps per lane quarter, 2 or 4 for 128-row tiles).
+// `ew` epilogue warps per lane quarter, 2 or 4 for 128-row tiles).  A may
+// be sliced with more digits (kS): its first kSF32 slices are used.
 int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,
              int *err, cudaStream_t st, int ew = 2);
 

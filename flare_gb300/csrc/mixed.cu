@@ -28,7 +28,6 @@ namespace fgb {
 namespace {
 using namespace gemm64;
 
-constexpr int kRowChunkMixed = 32768;
 
 // S^T (M x nd) -> ST (nd x M) scaled by alpha*valid (for B = S^T diag(a) S)
 __global__ void k_scaled_transpose(int M, int nd, const double *__restrict__ S,
@@ -196,18 +195,10 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool fixed) {
   const bool foldable = m->power == 2.0 || m->power == 1.0;
   int rc;
-  if (foldable) {
-    // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact
-    // integer slicing (ozaki.cu).
-    rc = kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st,
-                         fixed);
-  } else {
-    // powers other than 1 and 2: the FP64 kernel, adjoint and variance GEMMs
-    rc = kernel_stage_fp64(m, N, counts, want_grad && !foldable, want_var,
-                           d_e_atom, d_gB2, d_var, st);
-  }
-  if (rc || !want_grad || !foldable) return rc;
-  if (!m->bmap_ready) {
+  if (!foldable)   // powers other than 1 and 2: FP64 kernel, adjoint, variance
+    return kernel_stage_fp64(m, N, counts, want_grad, want_var, d_e_atom,
+                             d_gB2, d_var, st);
+  if (want_grad && !m->bmap_ready) {
     if (fixed) {
       set_error("mixed force stage: folded matrices not built before a fixed call");
       return FGB_EINVAL;
@@ -220,53 +211,49 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   const float sig2 = (float)(m->sigma * m->sigma);
   const size_t per = quad ? (size_t)nd * nd : (size_t)nd;
   if (quad && (rc = m->ws.ozerr.ensure(sizeof(int)))) return rc;
-  int base = 0;
-  for (int s = 0; s < p.n_species; s++) {
-    const int Ns = counts[s];
-    const int *perm_s = m->ws.perm.as<int>() + base;
-    base += Ns;
-    if (Ns == 0 || m->h_counts[s] == 0) continue;   // gB2 stays zero
-    const float *Bs = m->Bmap.as<float>() + per * s;
-    for (int r0 = 0; r0 < Ns; r0 += kRowChunkMixed) {
-      const int Mr = std::min(kRowChunkMixed, Ns - r0);
-      const int *perm = perm_s + r0;
-      if (quad && (rc = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
-        return rc;
-      StageTimer _pt(kStMappedGemm, st, quad ? 3 : 1);
-      if (quad) {
-        // Y = D^ B_s on the tensor cores (FP32-level exact slices)
-        if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
-                             m->ws.norms.as<double>()},
-                            m->ws.ozA4, st, oz::kSF32)))
-          return rc;
-        auto usable = [m](int v) { return m->ozB_ready[oz::f32_set(v)]; };
-        auto launch = [&](int v) -> int {
-          const int set = oz::f32_set(v);
-          int r;
-          if (!m->ozB_ready[set]) {
-            if (fixed) {
-              set_error("mixed force stage: tile variant not prepared");
-              return FGB_EINVAL;
-            }
-            if ((r = build_fold_slices(m, set, st))) return r;
+  // Forces of one row chunk, right after its kernel and variance GEMMs: the
+  // FP32-level operand is the first four of the rows' nine slices (their
+  // most significant digits, within half a unit of the 24-bit rounding),
+  // read in place from ws.ozA.
+  const ChunkHook forces = [&](int s, int Mr, const int *perm) -> int {
+    int r;
+    if (quad && (r = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
+      return r;
+    StageTimer _pt(kStMappedGemm, st, quad ? 2 : 1);
+    if (quad) {
+      // Y = D^ B_s on the tensor cores (FP32-level exact slices)
+      auto usable = [m](int v) { return m->ozB_ready[oz::f32_set(v)]; };
+      auto launch = [&](int v) -> int {
+        const int set = oz::f32_set(v);
+        int q;
+        if (!m->ozB_ready[set]) {
+          if (fixed) {
+            set_error("mixed force stage: tile variant not prepared");
+            return FGB_EINVAL;
           }
-          return oz::gemm_f32(m->ws.ozA4, *m->ozB[set][s],
-                              m->ws.yf.as<float>(), nd, m->ws.ozerr.as<int>(),
-                              st, oz::kEWF32v[v]);
-        };
-        int v = 0;
-        if ((rc = tune::run(tune::kOpForceGemm, Mr, nd, nd, oz::kF32Variants,
-                            launch, usable, st, fixed, &v)))
-          return rc;
-      }
-      k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
-          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
-          quad ? m->ws.yf.as<float>() : nullptr, quad ? nullptr : Bs,
-          quad ? 2.f * sig2 : sig2, d_gB2);
-      FGB_LAUNCH_CHECK("k_mapped_grad");
+          if ((q = build_fold_slices(m, set, st))) return q;
+        }
+        return oz::gemm_f32(m->ws.ozA, *m->ozB[set][s], m->ws.yf.as<float>(),
+                            nd, m->ws.ozerr.as<int>(), st, oz::kEWF32v[v]);
+      };
+      int v = 0;
+      if ((r = tune::run(tune::kOpForceGemm, Mr, nd, nd, oz::kF32Variants,
+                         launch, usable, st, fixed, &v)))
+        return r;
     }
-  }
-  return FGB_OK;
+    k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+        Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+        quad ? m->ws.yf.as<float>() : nullptr,
+        quad ? nullptr : m->Bmap.as<float>() + per * s,
+        quad ? 2.f * sig2 : sig2, d_gB2);
+    FGB_LAUNCH_CHECK("k_mapped_grad");
+    return FGB_OK;
+  };
+  // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact
+  // integer slicing (ozaki.cu); species with no sparse environments keep
+  // zero energy gradients.
+  return kernel_stage_oz(m, N, counts, false, want_var, d_e_atom, d_var, st,
+                         fixed, want_grad ? &forces : nullptr);
 }
 
 }  // namespace fgb

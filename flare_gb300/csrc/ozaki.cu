@@ -17,14 +17,14 @@
 //                    sparse GP (energy 4e-12 eV/atom, std 4e-13 against FP64)
 //   S = 4, TN = 128: FP32-level (2^-24); the alpha-folded force GEMM
 //
-// Data movement: slices are written by k_oz_slice directly in the tensor
+// Data movement: slices are written by k_oz_slice8 directly in the tensor
 // core's no-swizzle K-major canonical layout (8 x 16-byte core matrices),
 // tiled so that the S slices of every (row tile, 16-wide k chunk) are one
 // contiguous block.  One thread streams each chunk with two cp.async.bulk
-// copies into a shared-memory ring (mbarrier transaction counts), issues the
-// chunk's pair products as tcgen05.mma with the B slices stacked along N
-// (mma_kstep) and commits them to the stage's "consumed" mbarrier; every
-// wait is bounded and reports through `err`.
+// copies into a shared-memory ring (mbarrier transaction counts), another
+// issues the chunk's pair products as tcgen05.mma with the B slices stacked
+// along N (mma_kstep) and commits them to the stage's "consumed" mbarrier;
+// every wait is bounded and reports through `err`.
 #include <cuda_bf16.h>
 
 #include "fgb_internal.h"
@@ -248,78 +248,97 @@ __device__ __forceinline__ uint32_t bf16_bits(long long q) {
 }
 
 // The S base-64 digits of X (|X| < 2^(6S)) for 8 consecutive k, stored as
-// 16-byte rows of the canonical layout: slice a at out + a * stride.
+// 16-byte rows of the canonical layout: slice a at out + a * stride.  The
+// digits are balanced: U = X + sum_{a >= 2} 32 2^(6(S-a)) has plain base-64
+// digits u_2..u_S below its top one, d_a = u_a - 32 in [-32, 31] and d_1 =
+// U >> 6(S-1) in [-64, 64]; X = sum_a d_a 2^(6(S-a)) exactly.  A digit is a
+// bit-field extract, and its BF16 bits come from one FP32 subtraction.
 template <int S>
 __device__ __forceinline__ void store_digits8(long long (&X)[8],
                                               __nv_bfloat16 *out,
                                               size_t stride) {
+  constexpr long long kBias = [] {
+    long long b = 0;
+    for (int a = 2; a <= S; a++) b += 32LL << (kBeta * (S - a));
+    return b;
+  }();
+  long long U[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) U[j] = X[j] + kBias;
 #pragma unroll
   for (int a = 1; a <= S; a++) {
     const int sh = kBeta * (S - a);
     uint32_t w[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
-      long long q0 = sh > 0 ? (X[j] + (1LL << (sh - 1))) >> sh : X[j];
-      long long q1 = sh > 0 ? (X[j + 1] + (1LL << (sh - 1))) >> sh : X[j + 1];
-      X[j] -= q0 << sh;
-      X[j + 1] -= q1 << sh;
-      w[j / 2] = bf16_bits(q0) | (bf16_bits(q1) << 16);
+      int d[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++)
+        d[h] = a == 1 ? (int)(U[j + h] >> sh)
+                      : (int)((unsigned)(U[j + h] >> sh) & 63u) - 32;
+      w[j / 2] = bf16_bits(d[0]) | (bf16_bits(d[1]) << 16);
     }
     *reinterpret_cast<uint4 *>(out + (size_t)(a - 1) * stride) =
         make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
-// Warp per row: scale to (-1, 1) by a power of two, split into S slices.
-// The scaled value y is taken as the integer X = rn(y 2^(6S)) (exact for
-// |y| >= 2^-1 of the row's top binade, rounded at 2^(-6S) below that); the
-// slices are the base-64 digits of X, each rounded to nearest, extracted
-// with 64-bit integer arithmetic: q_a = round(R / 2^(6(S-a))),
-// R -= q_a 2^(6(S-a)).  Each lane converts 8 consecutive k and writes one
-// 16-byte core-matrix row per slice.
+// Row slicing: scale each row to (-1, 1) by a power of two 2^e (e from the
+// row's largest magnitude), take the scaled value y as the integer
+// X = rn(y 2^(6S)) (exact for |y| >= 2^-1 of the row's top binade, rounded
+// at 2^(-6S) below that) and store its S balanced base-64 digits
+// (store_digits8).  A warp takes 8 rows (one core-matrix row group) and 32
+// consecutive k at a time, lane = row + 8 x (k group of 8), so that the
+// 16-byte row pieces a store instruction writes for one slice are two
+// contiguous 256-byte blocks (one 16-k chunk each) rather than 32 scattered
+// pieces.  Row maxima: a first pass over the row, reduced over the 4 lanes
+// of each row.
 template <int S>
-__global__ void k_oz_slice(int R, int K, int RP, int KP, int TR,
-                           const double *__restrict__ src, long long ld,
-                           const int *__restrict__ perm,
-                           const double *__restrict__ rownorm, double thresh,
-                           __nv_bfloat16 *__restrict__ out,
-                           double *__restrict__ scale) {
-  const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+__global__ void __launch_bounds__(256)
+k_oz_slice8(int R, int K, int RP, int KP, int TR,
+            const double *__restrict__ src, long long ld,
+            const int *__restrict__ perm, const double *__restrict__ rownorm,
+            double thresh, __nv_bfloat16 *__restrict__ out,
+            double *__restrict__ scale) {
+  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (m >= RP) return;
+  const int m0 = warp * 8;
+  if (m0 >= RP) return;
+  const int r = lane & 7, g = lane >> 3;
+  const int m = m0 + r;
   bool valid = m < R;
   long long row = 0;
   double inv = 1.0;
   if (valid) {
     row = perm ? (long long)perm[m] : (long long)m;
     if (rownorm) {
-      double n = rownorm[row];
+      const double n = rownorm[row];
       if (n >= thresh) inv = 1.0 / n;
       else valid = false;
     }
   }
-  // row max of |src| on the bit patterns (non-negative doubles order as
-  // integers)
+  const double *sr = src + row * ld;
   unsigned long long mb = 0;
   if (valid)
-    for (int k = lane; k < K; k += 32)
-      mb = max(mb, (unsigned long long)__double_as_longlong(src[row * ld + k]) &
-                       0x7FFFFFFFFFFFFFFFULL);
+    for (int k0 = g * 8; k0 < K; k0 += 32)
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1)
-    mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, off));
+      for (int j = 0; j < 8; j++)
+        if (k0 + j < K)
+          mb = max(mb, (unsigned long long)__double_as_longlong(sr[k0 + j]) &
+                           0x7FFFFFFFFFFFFFFFULL);
+  mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, 8));
+  mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, 16));
   const double mx = __longlong_as_double((long long)mb) * inv;
   const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
-  if (lane == 0) scale[m] = ldexp(1.0, e);
+  if (g == 0) scale[m] = ldexp(1.0, e);
   const size_t stride = (size_t)TR * kKC;
-  for (int k0 = lane * 8; k0 < KP; k0 += 256) {
+  for (int k0 = g * 8; k0 < KP; k0 += 32) {
     long long X[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int k = k0 + j;
       X[j] = (valid && k < K)
-                 ? fixed_rn(rownorm ? src[row * ld + k] * inv : src[row * ld + k],
-                            kBeta * S - e)
+                 ? fixed_rn(rownorm ? sr[k] * inv : sr[k], kBeta * S - e)
                  : 0;
     }
     store_digits8<S>(X, out + tiled_index<S>(m, k0, KP, TR), stride);
@@ -380,7 +399,7 @@ __device__ __forceinline__ int wait_or_abort(uint64_t *bar, uint32_t phase,
 template <class C, class Epi>
 __global__ void __launch_bounds__(C::THREADS, 1)
 k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
-          const __nv_bfloat16 *__restrict__ Asl,
+          int SA, const __nv_bfloat16 *__restrict__ Asl,
           const double *__restrict__ Ascale,
           const __nv_bfloat16 *__restrict__ Bsl,
           const double *__restrict__ Bscale, int tri, Epi epi,
@@ -446,7 +465,9 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
         int mt, nt;
         tile_rc(t, mt, nt);
         const int nch = tile_nch(nt);
-        const __nv_bfloat16 *a = Asl + (size_t)mt * KCH * (S * kTM * kKC);
+        // A blocks hold SA >= S slices per chunk; the first S (the most
+        // significant digits) are this product's operand
+        const __nv_bfloat16 *a = Asl + (size_t)mt * KCH * (SA * kTM * kKC);
         const __nv_bfloat16 *bsrc = Bsl + (size_t)nt * KCH * (S * TN * kKC);
         for (int c = 0; c < nch; c++, g++) {
           const int b = (int)(g % NST);
@@ -459,7 +480,7 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
           }
           unsigned char *st = smem + b * C::Stage;
           tc::mbar_expect_tx(&bar_load[b], C::Stage);
-          tc::bulk_g2s(st, a + (size_t)c * (S * kTM * kKC), S * C::TileA,
+          tc::bulk_g2s(st, a + (size_t)c * (SA * kTM * kKC), S * C::TileA,
                        &bar_load[b]);
           tc::bulk_g2s(st + S * C::TileA, bsrc + (size_t)c * (S * TN * kKC),
                        S * C::TileB, &bar_load[b]);
@@ -672,12 +693,12 @@ template <int S>
 static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   int rc;
   if ((rc = prepare(sp.rows, sp.K, sp.TR, S, out))) return rc;
-  const long long threads = (long long)out.RP * 32;
-  k_oz_slice<S><<<ceil_div(threads, 256), 256, 0, st>>>(
+  const long long threads = (long long)(out.RP / 8) * 32;   // RP % 8 == 0
+  k_oz_slice8<S><<<ceil_div(threads, 256), 256, 0, st>>>(
       sp.rows, sp.K, out.RP, out.KP, sp.TR, sp.src, sp.ld, sp.perm,
       sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
       out.scale.as<double>());
-  FGB_LAUNCH_CHECK("k_oz_slice");
+  FGB_LAUNCH_CHECK("k_oz_slice8");
   return FGB_OK;
 }
 
@@ -688,11 +709,13 @@ int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S) {
   return FGB_EINVAL;
 }
 
+
 template <class C, class Epi>
 static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
                   int *err, cudaStream_t st) {
+  // A may carry more (less significant) slices than the product uses
   if (A.K != B.K || A.KP != B.KP || A.TR != kTM || B.TR != C::TN ||
-      A.S != C::S || B.S != C::S) {
+      A.S < C::S || B.S != C::S) {
     set_error("ozaki gemm: operand layouts disagree");
     return FGB_EINVAL;
   }
@@ -706,7 +729,7 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
   const int MT = A.RP / kTM, NTt = B.RP / C::TN;
   const int grid = std::max(1, std::min(MT * NTt, sms));
   k_oz_gemm<C, Epi><<<grid, C::THREADS, C::Smem, st>>>(
-      A.rows, B.rows, A.K, A.KP, MT, NTt, make_fastdiv(NTt),
+      A.rows, B.rows, A.K, A.KP, MT, NTt, make_fastdiv(NTt), A.S,
       A.q.as<__nv_bfloat16>(),
       A.scale.as<double>(), B.q.as<__nv_bfloat16>(), B.scale.as<double>(),
       tri ? 1 : 0, epi, err);
@@ -941,7 +964,7 @@ static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
 
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
-                    cudaStream_t st, bool fixed) {
+                    cudaStream_t st, bool fixed, const ChunkHook *after_chunk) {
   int rc;
   if (want_w) {
     set_error("tensor-core kernel stage: adjoint weights are not produced");
@@ -1055,6 +1078,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                         m->power, d_var, st)))
           return rc;
       }
+      if (after_chunk && (rc = (*after_chunk)(s, Mr, perm))) return rc;
     }
   }
   return FGB_OK;
