@@ -94,6 +94,10 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   T *sy = sg + kChunk * nm;
   int *ssp = (int *)(sy + kChunk * nh);
   T *red = (T *)(ssp + kChunk);
+  int *sord = (int *)(red + kChunk);      // chunk pairs, sorted by species
+  int *scnt = sord + kChunk;              // [warp][species] counts
+  int *sbeg = scnt + 2 * kMaxSpecies;     // species starts in sord
+  constexpr bool kFixed = NC > 0 && LC > 0;
   const int t = threadIdx.x;
   const int si = species[i];
   for (int e = t; e < nA; e += blockDim.x) A[e] = T(0);
@@ -115,15 +119,58 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     }
     ssp[t] = sj;
     __syncthreads();
-    const int cnt = (int)min((long long)kChunk, e_ - c0);
-    for (int e = t; e < nA; e += blockDim.x) {
-      int s = e / (nm * nh);
-      int n = (e / nh) % nm;
-      int lm = e % nh;
-      T acc = T(0);
-      for (int q = 0; q < cnt; q++)
-        if (ssp[q] == s) mac(acc, sg[q * nm + n], sy[q * nh + lm]);
-      A[e] += finish(acc);
+    if constexpr (kFixed) {
+      // The chunk's pairs grouped by neighbour species (pair order kept in
+      // each group): a thread per (species, lm) then sums only its species'
+      // pairs, with the n_max accumulators in registers and each Y value
+      // loaded once.  The sums run over the same pairs in the same order as
+      // entry-by-entry accumulation, so A is the same to the bit.
+      constexpr int NH = (LC + 1) * (LC + 1);
+      const int S = p.n_species, warp = t >> 5, lane = t & 31;
+      int rank = 0;
+      for (int s = 0; s < S; s++) {
+        const unsigned b = __ballot_sync(0xffffffffu, sj == s);
+        if (lane == 0) scnt[warp * kMaxSpecies + s] = __popc(b);
+        if (sj == s) rank = __popc(b & ((1u << lane) - 1u));
+      }
+      __syncthreads();
+      if (t == 0) {
+        int acc = 0;
+        for (int s = 0; s < S; s++) {
+          sbeg[s] = acc;
+          acc += scnt[s] + scnt[kMaxSpecies + s];
+        }
+        sbeg[S] = acc;
+      }
+      __syncthreads();
+      if (sj >= 0)
+        sord[sbeg[sj] + (warp ? scnt[sj] : 0) + rank] = t;
+      __syncthreads();
+      for (int it = t; it < S * NH; it += blockDim.x) {
+        const int s = it / NH, lm = it % NH;
+        T acc[NC];
+#pragma unroll
+        for (int n = 0; n < NC; n++) acc[n] = T(0);
+        for (int q = sbeg[s]; q < sbeg[s + 1]; q++) {
+          const int pq = sord[q];
+          const T y = sy[pq * NH + lm];
+#pragma unroll
+          for (int n = 0; n < NC; n++) mac(acc[n], sg[pq * NC + n], y);
+        }
+#pragma unroll
+        for (int n = 0; n < NC; n++) A[(s * NC + n) * NH + lm] += finish(acc[n]);
+      }
+    } else {
+      const int cnt = (int)min((long long)kChunk, e_ - c0);
+      for (int e = t; e < nA; e += blockDim.x) {
+        int s = e / (nm * nh);
+        int n = (e / nh) % nm;
+        int lm = e % nh;
+        T acc = T(0);
+        for (int q = 0; q < cnt; q++)
+          if (ssp[q] == s) mac(acc, sg[q * nm + n], sy[q * nh + lm]);
+        A[e] += finish(acc);
+      }
     }
     __syncthreads();
   }
@@ -133,15 +180,45 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   const int L1 = (LC > 0 ? LC : p.l_max) + 1, nr = p.n_species * nm,
             nd = p.n_d;
   T nrm = T(0);
-  for (int q = t; q < nd; q += blockDim.x) {
-    int n1, n2, l;
-    decode_b2(q, L1, nr, n1, n2, l);
-    const T *a1 = A + n1 * nh + l * l, *a2 = A + n2 * nh + l * l;
-    T v = T(0);
-    for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[m], a2[m]);
-    v = finish(v);
-    B2[(long long)i * nd + q] = to_double(v);
-    mac(nrm, v, v);
+  if constexpr (kFixed) {
+    // A thread per radial pair (n1 <= n2) computes its L+1 values (no index
+    // decoding per value); the row is staged in the basis-value buffers and
+    // written with coalesced stores when it fits there.
+    constexpr int L1c = LC + 1, NH = (LC + 1) * (LC + 1);
+    const bool stage = nd <= kChunk * (nm + nh);
+    T *out_s = sg;
+    const int npair = nr * (nr + 1) / 2;
+    for (int pi = t; pi < npair; pi += blockDim.x) {
+      int n1 = 0, rem = pi;
+      while (rem >= nr - n1) { rem -= nr - n1; n1++; }
+      const T *a1 = A + n1 * NH, *a2 = A + (n1 + rem) * NH;
+#pragma unroll
+      for (int l = 0; l < L1c; l++) {
+        T v = T(0);
+#pragma unroll
+        for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[l * l + m], a2[l * l + m]);
+        v = finish(v);
+        if (stage) out_s[pi * L1c + l] = v;
+        else B2[(long long)i * nd + pi * L1c + l] = to_double(v);
+        mac(nrm, v, v);
+      }
+    }
+    if (stage) {
+      __syncthreads();
+      for (int q = t; q < nd; q += blockDim.x)
+        B2[(long long)i * nd + q] = to_double(out_s[q]);
+    }
+  } else {
+    for (int q = t; q < nd; q += blockDim.x) {
+      int n1, n2, l;
+      decode_b2(q, L1, nr, n1, n2, l);
+      const T *a1 = A + n1 * nh + l * l, *a2 = A + n2 * nh + l * l;
+      T v = T(0);
+      for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[m], a2[m]);
+      v = finish(v);
+      B2[(long long)i * nd + q] = to_double(v);
+      mac(nrm, v, v);
+    }
   }
   nrm = block_sum(finish(nrm), red);
   if (t == 0) norms[i] = to_double(sqrt(nrm));
@@ -316,8 +393,11 @@ __global__ void k_struct_reduce(int n_struc, const int *__restrict__ atom_off,
 }  // namespace
 
 size_t b2_forward_smem(const B2Params &p) {
+  // A | g | Y | pair species | reduction | species-sorted pair order and
+  // per-warp species counts (2 x kMaxSpecies) and starts (kMaxSpecies + 1)
   return sizeof(double) * (p.n_A + (size_t)kChunk * (p.n_max + p.n_harm)) +
-         sizeof(int) * kChunk + sizeof(double) * kChunk;
+         sizeof(int) * kChunk + sizeof(double) * kChunk +
+         sizeof(int) * (kChunk + 3 * kMaxSpecies + 1);
 }
 
 size_t b2_adjoint_smem(const B2Params &p) {
