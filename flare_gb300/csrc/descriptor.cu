@@ -240,9 +240,15 @@ __device__ __forceinline__ double3 pair_out(float x, float y, float z) {
   return make_double3(f2d_exact(x), f2d_exact(y), f2d_exact(z));
 }
 
-// Shared memory: u[nA] | A[nA] | w[nd] (the atom's dE/dB2 row, when it fits)
+// Atoms per block of the adjoint and its block size: ~42 pairs per atom,
+// so three atoms' pairs fill the 128 threads of the pair loop.
+constexpr int kAdjAtoms = 3;
+constexpr int kAdjThreads = 128;
+
+// Shared memory, per atom of the block: u[nA] | A[nA] | w[nd] (the atom's
+// dE/dB2 row, when it fits).
 template <typename T, int NC, int LC>
-__global__ void __launch_bounds__(kChunk, sizeof(T) == 4 ? 8 : 4)
+__global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 4 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
@@ -250,41 +256,55 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              int w_in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
-  const int i = blockIdx.x;
-  if (i >= n_atoms) return;
+  const int i0 = blockIdx.x * kAdjAtoms;
+  if (i0 >= n_atoms) return;
+  const int na = min(kAdjAtoms, n_atoms - i0);
   constexpr int NA = NC > 0 ? NC : kMaxNmax;
   const int nh = LC > 0 ? (LC + 1) * (LC + 1) : p.n_harm;
   const int nm = NC > 0 ? NC : p.n_max;
   const int nA = p.n_species * nm * nh, nr = p.n_species * nm,
             L1 = (LC > 0 ? LC : p.l_max) + 1, nd = p.n_d;
-  T *u = smem;
-  T *A = u + nA;
-  T *W = w_in_smem ? A + nA : nullptr;
+  const int per = 2 * nA + (w_in_smem ? nd : 0);   // T values per atom
   const int t = threadIdx.x;
-  const double *w = gB2 + (long long)i * nd;
-  for (int e = t; e < nA; e += blockDim.x)
-    A[e] = as_compute(A_in[(long long)i * nA + e], T(0));
-  if (W)
-    for (int q = t; q < nd; q += blockDim.x) W[q] = as_compute(w[q], T(0));
+  for (int a = 0; a < na; a++) {
+    T *A = smem + (size_t)a * per + nA;
+    T *W = w_in_smem ? A + nA : nullptr;
+    const long long i = i0 + a;
+    for (int e = t; e < nA; e += blockDim.x)
+      A[e] = as_compute(A_in[i * nA + e], T(0));
+    if (W)
+      for (int q = t; q < nd; q += blockDim.x)
+        W[q] = as_compute(gB2[i * nd + q], T(0));
+  }
   __syncthreads();
-  for (int e = t; e < nA; e += blockDim.x) {
-    int c = e / nh, lm = e % nh;
+  // u = dE/dA: u[c][lm] = sum_b (1 + [b == c]) w((c,b), l) A[b][lm], a
+  // thread per (atom, entry)
+  for (int it = t; it < na * nA; it += blockDim.x) {
+    const int a = it / nA, e = it % nA;
+    const T *A = smem + (size_t)a * per + nA;
+    T *u = smem + (size_t)a * per;
+    const T *W = w_in_smem ? A + nA : nullptr;
+    const double *w = gB2 + (long long)(i0 + a) * nd;
+    const int c = e / nh, lm = e % nh;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
     T acc = T(0);
     for (int bb = 0; bb < nr; bb++) {
-      int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
+      const int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
       const int wi = pair_index(lo, hi, nr) * L1 + l;
-      T wv = W ? W[wi] : as_compute(w[wi], T(0));
-      T f = (bb == c) ? T(2) : T(1);
+      const T wv = W ? W[wi] : as_compute(w[wi], T(0));
+      const T f = (bb == c) ? T(2) : T(1);
       acc += f * wv * A[bb * nh + lm];
     }
     u[e] = acc;
   }
   __syncthreads();
-  const int si = species[i];
-  const long long b = offsets[i], e_ = offsets[i + 1];
-  for (long long pp = b + t; pp < e_; pp += blockDim.x) {
+  const long long pbeg = offsets[i0], pend = offsets[i0 + na];
+  for (long long pp = pbeg + t; pp < pend; pp += blockDim.x) {
+    int a = 0;
+    while (a + 1 < na && pp >= offsets[i0 + a + 1]) a++;
+    const T *u = smem + (size_t)a * per;
+    const int si = species[i0 + a];
     int j = nbr_j[pp];
     double4_16a r = rel[pp];
     int sj = species[j];
@@ -457,13 +477,14 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       cudaStream_t st, bool fp32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
-  size_t sm = fp32 ? b2_adjoint_smem(p) / 2 : b2_adjoint_smem(p);
+  // per atom of a block: u and A, and the atom's dE/dB2 row when it fits
+  size_t sm = (fp32 ? b2_adjoint_smem(p) / 2 : b2_adjoint_smem(p)) * kAdjAtoms;
   if (sm > 200 * 1024) {
     set_error("B2 adjoint needs %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  // the atom's dE/dB2 row in shared memory too, when it fits
-  const size_t wbytes = (fp32 ? sizeof(float) : sizeof(double)) * (size_t)p.n_d;
+  const size_t wbytes =
+      (fp32 ? sizeof(float) : sizeof(double)) * (size_t)p.n_d * kAdjAtoms;
   const int w_in_smem = sm + wbytes <= 96 * 1024 ? 1 : 0;
   if (w_in_smem) sm += wbytes;
   cudaError_t e = cudaSuccess;
@@ -472,9 +493,10 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
     if (e != cudaSuccess) return;
-    fn<<<N, kChunk, sm, st>>>(p, N, nl->offsets.as<long long>(),
-                              nl->nbr_j.as<int>(), nl->nbr_rel.as<double4_16a>(),
-                              d_species, d_A, d_gB2, d_pair_grad, w_in_smem);
+    fn<<<ceil_div(N, kAdjAtoms), kAdjThreads, sm, st>>>(
+        p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad,
+        w_in_smem);
   };
   if (fp32) dispatch_nl<AdjK, float>(p, go);
   else dispatch_nl<AdjK, double>(p, go);
