@@ -246,9 +246,12 @@ constexpr int kAdjAtoms = 3;
 constexpr int kAdjThreads = 128;
 
 // Shared memory, per atom of the block: u[nA] | A[nA] | w[nd] (the atom's
-// dE/dB2 row, when it fits).
+// dE/dB2 row, when it fits).  The pair loop is latency-bound (recurrence
+// chains): the FP32 kernel is held to 64 registers for 8 blocks (32 warps)
+// per SM, which measured 0.36 ms against 0.51 ms at 4 blocks (128
+// registers) on the alloy workload, despite a few spilled values.
 template <typename T, int NC, int LC>
-__global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 8 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
