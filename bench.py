@@ -425,6 +425,15 @@ def run_ours(args, rank, world, local):
                                    "file)",
                     "flop_per_launch": alg, "avg_launch_ms": avg_ms}
     gpu_launches = int(sum(v[1] for v in stage.values()))
+    guard = None
+    if args.precision == "mixed" and c["power"] in (1, 2):
+        import ctypes
+        fmax, f64 = ctypes.c_double(0.0), ctypes.c_int(0)
+        _lib.check(L.fgb_model_fold_guard(model.h, ctypes.byref(fmax),
+                                          ctypes.byref(f64), sptr))
+        guard = {"fold_max": fmax.value,
+                 "force_stage": "fp64-level" if f64.value else "fp32-level",
+                 "threshold": 200.0}
 
     result = {
         "metric": METRIC, "value": value, "unit": "atoms/s",
@@ -449,6 +458,7 @@ def run_ours(args, rank, world, local):
                                for k_, v in stage.items() if v[1]},
         "gpu_launches": gpu_launches,
         "errors_vs_fp64": errors,
+        "fold_guard": guard,
         "clocks": clocks.summary(local),
         "autotune": autotune_table(),
     }

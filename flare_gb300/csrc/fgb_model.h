@@ -47,6 +47,11 @@ struct fgb_model_s {
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB[fgb::oz::kF32Sets];
   bool ozB_ready[fgb::oz::kF32Sets] = {};
   bool bmap_ready = false;
+  // largest folded coefficient sigma^2 |B_s| and the guard it sets: forces
+  // at FP64 level (product, gradient, adjoint) when it is large
+  double fold_max = 0.0;
+  bool force_f64 = false;
+  std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB64;   // FP64-level B_s rows
   // mixed path: sliced sparse set and L_inv panels per species (tensor
   // cores), one set per B tile width of the autotuner's candidates
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS[fgb::oz::kF64Variants],
@@ -59,6 +64,10 @@ struct fgb_model_s {
 };
 
 namespace fgb {
+// Above this largest folded coefficient the mixed path's force stage runs
+// at FP64 level (the FP32-level stage errs by ~2.5e-7 eV/A per unit).
+constexpr double kFoldMaxF32 = 200.0;
+
 // A prediction repeated on the atoms, species and cells of the model's last
 // full call at new positions (a molecular-dynamics step).  The geometry, the
 // species permutation and the workspace of that call are reused, the

@@ -15,6 +15,8 @@
 // Y = B2 beta_s (and B2 Q_s) run on the tensor cores by exact slicing (FP64
 // level); forces and stresses come from dE/dB2 through the reverse-mode B2
 // adjoint, as in the prediction pipeline.
+#include <algorithm>
+#include <cmath>
 #include <memory>
 #include <vector>
 
@@ -132,6 +134,9 @@ struct fgb_mapped_s {
   int power = 2;
   bool normalized = true;
   bool has_var = false;
+  // mixed precision: FP32 adjoint unless the largest |beta| exceeds the
+  // fold guard's threshold (then the adjoint stays FP64)
+  bool adjoint_f64 = false;
   DevBuf beta;                                        // FP64, per species
   std::vector<std::unique_ptr<oz::Sliced>> ozBeta;    // power 2: beta_s rows
   std::vector<std::unique_ptr<oz::Sliced>> ozQ;       // variance map: Q_s^T rows
@@ -174,6 +179,9 @@ extern "C" int fgb_mapped_create(fgb_mapped_t *out, fgb_b2_t b2, int power,
       return FGB_EINVAL;
     }
   auto *m = new fgb_mapped_s();
+  double bmax = 0.0;
+  for (size_t i = 0; i < per * S; i++) bmax = std::max(bmax, std::fabs(h_beta[i]));
+  m->adjoint_f64 = bmax > kFoldMaxF32;
   m->b2 = b2->p;
   m->power = power;
   m->normalized = normalized != 0;
@@ -335,7 +343,7 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   if (want_grad) {
     if ((rc = launch_b2_adjoint(p, &m->nl, d_species, ws.A.as<double>(),
                                 ws.gB2.as<double>(), ws.pair_grad.as<double3>(),
-                                st, mixed)) ||
+                                st, mixed && !m->adjoint_f64)) ||
         (rc = launch_forces(&m->nl, ws.pair_grad.as<double3>(),
                             ws.forces.as<double>(), ws.virial.as<double>(),
                             st)))

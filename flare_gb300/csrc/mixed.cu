@@ -15,6 +15,8 @@
 // dE/dB2 = (dE/dd^ - (d^ . dE/dd^) d^) / |d| in FP32; the per-pair adjoint
 // then runs in FP32.  Other powers use the FP64 kernel, adjoint and variance
 // GEMMs.
+#include <cstring>
+
 #include "fgb_df.cuh"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
@@ -123,6 +125,47 @@ __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
   }
 }
 
+// The same in FP64, for the guarded path (large folded coefficients):
+// Y = D^ B_s from the FP64-level product, or the FP64 fold vector.
+__global__ void k_mapped_grad64(int Mr, int nd, const int *__restrict__ perm,
+                                const double *__restrict__ norms,
+                                const double *__restrict__ B2,
+                                const double *__restrict__ Y,
+                                const double *__restrict__ beta, double scale,
+                                double *__restrict__ gB2) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= Mr) return;
+  const int atom = perm[warp];
+  const double n = norms[atom];
+  const bool ok = n >= kEmptyThresh;
+  const double inv = ok ? 1.0 / n : 0.0;
+  const double *b = B2 + (long long)atom * nd;
+  const double *y = Y ? Y + (long long)warp * nd : nullptr;
+  double q = 0.0;
+  for (int k = lane; k < nd; k += 32) q += (b[k] * inv) * (y ? y[k] : beta[k]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+  for (int k = lane; k < nd; k += 32) {
+    const double g = scale * (y ? y[k] : beta[k]);
+    gB2[(long long)atom * nd + k] = (g - scale * q * (b[k] * inv)) * inv;
+  }
+}
+
+// Largest |x| over n doubles into *out (bits of non-negative doubles order
+// as integers; *out zeroed by the caller).
+__global__ void k_max_abs(long long n, const double *__restrict__ x,
+                          unsigned long long *__restrict__ out) {
+  unsigned long long mb = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    mb = max(mb, (unsigned long long)__double_as_longlong(x[i]) &
+                     0x7FFFFFFFFFFFFFFFULL);
+  for (int off = 16; off > 0; off >>= 1)
+    mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, mb);
+}
+
 }  // namespace
 
 // FP32-level slices of the folded matrices for B tiles of set `set`.
@@ -152,10 +195,8 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
   int rc;
   if ((rc = m->Bmap.ensure(sizeof(float) * (per * S + 1)))) return rc;
   FGB_CUDA(cudaMemsetAsync(m->Bmap.p, 0, sizeof(float) * per * S, st));
-  if (quad) {
-    if ((rc = m->Bfold.ensure(sizeof(double) * (per * S + 1)))) return rc;
-    FGB_CUDA(cudaMemsetAsync(m->Bfold.p, 0, sizeof(double) * per * S, st));
-  }
+  if ((rc = m->Bfold.ensure(sizeof(double) * (per * S + 1)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(m->Bfold.p, 0, sizeof(double) * per * S, st));
   DevBuf ST, STa;
   for (bool &r : m->ozB_ready) r = false;
   for (int s = 0; s < S; s++) {
@@ -181,9 +222,46 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
           Ms, nd, Ss, m->alpha.as<double>() + c,
           m->svalid.as<unsigned char>() + c, Bs);
       FGB_LAUNCH_CHECK("k_fold_vec");
+      k_fold_vec64<<<ceil_div(nd, 128), 128, 0, st>>>(
+          Ms, nd, Ss, m->alpha.as<double>() + c,
+          m->svalid.as<unsigned char>() + c,
+          m->Bfold.as<double>() + per * s);
+      FGB_LAUNCH_CHECK("k_fold_vec64");
     }
   }
-  if (quad && (rc = build_fold_slices(m, 0, st))) return rc;
+  // Guard: the FP32-level force stage errs by about 2.5e-7 eV/A per unit
+  // of the largest folded coefficient sigma^2 |sum alpha s^ s^T| (measured
+  // over models with coefficients from 7.5 to 9e6); above kFoldMaxF32 the
+  // force product, the gradient and the adjoint run at FP64 level instead.
+  DevBuf mx;
+  if ((rc = mx.ensure(sizeof(unsigned long long)))) return rc;
+  FGB_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), st));
+  k_max_abs<<<256, 256, 0, st>>>((long long)per * S, m->Bfold.as<double>(),
+                                 mx.as<unsigned long long>());
+  FGB_LAUNCH_CHECK("k_max_abs");
+  unsigned long long hb = 0;
+  FGB_CUDA(cudaMemcpyAsync(&hb, mx.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  double bmax;
+  std::memcpy(&bmax, &hb, sizeof(bmax));
+  m->fold_max = bmax * m->sigma * m->sigma;
+  m->force_f64 = m->fold_max > kFoldMaxF32;
+  if (quad) {
+    if (m->force_f64) {
+      // B_s rows in FP64-level slices (B tiles of kTN rows)
+      m->ozB64.clear();
+      for (int s = 0; s < S; s++) {
+        m->ozB64.emplace_back(new oz::Sliced());
+        if (m->h_counts[s] == 0) continue;
+        if ((rc = oz::slice({nd, nd, oz::kTN, m->Bfold.as<double>() + per * s,
+                             nd, nullptr, nullptr},
+                            *m->ozB64[s], st)))
+          return rc;
+      }
+    } else if ((rc = build_fold_slices(m, 0, st))) {
+      return rc;
+    }
+  }
   FGB_CUDA(cudaStreamSynchronize(st));
   m->bmap_ready = true;
   return FGB_OK;
@@ -217,6 +295,23 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
   // read in place from ws.ozA.
   const ChunkHook forces = [&](int s, int Mr, const int *perm) -> int {
     int r;
+    if (m->force_f64) {
+      // large folded coefficients: FP64-level product and FP64 gradient
+      if (quad && (r = m->ws.kmat.ensure(sizeof(double) * (size_t)Mr * nd)))
+        return r;
+      StageTimer _pt(kStMappedGemm, st, quad ? 2 : 1);
+      if (quad && (r = oz::gemm_store(m->ws.ozA, *m->ozB64[s],
+                                      m->ws.kmat.as<double>(), nd,
+                                      m->ws.ozerr.as<int>(), st)))
+        return r;
+      k_mapped_grad64<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+          quad ? m->ws.kmat.as<double>() : nullptr,
+          quad ? nullptr : m->Bfold.as<double>() + per * s,
+          quad ? 2.0 * m->sigma * m->sigma : m->sigma * m->sigma, d_gB2);
+      FGB_LAUNCH_CHECK("k_mapped_grad64");
+      return FGB_OK;
+    }
     if (quad && (r = m->ws.yf.ensure(sizeof(float) * (size_t)Mr * nd)))
       return r;
     StageTimer _pt(kStMappedGemm, st, quad ? 2 : 1);
@@ -266,6 +361,24 @@ using namespace fgb;
 //   power 1: sigma^2 sum_t alpha_t s^_t          (n_d)
 // over the valid sparse environments of the species (s^ = s / |s|), in
 // FP64 on the device.
+extern "C" int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
+                                    int *h_fp64_forces, void *stream) {
+  if (!m || (m->power != 1.0 && m->power != 2.0)) {
+    set_error("fgb_model_fold_guard: invalid arguments (power 1 or 2 models)");
+    return FGB_EINVAL;
+  }
+  if (!m->solved) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  int rc;
+  if (!m->bmap_ready && (rc = build_fold(m, (cudaStream_t)stream))) return rc;
+  if (h_fold_max) *h_fold_max = m->fold_max;
+  if (h_fp64_forces) *h_fp64_forces = m->force_f64 ? 1 : 0;
+  return FGB_OK;
+}
+
 extern "C" int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream) {
   if (!m || !h_beta || (m->power != 1.0 && m->power != 2.0)) {
     set_error("fgb_model_mapping: invalid arguments (power 1 or 2 models)");

@@ -468,6 +468,8 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   }
   m->solved = false;
   m->bmap_ready = false;
+  m->force_f64 = false;
+  m->fold_max = 0.0;
   for (bool &r : m->oz_ready) r = false;
   for (bool &r : m->ozB_ready) r = false;
   if (!h_alpha || !h_L_inv) return FGB_OK;
@@ -630,10 +632,12 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (want_grad) {
     {
       StageTimer _pt(kStB2Adjoint, st);
+      // FP32 adjoint in the mixed path, unless the fold guard asked for
+      // FP64-level forces
       if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
                                   m->ws.gB2.as<double>(),
                                   m->ws.pair_grad.as<double3>(), st,
-                                  precision == FGB_PREC_MIXED)))
+                                  precision == FGB_PREC_MIXED && !m->force_f64)))
         return rc;
     }
     {

@@ -108,6 +108,20 @@ def mapping_coefficients(sgp, kernel_index=0):
     return np.stack([full[s][iu] * factor for s in range(S)])
 
 
+def fold_guard(sgp):
+    """The mixed path's force-precision guard: (largest |sigma^2 sum alpha
+    s^ s^T| entry, True when the force stage runs at FP64 level).  The
+    FP32-level force stage errs by about 2.5e-7 eV/A per unit of that
+    entry, so models whose entry exceeds 200 get FP64-level forces."""
+    m = sgp._device_model()
+    fmax = ctypes.c_double(0.0)
+    f64 = ctypes.c_int(0)
+    check(lib().fgb_model_fold_guard(m.h, ctypes.byref(fmax),
+                                     ctypes.byref(f64), stream_ptr()),
+          "fold_guard")
+    return fmax.value, bool(f64.value)
+
+
 def write_mapping_coefficients(sgp, file_name, contributor, kernel_index=0):
     """SparseGP::write_mapping_coefficients (sparse_gp.cpp:1199-1264)."""
     coeffs = mapping_coefficients(sgp, kernel_index)

@@ -52,7 +52,10 @@ enum {
   FGB_PREC_FP64 = 0,  /* FP64 adjoint path                                   */
   FGB_PREC_MIXED = 1  /* double-float descriptors, FP64-accurate tensor-core
                          kernel/variance GEMMs (exact slicing), FP32-level
-                         tensor-core force GEMM and FP32 adjoint            */
+                         tensor-core force GEMM and FP32 adjoint; models
+                         whose largest folded coefficient exceeds 200
+                         (fgb_model_fold_guard) get the force stage at
+                         FP64 level instead                                  */
 };
 
 /* prediction outputs */
@@ -255,6 +258,15 @@ int fgb_md_read(fgb_md_t md, double *h_positions, double *h_velocities,
  * symmetric) or sigma^2 sum_t alpha_t s^_t (power 1; n_d), FP64. */
 int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream);
 
+/* The mixed path's force-precision guard for a solved power-1 or power-2
+ * model: h_fold_max = the largest |sigma^2 sum_t alpha_t s^_t s^_t^T| entry
+ * (power 1: of the vector), h_fp64_forces = 1 when it exceeds 200 and the
+ * mixed path's force stage (force product, mapped gradient, B2 adjoint)
+ * therefore runs at FP64 level, 0 when it runs at FP32 level.  Either may
+ * be NULL. */
+int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
+                         int *h_fp64_forces, void *stream);
+
 /* Thin Q (rows x cols, column-major) of the Householder QR of A (rows x
  * cols, column-major, rows >= cols), device buffers; the varmap
  * coefficients (normalized_dot_product.cpp:769-830) are its leading rows. */
@@ -272,8 +284,8 @@ int fgb_qr_thin_q(int rows, int cols, const double *d_A, double *d_Q,
  * 179-193) gives v_i = 1 - |Q_s^T B2/|B2||^2 per atom (FGB_WANT_LOCAL_VAR;
  * the std is sign(v) sqrt|v|).  Outputs as in fgb_predict, plus per-atom
  * energies (any output may be NULL); precision FGB_PREC_FP64, or
- * FGB_PREC_MIXED (descriptor in double-float, adjoint in FP32, the beta
- * product still FP64-level). */
+ * FGB_PREC_MIXED (descriptor in double-float, adjoint in FP32 unless the
+ * largest |beta| exceeds 200, the beta product still FP64-level). */
 typedef struct fgb_mapped_s *fgb_mapped_t;
 int fgb_mapped_create(fgb_mapped_t *out, fgb_b2_t b2, int power,
                       int normalized, const double *h_beta,

@@ -177,3 +177,34 @@ def test_mixed_precision_within_budget(power):
     mae = np.abs(a["forces"] - b["forces"]).mean()
     assert mae <= 1e-4, mae
     np.testing.assert_allclose(b["stress"], a["stress"], atol=1e-5)
+
+
+@pytest.mark.parametrize("power", [2, 1])
+def test_mixed_guard_large_fold(power):
+    """Ill-conditioned model (|alpha| ~ 1e9 from near-duplicate sparse
+    environments; largest folded coefficient sigma^2 |sum alpha s^ s^T|
+    ~ 1e5-1e6): the FP32-level force stage would err by ~0.1 eV/A, so the
+    fold guard must switch the force product, mapped gradient and adjoint
+    to FP64 level; forces then agree with the FP64 path to 1e-6 eV/A MAE
+    and the oracle's energy to 1e-6 eV/atom."""
+    from flare_gb300 import mapped
+    ogp, b2a = small_two_species(seed=5, n_train=2, power=power)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    fmax, f64 = mapped.fold_guard(ggp)
+    assert f64 and fmax > 200.0, (fmax, f64)
+    cell, sp, pos = random_atoms(seed=55)
+    E, F, Sg, V = oracle_predict(ogp, b2a, cell, sp, pos)
+    b = gpu_predict(ggp, calc, [(cell, sp, pos)], precision="mixed")
+    assert abs(b["energy"][0] - E) / len(sp) <= 1e-6
+    assert np.abs(b["forces"] - F).mean() <= 1e-6
+    np.testing.assert_allclose(b["local_var"], V, rtol=0, atol=1e-8)
+
+
+def test_mixed_guard_keeps_fast_path():
+    """A well-conditioned FCC model (largest folded coefficient ~6) stays on
+    the FP32-level force stage."""
+    from flare_gb300 import mapped
+    ogp, b2a = c1_model(n_train=8, n_sparse=120)
+    ggp, _ = to_gpu_sgp(ogp, b2a)
+    fmax, f64 = mapped.fold_guard(ggp)
+    assert not f64 and 0.0 < fmax < 200.0, (fmax, f64)
