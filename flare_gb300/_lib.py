@@ -53,6 +53,7 @@ SIGNATURES = {
     "fgb_model_set": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "fgb_model_set_R_inv": (_i, [_vp, _vp]),
     "fgb_predict_sor": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_predict_dtc": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_predict": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _i, _vp, _vp,
                          _vp, _vp, _vp]),
     "fgb_predict_host": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _d, _i, _i, _vp,
@@ -60,6 +61,7 @@ SIGNATURES = {
     "fgb_envs_envs": (_i, [_vp, _vp, _i, _vp, _vp, _i, _i, _d, _d, _vp,
                            _vp]),
     "fgb_envs_struc": (_i, [_vp, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_self_kernel_struc": (_i, [_vp, _d, _d, _vp, _vp, _vp, _vp]),
     "fgb_predict_plain": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_oz_dgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
     "fgb_oz_sgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),

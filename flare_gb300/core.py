@@ -148,6 +148,21 @@ class NormalizedDotProduct:
         sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
         return envs_struc_gpu(envs, struc, sig, self.power)
 
+    def self_kernel_struc(self, struc, hyps=None):
+        """Prior variances of a structure's energy, forces and stress
+        [1 + 3N + 6] (normalized_dot_product.cpp:450-586; the C++ method
+        behind predict_DTC); ``struc`` is a Structure (FP64 on the GPU)."""
+        sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
+        calc = struc.descriptor_calculators[0]
+        out = torch.zeros(1 + 3 * struc.noa + 6, dtype=torch.float64,
+                          device=_device())
+        d = struc._inputs()
+        check(lib().fgb_self_kernel_struc(calc.handle, sig, self.power,
+                                          struc.nlist().h, ptr(d["species"]),
+                                          ptr(out), stream_ptr()),
+              "self_kernel_struc")
+        return out.cpu().numpy()
+
 
 # ------------------------------------------------------- descriptors
 class DescriptorValues:
@@ -971,9 +986,24 @@ class SparseGP(_Training):
         structure.variance_efs = var.cpu().numpy()
 
     def predict_DTC(self, structure):
-        raise NotImplementedError(
-            "predict_DTC needs self_kernel_struc "
-            "(normalized_dot_product.cpp:451-586), which is not built")
+        """sparse_gp.cpp:694-729: mean_efs and the DTC variances K_self -
+        diag(K^T Kuu^-1 K) + diag(K^T Sigma K) over all 1 + 3N + 6 outputs
+        (FP64; K_self is NormalizedDotProduct::self_kernel_struc)."""
+        if self.R_inv is None:
+            raise RuntimeError(
+                "L_inv must be up to date to make predictions. Please call "
+                "update_matrices_QR and try again.")
+        m = self._device_model(structure.descriptor_calculators)
+        dev = _device()
+        n_out = 1 + 3 * structure.noa + 6
+        mean = torch.zeros(n_out, dtype=torch.float64, device=dev)
+        var = torch.zeros(n_out, dtype=torch.float64, device=dev)
+        d = structure._inputs()
+        check(lib().fgb_predict_dtc(m.h, structure.nlist().h, ptr(d["species"]),
+                                    ptr(mean), ptr(var), stream_ptr()),
+              "predict_DTC")
+        structure.mean_efs = mean.cpu().numpy()
+        structure.variance_efs = var.cpu().numpy()
 
     # -------------------------------------------------- mapped models
     def write_mapping_coefficients(self, file_name, contributor,

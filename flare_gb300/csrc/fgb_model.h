@@ -40,6 +40,8 @@ struct fgb_model_s {
   fgb::DevBuf Lp;       // per-species L_inv panels
   fgb::DevBuf RinvT;    // R_inv^T (M x M, lower triangular) for SOR
   bool has_rinv = false;
+  fgb::DevBuf Lfull;    // L_inv (M x M, lower triangular) for DTC, on demand
+  bool lfull_ready = false;
   fgb::DevBuf Bmap;     // mixed path: per species n_d x n_d FP32 folded matrix
   fgb::DevBuf Bfold;    // the folded matrices in FP64 (power 2), per species
   // the folded matrices in FP32-level slices (tensor-core force GEMM), one
@@ -124,4 +126,9 @@ int envs_struc_impl(const B2Params &p, double sigma, double power,
                     const int *h_counts, const double *d_sparse,
                     fgb_nlist_s *nl, const int *d_species, double *d_kern,
                     fgb_workspace &ws, cudaStream_t st);
+// self_kernel_struc of one structure into d_out[1 + 3N + 6] (dtc.cu); with
+// have_dervs the workspace already holds B2, norms and dB2 of this list.
+int self_kernel_impl(const B2Params &p, double sigma, double power,
+                     fgb_nlist_s *nl, const int *d_species, double *d_out,
+                     fgb_workspace &ws, cudaStream_t st, bool have_dervs);
 }  // namespace fgb

@@ -180,6 +180,14 @@ __global__ void k_sum_parts(int M, int ntiles, const double *__restrict__ part,
   out[m] = s;
 }
 
+// variance_efs = K_self - Q_self + V_SOR (sparse_gp.cpp:726)
+__global__ void k_dtc_combine(long long n, const double *__restrict__ kself,
+                              const double *__restrict__ q,
+                              double *__restrict__ v) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = kself[i] - q[i] + v[i];
+}
+
 __global__ void k_kt_alpha(int M, long long ncol, const double *__restrict__ KT,
                            const double *__restrict__ alpha,
                            double *__restrict__ out) {
@@ -468,6 +476,7 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   }
   m->solved = false;
   m->bmap_ready = false;
+  m->lfull_ready = false;
   m->force_f64 = false;
   m->fold_max = 0.0;
   for (bool &r : m->oz_ready) r = false;
@@ -809,6 +818,86 @@ extern "C" int fgb_predict_sor(fgb_model_t m, fgb_nlist_t nl,
                                                    part.as<double>(),
                                                    d_variance_efs);
   FGB_LAUNCH_CHECK("k_sum_parts");
+  FGB_CUDA(cudaStreamSynchronize(st));
+  return FGB_OK;
+}
+
+extern "C" int fgb_predict_dtc(fgb_model_t m, fgb_nlist_t nl,
+                               const int *d_species, double *d_mean_efs,
+                               double *d_variance_efs, void *stream) {
+  if (!m || !nl || !d_mean_efs || !d_variance_efs) {
+    set_error("fgb_predict_dtc: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (!m->solved || !m->has_rinv) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = nl->n_atoms, M = m->M;
+  const long long ncol = 1 + 3LL * N + 6;
+  if (ncol > (1LL << 30)) { set_error("fgb_predict_dtc: structure too large"); return FGB_EINVAL; }
+  int rc;
+  if (!m->lfull_ready && M > 0) {
+    if ((rc = m->Lfull.ensure(sizeof(double) * (size_t)M * M))) return rc;
+    FGB_CUDA(cudaMemcpy(m->Lfull.p, m->h_L_inv.data(),
+                        sizeof(double) * (size_t)M * M, cudaMemcpyHostToDevice));
+    m->lfull_ready = true;
+  }
+  DevBuf kern, kt, part, kself, q;
+  const int ntiles = ceil_div(M, BN);
+  if ((rc = kern.ensure(sizeof(double) * ((size_t)M * ncol + 1))) ||
+      (rc = kt.ensure(sizeof(double) * ((size_t)M * ncol + 1))) ||
+      (rc = part.ensure(sizeof(double) * ((size_t)ncol * ntiles + 1))) ||
+      (rc = kself.ensure(sizeof(double) * ncol)) ||
+      (rc = q.ensure(sizeof(double) * ncol)))
+    return rc;
+  if ((rc = envs_struc_impl(m->b2, m->sigma, m->power, m->h_counts.data(),
+                            m->Sraw.as<double>(), nl, d_species,
+                            kern.as<double>(), m->ws, st)))
+    return rc;
+  // K_self from the descriptors and stored gradients envs_struc left in the
+  // workspace (envs_struc_impl computes them only when M > 0 and N > 0)
+  if ((rc = self_kernel_impl(m->b2, m->sigma, m->power, nl, d_species,
+                             kself.as<double>(), m->ws, st, M > 0)))
+    return rc;
+  if (M == 0) {
+    FGB_CUDA(cudaMemsetAsync(d_mean_efs, 0, sizeof(double) * ncol, st));
+    FGB_CUDA(cudaMemcpyAsync(d_variance_efs, kself.p, sizeof(double) * ncol,
+                             cudaMemcpyDeviceToDevice, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+    return FGB_OK;
+  }
+  k_transpose_rm<<<ceil_div((long long)M * ncol, 256), 256, 0, st>>>(
+      M, (int)ncol, kern.as<double>(), kt.as<double>());
+  FGB_LAUNCH_CHECK("k_transpose_rm");
+  k_kt_alpha<<<ceil_div(ncol, 128), 128, 0, st>>>(M, ncol, kt.as<double>(),
+                                                  m->alpha.as<double>(),
+                                                  d_mean_efs);
+  FGB_LAUNCH_CHECK("k_kt_alpha");
+  dim3 g(ntiles, ceil_div(ncol, BM));
+  // diag(K^T Kuu^-1 K) = column sums of (L_inv K)^2 (sparse_gp.cpp:723)
+  k_variance_gemm<<<g, GT, 0, st>>>((int)ncol, M, M, kt.as<double>(),
+                                    m->Lfull.as<double>(), part.as<double>(),
+                                    ntiles);
+  FGB_LAUNCH_CHECK("k_variance_gemm");
+  k_sum_parts<<<ceil_div(ncol, 128), 128, 0, st>>>((int)ncol, ntiles,
+                                                   part.as<double>(),
+                                                   q.as<double>());
+  FGB_LAUNCH_CHECK("k_sum_parts");
+  // diag(K^T Sigma K) = column sums of (R_inv^T K)^2 (sparse_gp.cpp:724)
+  k_variance_gemm<<<g, GT, 0, st>>>((int)ncol, M, M, kt.as<double>(),
+                                    m->RinvT.as<double>(), part.as<double>(),
+                                    ntiles);
+  FGB_LAUNCH_CHECK("k_variance_gemm");
+  k_sum_parts<<<ceil_div(ncol, 128), 128, 0, st>>>((int)ncol, ntiles,
+                                                   part.as<double>(),
+                                                   d_variance_efs);
+  FGB_LAUNCH_CHECK("k_sum_parts");
+  k_dtc_combine<<<ceil_div(ncol, 256), 256, 0, st>>>(
+      ncol, kself.as<double>(), q.as<double>(), d_variance_efs);
+  FGB_LAUNCH_CHECK("k_dtc_combine");
   FGB_CUDA(cudaStreamSynchronize(st));
   return FGB_OK;
 }

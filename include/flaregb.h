@@ -183,6 +183,14 @@ int fgb_model_set_R_inv(fgb_model_t m, const double *h_R_inv);
 int fgb_predict_sor(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
                     double *d_mean_efs, double *d_variance_efs, void *stream);
 
+/* SparseGP::predict_DTC (sparse_gp.cpp:694-729) for ONE structure in FP64:
+ * mean_efs = K^T alpha and variance_efs = K_self - diag(K^T Kuu^-1 K) +
+ * diag(K^T Sigma K), Kuu^-1 = L_inv^T L_inv, Sigma = R_inv R_inv^T, K_self
+ * from fgb_self_kernel_struc.  Needs fgb_model_set_R_inv.  d_mean_efs,
+ * d_variance_efs: [1 + 3N + 6]. */
+int fgb_predict_dtc(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
+                    double *d_mean_efs, double *d_variance_efs, void *stream);
+
 /* Full prediction for a packed batch of structures (device pointers):
  * neighbours (cutoff = Structure cutoff), B2, kernel against the sparse set,
  * mean energy / forces / stress by the reverse-mode adjoint and the local
@@ -374,6 +382,17 @@ int fgb_envs_struc(fgb_b2_t b2, double sigma, double power,
                    const int *h_counts, const double *d_sparse,
                    fgb_nlist_t nl, const int *d_species, double *d_kern,
                    void *stream);
+
+/* NormalizedDotProduct::self_kernel_struc (normalized_dot_product.cpp:
+ * 450-586) in FP64: the prior variances of ONE structure's energy, forces
+ * and stress, d_out[1 + 3N + 6] (energy, 3N force components, stress xx xy
+ * xz yy yz zz).  Computed without the reference's 3P x 3P force_force
+ * matrix: force entries as local sums over each atom's neighbourhood,
+ * energy and stress over atom pairs.  FGB_EINVAL with the reference's
+ * message where a descriptor dot product is below 1e-8 and power < 2. */
+int fgb_self_kernel_struc(fgb_b2_t b2, double sigma, double power,
+                          fgb_nlist_t nl, const int *d_species, double *d_out,
+                          void *stream);
 
 /* Plain FP64 form of SparseGP::predict_local_uncertainties for one
  * structure: envs_struc (stored gradients), mean_efs = K^T alpha, and the

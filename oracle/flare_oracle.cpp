@@ -17,6 +17,7 @@
 //   * single-bond (A_nlm) accumulation    src/flare_pp/descriptors/b2.cpp:244-399
 //   * B2 contraction + stored gradients   src/flare_pp/descriptors/b2.cpp:181-242
 //   * envs_struc kernel scatter loop      src/flare_pp/kernels/normalized_dot_product.cpp:117-214
+//   * self_kernel_struc (DTC prior)       src/flare_pp/kernels/normalized_dot_product.cpp:450-586
 //
 // Canonical floating-point order: built with -ffp-contract=off so that no
 // multiply-add is fused; wrapping and neighbour distances use the operation
@@ -520,6 +521,97 @@ void orc_envs_struc_block(int Ms, int Ns, int n_atoms, int c_sparse,
       }
     }
   }
+}
+
+// Prior variances of one structure's energy, forces and stress for one
+// species block (normalized_dot_product.cpp:450-586): every atom pair
+// i <= j of the block (twice when i != j), every pair of their neighbour
+// entries, the same force component on both sides.  dot_vals = D D^T
+// (Ns x Ns), force_dot = dD D^T (3Ps x Ns), force_force = dD dD^T
+// (3Ps x 3Ps), struc_force_dots (3Ps).  Rows are summed into `out` (1 + 3
+// n_atoms + 6) in atom order after the per-atom rows are complete, as the
+// reference reduces par_mat.  Returns -1 where a dot product is below the
+// empty threshold and power < 2 (the reference throws invalid_argument).
+int orc_self_kernel_block(int Ns, int n_atoms, const double *norms,
+                          const double *dot_vals, const double *force_dot,
+                          const double *force_force,
+                          const double *struc_force_dots,
+                          const int *neighbor_counts, const int *cum_neighbor,
+                          const int *atom_indices, const int *neighbor_indices,
+                          const double *neighbor_coords, double sig_sq,
+                          double power, double vol_inv, double *out) {
+  const double empty_thresh = 1e-8;
+  const double vol_inv_sq = vol_inv * vol_inv;
+  const long long ncol = 1 + 3LL * n_atoms + 6;
+  long long fcols = 0;
+  for (int j = 0; j < Ns; j++) fcols += neighbor_counts[j];
+  fcols *= 3;
+  std::vector<double> par((size_t)Ns * ncol, 0.0);
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+  for (int i = 0; i < Ns; i++) {
+    const double norm_i = norms[i];
+    if (norm_i < empty_thresh) continue;
+    const double norm_i2 = norm_i * norm_i;
+    const double norm_i3 = norm_i2 * norm_i;
+    double *row = par.data() + (size_t)i * ncol;
+    for (int j = i; j < Ns; j++) {
+      const double norm_j = norms[j];
+      if (norm_j < empty_thresh) continue;
+      const double mult_fac = i == j ? 1.0 : 2.0;
+      const double norm_j2 = norm_j * norm_j;
+      const double norm_j3 = norm_j2 * norm_j;
+      const double norm_ij = norm_i * norm_j;
+      const double norm_dot = dot_vals[(size_t)i * Ns + j] / norm_ij;
+      const double c1 = (power - 1) * power * std::pow(norm_dot, power - 2);
+      if (std::fabs(norm_dot) < empty_thresh && power < 2) { bad = 1; continue; }
+      const double c2 = power * std::pow(norm_dot, power - 1);
+      row[0] += sig_sq * mult_fac * std::pow(norm_dot, power);
+      const int n1 = neighbor_counts[i], cn1 = cum_neighbor[i];
+      const int ci1 = atom_indices[i];
+      const int n2 = neighbor_counts[j], cn2 = cum_neighbor[j];
+      const int ci2 = atom_indices[j];
+      for (int k = 0; k < n1; k++) {
+        const long long ind1 = cn1 + k;
+        const int ni1 = neighbor_indices[ind1];
+        for (int l = 0; l < n2; l++) {
+          const long long ind2 = cn2 + l;
+          const int ni2 = neighbor_indices[ind2];
+          int stress_counter = 0;
+          for (int m = 0; m < 3; m++) {
+            const long long f1 = 3 * ind1 + m, f2 = 3 * ind2 + m;
+            const double v1 = force_dot[f1 * Ns + j] / norm_ij -
+                              norm_dot * struc_force_dots[f1] / norm_i2;
+            const double v2 = force_dot[f2 * Ns + i] / norm_ij -
+                              norm_dot * struc_force_dots[f2] / norm_j2;
+            const double v3 = force_force[f1 * fcols + f2] / norm_ij;
+            const double v4 = struc_force_dots[f1] * force_dot[f2 * Ns + i] /
+                              (norm_i3 * norm_j);
+            const double v5 = struc_force_dots[f2] * force_dot[f1 * Ns + j] /
+                              (norm_i * norm_j3);
+            const double v6 = struc_force_dots[f1] * struc_force_dots[f2] *
+                              norm_dot / (norm_i2 * norm_j2);
+            const double kv =
+                sig_sq * mult_fac * (c1 * v1 * v2 + c2 * (v3 - v4 - v5 + v6));
+            if (ci1 == ci2) row[1 + ci1 * 3 + m] += kv;
+            if (ci1 == ni2) row[1 + ci1 * 3 + m] -= kv;
+            if (ni1 == ci2) row[1 + ni1 * 3 + m] -= kv;
+            if (ni1 == ni2) row[1 + ni1 * 3 + m] += kv;
+            for (int n = m; n < 3; n++) {
+              const double x1 = neighbor_coords[ind1 * 3 + n];
+              const double x2 = neighbor_coords[ind2 * 3 + n];
+              row[1 + 3 * n_atoms + stress_counter] += kv * x1 * x2 * vol_inv_sq;
+              stress_counter++;
+            }
+          }
+        }
+      }
+    }
+  }
+  if (bad) return -1;
+  for (int i = 0; i < Ns; i++)
+    for (long long c = 0; c < ncol; c++) out[c] += par[(size_t)i * ncol + c];
+  return 0;
 }
 
 }  // extern "C"

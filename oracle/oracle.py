@@ -72,6 +72,10 @@ def lib():
             ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
             dp, dp, ip, ip, ip, ip, dp, ctypes.c_double, ctypes.c_double,
             ctypes.c_double, dp]
+        L.orc_self_kernel_block.argtypes = [
+            ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, ip, ip, ip, ip, dp,
+            ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
+        L.orc_self_kernel_block.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -367,6 +371,43 @@ class NormalizedDotProduct:
         return K
 
 
+    def self_kernel_struc(self, struc, hyps=None):
+        """Prior variances of E, F, S (normalized_dot_product.cpp:450-586):
+        [1 + 3N + 6], the per-species loop over atom pairs and neighbour
+        entries with dot_vals, force_dot and force_force precomputed as the
+        reference does."""
+        sig = self.sigma if hyps is None else hyps[0]
+        n_atoms = struc.n_atoms
+        out = np.zeros(1 + 3 * n_atoms + 6)
+        for s in range(struc.n_types):
+            D = np.ascontiguousarray(struc.descriptors[s])
+            Ns = D.shape[0]
+            if Ns == 0:
+                continue
+            fd = struc.descriptor_force_dervs[s]
+            dot_vals = np.ascontiguousarray(D @ D.T)
+            force_dot = np.ascontiguousarray(fd @ D.T) if fd.shape[0] else \
+                np.zeros((0, Ns))
+            force_force = np.ascontiguousarray(fd @ fd.T) if fd.shape[0] else \
+                np.zeros((0, 0))
+            rc = lib().orc_self_kernel_block(
+                Ns, n_atoms, _dp(np.ascontiguousarray(struc.descriptor_norms[s])),
+                _dp(dot_vals), _dp(force_dot), _dp(force_force),
+                _dp(np.ascontiguousarray(struc.descriptor_force_dots[s])),
+                _ip(np.ascontiguousarray(struc.neighbor_counts[s], np.int32)),
+                _ip(np.ascontiguousarray(struc.cumulative_neighbor_counts[s],
+                                         np.int32)),
+                _ip(np.ascontiguousarray(struc.atom_indices[s], np.int32)),
+                _ip(np.ascontiguousarray(struc.neighbor_indices[s], np.int32)),
+                _dp(np.ascontiguousarray(struc.neighbor_coordinates[s])),
+                sig * sig, self.power, 1.0 / struc.volume, _dp(out))
+            if rc != 0:
+                raise ValueError(
+                    "Dot product of descriptors is 0, and the negative power "
+                    "function in force-force kernel diverges.")
+        return out
+
+
 # --------------------------------------------------------------- SparseGP
 class SparseGP:
     """sparse_gp.cpp:14-757 (prediction + the QR solve)."""
@@ -622,6 +663,19 @@ class SparseGP:
         structure.mean_efs = km.T @ self.alpha
         vs = km.T @ self.R_inv
         structure.variance_efs = np.einsum("ij,ij->i", vs, vs)
+
+    def predict_DTC(self, structure):
+        """sparse_gp.cpp:694-729: mean_efs, and variance_efs = K_self -
+        diag(K^T Kuu^-1 K) + diag(K^T Sigma K)."""
+        self._check()
+        km = self._kernel_mat(structure)
+        structure.mean_efs = km.T @ self.alpha
+        K_self = np.zeros(km.shape[1])
+        for i, k in enumerate(self.kernels):
+            K_self += k.self_kernel_struc(structure.descriptors[i])
+        Q_self = np.einsum("ij,ij->j", km, self.Kuu_inverse @ km)
+        V_SOR = np.einsum("ij,ij->j", km, self.Sigma @ km)
+        structure.variance_efs = K_self - Q_self + V_SOR
 
     # sparse_gp.cpp:94-139
     def compute_cluster_uncertainties(self, structure):

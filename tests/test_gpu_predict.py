@@ -208,3 +208,64 @@ def test_mixed_guard_keeps_fast_path():
     ggp, _ = to_gpu_sgp(ogp, b2a)
     fmax, f64 = mapped.fold_guard(ggp)
     assert not f64 and 0.0 < fmax < 200.0, (fmax, f64)
+
+
+@pytest.mark.parametrize("power", [2, 1])
+@pytest.mark.parametrize("multicut", [False, True])
+def test_self_kernel_struc_matches_oracle(power, multicut):
+    """NormalizedDotProduct::self_kernel_struc (normalized_dot_product.cpp:
+    450-586) on a 16-atom, 2-species cell in a 4 A box (every atom its own
+    neighbour through images) against the oracle's restatement of the
+    reference loop; FP64, relative 1e-10 of the largest entry."""
+    import flare_gb300 as fg
+    S = 2
+    cutoffs = (5.0 * np.ones((S, S)) + np.eye(S) - 1) if multicut else None
+    b2a = b2_args(S, 3, 2, 5.0, cutoffs=cutoffs)
+    cell, sp, pos = random_atoms(seed=17)
+    st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    ref = oracle.NormalizedDotProduct(1.3, power).self_kernel_struc(
+        st.descriptors[0])
+    calc = fg.B2(*b2a[:5], cutoffs=b2a[5])
+    got = fg.NormalizedDotProduct(1.3, power).self_kernel_struc(
+        fg.Structure(cell, sp, pos, 5.0, [calc]))
+    np.testing.assert_allclose(got, ref, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())
+
+
+def test_self_kernel_struc_fcc():
+    """The same on a 108-atom FCC cell (3 x 3 x 3 cells, rc 4.5 A, one
+    species), where neighbourhoods hold distinct atoms."""
+    import flare_gb300 as fg
+    b2a = b2_args(1, 6, 3, 4.5)
+    cell, sp, pos = syn.fcc_al(n_cells=3, seed=11)
+    st = oracle.Structure(cell, sp, pos, 4.5, [oracle.B2Settings(*b2a)])
+    ref = oracle.NormalizedDotProduct(2.0, 2).self_kernel_struc(
+        st.descriptors[0])
+    calc = fg.B2(*b2a[:5], cutoffs=b2a[5])
+    got = fg.NormalizedDotProduct(2.0, 2).self_kernel_struc(
+        fg.Structure(cell, sp, pos, 4.5, [calc]))
+    np.testing.assert_allclose(got, ref, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())
+
+
+def test_predict_dtc_matches_oracle():
+    """SparseGP::predict_DTC (sparse_gp.cpp:694-729): mean and the DTC
+    variances of every output against the oracle (FP64; variances within
+    1e-10 of the largest prior variance)."""
+    import flare_gb300 as fg
+    ogp, b2a = small_two_species(seed=5, n_train=2)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    ggp.R_inv = ogp.R_inv
+    cell, sp, pos = random_atoms(seed=55)
+    st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    ogp.predict_DTC(st)
+    g = fg.Structure(cell, sp, pos, 5.0, [calc])
+    ggp.predict_DTC(g)
+    np.testing.assert_allclose(g.mean_efs, st.mean_efs, rtol=0,
+                               atol=1e-8 * np.abs(st.mean_efs).max())
+    # the variance is K_self - Q_self + V_SOR with K_self and Q_self of
+    # similar size (this model's L_inv is large): FP64 agreement is relative
+    # to the terms, not to their difference
+    ks = ogp.kernels[0].self_kernel_struc(st.descriptors[0])
+    np.testing.assert_allclose(g.variance_efs, st.variance_efs, rtol=0,
+                               atol=1e-10 * np.abs(ks).max())

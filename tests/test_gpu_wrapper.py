@@ -64,7 +64,7 @@ def oracle_twin(w, b2a, sae, data):
     return ogp, ob2
 
 
-@pytest.mark.parametrize("vt", ["local", "SOR"])
+@pytest.mark.parametrize("vt", ["local", "SOR", "DTC"])
 @pytest.mark.parametrize("multicut", [False, True])
 def test_calculator_matches_oracle(vt, multicut):
     import flare_gb300 as fg
@@ -77,8 +77,10 @@ def test_calculator_matches_oracle(vt, multicut):
     st = oracle.Structure(cell, sp, pos, 5.0, [ob2])
     if vt == "local":
         ogp.predict_local_uncertainties(st)
-    else:
+    elif vt == "SOR":
         ogp.predict_SOR(st)
+    else:
+        ogp.predict_DTC(st)
     ref = oracle.calculator_results(st, vt, w.hyps[0], sae)
     scale = max(1.0, abs(ref["energy"]))
     assert abs(calc.results["energy"] - ref["energy"]) < 1e-8 * scale

@@ -131,3 +131,90 @@ def test_local_variances_nonnegative_and_sparse_points_small():
     st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
     v = gp.compute_cluster_uncertainties(st)[0]
     assert np.all(v > -1e-8)
+
+
+def _unit_rows(st):
+    dv = st.descriptors[0]
+    out = []
+    for s in range(dv.n_types):
+        D, n = dv.descriptors[s], dv.descriptor_norms[s]
+        ok = n >= 1e-8
+        U = np.zeros_like(D)
+        U[ok] = D[ok] / n[ok, None]
+        out.append(U)
+    return out
+
+
+@pytest.mark.parametrize("power", [1, 2])
+def test_self_kernel_struc_finite_difference(power):
+    """self_kernel_struc (normalized_dot_product.cpp:450-586) is the diagonal
+    of the structure-structure kernel: the energy entry equals
+    sigma^2 sum_ij c_ij^power, a force entry the mixed second derivative of
+    that sum with respect to one atom's coordinate in each structure, a
+    stress entry the mixed second derivative with respect to the
+    deformation x_m += h x_n of each cell, over V^2.  Four-point central
+    differences, h = 3e-4 (truncation ~1e-6 relative, rounding ~1e-7
+    absolute)."""
+    b2a = b2_args(2, 3, 2, 4.0)
+    b2 = oracle.B2Settings(*b2a)
+    cell, sp, pos = random_atoms(seed=7)
+    sig = 1.5
+    k = oracle.NormalizedDotProduct(sig, power)
+    st = oracle.Structure(cell, sp, pos, 4.0, [b2])
+    K = k.self_kernel_struc(st.descriptors[0])
+    n = len(sp)
+    assert K.shape == (1 + 3 * n + 6,)
+
+    def rows(c, p):
+        return _unit_rows(oracle.Structure(c, sp, p, 4.0, [b2],
+                                           compute_dervs=False))
+
+    def kee(A, B):
+        return sig * sig * sum(float(np.sum((a @ b.T) ** power))
+                               for a, b in zip(A, B))
+
+    U0 = rows(cell, pos)
+    assert abs(K[0] - kee(U0, U0)) <= 1e-12 * abs(K[0])
+    h = 3e-4
+    for a, m in [(0, 0), (3, 1), (9, 2), (14, 0)]:
+        P = []
+        for d in (h, -h):
+            q = pos.copy()
+            q[a, m] += d
+            P.append(rows(cell, q))
+        fd = (kee(P[0], P[0]) - kee(P[0], P[1]) - kee(P[1], P[0]) +
+              kee(P[1], P[1])) / (4 * h * h)
+        assert abs(K[1 + 3 * a + m] - fd) <= 2e-5 * abs(fd) + 1e-6, (a, m)
+    vol = abs(np.linalg.det(cell))
+    for c, (m, nn) in enumerate([(0, 0), (0, 1), (0, 2), (1, 1), (1, 2),
+                                 (2, 2)]):
+        # a stretch moves pairs across the cutoff, whose quadratic form has
+        # a jump in the second derivative: the difference then converges
+        # only linearly in h, so diagonal entries use a smaller step
+        hs = 1e-5 if m == nn else h
+        P = []
+        for d in (hs, -hs):
+            F = np.eye(3)
+            F[m, nn] += d
+            P.append(rows(cell @ F.T, pos @ F.T))
+        fd = (kee(P[0], P[0]) - kee(P[0], P[1]) - kee(P[1], P[0]) +
+              kee(P[1], P[1])) / (4 * hs * hs) / vol ** 2
+        assert abs(K[1 + 3 * n + c] - fd) <= 2e-5 * abs(fd) + 1e-8, (m, nn)
+
+
+def test_predict_dtc_variances_relation():
+    """predict_DTC (sparse_gp.cpp:694-729) against its definition assembled
+    from the oracle's own parts, and SOR's variances plus K_self -
+    diag(K^T Kuu^-1 K)."""
+    ogp, b2a = small_two_species(seed=5, n_train=2)
+    cell, sp, pos = random_atoms(seed=55)
+    st = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    ogp.predict_DTC(st)
+    dtc = st.variance_efs.copy()
+    ogp.predict_SOR(st)
+    sor = st.variance_efs.copy()
+    km = ogp._kernel_mat(st)
+    ks = ogp.kernels[0].self_kernel_struc(st.descriptors[0])
+    q = np.einsum("ij,ij->j", km, ogp.Kuu_inverse @ km)
+    np.testing.assert_allclose(dtc, ks - q + sor,
+                               atol=1e-9 * np.abs(ks).max())
