@@ -148,6 +148,23 @@ class NormalizedDotProduct:
         sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
         return envs_struc_gpu(envs, struc, sig, self.power)
 
+    def struc_struc(self, struc1, struc2, hyps=None):
+        """Kernel between every output (energy, 3N forces, 6 stresses) of
+        two structures, (1 + 3 N1 + 6) x (1 + 3 N2 + 6)
+        (normalized_dot_product.cpp:216-448); Structures (FP64 on the
+        GPU)."""
+        sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
+        calc = struc1.descriptor_calculators[0]
+        out = torch.zeros((1 + 3 * struc1.noa + 6, 1 + 3 * struc2.noa + 6),
+                          dtype=torch.float64, device=_device())
+        d1, d2 = struc1._inputs(), struc2._inputs()
+        check(lib().fgb_struc_struc(calc.handle, sig, self.power,
+                                    struc1.nlist().h, ptr(d1["species"]),
+                                    struc2.nlist().h, ptr(d2["species"]),
+                                    ptr(out), stream_ptr()),
+              "struc_struc")
+        return out.cpu().numpy()
+
     def self_kernel_struc(self, struc, hyps=None):
         """Prior variances of a structure's energy, forces and stress
         [1 + 3N + 6] (normalized_dot_product.cpp:450-586; the C++ method

@@ -126,9 +126,15 @@ int envs_struc_impl(const B2Params &p, double sigma, double power,
                     const int *h_counts, const double *d_sparse,
                     fgb_nlist_s *nl, const int *d_species, double *d_kern,
                     fgb_workspace &ws, cudaStream_t st);
-// self_kernel_struc of one structure into d_out[1 + 3N + 6] (dtc.cu); with
+// self_kernel_struc of one structure into d_out[1 + 3N + 6] (struc_kernels.cu); with
 // have_dervs the workspace already holds B2, norms and dB2 of this list.
 int self_kernel_impl(const B2Params &p, double sigma, double power,
                      fgb_nlist_s *nl, const int *d_species, double *d_out,
                      fgb_workspace &ws, cudaStream_t st, bool have_dervs);
+// struc_struc of two structures into d_out[(1 + 3 N1 + 6) x (1 + 3 N2 + 6)]
+// row-major (struc_kernels.cu).
+int struc_struc_impl(const B2Params &p, double sigma, double power,
+                     fgb_nlist_s *nl1, const int *d_species1,
+                     fgb_nlist_s *nl2, const int *d_species2, double *d_out,
+                     cudaStream_t st);
 }  // namespace fgb

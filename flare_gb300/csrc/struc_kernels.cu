@@ -1,22 +1,22 @@
-// Prior variances of one structure's energy, forces and stress under the
-// NormalizedDotProduct kernel: self_kernel_struc
-// (kernels/normalized_dot_product.cpp:450-586), the K_self term of
-// SparseGP::predict_DTC (bffs/sparse_gp.cpp:694-729).
+// Structure kernels of the NormalizedDotProduct kernel on the GPU in FP64:
+// self_kernel_struc (kernels/normalized_dot_product.cpp:450-586; the K_self
+// term of SparseGP::predict_DTC, bffs/sparse_gp.cpp:694-729) and
+// struc_struc (normalized_dot_product.cpp:216-448).
 //
-// The reference forms, per species, force_force = dD dD^T over every pair of
-// neighbour entries (3P x 3P) and loops over atom pairs x neighbour-entry
-// pairs.  Each force-force term is the bilinear form
+// The reference forms, per species, force_force = dD1 dD2^T over every pair
+// of neighbour entries (3P1 x 3P2) and loops over atom pairs x entry pairs.
+// Each force-force term is the bilinear form
 //     g_p^T H_ij g_q,   H_ij = d2 k(d_i, d_j) / dd_i dd_j
 //     = sig2 [ xi (xi-1) c^(xi-2) (P_i u_j)(P_j u_i)^T + xi c^(xi-1) P_i P_j ]
 // with u = d/|d|, c = u_i.u_j, P = (I - u u^T)/|d|, and the four index
-// tests of the reference's scatter make the entry of atom a
-//     sum_ij G_ia^T H_ij G_ja,   G_ia = dd_i/dr_a = sum_p (delta(a, n_p) -
+// tests of the reference's scatter make the entry of atoms (a, b)
+//     sum_ij G_ia^T H_ij G_jb,   G_ia = dd_i/dr_a = sum_p (delta(a, n_p) -
 //                                                   delta(a, i)) g_p,
-// non-zero only for i = a and the neighbours of a.  So the force entries are
-// a local sum per atom over its neighbourhood (k_dtc_force_var), and the
-// energy and stress entries one sum over atom pairs of 19 dot products with
-// the stress-weighted rows W_i,mn = sum_p g_p,m x_p,n (k_dtc_struct_tiles).
-// Nothing of size P x P is formed.
+// non-zero only for i = a and the neighbours of a.  Stress entries use the
+// rows W_i,mn = sum_p g_p,m x_p,n over V, energy-force entries
+// -sig2 xi c^(xi-1) u_i.(P_j G_jb).  So every entry is a sum over atom or
+// neighbourhood pairs of a few dot products of projected rows; nothing of
+// size P x P is formed.
 #include <algorithm>
 #include <vector>
 
@@ -336,6 +336,148 @@ __global__ void k_dtc_struct_final(int n_tiles, int N, const double *__restrict_
   else out[1 + 3LL * N + (q - 1)] = sig2 * vol_inv * vol_inv * s;
 }
 
+// ---------------------------------------------------------- struc_struc
+// Output groups of one structure: the energy (C = 1, items = atoms), each
+// atom's three force components (items = its neighbourhood slots) and the
+// stress in two halves of three components (items = atoms).
+struct SsGroup {
+  int beg, end;          // item range
+  int idx_shift;         // item -> row index of `base`
+  int C;                 // components (1 or 3)
+  const double *base;    // component rows (C > 1)
+  long long stride;      // doubles per row index
+  int comp0;             // first component within a row index
+  long long out0;        // output index of component 0
+  double scale;          // 1, or 1/V for stress
+};
+struct SsWork {
+  int g1, g2;
+  long long p0, p1;      // item pairs [p0, p1) of the group pair
+};
+struct SsPair {
+  int g1, g2, w0, w1;    // work items [w0, w1) of the group pair
+};
+
+// One block per work item, one warp per item pair: c, A_p = R1_p.u_j,
+// B_q = R2_q.u_i, Y_pq = R1_p.R2_q; lane L < C1 C2 keeps entry (L / C2,
+// L % C2) of the partial sum.
+template <int C1, int C2>
+__global__ void __launch_bounds__(kDT)
+k_ss(const SsWork *__restrict__ work, const SsGroup *__restrict__ G1,
+     const SsGroup *__restrict__ G2, const int *__restrict__ row1,
+     const int *__restrict__ row2, const int *__restrict__ sp1,
+     const int *__restrict__ sp2, const double *__restrict__ U1,
+     const double *__restrict__ U2, int nd, double xi,
+     double *__restrict__ part, int *__restrict__ bad) {
+  __shared__ double red[kDT / 32][C1 * C2];
+  const SsWork wk = work[blockIdx.x];
+  const SsGroup g1 = G1[wk.g1], g2 = G2[wk.g2];
+  const int n2 = g2.end - g2.beg;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (long long pr = wk.p0 + warp; pr < wk.p1; pr += kDT / 32) {
+    const int xi1 = g1.beg + (int)(pr / n2), xi2 = g2.beg + (int)(pr % n2);
+    const int ri = row1[xi1], rj = row2[xi2];
+    if (ri < 0 || rj < 0 || sp1[ri] != sp2[rj]) continue;
+    const double *ui = U1 + (long long)ri * nd, *uj = U2 + (long long)rj * nd;
+    const double *r1 = g1.base + (long long)(xi1 - g1.idx_shift) * g1.stride +
+                       (long long)g1.comp0 * nd;
+    const double *r2 = g2.base + (long long)(xi2 - g2.idx_shift) * g2.stride +
+                       (long long)g2.comp0 * nd;
+    double c = 0, A[3] = {0, 0, 0}, B[3] = {0, 0, 0}, Y[3][3] = {};
+    for (int k = lane; k < nd; k += 32) {
+      const double vi = ui[k], vj = uj[k];
+      c += vi * vj;
+      double a1[3], b1[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        a1[q] = C1 > 1 ? r1[(long long)q * nd + k] : 0.0;
+        b1[q] = C2 > 1 ? r2[(long long)q * nd + k] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        if (C1 > 1) A[q] += a1[q] * vj;
+        if (C2 > 1) B[q] += b1[q] * vi;
+      }
+      if (C1 > 1 && C2 > 1) {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+          for (int q = 0; q < 3; q++) Y[p][q] += a1[p] * b1[q];
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      c += __shfl_xor_sync(0xffffffffu, c, off);
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        if (C1 > 1) A[q] += __shfl_xor_sync(0xffffffffu, A[q], off);
+        if (C2 > 1) B[q] += __shfl_xor_sync(0xffffffffu, B[q], off);
+      }
+      if (C1 > 1 && C2 > 1) {
+#pragma unroll
+        for (int p = 0; p < 3; p++)
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            Y[p][q] += __shfl_xor_sync(0xffffffffu, Y[p][q], off);
+      }
+    }
+    if (C1 == 1 && C2 == 1) {
+      if (xi < 2.0 && fabs(c) < kEmptyThresh && lane == 0) atomicOr(bad, 1);
+      acc += pw(c, xi);
+    } else if (lane < C1 * C2) {
+      const double f1 = xi * pw(c, xi - 1);
+      const int p = lane / C2, q = lane % C2;
+      double v;
+      if (C1 == 1) {
+        v = -f1 * B[q];
+      } else if (C2 == 1) {
+        v = -f1 * A[p];
+      } else {
+        const double f2 = (xi - 1) * xi * pw(c, xi - 2);
+        double a = 0, b = 0, y = 0;
+#pragma unroll
+        for (int pp = 0; pp < 3; pp++) {
+          if (pp == p) a = A[pp];
+#pragma unroll
+          for (int qq = 0; qq < 3; qq++)
+            if (pp == p && qq == q) y = Y[pp][qq];
+        }
+#pragma unroll
+        for (int qq = 0; qq < 3; qq++)
+          if (qq == q) b = B[qq];
+        v = f2 * a * b + f1 * y;
+      }
+      acc += v;
+    }
+  }
+  if (lane < C1 * C2) red[warp][lane] = acc;
+  __syncthreads();
+  if (threadIdx.x < C1 * C2) {
+    double t = 0.0;
+    for (int w = 0; w < kDT / 32; w++) t += red[w][threadIdx.x];
+    part[(long long)blockIdx.x * C1 * C2 + threadIdx.x] = t;
+  }
+}
+
+// Sum each group pair's work items in order and write its entries.
+template <int C1, int C2>
+__global__ void k_ss_final(int n_pairs, const SsPair *__restrict__ pairs,
+                           const SsGroup *__restrict__ G1,
+                           const SsGroup *__restrict__ G2,
+                           const double *__restrict__ part, double sig2,
+                           long long ncol, double *__restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n_pairs * C1 * C2) return;
+  const int gp = (int)(t / (C1 * C2)), L = (int)(t % (C1 * C2));
+  const SsPair pr = pairs[gp];
+  double s = 0.0;
+  for (int w = pr.w0; w < pr.w1; w++) s += part[(long long)w * C1 * C2 + L];
+  const SsGroup g1 = G1[pr.g1], g2 = G2[pr.g2];
+  out[(g1.out0 + L / C2) * ncol + g2.out0 + L % C2] =
+      sig2 * g1.scale * g2.scale * s;
+}
+
 }  // namespace
 
 int self_kernel_impl(const B2Params &p, double sigma, double power,
@@ -480,6 +622,235 @@ int self_kernel_impl(const B2Params &p, double sigma, double power,
   return FGB_OK;
 }
 
+
+namespace {
+
+// One structure's rows for struc_struc: B2 and stored gradients, unit rows
+// U and projected stress rows W (sorted row order), every neighbourhood
+// slot's projected gradient rows G, and the item rows (atoms, then slots).
+struct SsSide {
+  int N = 0;
+  double vol = 1.0;
+  long long T = 0;
+  std::vector<long long> base;        // slot base per atom (N + 1)
+  fgb_workspace ws;
+  DevBuf dperm, dinv, dsrow, U, W, dbase, srows, G, item_row;
+};
+
+int ss_prepare(const B2Params &p, fgb_nlist_s *nl, const int *d_species,
+               SsSide &sd, cudaStream_t st) {
+  if (nl->n_struc != 1) {
+    set_error("struc_struc needs single-structure neighbour lists");
+    return FGB_EINVAL;
+  }
+  const int N = nl->n_atoms, S = p.n_species, nd = p.n_d;
+  const long long P = nl->n_pairs;
+  sd.N = N;
+  sd.vol = nl->h_volume[0];
+  int rc;
+  fgb_workspace &ws = sd.ws;
+  if ((rc = check_species(d_species, N, S, ws.flag, st))) return rc;
+  if ((rc = ws.A.ensure(sizeof(double) * ((size_t)N * p.n_A + 1))) ||
+      (rc = ws.B2.ensure(sizeof(double) * ((size_t)N * nd + 1))) ||
+      (rc = ws.norms.ensure(sizeof(double) * (N + 1))) ||
+      (rc = ws.dB2.ensure(sizeof(double) * ((size_t)3 * P * nd + 1))) ||
+      (rc = ws.fdots.ensure(sizeof(double) * (3 * P + 1))))
+    return rc;
+  if (N > 0 &&
+      ((rc = launch_b2_forward(p, nl, d_species, ws.A.as<double>(),
+                               ws.B2.as<double>(), ws.norms.as<double>(), st)) ||
+       (rc = launch_b2_dervs(p, nl, d_species, ws.A.as<double>(),
+                             ws.B2.as<double>(), ws.dB2.as<double>(),
+                             ws.fdots.as<double>(), st))))
+    return rc;
+  std::vector<int> hs(N), perm, inv(N), srow, item_row;
+  std::vector<double> hn(N);
+  if (N > 0) {
+    FGB_CUDA(cudaMemcpyAsync(hs.data(), d_species, sizeof(int) * N,
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaMemcpyAsync(hn.data(), ws.norms.p, sizeof(double) * N,
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+  }
+  for (int s = 0; s < S; s++)
+    for (int a = 0; a < N; a++)
+      if (hs[a] == s) {
+        inv[a] = (int)perm.size();
+        item_row.push_back(hn[a] >= kEmptyThresh ? (int)perm.size() : -1);
+        perm.push_back(a);
+        srow.push_back(s);
+      }
+  if ((rc = sd.dperm.ensure(sizeof(int) * (N + 1))) ||
+      (rc = sd.dinv.ensure(sizeof(int) * (N + 1))) ||
+      (rc = sd.dsrow.ensure(sizeof(int) * (N + 1))) ||
+      (rc = sd.U.ensure(sizeof(double) * ((size_t)N * nd + 1))) ||
+      (rc = sd.W.ensure(sizeof(double) * ((size_t)N * 6 * nd + 1))) ||
+      (rc = sd.dbase.ensure(sizeof(long long) * (N + 1))))
+    return rc;
+  sd.base.assign(N + 1, 0);
+  if (N == 0) {
+    sd.T = 0;
+    return sd.item_row.ensure(sizeof(int));
+  }
+  FGB_CUDA(cudaMemcpyAsync(sd.dperm.p, perm.data(), sizeof(int) * N,
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(sd.dinv.p, inv.data(), sizeof(int) * N,
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(sd.dsrow.p, srow.data(), sizeof(int) * N,
+                           cudaMemcpyHostToDevice, st));
+  k_dtc_rows<<<N, kDT, 0, st>>>(N, nd, sd.dperm.as<int>(), ws.B2.as<double>(),
+                                ws.norms.as<double>(),
+                                nl->offsets.as<long long>(),
+                                nl->nbr_rel.as<double4_16a>(), ws.dB2.as<double>(),
+                                sd.U.as<double>(), sd.W.as<double>());
+  FGB_LAUNCH_CHECK("k_dtc_rows");
+  DevBuf cnt;
+  if ((rc = cnt.ensure(sizeof(int) * N))) return rc;
+  k_dtc_slot_count<<<ceil_div(N, 128), 128, 0, st>>>(
+      N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(), cnt.as<int>());
+  FGB_LAUNCH_CHECK("k_dtc_slot_count");
+  std::vector<int> hc(N);
+  FGB_CUDA(cudaMemcpyAsync(hc.data(), cnt.p, sizeof(int) * N,
+                           cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  for (int a = 0; a < N; a++) sd.base[a + 1] = sd.base[a] + hc[a];
+  sd.T = sd.base[N];
+  if ((rc = sd.srows.ensure(sizeof(int) * sd.T)) ||
+      (rc = sd.G.ensure(sizeof(double) * (size_t)sd.T * 3 * nd)) ||
+      (rc = sd.item_row.ensure(sizeof(int) * (N + sd.T))))
+    return rc;
+  FGB_CUDA(cudaMemcpyAsync(sd.dbase.p, sd.base.data(), sizeof(long long) * (N + 1),
+                           cudaMemcpyHostToDevice, st));
+  k_dtc_slots<<<N, kDT, 0, st>>>(
+      0, N, nd, sd.dinv.as<int>(), ws.norms.as<double>(),
+      nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+      nl->nbr_twin.as<long long>(), ws.dB2.as<double>(), sd.U.as<double>(),
+      sd.dbase.as<long long>(), sd.srows.as<int>(), sd.G.as<double>());
+  FGB_LAUNCH_CHECK("k_dtc_slots");
+  // items: atoms (sorted rows, -1 where empty), then slots
+  FGB_CUDA(cudaMemcpyAsync(sd.item_row.p, item_row.data(), sizeof(int) * N,
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(sd.item_row.as<int>() + N, sd.srows.p,
+                           sizeof(int) * sd.T, cudaMemcpyDeviceToDevice, st));
+  return FGB_OK;
+}
+
+// Groups of one side: energy, atoms 0..N-1, stress halves.
+std::vector<SsGroup> ss_groups(const SsSide &sd, int nd) {
+  std::vector<SsGroup> g;
+  const int N = sd.N;
+  g.push_back({0, N, 0, 1, nullptr, 0, 0, 0, 1.0});
+  for (int a = 0; a < N; a++)
+    g.push_back({N + (int)sd.base[a], N + (int)sd.base[a + 1], N, 3,
+                 sd.G.as<double>(), 3LL * nd, 0, 1 + 3LL * a, 1.0});
+  for (int h = 0; h < 2; h++)
+    g.push_back({0, N, 0, 3, sd.W.as<double>(), 6LL * nd, 3 * h,
+                 1 + 3LL * N + 3 * h, 1.0 / sd.vol});
+  return g;
+}
+
+template <int C1, int C2>
+int ss_launch(const std::vector<std::pair<int, int>> &gps,
+              const std::vector<SsGroup> &h1, const std::vector<SsGroup> &h2,
+              const DevBuf &d1, const DevBuf &d2, const SsSide &s1,
+              const SsSide &s2, int nd, double xi, double sig2, long long ncol,
+              double *d_out, DevBuf &bad, cudaStream_t st) {
+  constexpr long long kChunk = 2048;   // item pairs per work item
+  std::vector<SsWork> work;
+  std::vector<SsPair> pairs;
+  for (const auto &gp : gps) {
+    const long long n = (long long)(h1[gp.first].end - h1[gp.first].beg) *
+                        (h2[gp.second].end - h2[gp.second].beg);
+    SsPair pr{gp.first, gp.second, (int)work.size(), 0};
+    for (long long p0 = 0; p0 < n; p0 += kChunk)
+      work.push_back({gp.first, gp.second, p0, std::min(n, p0 + kChunk)});
+    pr.w1 = (int)work.size();
+    pairs.push_back(pr);
+  }
+  if (pairs.empty()) return FGB_OK;
+  DevBuf dw, dp, part;
+  int rc;
+  if ((rc = dw.ensure(sizeof(SsWork) * (work.size() + 1))) ||
+      (rc = dp.ensure(sizeof(SsPair) * pairs.size())) ||
+      (rc = part.ensure(sizeof(double) * C1 * C2 * (work.size() + 1))))
+    return rc;
+  if (!work.empty())
+    FGB_CUDA(cudaMemcpyAsync(dw.p, work.data(), sizeof(SsWork) * work.size(),
+                             cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(dp.p, pairs.data(), sizeof(SsPair) * pairs.size(),
+                           cudaMemcpyHostToDevice, st));
+  if (!work.empty()) {
+    k_ss<C1, C2><<<(unsigned)work.size(), kDT, 0, st>>>(
+        dw.as<SsWork>(), d1.as<SsGroup>(), d2.as<SsGroup>(),
+        s1.item_row.as<int>(), s2.item_row.as<int>(), s1.dsrow.as<int>(),
+        s2.dsrow.as<int>(), s1.U.as<double>(), s2.U.as<double>(), nd, xi,
+        part.as<double>(), bad.as<int>());
+    FGB_LAUNCH_CHECK("k_ss");
+  }
+  const long long nt = (long long)pairs.size() * C1 * C2;
+  k_ss_final<C1, C2><<<ceil_div(nt, 256), 256, 0, st>>>(
+      (int)pairs.size(), dp.as<SsPair>(), d1.as<SsGroup>(), d2.as<SsGroup>(),
+      part.as<double>(), sig2, ncol, d_out);
+  FGB_LAUNCH_CHECK("k_ss_final");
+  // the work lists are freed on return
+  FGB_CUDA(cudaStreamSynchronize(st));
+  return FGB_OK;
+}
+
+}  // namespace
+
+int struc_struc_impl(const B2Params &p, double sigma, double power,
+                     fgb_nlist_s *nl1, const int *d_species1,
+                     fgb_nlist_s *nl2, const int *d_species2, double *d_out,
+                     cudaStream_t st) {
+  SsSide s1, s2;
+  int rc;
+  if ((rc = ss_prepare(p, nl1, d_species1, s1, st)) ||
+      (rc = ss_prepare(p, nl2, d_species2, s2, st)))
+    return rc;
+  const int nd = p.n_d;
+  const long long nrow = 1 + 3LL * s1.N + 6, ncol = 1 + 3LL * s2.N + 6;
+  FGB_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * nrow * ncol, st));
+  const std::vector<SsGroup> h1 = ss_groups(s1, nd), h2 = ss_groups(s2, nd);
+  DevBuf d1, d2, bad;
+  if ((rc = d1.ensure(sizeof(SsGroup) * h1.size())) ||
+      (rc = d2.ensure(sizeof(SsGroup) * h2.size())) ||
+      (rc = bad.ensure(sizeof(int))))
+    return rc;
+  FGB_CUDA(cudaMemcpyAsync(d1.p, h1.data(), sizeof(SsGroup) * h1.size(),
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemcpyAsync(d2.p, h2.data(), sizeof(SsGroup) * h2.size(),
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  // group pairs by component counts (energy groups have one component)
+  std::vector<std::pair<int, int>> gp11, gp13, gp31, gp33;
+  for (int a = 0; a < (int)h1.size(); a++)
+    for (int b = 0; b < (int)h2.size(); b++) {
+      const int c1 = h1[a].C, c2 = h2[b].C;
+      (c1 == 1 ? (c2 == 1 ? gp11 : gp13) : (c2 == 1 ? gp31 : gp33))
+          .push_back({a, b});
+    }
+  const double sig2 = sigma * sigma;
+  if ((rc = ss_launch<1, 1>(gp11, h1, h2, d1, d2, s1, s2, nd, power, sig2, ncol,
+                            d_out, bad, st)))
+    return rc;
+  int hbad = 0;
+  FGB_CUDA(cudaMemcpy(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (hbad) {
+    set_error("Dot product of descriptors is 0, and the negative power "
+              "function in force-force kernel diverges.");
+    return FGB_EINVAL;
+  }
+  if ((rc = ss_launch<1, 3>(gp13, h1, h2, d1, d2, s1, s2, nd, power, sig2, ncol,
+                            d_out, bad, st)) ||
+      (rc = ss_launch<3, 1>(gp31, h1, h2, d1, d2, s1, s2, nd, power, sig2, ncol,
+                            d_out, bad, st)) ||
+      (rc = ss_launch<3, 3>(gp33, h1, h2, d1, d2, s1, s2, nd, power, sig2, ncol,
+                            d_out, bad, st)))
+    return rc;
+  return FGB_OK;
+}
+
 }  // namespace fgb
 
 using namespace fgb;
@@ -499,3 +870,17 @@ extern "C" int fgb_self_kernel_struc(fgb_b2_t b2, double sigma, double power,
   return rc;
 }
 
+extern "C" int fgb_struc_struc(fgb_b2_t b2, double sigma, double power,
+                               fgb_nlist_t nl1, const int *d_species1,
+                               fgb_nlist_t nl2, const int *d_species2,
+                               double *d_out, void *stream) {
+  if (!b2 || !nl1 || !nl2 || !d_out) {
+    set_error("fgb_struc_struc: invalid arguments");
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = struc_struc_impl(b2->p, sigma, power, nl1, d_species1, nl2,
+                            d_species2, d_out, st);
+  if (!rc) FGB_CUDA(cudaStreamSynchronize(st));
+  return rc;
+}

@@ -394,6 +394,16 @@ int fgb_self_kernel_struc(fgb_b2_t b2, double sigma, double power,
                           fgb_nlist_t nl, const int *d_species, double *d_out,
                           void *stream);
 
+/* NormalizedDotProduct::struc_struc (normalized_dot_product.cpp:216-448)
+ * in FP64: the kernel between every output of structure 1 (energy, 3 N1
+ * force components, 6 stress components) and every output of structure 2,
+ * d_out[(1 + 3 N1 + 6) x (1 + 3 N2 + 6)] row-major.  Both lists are
+ * single-structure builds with the same B2 settings.  Errors as
+ * fgb_self_kernel_struc. */
+int fgb_struc_struc(fgb_b2_t b2, double sigma, double power, fgb_nlist_t nl1,
+                    const int *d_species1, fgb_nlist_t nl2,
+                    const int *d_species2, double *d_out, void *stream);
+
 /* Plain FP64 form of SparseGP::predict_local_uncertainties for one
  * structure: envs_struc (stored gradients), mean_efs = K^T alpha, and the
  * local variances via the envs_envs route.  d_mean_efs[1+3N+6],

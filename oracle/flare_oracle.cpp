@@ -18,6 +18,7 @@
 //   * B2 contraction + stored gradients   src/flare_pp/descriptors/b2.cpp:181-242
 //   * envs_struc kernel scatter loop      src/flare_pp/kernels/normalized_dot_product.cpp:117-214
 //   * self_kernel_struc (DTC prior)       src/flare_pp/kernels/normalized_dot_product.cpp:450-586
+//   * struc_struc                         src/flare_pp/kernels/normalized_dot_product.cpp:216-448
 //
 // Canonical floating-point order: built with -ffp-contract=off so that no
 // multiply-add is fused; wrapping and neighbour distances use the operation
@@ -611,6 +612,148 @@ int orc_self_kernel_block(int Ns, int n_atoms, const double *norms,
   if (bad) return -1;
   for (int i = 0; i < Ns; i++)
     for (long long c = 0; c < ncol; c++) out[c] += par[(size_t)i * ncol + c];
+  return 0;
+}
+
+// Structure-structure kernel block of one species
+// (normalized_dot_product.cpp:216-448): energy/energy, energy/force,
+// energy/stress and their transposes, force/force, force/stress,
+// stress/force and stress/stress entries of the (1 + 3 N1 + 6) x
+// (1 + 3 N2 + 6) row-major matrix `out`, accumulated in the reference's
+// loop order (i over structure 1, j over structure 2, then neighbour
+// entries).  dot_vals = D1 D2^T, force_dot_1 = dD1 D2^T (3P1 x N2s),
+// force_dot_2 = dD2 D1^T (3P2 x N1s), force_force = dD1 dD2^T (3P1 x 3P2).
+// Returns -1 where a dot product is below the empty threshold and
+// power < 2 (the reference throws invalid_argument).
+int orc_struc_struc_block(
+    int N1s, int N2s, int n_atoms_1, int n_atoms_2, const double *norms_1,
+    const double *norms_2, const double *dot_vals, const double *force_dot_1,
+    const double *force_dot_2, const double *force_force,
+    const double *sfd_1, const double *sfd_2, const int *nc_1,
+    const int *cn_1, const int *ai_1, const int *ni_1, const double *co_1,
+    const int *nc_2, const int *cn_2, const int *ai_2, const int *ni_2,
+    const double *co_2, double sig_sq, double power, double vol_inv_1,
+    double vol_inv_2, double *out) {
+  const double empty_thresh = 1e-8;
+  const long long n2 = 1 + 3LL * n_atoms_2 + 6;
+  const int stress_inds[3] = {0, 3, 5};
+  long long fc2 = 0;
+  for (int j = 0; j < N2s; j++) fc2 += nc_2[j];
+  fc2 *= 3;
+  auto K = [&](long long r, long long c) -> double & { return out[r * n2 + c]; };
+  const long long s1 = 1 + 3LL * n_atoms_1, s2 = 1 + 3LL * n_atoms_2;
+  for (int i = 0; i < N1s; i++) {
+    const double norm_i = norms_1[i];
+    if (norm_i < empty_thresh) continue;
+    const double norm_i2 = norm_i * norm_i, norm_i3 = norm_i2 * norm_i;
+    for (int j = 0; j < N2s; j++) {
+      const double norm_j = norms_2[j];
+      if (norm_j < empty_thresh) continue;
+      const double norm_j2 = norm_j * norm_j, norm_j3 = norm_j2 * norm_j;
+      const double norm_ij = norm_i * norm_j;
+      const double dv = dot_vals[(long long)i * N2s + j];
+      const double norm_dot = dv / norm_ij;
+      const double c1 = (power - 1) * power * std::pow(norm_dot, power - 2);
+      if (std::fabs(norm_dot) < empty_thresh && power < 2) return -1;
+      const double c2 = power * std::pow(norm_dot, power - 1);
+      K(0, 0) += sig_sq * std::pow(norm_dot, power);
+      const int n_neigh_1 = nc_1[i], c_neigh_1 = cn_1[i], c_ind_1 = ai_1[i];
+      const int n_neigh_2 = nc_2[j], c_neigh_2 = cn_2[j], c_ind_2 = ai_2[j];
+      // energy / force and energy / stress
+      for (int k = 0; k < n_neigh_2; k++) {
+        const long long ind = c_neigh_2 + k;
+        const int nb = ni_2[ind];
+        int sc = 0;
+        for (int comp = 0; comp < 3; comp++) {
+          const long long fi = 3 * ind + comp;
+          const double f1 = force_dot_2[fi * N1s + i] / norm_ij;
+          const double f2 = dv * sfd_2[fi] / (norm_i * norm_j3);
+          const double fk = sig_sq * c2 * (f1 - f2);
+          K(0, 1 + 3 * nb + comp) -= fk;
+          K(0, 1 + 3 * c_ind_2 + comp) += fk;
+          for (int comp2 = comp; comp2 < 3; comp2++) {
+            K(0, s2 + sc) -= fk * co_2[ind * 3 + comp2] * vol_inv_2;
+            sc++;
+          }
+        }
+      }
+      // force / energy and stress / energy
+      for (int k = 0; k < n_neigh_1; k++) {
+        const long long ind = c_neigh_1 + k;
+        const int nb = ni_1[ind];
+        int sc = 0;
+        for (int comp = 0; comp < 3; comp++) {
+          const long long fi = 3 * ind + comp;
+          const double f1 = force_dot_1[fi * N2s + j] / norm_ij;
+          const double f2 = dv * sfd_1[fi] / (norm_j * norm_i3);
+          const double fk = sig_sq * c2 * (f1 - f2);
+          K(1 + 3 * nb + comp, 0) -= fk;
+          K(1 + 3 * c_ind_1 + comp, 0) += fk;
+          for (int comp2 = comp; comp2 < 3; comp2++) {
+            K(s1 + sc, 0) -= fk * co_1[ind * 3 + comp2] * vol_inv_1;
+            sc++;
+          }
+        }
+      }
+      // force / force, force / stress, stress / force, stress / stress
+      for (int k = 0; k < n_neigh_1; k++) {
+        const long long ind1 = c_neigh_1 + k;
+        const int n_ind_1 = ni_1[ind1];
+        for (int l = 0; l < n_neigh_2; l++) {
+          const long long ind2 = c_neigh_2 + l;
+          const int n_ind_2 = ni_2[ind2];
+          for (int m = 0; m < 3; m++) {
+            const long long f_ind_1 = 3 * ind1 + m;
+            for (int n = 0; n < 3; n++) {
+              const long long f_ind_2 = 3 * ind2 + n;
+              const double v1 = force_dot_1[f_ind_1 * N2s + j] / norm_ij -
+                                norm_dot * sfd_1[f_ind_1] / norm_i2;
+              const double v2 = force_dot_2[f_ind_2 * N1s + i] / norm_ij -
+                                norm_dot * sfd_2[f_ind_2] / norm_j2;
+              const double v3 = force_force[f_ind_1 * fc2 + f_ind_2] / norm_ij;
+              const double v4 = sfd_1[f_ind_1] * force_dot_2[f_ind_2 * N1s + i] /
+                                (norm_i3 * norm_j);
+              const double v5 = sfd_2[f_ind_2] * force_dot_1[f_ind_1 * N2s + j] /
+                                (norm_i * norm_j3);
+              const double v6 = sfd_1[f_ind_1] * sfd_2[f_ind_2] * norm_dot /
+                                (norm_i2 * norm_j2);
+              const double kv =
+                  sig_sq * (c1 * v1 * v2 + c2 * (v3 - v4 - v5 + v6));
+              K(1 + c_ind_1 * 3 + m, 1 + c_ind_2 * 3 + n) += kv;
+              K(1 + c_ind_1 * 3 + m, 1 + n_ind_2 * 3 + n) -= kv;
+              K(1 + n_ind_1 * 3 + m, 1 + c_ind_2 * 3 + n) -= kv;
+              K(1 + n_ind_1 * 3 + m, 1 + n_ind_2 * 3 + n) += kv;
+              int si = stress_inds[m];
+              for (int p = m; p < 3; p++) {
+                const double x1 = co_1[ind1 * 3 + p];
+                K(s1 + si, 1 + c_ind_2 * 3 + n) -= kv * x1 * vol_inv_1;
+                K(s1 + si, 1 + n_ind_2 * 3 + n) += kv * x1 * vol_inv_1;
+                si++;
+              }
+              int sj = stress_inds[n];
+              for (int p = n; p < 3; p++) {
+                const double x2 = co_2[ind2 * 3 + p];
+                K(1 + c_ind_1 * 3 + m, s2 + sj) -= kv * x2 * vol_inv_2;
+                K(1 + n_ind_1 * 3 + m, s2 + sj) += kv * x2 * vol_inv_2;
+                sj++;
+              }
+              si = stress_inds[m];
+              for (int p = m; p < 3; p++) {
+                const double x1 = co_1[ind1 * 3 + p];
+                sj = stress_inds[n];
+                for (int q = n; q < 3; q++) {
+                  const double x2 = co_2[ind2 * 3 + q];
+                  K(s1 + si, s2 + sj) += kv * x1 * x2 * vol_inv_1 * vol_inv_2;
+                  sj++;
+                }
+                si++;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
   return 0;
 }
 

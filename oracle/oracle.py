@@ -76,6 +76,10 @@ def lib():
             ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, ip, ip, ip, ip, dp,
             ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
         L.orc_self_kernel_block.restype = ctypes.c_int
+        L.orc_struc_struc_block.argtypes = (
+            [ctypes.c_int] * 4 + [dp] * 8 + [ip, ip, ip, ip, dp] * 2 +
+            [ctypes.c_double] * 4 + [dp])
+        L.orc_struc_struc_block.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -370,6 +374,42 @@ class NormalizedDotProduct:
                 1.0 / struc.volume, _dp(K))
         return K
 
+
+    def struc_struc(self, struc1, struc2, hyps=None):
+        """Structure-structure kernel (normalized_dot_product.cpp:216-448):
+        (1 + 3 N1 + 6) x (1 + 3 N2 + 6), per species with dot_vals,
+        force_dot_1/2 and force_force precomputed as the reference does."""
+        sig = self.sigma if hyps is None else hyps[0]
+        out = np.zeros((1 + 3 * struc1.n_atoms + 6, 1 + 3 * struc2.n_atoms + 6))
+        c = np.ascontiguousarray
+        for s in range(struc1.n_types):
+            D1, D2 = c(struc1.descriptors[s]), c(struc2.descriptors[s])
+            if D1.shape[0] == 0 or D2.shape[0] == 0:
+                continue
+            f1, f2 = struc1.descriptor_force_dervs[s], struc2.descriptor_force_dervs[s]
+            side = []
+            for st in (struc1, struc2):
+                side += [c(st.descriptor_force_dots[s]),
+                         c(st.neighbor_counts[s], np.int32),
+                         c(st.cumulative_neighbor_counts[s], np.int32),
+                         c(st.atom_indices[s], np.int32),
+                         c(st.neighbor_indices[s], np.int32),
+                         c(st.neighbor_coordinates[s])]
+            args = [D1.shape[0], D2.shape[0], struc1.n_atoms, struc2.n_atoms,
+                    _dp(c(struc1.descriptor_norms[s])),
+                    _dp(c(struc2.descriptor_norms[s])), _dp(c(D1 @ D2.T)),
+                    _dp(c(f1 @ D2.T)), _dp(c(f2 @ D1.T)), _dp(c(f1 @ f2.T)),
+                    _dp(side[0]), _dp(side[6])]
+            for k in (0, 6):
+                args += [_ip(side[k + 1]), _ip(side[k + 2]), _ip(side[k + 3]),
+                         _ip(side[k + 4]), _dp(side[k + 5])]
+            args += [sig * sig, self.power, 1.0 / struc1.volume,
+                     1.0 / struc2.volume, _dp(out)]
+            if lib().orc_struc_struc_block(*args) != 0:
+                raise ValueError(
+                    "Dot product of descriptors is 0, and the negative power "
+                    "function in force-force kernel diverges.")
+        return out
 
     def self_kernel_struc(self, struc, hyps=None):
         """Prior variances of E, F, S (normalized_dot_product.cpp:450-586):

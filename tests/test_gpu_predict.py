@@ -269,3 +269,49 @@ def test_predict_dtc_matches_oracle():
     ks = ogp.kernels[0].self_kernel_struc(st.descriptors[0])
     np.testing.assert_allclose(g.variance_efs, st.variance_efs, rtol=0,
                                atol=1e-10 * np.abs(ks).max())
+
+
+@pytest.mark.parametrize("power", [2, 1])
+@pytest.mark.parametrize("multicut", [False, True])
+def test_struc_struc_matches_oracle(power, multicut):
+    """NormalizedDotProduct::struc_struc (normalized_dot_product.cpp:216-448)
+    between two 16-atom, 2-species cells against the oracle's restatement
+    of the reference loop: every energy, force and stress entry, FP64,
+    1e-10 of the largest entry."""
+    import flare_gb300 as fg
+    S = 2
+    cutoffs = (5.0 * np.ones((S, S)) + np.eye(S) - 1) if multicut else None
+    b2a = b2_args(S, 3, 2, 5.0, cutoffs=cutoffs)
+    (c1, sp1, p1), (c2, sp2, p2) = random_atoms(seed=21), random_atoms(seed=22)
+    sp2 = sp2[::-1].copy()
+    ob2 = oracle.B2Settings(*b2a)
+    o1 = oracle.Structure(c1, sp1, p1, 5.0, [ob2])
+    o2 = oracle.Structure(c2, sp2, p2, 5.0, [ob2])
+    ref = oracle.NormalizedDotProduct(1.3, power).struc_struc(
+        o1.descriptors[0], o2.descriptors[0])
+    calc = fg.B2(*b2a[:5], cutoffs=b2a[5])
+    got = fg.NormalizedDotProduct(1.3, power).struc_struc(
+        fg.Structure(c1, sp1, p1, 5.0, [calc]),
+        fg.Structure(c2, sp2, p2, 5.0, [calc]))
+    assert got.shape == ref.shape
+    np.testing.assert_allclose(got, ref, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())
+
+
+def test_struc_struc_fcc_different_sizes():
+    """struc_struc between a 32-atom and a 108-atom FCC cell (rc 4.5 A, one
+    species): rectangular blocks, distinct-atom neighbourhoods."""
+    import flare_gb300 as fg
+    b2a = b2_args(1, 5, 3, 4.5)
+    c1, sp1, p1 = syn.fcc_al(n_cells=2, seed=31)
+    c2, sp2, p2 = syn.fcc_al(n_cells=3, seed=32)
+    ob2 = oracle.B2Settings(*b2a)
+    ref = oracle.NormalizedDotProduct(2.0, 2).struc_struc(
+        oracle.Structure(c1, sp1, p1, 4.5, [ob2]).descriptors[0],
+        oracle.Structure(c2, sp2, p2, 4.5, [ob2]).descriptors[0])
+    calc = fg.B2(*b2a[:5], cutoffs=b2a[5])
+    got = fg.NormalizedDotProduct(2.0, 2).struc_struc(
+        fg.Structure(c1, sp1, p1, 4.5, [calc]),
+        fg.Structure(c2, sp2, p2, 4.5, [calc]))
+    np.testing.assert_allclose(got, ref, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())

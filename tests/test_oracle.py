@@ -218,3 +218,83 @@ def test_predict_dtc_variances_relation():
     q = np.einsum("ij,ij->j", km, ogp.Kuu_inverse @ km)
     np.testing.assert_allclose(dtc, ks - q + sor,
                                atol=1e-9 * np.abs(ks).max())
+
+
+def test_struc_struc_relations():
+    """struc_struc (normalized_dot_product.cpp:216-448) against the
+    reference's own kernel tests (ctests/test_kernels.cpp): the energy entry
+    is the sum of envs_envs over all atom pairs (:35-53), row 0 the column
+    sums of envs_struc (:55-75), the matrix of (s2, s1) the transpose of
+    (s1, s2), and force and stress entries the first and mixed second
+    differences of the energy entry under atom moves and cell strains
+    (:140-760; delta 1e-4 for first and 3e-4 for mixed second
+    differences)."""
+    b2 = oracle.B2Settings(*b2_args(2, 3, 2, 4.0))
+    k = oracle.NormalizedDotProduct(1.5, 2)
+    (c1, sp1, p1), (c2, sp2, p2) = random_atoms(seed=3), random_atoms(seed=4)
+    sp2 = sp2[::-1].copy()
+    st = lambda c, s, p, d=True: oracle.Structure(c, s, p, 4.0, [b2],
+                                                   compute_dervs=d)
+    s1, s2 = st(c1, sp1, p1), st(c2, sp2, p2)
+    K = k.struc_struc(s1.descriptors[0], s2.descriptors[0])
+    n1, n2 = len(sp1), len(sp2)
+    assert K.shape == (1 + 3 * n1 + 6, 1 + 3 * n2 + 6)
+    e1 = oracle.ClusterDescriptor.from_values(s1.descriptors[0])
+    e2 = oracle.ClusterDescriptor.from_values(s2.descriptors[0])
+    assert abs(K[0, 0] - k.envs_envs(e1, e2).sum()) < 1e-10 * abs(K[0, 0])
+    np.testing.assert_allclose(k.envs_struc(e1, s2.descriptors[0]).sum(0),
+                               K[0], rtol=0, atol=1e-10 * np.abs(K[0]).max())
+    Kt = k.struc_struc(s2.descriptors[0], s1.descriptors[0])
+    np.testing.assert_allclose(Kt.T, K, rtol=0, atol=1e-10 * np.abs(K).max())
+
+    def ee(ca, pa, cb, pb):
+        return k.struc_struc(st(ca, sp1, pa).descriptors[0],
+                             st(cb, sp2, pb).descriptors[0])[0, 0]
+
+    def move(p, a, m, d):
+        q = p.copy()
+        q[a, m] += d
+        return q
+
+    def strain(c, p, m, n, d):
+        F = np.eye(3)
+        F[m, n] += d
+        return c @ F.T, p @ F.T
+
+    h = 1e-4
+    # energy / force (structure 2's atom 5, y) and force / energy
+    fd = -(ee(c1, p1, c2, move(p2, 5, 1, h)) -
+           ee(c1, p1, c2, move(p2, 5, 1, -h))) / (2 * h)
+    assert abs(K[0, 1 + 3 * 5 + 1] - fd) < 1e-5 * max(1, abs(fd))
+    fd = -(ee(c1, move(p1, 2, 0, h), c2, p2) -
+           ee(c1, move(p1, 2, 0, -h), c2, p2)) / (2 * h)
+    assert abs(K[1 + 3 * 2, 0] - fd) < 1e-5 * max(1, abs(fd))
+    # energy / stress xy
+    vol2 = abs(np.linalg.det(c2))
+    fd = -(ee(c1, p1, *strain(c2, p2, 0, 1, h)) -
+           ee(c1, p1, *strain(c2, p2, 0, 1, -h))) / (2 * h)
+    assert abs(K[0, 1 + 3 * n2 + 1] * vol2 - fd) < 1e-5 * max(1, abs(fd))
+    # mixed second differences: h = 3e-4 (rounding grows as 1/h^2)
+    h = 3e-4
+    # force / force
+    for (a, m, b, n) in [(1, 0, 4, 2), (7, 2, 7, 2), (12, 1, 0, 0)]:
+        P1 = [move(p1, a, m, d) for d in (h, -h)]
+        P2 = [move(p2, b, n, d) for d in (h, -h)]
+        fd = (ee(c1, P1[0], c2, P2[0]) + ee(c1, P1[1], c2, P2[1]) -
+              ee(c1, P1[0], c2, P2[1]) - ee(c1, P1[1], c2, P2[0])) / (4 * h * h)
+        got = K[1 + 3 * a + m, 1 + 3 * b + n]
+        assert abs(got - fd) < 2e-5 * abs(fd) + 1e-6, (a, m, b, n, got, fd)
+    # force / stress (atom 3 z of 1, yz of 2) and stress / stress (xz, xz)
+    S2 = [strain(c2, p2, 1, 2, d) for d in (h, -h)]
+    P1 = [move(p1, 3, 2, d) for d in (h, -h)]
+    fd = (ee(c1, P1[0], *S2[0]) + ee(c1, P1[1], *S2[1]) -
+          ee(c1, P1[0], *S2[1]) - ee(c1, P1[1], *S2[0])) / (4 * h * h)
+    got = K[1 + 3 * 3 + 2, 1 + 3 * n2 + 4] * vol2
+    assert abs(got - fd) < 2e-5 * abs(fd) + 1e-6, (got, fd)
+    vol1 = abs(np.linalg.det(c1))
+    S1 = [strain(c1, p1, 0, 2, d) for d in (h, -h)]
+    S2 = [strain(c2, p2, 0, 2, d) for d in (h, -h)]
+    fd = (ee(*S1[0], *S2[0]) + ee(*S1[1], *S2[1]) -
+          ee(*S1[0], *S2[1]) - ee(*S1[1], *S2[0])) / (4 * h * h)
+    got = K[1 + 3 * n1 + 2, 1 + 3 * n2 + 2] * vol1 * vol2
+    assert abs(got - fd) < 2e-5 * abs(fd) + 1e-6, (got, fd)
