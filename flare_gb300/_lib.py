@@ -15,7 +15,9 @@ FGB_OK, FGB_EINVAL, FGB_ENOMEM, FGB_ECUDA, FGB_ETIMEOUT, FGB_ESTALE, \
 FGB_PREC_FP64, FGB_PREC_MIXED = 0, 1
 FGB_WANT_ENERGY, FGB_WANT_FORCES, FGB_WANT_STRESS, FGB_WANT_LOCAL_VAR = \
     1, 2, 4, 8
-RADIAL = {"chebyshev": 0}
+RADIAL = {"chebyshev": 0, "weighted_chebyshev": 1, "equispaced_gaussians": 2,
+          "weighted_positive_chebyshev": 3, "positive_chebyshev": 4,
+          "bessel": 5, "fourier_quarter": 6, "fourier_half": 7, "fourier": 8}
 CUTOFF = {"quadratic": 0, "hard": 1, "cosine": 2, "polynomial": 3, "power": 4}
 
 # Every symbol the header declares, with (restype, argtypes).

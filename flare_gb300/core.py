@@ -67,9 +67,9 @@ class B2:
         if self.cutoffs.shape != (S, S):
             raise ValueError("cutoffs must be n_species x n_species")
         if self.radial_basis not in _lib.RADIAL:
-            raise NotImplementedError(
-                f"radial basis {self.radial_basis!r} is not built "
-                f"(available: {sorted(_lib.RADIAL)})")
+            raise ValueError(
+                f"unknown radial basis {self.radial_basis!r} "
+                f"(radial.cpp:381-408 names: {sorted(_lib.RADIAL)})")
         if self.cutoff_function not in _lib.CUTOFF:
             raise ValueError(f"unknown cutoff function {self.cutoff_function!r}")
         self._handle = None

@@ -258,10 +258,18 @@ extern "C" int fgb_b2_create(fgb_b2_t *out, int radial_basis,
                              int n_cutoff_hyps, int n_species, int n_max,
                              int l_max, const double *h_cutoffs) {
   if (!out) { set_error("fgb_b2_create: null output"); return FGB_EINVAL; }
-  if (radial_basis != FGB_RADIAL_CHEBYSHEV) {
-    set_error("fgb_b2_create: radial basis %d not built (chebyshev only)",
+  if (radial_basis < FGB_RADIAL_CHEBYSHEV || radial_basis > FGB_RADIAL_FOURIER) {
+    set_error("fgb_b2_create: unknown radial basis %d", radial_basis);
+    return FGB_EINVAL;
+  }
+  const bool three = radial_basis == FGB_RADIAL_WEIGHTED_CHEBYSHEV ||
+                     radial_basis == FGB_RADIAL_EQUISPACED_GAUSSIANS ||
+                     radial_basis == FGB_RADIAL_WEIGHTED_POSITIVE_CHEBYSHEV ||
+                     radial_basis == FGB_RADIAL_FOURIER;
+  if (three && (n_radial_hyps < 3 || !radial_hyps)) {
+    set_error("fgb_b2_create: radial basis %d needs three radial_hyps",
               radial_basis);
-    return FGB_ENOTSUP;
+    return FGB_EINVAL;
   }
   if (cutoff_function < FGB_CUTOFF_QUADRATIC ||
       cutoff_function > FGB_CUTOFF_POWER) {
@@ -296,6 +304,7 @@ extern "C" int fgb_b2_create(fgb_b2_t *out, int radial_basis,
   p.n_A = p.n_rad * p.n_harm;
   p.n_d = p.n_rad * (p.n_rad + 1) / 2 * (l_max + 1);
   p.r1 = radial_hyps[0];
+  p.radial_hyp2 = n_radial_hyps > 2 ? radial_hyps[2] : 0.0;
   p.n_cutoff_hyps = n_cutoff_hyps < 4 ? n_cutoff_hyps : 4;
   for (int k = 0; k < p.n_cutoff_hyps; k++) p.cutoff_hyps[k] = cutoff_hyps[k];
   p.max_cutoff = 0;

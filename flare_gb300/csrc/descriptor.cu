@@ -428,13 +428,14 @@ size_t b2_adjoint_smem(const B2Params &p) {
 }
 
 // The descriptor sizes with compile-time specialisations (registers instead
-// of local memory for the per-pair basis values); others take the
-// runtime-sized kernels.
+// of local memory for the per-pair basis values; Chebyshev basis); others
+// take the runtime-sized kernels.
 template <template <typename, int, int> class K, typename T, typename F>
 static void dispatch_nl(const B2Params &p, F &&f) {
-  if (p.n_max == 8 && p.l_max == 4) f(K<T, 8, 4>{});
-  else if (p.n_max == 8 && p.l_max == 3) f(K<T, 8, 3>{});
-  else if (p.n_max == 10 && p.l_max == 6) f(K<T, 10, 6>{});
+  const bool cheb = p.radial_basis == FGB_RADIAL_CHEBYSHEV;
+  if (cheb && p.n_max == 8 && p.l_max == 4) f(K<T, 8, 4>{});
+  else if (cheb && p.n_max == 8 && p.l_max == 3) f(K<T, 8, 3>{});
+  else if (cheb && p.n_max == 10 && p.l_max == 6) f(K<T, 10, 6>{});
   else f(K<T, 0, 0>{});
 }
 

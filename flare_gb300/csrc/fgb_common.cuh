@@ -40,6 +40,7 @@ struct B2Params {
   int n_species, n_max, l_max;
   int n_harm, n_rad, n_A, n_d;
   double r1;             // radial_hyps[0]
+  double radial_hyp2;    // radial_hyps[2] (0 when absent)
   double cutoff_hyps[4];
   int n_cutoff_hyps;
   double cutoffs[kMaxSpecies * kMaxSpecies];   // per species pair
@@ -116,17 +117,142 @@ __device__ __forceinline__ void cutoff_eval(const B2Params &p, T r, T rc,
   fc = T(0); dfc = T(0);
 }
 
-// Chebyshev radial basis on x = (r - r1)/(rc - r1) (radial.cpp:138-169)
-// times the cutoff (radial.cpp:344-379).  Writes g[n] and dg/dr[n]
-// (radial derivative; Cartesian derivatives are dg/dr * x_k / r); dg may be
-// null.  NC > 0 fixes n_max at compile time (loops unrolled, arrays of the
-// caller kept in registers); NC = 0 reads it from p.
+// Conversions between the compute types and FP64 (the double-float type
+// adds its own in fgb_df.cuh).
+__device__ __forceinline__ double rad_to_double(double x) { return x; }
+__device__ __forceinline__ double rad_to_double(float x) { return (double)x; }
+template <typename T> __device__ __forceinline__ T rad_from_double(double x);
+template <> __device__ __forceinline__ double rad_from_double<double>(double x) {
+  return x;
+}
+template <> __device__ __forceinline__ float rad_from_double<float>(double x) {
+  return (float)x;
+}
+
+// The radial bases other than Chebyshev (radial.cpp:6-336), in FP64 for
+// every compute type: b[n] and db/dr[n] before the cutoff.  r2 is the pair
+// cutoff (the descriptor overwrites radial_hyps[1] with it, b2.cpp:352);
+// every basis but the Gaussians is zero outside [radial_hyps[0], r2].
+static __device__ __noinline__ void radial_basis_f64(const B2Params &p, double r,
+                                              double r2, int N, double *b,
+                                              double *db) {
+  const double r1 = p.r1, h2 = p.radial_hyp2;
+  for (int n = 0; n < N; n++) { b[n] = 0.0; db[n] = 0.0; }
+  switch (p.radial_basis) {
+    case FGB_RADIAL_EQUISPACED_GAUSSIANS: {
+      // width radial_hyps[0], centres from radial_hyps[1] to radial_hyps[2]
+      const double sigma = r1, first = r2, sep = h2 - r2;
+      const double norm = 1.0 / (sigma * sqrt(2.0 * kPi));
+      const double s2 = 1.0 / (sigma * sigma), hs2 = s2 / 2.0;
+      for (int n = 0; n < N; n++) {
+        const double mean = first + (n * sep / (N - 1));
+        const double d = r - mean;
+        b[n] = norm * exp(-hs2 * d * d);
+        db[n] = -s2 * b[n] * d;
+      }
+      return;
+    }
+    default: break;
+  }
+  if (r < r1 || r > r2) return;
+  switch (p.radial_basis) {
+    case FGB_RADIAL_POSITIVE_CHEBYSHEV: {
+      // (1 - T_n)/2; the reference's recurrence runs on the transformed
+      // values themselves (radial.cpp:195-206)
+      const double c = 1.0 / (r2 - r1), x = (r - r1) * c;
+      for (int n = 0; n < N; n++) {
+        if (n == 0) { b[n] = 1.0; db[n] = 0.0; continue; }
+        double t, dt;
+        if (n == 1) { t = x; dt = c; }
+        else {
+          t = 2.0 * x * b[n - 1] - b[n - 2];
+          dt = 2.0 * b[n - 1] * c + 2.0 * x * db[n - 1] - db[n - 2];
+        }
+        b[n] = 0.5 * (1.0 - t);
+        db[n] = -0.5 * dt;
+      }
+      return;
+    }
+    case FGB_RADIAL_WEIGHTED_CHEBYSHEV:
+    case FGB_RADIAL_WEIGHTED_POSITIVE_CHEBYSHEV: {
+      // T_n of the exponentially weighted coordinate (lambda = h2)
+      const bool pos = p.radial_basis == FGB_RADIAL_WEIGHTED_POSITIVE_CHEBYSHEV;
+      const double c = 1.0 / (r2 - r1), x = (r - r1) * c;
+      const double e = exp(-h2 * (x - 1.0)), lc = exp(h2) - 1.0;
+      const double xw = 1.0 - 2.0 * (e - 1.0) / lc, dxdr = 2.0 * c * h2 * e / lc;
+      double t0 = 1.0, d0 = 0.0, t1 = xw, d1 = 1.0;
+      for (int n = 0; n < N; n++) {
+        if (n == 0) { b[n] = 1.0; db[n] = 0.0; continue; }
+        double t, dt;
+        if (n == 1) { t = t1; dt = d1; }
+        else {
+          t = 2.0 * xw * t1 - t0;
+          dt = 2.0 * t1 + 2.0 * xw * d1 - d0;
+          t0 = t1; d0 = d1; t1 = t; d1 = dt;
+        }
+        if (pos) { b[n] = 0.5 * (1.0 - t); db[n] = -0.5 * dt * dxdr; }
+        else { b[n] = t; db[n] = dt * dxdr; }
+      }
+      return;
+    }
+    case FGB_RADIAL_BESSEL: {
+      const double c = r2 - r1, c1 = sqrt(2.0 / c), d = r - r1;
+      for (int n = 0; n < N; n++) {
+        const double a = kPi * (n + 1) * d, q = a / c, e = c * d * d;
+        b[n] = c1 * sin(q) / d;
+        db[n] = c1 * (a * cos(q) - c * sin(q)) / e;
+      }
+      return;
+    }
+    case FGB_RADIAL_FOURIER_QUARTER:
+    case FGB_RADIAL_FOURIER_HALF:
+    case FGB_RADIAL_FOURIER: {
+      // 1, cos(k w x), sin(k w x), ... with w = pi/2, pi or pi h2
+      const double c = 1.0 / (r2 - r1), x = (r - r1) * c;
+      const double w = p.radial_basis == FGB_RADIAL_FOURIER_QUARTER
+                           ? kPi / 2.0
+                           : (p.radial_basis == FGB_RADIAL_FOURIER_HALF
+                                  ? kPi : kPi * h2);
+      int kc = 1, ks = 1;
+      for (int n = 0; n < N; n++) {
+        if (n == 0) { b[n] = 1.0; db[n] = 0.0; }
+        else if (n % 2 == 1) {
+          const double a = w * kc++;
+          b[n] = cos(a * x); db[n] = -sin(a * x) * a * c;
+        } else {
+          const double a = w * ks++;
+          b[n] = sin(a * x); db[n] = cos(a * x) * a * c;
+        }
+      }
+      return;
+    }
+    default: return;
+  }
+}
+
+// Radial basis on x = (r - r1)/(rc - r1) times the cutoff (radial.cpp:
+// 344-379): Chebyshev (radial.cpp:138-169) in the compute type T, the
+// other bases through radial_basis_f64.  Writes g[n] and dg/dr[n] (radial
+// derivative; Cartesian derivatives are dg/dr * x_k / r); dg may be null.
+// NC > 0 fixes n_max at compile time (loops unrolled, arrays of the caller
+// kept in registers) and is used for the Chebyshev basis only; NC = 0 reads
+// n_max from p.
 template <typename T, int NC = 0>
 __device__ __forceinline__ void radial_eval(const B2Params &p, T r, T rc,
                                             T *g, T *dg) {
   T fc, dfc;
   cutoff_eval<T>(p, r, rc, fc, dfc);
   const int N = NC > 0 ? NC : p.n_max;
+  if (NC == 0 && p.radial_basis != FGB_RADIAL_CHEBYSHEV) {
+    double b[kMaxNmax], db[kMaxNmax];
+    radial_basis_f64(p, rad_to_double(r), rad_to_double(rc), N, b, db);
+    for (int n = 0; n < N; n++) {
+      const T bn = rad_from_double<T>(b[n]);
+      g[n] = bn * fc;
+      if (dg) dg[n] = rad_from_double<T>(db[n]) * fc + bn * dfc;
+    }
+    return;
+  }
   T r1 = T(p.r1);
   if (r < r1 || r > rc) {
 #pragma unroll

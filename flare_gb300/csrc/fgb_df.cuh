@@ -179,6 +179,8 @@ __device__ __forceinline__ df sin(df a) { return df_from_double(::sin(to_double(
 __device__ __forceinline__ df pow(df a, df b) {
   return df_from_double(::pow(to_double(a), to_double(b)));
 }
+// radial bases other than Chebyshev are evaluated in FP64
+__device__ __forceinline__ double rad_to_double(df a) { return to_double(a); }
 
 }  // namespace dfm
 using dfm::df;
@@ -188,5 +190,8 @@ using dfm::f2d_exact;
 using dfm::two_sum;
 using dfm::fast_two_sum;
 __device__ __forceinline__ double to_double(double a) { return a; }
+template <> __device__ __forceinline__ df rad_from_double<df>(double x) {
+  return dfm::df_from_double(x);
+}
 
 }  // namespace fgb

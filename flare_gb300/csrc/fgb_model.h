@@ -112,6 +112,9 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
                     cudaStream_t st, bool fixed = false,
                     const ChunkHook *after_chunk = nullptr);
+// The folded matrices and the fold guard (force_f64) of a power-1/2 model,
+// built once before its first mixed prediction (synchronises).
+int prepare_mixed(fgb_model_s *m, cudaStream_t st);
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
                        double *d_gB2, double *d_var, cudaStream_t st,

@@ -134,8 +134,8 @@ struct fgb_mapped_s {
   int power = 2;
   bool normalized = true;
   bool has_var = false;
-  // mixed precision: FP32 adjoint unless the largest |beta| exceeds the
-  // fold guard's threshold (then the adjoint stays FP64)
+  // mixed precision: double-float descriptor and FP32 adjoint unless the
+  // largest |beta| exceeds the fold guard's threshold (then both FP64)
   bool adjoint_f64 = false;
   DevBuf beta;                                        // FP64, per species
   std::vector<std::unique_ptr<oz::Sliced>> ozBeta;    // power 2: beta_s rows
@@ -293,7 +293,7 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   }
   if ((rc = launch_b2_forward(p, &m->nl, d_species, ws.A.as<double>(),
                               ws.B2.as<double>(), ws.norms.as<double>(), st,
-                              mixed)))
+                              mixed && !m->adjoint_f64)))
     return rc;
   std::vector<int> counts;
   if ((rc = species_permutation(S, ws, d_species, N, counts, st))) return rc;

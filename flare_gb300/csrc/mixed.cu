@@ -267,6 +267,12 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
   return FGB_OK;
 }
 
+int prepare_mixed(fgb_model_s *m, cudaStream_t st) {
+  if ((m->power == 2.0 || m->power == 1.0) && !m->bmap_ready)
+    return build_fold(m, st);
+  return FGB_OK;
+}
+
 int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        bool want_grad, bool want_var, double *d_e_atom,
                        double *d_gB2, double *d_var, cudaStream_t st,

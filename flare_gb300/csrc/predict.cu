@@ -609,12 +609,16 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     if (want_grad)
       FGB_CUDA(cudaMemsetAsync(m->ws.gB2.p, 0, sizeof(double) * (size_t)N * p.n_d, st));
   }
+  // the fold guard is known before the descriptor: models with large folded
+  // coefficients take the descriptor, force product and adjoint at FP64
+  // level (a fixed call reuses the full call's fold)
+  if (mixed && !fixed && (rc = prepare_mixed(m, st))) return rc;
   {
     StageTimer _pt(kStB2Forward, st);
     // mixed precision: the descriptor in double-float (about 46 bits)
     if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
                                 m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-                                st, precision == FGB_PREC_MIXED)))
+                                st, mixed && !m->force_f64)))
       return rc;
   }
   std::vector<int> counts;

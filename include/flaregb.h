@@ -38,7 +38,17 @@ enum {
 };
 
 /* radial bases (radial.cpp:381-408) and cutoffs (cutoffs.cpp:87-103) */
-enum { FGB_RADIAL_CHEBYSHEV = 0 };
+enum {
+  FGB_RADIAL_CHEBYSHEV = 0,
+  FGB_RADIAL_WEIGHTED_CHEBYSHEV = 1,          /* radial_hyps[2] = lambda */
+  FGB_RADIAL_EQUISPACED_GAUSSIANS = 2,        /* [sigma, first, final]   */
+  FGB_RADIAL_WEIGHTED_POSITIVE_CHEBYSHEV = 3, /* radial_hyps[2] = lambda */
+  FGB_RADIAL_POSITIVE_CHEBYSHEV = 4,
+  FGB_RADIAL_BESSEL = 5,
+  FGB_RADIAL_FOURIER_QUARTER = 6,
+  FGB_RADIAL_FOURIER_HALF = 7,
+  FGB_RADIAL_FOURIER = 8                      /* radial_hyps[2] = factor */
+};
 enum {
   FGB_CUTOFF_QUADRATIC = 0,
   FGB_CUTOFF_HARD = 1,
@@ -269,9 +279,9 @@ int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream);
 /* The mixed path's force-precision guard for a solved power-1 or power-2
  * model: h_fold_max = the largest |sigma^2 sum_t alpha_t s^_t s^_t^T| entry
  * (power 1: of the vector), h_fp64_forces = 1 when it exceeds 200 and the
- * mixed path's force stage (force product, mapped gradient, B2 adjoint)
- * therefore runs at FP64 level, 0 when it runs at FP32 level.  Either may
- * be NULL. */
+ * mixed path's descriptor and force stage (force product, mapped gradient,
+ * B2 adjoint) therefore run at FP64 level, 0 when they run in double-float
+ * and at FP32 level.  Either may be NULL. */
 int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
                          int *h_fp64_forces, void *stream);
 

@@ -8,7 +8,7 @@
 // What is restated, and from where (paths inside mir-group/flare):
 //   * cell algebra, wrapping, sweep      src/flare_pp/structure.cpp:7-43,120-165
 //   * brute-force neighbour list          src/flare_pp/structure.cpp:52-118
-//   * Chebyshev radial basis              src/flare_pp/radial.cpp:138-169
+//   * radial bases (all nine)             src/flare_pp/radial.cpp:6-336,381-408
 //   * radial x cutoff product             src/flare_pp/radial.cpp:344-379
 //   * cutoff functions                    src/flare_pp/cutoffs.cpp:7-85
 //   * real spherical harmonics + grads    src/flare_pp/y_grad.cpp:667-2754
@@ -232,19 +232,92 @@ static void cutoff_fn(int id, double r, double rc, const double *ch, int nch,
   *v = 0; *dv = 0;
 }
 
+// Radial bases (radial.cpp:6-336), ids in the order of set_radial_basis
+// (radial.cpp:381-408): 0 chebyshev, 1 weighted_chebyshev,
+// 2 equispaced_gaussians, 3 weighted_positive_chebyshev,
+// 4 positive_chebyshev, 5 bessel, 6 fourier_quarter, 7 fourier_half,
+// 8 fourier.  Hyperparameters (h0, r2, h2) are radial_hyps[0], the pair
+// cutoff (the B2 descriptor overwrites radial_hyps[1] with it, b2.cpp:352)
+// and radial_hyps[2].  Values and radial derivatives; zero outside the
+// support [h0, r2] of every basis but the Gaussians.
 static void radial_fn(int id, double r, int N, double r1, double r2,
-                      double *g, double *dg) {
+                      double h2, double *g, double *dg) {
   for (int n = 0; n < N; n++) { g[n] = 0; dg[n] = 0; }
+  if (id == 2) {
+    // Gaussians of width h0 centred from radial_hyps[1] to radial_hyps[2]
+    const double sigma = r1, first = r2, sep = h2 - r2;
+    const double norm = 1 / (sigma * std::sqrt(2 * kPi));
+    const double s2 = 1 / (sigma * sigma), hs2 = s2 / 2;
+    for (int n = 0; n < N; n++) {
+      const double mean = first + (n * sep / (N - 1));
+      const double d = r - mean;
+      g[n] = norm * std::exp(-hs2 * d * d);
+      dg[n] = -s2 * g[n] * d;
+    }
+    return;
+  }
   if (r < r1 || r > r2) return;
-  if (id == 0) {
-    double c = 1 / (r2 - r1);
-    double x = (r - r1) * c;
+  if (id == 0 || id == 4) {
+    // Chebyshev polynomials T_n(x), x = (r - r1)/(r2 - r1); the positive
+    // variant is (1 - T_n)/2 with the reference's recurrence, which runs on
+    // the transformed values themselves (radial.cpp:195-206)
+    const double c = 1 / (r2 - r1), x = (r - r1) * c;
+    for (int n = 0; n < N; n++) {
+      if (n == 0) { g[n] = 1; dg[n] = 0; continue; }
+      double t, dt;
+      if (n == 1) { t = x; dt = c; }
+      else {
+        t = 2 * x * g[n - 1] - g[n - 2];
+        dt = 2 * g[n - 1] * c + 2 * x * dg[n - 1] - dg[n - 2];
+      }
+      if (id == 0) { g[n] = t; dg[n] = dt; }
+      else { g[n] = 0.5 * (1 - t); dg[n] = -0.5 * dt; }
+    }
+    return;
+  }
+  if (id == 1 || id == 3) {
+    // Chebyshev polynomials of an exponentially weighted coordinate
+    const double c = 1 / (r2 - r1), x = (r - r1) * c;
+    const double e = std::exp(-h2 * (x - 1)), lc = std::exp(h2) - 1;
+    const double xw = 1 - 2 * (e - 1) / lc, dxdr = 2 * c * h2 * e / lc;
+    double t0 = 1, d0 = 0, t1 = xw, d1 = 1;
+    for (int n = 0; n < N; n++) {
+      double t, dt;
+      if (n == 0) { g[n] = 1; dg[n] = 0; continue; }
+      if (n == 1) { t = t1; dt = d1; }
+      else {
+        t = 2 * xw * t1 - t0;
+        dt = 2 * t1 + 2 * xw * d1 - d0;
+        t0 = t1; d0 = d1; t1 = t; d1 = dt;
+      }
+      if (id == 1) { g[n] = t; dg[n] = dt * dxdr; }
+      else { g[n] = 0.5 * (1 - t); dg[n] = -0.5 * dt * dxdr; }
+    }
+    return;
+  }
+  if (id == 5) {
+    // spherical Bessel functions of order zero, zeros at r2
+    const double c = r2 - r1, c1 = std::sqrt(2 / c), d = r - r1;
+    for (int n = 0; n < N; n++) {
+      const double a = kPi * (n + 1) * d, b = a / c, e = c * d * d;
+      g[n] = c1 * std::sin(b) / d;
+      dg[n] = c1 * (a * std::cos(b) - c * std::sin(b)) / e;
+    }
+    return;
+  }
+  if (id >= 6 && id <= 8) {
+    // 1, cos(k w x), sin(k w x), ... with w = pi/2, pi or pi h2
+    const double c = 1 / (r2 - r1), x = (r - r1) * c;
+    const double w = id == 6 ? kPi / 2 : (id == 7 ? kPi : kPi * h2);
+    int kc = 1, ks = 1;
     for (int n = 0; n < N; n++) {
       if (n == 0) { g[n] = 1; dg[n] = 0; }
-      else if (n == 1) { g[n] = x; dg[n] = c; }
-      else {
-        g[n] = 2 * x * g[n - 1] - g[n - 2];
-        dg[n] = 2 * g[n - 1] * c + 2 * x * dg[n - 1] - dg[n - 2];
+      else if (n % 2 == 1) {
+        const double a = w * kc++;
+        g[n] = std::cos(a * x); dg[n] = -std::sin(a * x) * a * c;
+      } else {
+        const double a = w * ks++;
+        g[n] = std::sin(a * x); dg[n] = std::cos(a * x) * a * c;
       }
     }
   }
@@ -253,12 +326,13 @@ static void radial_fn(int id, double r, int N, double r1, double r2,
 // Radial x cutoff with Cartesian gradients (radial.cpp:344-379).
 // out: g[N], gx[N], gy[N], gz[N]
 void orc_radial(int radial_id, int cutoff_id, double x, double y, double z,
-                double r, double rc, int N, double r1, const double *ch,
-                int nch, double *g, double *gx, double *gy, double *gz) {
+                double r, double rc, int N, double r1, double h2,
+                const double *ch, int nch, double *g, double *gx, double *gy,
+                double *gz) {
   double fc, dfc;
   cutoff_fn(cutoff_id, r, rc, ch, nch, &fc, &dfc);
   std::vector<double> b(N), db(N);
-  radial_fn(radial_id, r, N, r1, rc, b.data(), db.data());
+  radial_fn(radial_id, r, N, r1, rc, h2, b.data(), db.data());
   double xr = x / r, yr = y / r, zr = z / r;
   for (int n = 0; n < N; n++) {
     g[n] = b[n] * fc;
@@ -347,7 +421,8 @@ void orc_ylm(double x, double y, double z, int L, double *Y, double *Yx,
 // Two-phase: call with B2 == nullptr to get Pb (return value).
 long long orc_b2(int n, const int *species, const int *counts,
                  const double *rel, const int *idx, int radial_id,
-                 int cutoff_id, double r1, const double *cutoff_hyps, int nch,
+                 int cutoff_id, double r1, double h2, const double *cutoff_hyps,
+                 int nch,
                  int S, int N, int L, const double *cutoffs, int *b2_count,
                  int *b2_idx, double *b2_coords, double *single_bond,
                  double *B2, double *norms, double *dervs,
@@ -396,7 +471,7 @@ long long orc_b2(int n, const int *species, const int *counts,
       b2_coords[3 * bp + 0] = x;
       b2_coords[3 * bp + 1] = y;
       b2_coords[3 * bp + 2] = z;
-      orc_radial(radial_id, cutoff_id, x, y, z, r, rc, N, r1, cutoff_hyps,
+      orc_radial(radial_id, cutoff_id, x, y, z, r, rc, N, r1, h2, cutoff_hyps,
                  nch, g.data(), gx.data(), gy.data(), gz.data());
       orc_ylm(x, y, z, L, h.data(), hx.data(), hy.data(), hz.data());
       int col = sj * N * nh;

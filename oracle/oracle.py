@@ -28,7 +28,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle.so")
 _lib = None
 
-RADIAL_IDS = {"chebyshev": 0}
+RADIAL_IDS = {"chebyshev": 0, "weighted_chebyshev": 1,
+              "equispaced_gaussians": 2, "weighted_positive_chebyshev": 3,
+              "positive_chebyshev": 4, "bessel": 5, "fourier_quarter": 6,
+              "fourier_half": 7, "fourier": 8}
 CUTOFF_IDS = {"quadratic": 0, "hard": 1, "cosine": 2, "polynomial": 3, "power": 4}
 
 
@@ -59,12 +62,13 @@ def lib():
         L.orc_radial.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double, ctypes.c_int,
-                                 ctypes.c_double, dp, ctypes.c_int, dp, dp, dp,
-                                 dp]
+                                 ctypes.c_double, ctypes.c_double, dp,
+                                 ctypes.c_int, dp, dp, dp, dp]
         L.orc_ylm.argtypes = [ctypes.c_double] * 3 + [ctypes.c_int, dp, dp, dp,
                                                       dp]
         L.orc_b2.argtypes = [ctypes.c_int, ip, ip, dp, ip, ctypes.c_int,
-                             ctypes.c_int, ctypes.c_double, dp, ctypes.c_int,
+                             ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                             dp, ctypes.c_int,
                              ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ip,
                              ip, dp, dp, dp, dp, dp, dp]
         L.orc_b2.restype = ctypes.c_longlong
@@ -104,13 +108,13 @@ def ylm(x, y, z, lmax):
 
 
 def radial(radial_basis, cutoff_function, x, y, z, r, rcut, nmax, r1=0.0,
-           cutoff_hyps=()):
+           cutoff_hyps=(), h2=0.0):
     ch = np.asarray(cutoff_hyps, dtype=np.float64).reshape(-1)
     if ch.size == 0:
         ch = np.zeros(1)
     out = [np.zeros(nmax) for _ in range(4)]
     lib().orc_radial(RADIAL_IDS[radial_basis], CUTOFF_IDS[cutoff_function], x,
-                     y, z, r, rcut, nmax, r1, _dp(ch), len(cutoff_hyps),
+                     y, z, r, rcut, nmax, r1, h2, _dp(ch), len(cutoff_hyps),
                      *[_dp(o) for o in out])
     return out
 
@@ -240,7 +244,9 @@ class Structure:
         args_pre = (n, _ip(sp), _ip(self.neighbor_count),
                     _dp(self.relative_positions), _ip(self.structure_indices),
                     RADIAL_IDS[b2.radial_basis], CUTOFF_IDS[b2.cutoff_function],
-                    b2.radial_hyps[0], _dp(ch), len(b2.cutoff_hyps), S, N, Lm,
+                    b2.radial_hyps[0],
+                    b2.radial_hyps[2] if len(b2.radial_hyps) > 2 else 0.0,
+                    _dp(ch), len(b2.cutoff_hyps), S, N, Lm,
                     _dp(b2.cutoffs))
         Pb = L.orc_b2(*args_pre, _ip(b2_count), None, None, None, None, None,
                       None, None)

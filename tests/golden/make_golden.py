@@ -61,11 +61,40 @@ def main():
                                      *[b.ctypes.data_as(dp) for b in bufs])
             out[i] = np.stack(bufs)
         R[name] = out
+
+    # Every radial basis (radial.cpp:6-336) with the quadratic cutoff, the
+    # hyperparameters as the B2 descriptor passes them: radial_hyps[1]
+    # replaced by the pair cutoff (b2.cpp:352).
+    basis_cases = [("chebyshev", [0.5, rcut]),
+                   ("weighted_chebyshev", [0.5, rcut, 3.0]),
+                   ("equispaced_gaussians", [0.5, rcut, 0.8]),
+                   ("weighted_positive_chebyshev", [0.5, rcut, 3.0]),
+                   ("positive_chebyshev", [0.5, rcut]),
+                   ("bessel", [0.0, rcut]),
+                   ("fourier_quarter", [0.5, rcut]),
+                   ("fourier_half", [0.5, rcut]),
+                   ("fourier", [0.5, rcut, 0.75])]
+    B = {}
+    zero = np.zeros(1)
+    for name, rh in basis_cases:
+        out = np.zeros((48, 4, N))
+        rha = np.asarray(rh, dtype=np.float64)
+        for i in range(48):
+            x, y, z = rpts[i]
+            bufs = [np.zeros(N) for _ in range(4)]
+            lib.ref_calculate_radial(name.encode(), b"quadratic", x, y, z,
+                                     rr[i], rcut, N, rha.ctypes.data_as(dp),
+                                     len(rh), zero.ctypes.data_as(dp), 0,
+                                     *[b.ctypes.data_as(dp) for b in bufs])
+            out[i] = np.stack(bufs)
+        B[name] = out
     np.savez_compressed(
         os.path.join(HERE, "per_pair.npz"), ylm_points=pts, ylm_lmax=L,
         ylm=Y, radial_points=rpts, radial_r=rr, radial_rcut=rcut,
         radial_nmax=N, **{f"radial_{k}": v for k, v in R.items()},
-        **{f"cutoff_hyps_{k}": np.asarray(ch) for k, ch in cut_cases})
+        **{f"cutoff_hyps_{k}": np.asarray(ch) for k, ch in cut_cases},
+        **{f"basis_{k}": v for k, v in B.items()},
+        **{f"basis_hyps_{k}": np.asarray(rh) for k, rh in basis_cases})
     print("wrote per_pair.npz")
 
 

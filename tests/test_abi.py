@@ -39,9 +39,17 @@ def test_b2_create_rejects_bad_settings(flaregb_lib):
                                    11, None)
     assert rc == _lib.FGB_EINVAL
     assert b"l_max" in flaregb_lib.fgb_last_error()
-    rc = flaregb_lib.fgb_b2_create(ctypes.byref(h), 7, 0, rh, 2, None, 0, 1, 8,
+    rc = flaregb_lib.fgb_b2_create(ctypes.byref(h), 9, 0, rh, 2, None, 0, 1, 8,
                                    3, None)
-    assert rc == _lib.FGB_ENOTSUP
+    assert rc == _lib.FGB_EINVAL
+    # weighted Chebyshev needs lambda = radial_hyps[2]
+    rc = flaregb_lib.fgb_b2_create(ctypes.byref(h), 1, 0, rh, 2, None, 0, 1, 8,
+                                   3, None)
+    assert rc == _lib.FGB_EINVAL
+    rc = flaregb_lib.fgb_b2_create(ctypes.byref(h), 5, 0, rh, 2, None, 0, 1, 8,
+                                   3, None)
+    assert rc == _lib.FGB_OK
+    assert flaregb_lib.fgb_b2_destroy(h) == 0
     rc = flaregb_lib.fgb_b2_create(ctypes.byref(h), 0, 0, rh, 2, None, 0, 1, 8,
                                    3, None)
     assert rc == _lib.FGB_OK
@@ -50,7 +58,7 @@ def test_b2_create_rejects_bad_settings(flaregb_lib):
 
 def test_python_errors_map_to_reference_exceptions():
     import flare_gb300 as fg
-    with pytest.raises(NotImplementedError):
-        fg.B2("bessel", "quadratic", [0, 5], [], [1, 8, 3])
+    with pytest.raises(ValueError):
+        fg.B2("legendre", "quadratic", [0, 5], [], [1, 8, 3])
     with pytest.raises(ValueError):
         fg.B2("chebyshev", "quadratic", [0, 5], [], [1, 8])

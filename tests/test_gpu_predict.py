@@ -315,3 +315,55 @@ def test_struc_struc_fcc_different_sizes():
         fg.Structure(c2, sp2, p2, 4.5, [calc]))
     np.testing.assert_allclose(got, ref, rtol=0,
                                atol=1e-10 * np.abs(ref).max())
+
+
+BASES = [("chebyshev", [0.5, 5.0]), ("weighted_chebyshev", [0.5, 5.0, 3.0]),
+         ("equispaced_gaussians", [0.6, 5.0, 0.8]),
+         ("weighted_positive_chebyshev", [0.5, 5.0, 3.0]),
+         ("positive_chebyshev", [0.5, 5.0]), ("bessel", [0.0, 5.0]),
+         ("fourier_quarter", [0.5, 5.0]), ("fourier_half", [0.5, 5.0]),
+         ("fourier", [0.5, 5.0, 0.75])]
+
+
+@pytest.mark.parametrize("basis,rh", BASES, ids=[b for b, _ in BASES])
+def test_radial_bases_predict_matches_oracle(basis, rh):
+    """Every radial basis of radial.cpp:6-336 through the whole path: a
+    2-species model (per-pair cutoffs 4.5 / 5.0, so radial_hyps[1] is
+    overwritten per pair as in b2.cpp:352) trained by the oracle, then B2,
+    energy, forces, stress and local variance in FP64 against the oracle,
+    and the mixed path within its budget."""
+    import flare_gb300 as fg
+    from helpers import lj_labels, oracle_model
+    S = 2
+    cut = np.array([[5.0, 4.5], [4.5, 5.0]])
+    b2a = (basis, "quadratic", rh, [], [S, 4, 2], cut)
+    strucs, labels, sparse = [], [], []
+    for t in range(2):
+        c, s_, p_ = random_atoms(seed=600 + t)
+        strucs.append((c, s_, p_))
+        labels.append(lj_labels(c, s_, p_, S))
+        sparse.append([0, 3, 5, 8, 12])
+    ogp, _ = oracle_model(strucs, labels, sparse, b2a, sigma=1.4, power=2,
+                          noise=(0.3, 0.2, 0.4))
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    cell, sp, pos = random_atoms(seed=650)
+    o = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    g = fg.Structure(cell, sp, pos, 5.0, [calc])
+    B, _ = g.b2_values()
+    ob = o.descriptors[0].atom_B2
+    np.testing.assert_allclose(B.cpu().numpy(), ob, rtol=1e-11,
+                               atol=1e-12 * np.abs(ob).max())
+    E, F, Sg, V = oracle_predict(ogp, b2a, cell, sp, pos)
+    a = gpu_predict(ggp, calc, [(cell, sp, pos)])
+    assert abs(a["energy"][0] - E) <= 1e-9 * max(1, abs(E))
+    Fs = max(1.0, np.abs(F).max())
+    np.testing.assert_allclose(a["forces"], F, rtol=0, atol=1e-8 * Fs)
+    np.testing.assert_allclose(a["stress"][0], Sg, rtol=0,
+                               atol=1e-9 * max(1.0, np.abs(Sg).max()))
+    np.testing.assert_allclose(a["local_var"], V, rtol=0, atol=1e-9)
+    # mixed: this tiny-cell model is far from physical (|E| ~ 1e9 eV, forces
+    # ~1e5 eV/A), so both bounds also carry a term relative to the values,
+    # as the FP64 bounds above do
+    b = gpu_predict(ggp, calc, [(cell, sp, pos)], precision="mixed")
+    assert abs(b["energy"][0] - E) <= 1e-6 * len(sp) + 1e-11 * abs(E)
+    assert np.abs(b["forces"] - F).mean() <= 1e-4 + 1e-9 * Fs

@@ -36,6 +36,27 @@ def test_radial_matches_reference_golden(cut):
         np.testing.assert_array_equal(mine, g["radial_" + cut][i])
 
 
+BASES = ["chebyshev", "weighted_chebyshev", "equispaced_gaussians",
+         "weighted_positive_chebyshev", "positive_chebyshev", "bessel",
+         "fourier_quarter", "fourier_half", "fourier"]
+
+
+@pytest.mark.parametrize("basis", BASES)
+def test_radial_bases_match_reference_golden(basis):
+    """Every radial basis (radial.cpp:6-336) times the quadratic cutoff,
+    against the reference's own compiled functions; the same operations in
+    the same order, so within a few units of the last place."""
+    g = np.load(GOLD)
+    rh = list(g["basis_hyps_" + basis])
+    ref = g["basis_" + basis]
+    for i, p in enumerate(g["radial_points"]):
+        mine = np.stack(oracle.radial(
+            basis, "quadratic", *p, g["radial_r"][i], rh[1],
+            int(g["radial_nmax"]), rh[0], [], rh[2] if len(rh) > 2 else 0.0))
+        np.testing.assert_allclose(mine, ref[i], rtol=1e-13,
+                                   atol=1e-13 * max(1.0, np.abs(ref[i]).max()))
+
+
 def test_ylm_gradient_finite_difference():
     """test_y_grad.cpp: gradients against central differences."""
     r = np.random.Generator(np.random.PCG64(5))
