@@ -375,6 +375,20 @@ def run_ours(args, rank, world, local):
     h2d = pos.nbytes + sp.nbytes + cells.nbytes + offsets.nbytes
     d2h = 8 * (B + 3 * N + 6 * B + N)
 
+    guard = None
+    if args.precision == "mixed":
+        import ctypes
+        fmax, f64 = ctypes.c_double(0.0), ctypes.c_int(0)
+        sl, est = ctypes.c_int(0), ctypes.c_double(0.0)
+        _lib.check(L.fgb_model_mixed_plan(model.h, ctypes.byref(sl),
+                                          ctypes.byref(est), ctypes.byref(fmax),
+                                          ctypes.byref(f64), sptr))
+        guard = {"kernel_slices": sl.value,
+                 "slice_err_ev_per_atom": est.value,
+                 "fold_max": fmax.value,
+                 "force_stage": "fp64-level" if f64.value else "fp32-level",
+                 "fold_threshold": 200.0}
+
     # ---- dominant kernel roofline
     sizes = species_sizes(sp, offsets, gp)
     nd_ = b2.n_descriptors
@@ -393,9 +407,11 @@ def run_ours(args, rank, world, local):
     alg = fp64_flops[gemm_stage] / max(launches_per_step, 1)
     fp64_peak = measure_fp64_peak(torch)
     if tensor:
-        # the algorithm executed on the tensor pipe: 45 BF16 slice products
-        # per FP64 product (9 slices of 6 bits, a + b <= 10)
-        flop = OZ_PRODUCTS * alg
+        # the algorithm executed on the tensor pipe: S(S+1)/2 BF16 slice
+        # products per FP64 product (S slices of 6 bits, a + b <= S + 1)
+        S_ = guard["kernel_slices"] if guard else 9
+        products = S_ * (S_ + 1) // 2
+        flop = products * alg
         peak, peak_src = bf16_peak()
         roofline = {"kernel": gemm_stage + " (tcgen05, exact BF16 slicing)",
                     "bound": "tensor", "achieved": flop / (avg_ms * 1e-3) / 1e12,
@@ -411,7 +427,8 @@ def run_ours(args, rank, world, local):
                     "flop_per_launch": flop, "avg_launch_ms": avg_ms,
                     "fp64_equivalent_tflops": alg / (avg_ms * 1e-3) / 1e12,
                     "fp64_dgemm_measured_tflops": fp64_peak,
-                    "note": "achieved counts the 45 BF16 slice products the "
+                    "slices": S_, "products_per_fp64_product": products,
+                    "note": "achieved counts the BF16 slice products the "
                             "kernel executes per FP64 product; the stage time "
                             "includes the row-slicing kernel"}
     else:
@@ -425,15 +442,6 @@ def run_ours(args, rank, world, local):
                                    "file)",
                     "flop_per_launch": alg, "avg_launch_ms": avg_ms}
     gpu_launches = int(sum(v[1] for v in stage.values()))
-    guard = None
-    if args.precision == "mixed" and c["power"] in (1, 2):
-        import ctypes
-        fmax, f64 = ctypes.c_double(0.0), ctypes.c_int(0)
-        _lib.check(L.fgb_model_fold_guard(model.h, ctypes.byref(fmax),
-                                          ctypes.byref(f64), sptr))
-        guard = {"fold_max": fmax.value,
-                 "force_stage": "fp64-level" if f64.value else "fp32-level",
-                 "threshold": 200.0}
 
     result = {
         "metric": METRIC, "value": value, "unit": "atoms/s",
@@ -458,7 +466,7 @@ def run_ours(args, rank, world, local):
                                for k_, v in stage.items() if v[1]},
         "gpu_launches": gpu_launches,
         "errors_vs_fp64": errors,
-        "fold_guard": guard,
+        "mixed_plan": guard,
         "clocks": clocks.summary(local),
         "autotune": autotune_table(),
     }
@@ -480,8 +488,6 @@ def run_ours(args, rank, world, local):
         result["sample_energy_per_atom"] = float(res_e[0] / 1000)
         print(json.dumps(result), flush=True)
 
-
-OZ_PRODUCTS = 45
 
 
 def oz_eligible(gp, b2):

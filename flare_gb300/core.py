@@ -496,6 +496,11 @@ class _Training:
         self.label_count = [0]
         self.y = np.zeros(0)
         self.noise_vector = np.zeros(0)
+        # per label 1/rel_noise^2 of its kind, zero elsewhere
+        # (sparse_gp.cpp:518-532), for set_hyperparameters
+        self.e_noise_one = np.zeros(0)
+        self.f_noise_one = np.zeros(0)
+        self.s_noise_one = np.zeros(0)
         self.n_labels = 0
         self.n_strucs = 0
         self.n_energy_labels = 0
@@ -554,6 +559,13 @@ class _Training:
                                                rel_f_noise ** 2)
         nv[n_energy + n_force:] = 1 / (self.stress_noise ** 2 * rel_s_noise ** 2)
         self.noise_vector = np.concatenate([self.noise_vector, nv])
+        ones = [np.zeros(nl) for _ in range(3)]
+        ones[0][:n_energy] = 1 / (rel_e_noise * rel_e_noise)
+        ones[1][n_energy:n_energy + n_force] = 1 / (rel_f_noise * rel_f_noise)
+        ones[2][n_energy + n_force:] = 1 / (rel_s_noise * rel_s_noise)
+        self.e_noise_one = np.concatenate([self.e_noise_one, ones[0]])
+        self.f_noise_one = np.concatenate([self.f_noise_one, ones[1]])
+        self.s_noise_one = np.concatenate([self.s_noise_one, ones[2]])
         for i, k in enumerate(self.kernels):
             n_sparse = self.sparse_descriptors[i].n_clusters
             blk = np.zeros((n_sparse, nl))
@@ -802,6 +814,32 @@ class _Training:
                               np.zeros((k.shape[0], self.n_labels))
                               for k in self.Kuf_kernels])
 
+    def set_hyperparameters(self, hyps):
+        """sparse_gp.cpp:1163-1198: new kernel hyperparameters and noises.
+        The NormalizedDotProduct kernel matrices scale by (sigma_new /
+        sigma_old)^2 (Kuu_grad / Kuf_grad, normalized_dot_product.cpp:
+        588-623); the noise vector is rebuilt from the per-label relative
+        noises, then update_matrices_QR."""
+        hyps = np.asarray(hyps, np.float64).reshape(-1)
+        idx = 0
+        for i, k in enumerate(self.kernels):
+            n = len(k.kernel_hyperparameters)
+            new = hyps[idx:idx + n]
+            f = new[0] * new[0] / (k.sigma * k.sigma)
+            self.Kuu_kernels[i] = self.Kuu_kernels[i] * f
+            self.Kuf_kernels[i] = self.Kuf_kernels[i] * f
+            k.sigma = float(new[0])
+            idx += n
+        self._stack_Kuu()
+        self._stack_Kuf()
+        self.energy_noise = float(hyps[idx])
+        self.force_noise = float(hyps[idx + 1])
+        self.stress_noise = float(hyps[idx + 2])
+        self.noise_vector = (self.e_noise_one / self.energy_noise ** 2 +
+                             self.f_noise_one / self.force_noise ** 2 +
+                             self.s_noise_one / self.stress_noise ** 2)
+        self.update_matrices_QR()
+
     def update_matrices_QR(self):
         """sparse_gp.cpp:607-641 on the GPU in FP64 (fgb_solve_qr)."""
         M = self.Kuu.shape[0]
@@ -1021,6 +1059,22 @@ class SparseGP(_Training):
               "predict_DTC")
         structure.mean_efs = mean.cpu().numpy()
         structure.variance_efs = var.cpu().numpy()
+
+    def mixed_plan(self):
+        """The mixed path's precision plan for this model: slices of the
+        kernel and variance GEMMs (9, 8 or 7) with the largest energy
+        difference to 9 slices measured on the sparse set when they were
+        chosen, and the fold guard (largest folded coefficient, whether the
+        descriptor and forces run at FP64 level)."""
+        m = self._device_model()
+        S, fp64 = ctypes.c_int(0), ctypes.c_int(0)
+        est, fmax = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        check(lib().fgb_model_mixed_plan(m.h, ctypes.byref(S),
+                                         ctypes.byref(est), ctypes.byref(fmax),
+                                         ctypes.byref(fp64), stream_ptr()),
+              "mixed_plan")
+        return {"kernel_slices": S.value, "slice_err_ev_per_atom": est.value,
+                "fold_max": fmax.value, "fp64_forces": bool(fp64.value)}
 
     # -------------------------------------------------- mapped models
     def write_mapping_coefficients(self, file_name, contributor,

@@ -59,6 +59,12 @@ struct fgb_model_s {
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS[fgb::oz::kF64Variants],
       ozL[fgb::oz::kF64Variants];
   bool oz_ready[fgb::oz::kF64Variants] = {};
+  // slices of the kernel and variance GEMMs (9, 8 or 7) and the largest
+  // energy difference to 9 slices measured on the sparse set when they
+  // were chosen (choose_kernel_slices)
+  int oz_S = fgb::oz::kS;
+  double oz_err_est = 0.0;
+  bool slices_chosen = false;
   fgb_nlist_s nl;
   fgb_workspace ws;
   fgb_io io;
@@ -112,6 +118,9 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
                     cudaStream_t st, bool fixed = false,
                     const ChunkHook *after_chunk = nullptr);
+// Slice count of the mixed path's kernel and variance GEMMs, measured on
+// the model's sparse set (ozaki.cu; synchronises).
+int choose_kernel_slices(fgb_model_s *m, cudaStream_t st);
 // The folded matrices and the fold guard (force_f64) of a power-1/2 model,
 // built once before its first mixed prediction (synchronises).
 int prepare_mixed(fgb_model_s *m, cudaStream_t st);

@@ -268,8 +268,10 @@ static int build_fold(fgb_model_s *m, cudaStream_t st) {
 }
 
 int prepare_mixed(fgb_model_s *m, cudaStream_t st) {
-  if ((m->power == 2.0 || m->power == 1.0) && !m->bmap_ready)
-    return build_fold(m, st);
+  if (m->power != 2.0 && m->power != 1.0) return FGB_OK;   // FP64 stages
+  int rc;
+  if (!m->bmap_ready && (rc = build_fold(m, st))) return rc;
+  if (!m->slices_chosen && (rc = choose_kernel_slices(m, st))) return rc;
   return FGB_OK;
 }
 
@@ -380,6 +382,27 @@ extern "C" int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
   }
   int rc;
   if (!m->bmap_ready && (rc = build_fold(m, (cudaStream_t)stream))) return rc;
+  if (h_fold_max) *h_fold_max = m->fold_max;
+  if (h_fp64_forces) *h_fp64_forces = m->force_f64 ? 1 : 0;
+  return FGB_OK;
+}
+
+extern "C" int fgb_model_mixed_plan(fgb_model_t m, int *h_kernel_slices,
+                                    double *h_slice_err_est, double *h_fold_max,
+                                    int *h_fp64_forces, void *stream) {
+  if (!m) {
+    set_error("fgb_model_mixed_plan: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (!m->solved) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  int rc;
+  if ((rc = prepare_mixed(m, (cudaStream_t)stream))) return rc;
+  if (h_kernel_slices) *h_kernel_slices = m->oz_S;
+  if (h_slice_err_est) *h_slice_err_est = m->oz_err_est;
   if (h_fold_max) *h_fold_max = m->fold_max;
   if (h_fp64_forces) *h_fp64_forces = m->force_f64 ? 1 : 0;
   return FGB_OK;

@@ -27,6 +27,9 @@
 // every wait is bounded and reports through `err`.
 #include <cuda_bf16.h>
 
+#include <cmath>
+#include <type_traits>
+
 #include "fgb_internal.h"
 #include "fgb_ozaki.h"
 #include "fgb_tc.cuh"
@@ -83,6 +86,14 @@ struct Cfg {
 };
 using CfgF64 = Cfg<kS, 48, kStages, kMaxK, 3>;
 using CfgF64n = Cfg<kS, 32, kStages, kMaxK, 2>;
+// fewer slices: smaller stages, so a five-deep ring fits
+template <int S, int TN>
+using CfgS = typename std::conditional<
+    S == kS, typename std::conditional<TN == 48, CfgF64, CfgF64n>::type,
+    Cfg<S, TN, 5, kMaxK, TN / 16>>::type;
+static_assert(CfgS<8, 48>::EW == 3 && CfgS<8, 32>::EW == 2 &&
+                  CfgS<7, 48>::WCOLS == 16 && CfgS<7, 32>::WCOLS == 16,
+              "every FP64-level candidate: one 16-column chunk per epilogue warp");
 using CfgF32 = Cfg<kSF32, 128, 6, kMaxKF32, 2>;
 using CfgF32w = Cfg<kSF32, 128, 6, kMaxKF32, 4>;
 using CfgF32n = Cfg<kSF32, 64, 8, kMaxKF32, 2>;
@@ -704,6 +715,8 @@ static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
 
 int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S) {
   if (S == kS) return slice_s<kS>(sp, out, st);
+  if (S == 8) return slice_s<8>(sp, out, st);
+  if (S == 7) return slice_s<7>(sp, out, st);
   if (S == kSF32) return slice_s<kSF32>(sp, out, st);
   set_error("ozaki slice: unsupported slice count %d", S);
   return FGB_EINVAL;
@@ -737,11 +750,17 @@ static int gemm_c(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
   return FGB_OK;
 }
 
+template <int S, class Epi>
+int gemm_s(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
+           int *err, cudaStream_t st) {
+  if (B.TR == 32) return gemm_c<CfgS<S, 32>>(A, B, tri, epi, err, st);
+  return gemm_c<CfgS<S, 48>>(A, B, tri, epi, err, st);
+}
+
 template <class Epi>
 int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
          cudaStream_t st) {
-  if (B.TR == CfgF64n::TN) return gemm_c<CfgF64n>(A, B, tri, epi, err, st);
-  return gemm_c<CfgF64>(A, B, tri, epi, err, st);
+  return gemm_s<kS>(A, B, tri, epi, err, st);
 }
 
 int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
@@ -849,9 +868,10 @@ namespace {
 // environments and invalid sparse rows (the same expressions as the FP64
 // path).  Per row and tile it keeps sum_n alpha_n k_n (the energy partial,
 // finished in a fixed order by k_energy_final) and, for the variance GEMM,
-// writes k directly as exact BF16 slices (A operand layout, 128-row tiles,
-// K = N padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64
-// matrix is written only when the variance runs in FP64.
+// writes k directly as S BF16 slices (A operand layout, 128-row tiles, K = N
+// padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64 matrix
+// is written only when the variance runs in FP64.
+template <int S>
 struct EpiKernel {
   using Value = double;
   static constexpr bool kFloat = false;
@@ -886,9 +906,9 @@ struct EpiKernel {
       for (int h = 0; h < 2; h++) {
         long long X[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], 54 - eK);
-        store_digits8<kS>(X, Ksl + tiled_index<kS>(m, n0 + 8 * h, KPv, kTM),
-                      (size_t)kTM * kKC);
+        for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], kBeta * S - eK);
+        store_digits8<S>(X, Ksl + tiled_index<S>(m, n0 + 8 * h, KPv, kTM),
+                         (size_t)kTM * kKC);
       }
     }
     return acc;
@@ -933,11 +953,13 @@ __global__ void k_energy_final(int M, int ntiles, const double *__restrict__ par
 }  // namespace oz
 
 
-// Slice the model operands for B tiles of variant v: normalised sparse rows
-// (B of the kernel GEMM) and the L_inv panels (B of the variance GEMM), per
-// species.  Done once per variant, the first time the variant runs.
+// Slice the model operands for variant v (slice count and B tile height):
+// normalised sparse rows (B of the kernel GEMM) and the L_inv panels (B of
+// the variance GEMM), per species.  Done once per variant, the first time
+// the variant runs.
 static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
   const int S = m->b2.n_species, nd = m->b2.n_d, TN = oz::kTNF64v[v];
+  const int SL = oz::kSF64v[v];
   m->ozS[v].clear();
   m->ozL[v].clear();
   int rc;
@@ -949,18 +971,116 @@ static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
     if ((rc = oz::slice({Ms, nd, TN,
                          m->S.as<double>() + (size_t)m->h_offsets[s] * nd, nd,
                          nullptr, nullptr},
-                        *m->ozS[v][s], st)))
+                        *m->ozS[v][s], st, SL)))
       return rc;
     if ((rc = oz::slice({m->h_panel_rows[s], Ms, TN,
                          m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
                          nullptr},
-                        *m->ozL[v][s], st)))
+                        *m->ozL[v][s], st, SL)))
       return rc;
   }
   m->oz_ready[v] = true;
   return FGB_OK;
 }
 
+
+// Per-environment energies sum_t alpha_t k(s_i, s_t) of the sparse set's own
+// environments with S-slice operands (48-row B tiles), one per sparse row.
+static int probe_energies(fgb_model_s *m, int S, std::vector<double> &E,
+                          cudaStream_t st) {
+  const int v = oz::s_index(S) * oz::kF64PerS;
+  int rc;
+  if (!m->oz_ready[v] && (rc = build_oz_model(m, v, st))) return rc;
+  const int nd = m->b2.n_d, M = m->M;
+  int maxMs = 0;
+  for (int s = 0; s < m->b2.n_species; s++) maxMs = std::max(maxMs, m->h_counts[s]);
+  std::vector<int> id(maxMs);
+  for (int i = 0; i < maxMs; i++) id[i] = i;
+  DevBuf ident, erows, eout, err;
+  oz::Sliced A;
+  if ((rc = ident.ensure(sizeof(int) * (maxMs + 1))) ||
+      (rc = eout.ensure(sizeof(double) * (M + 1))) ||
+      (rc = err.ensure(sizeof(int))))
+    return rc;
+  FGB_CUDA(cudaMemcpyAsync(ident.p, id.data(), sizeof(int) * maxMs,
+                           cudaMemcpyHostToDevice, st));
+  FGB_CUDA(cudaMemsetAsync(eout.p, 0, sizeof(double) * (M + 1), st));
+  FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  const double sig2 = m->sigma * m->sigma;
+  for (int s = 0; s < m->b2.n_species; s++) {
+    const int Ms = m->h_counts[s], off = m->h_offsets[s];
+    if (Ms == 0) continue;
+    if ((rc = oz::slice({Ms, nd, oz::kTM, m->S.as<double>() + (size_t)off * nd,
+                         nd, nullptr, nullptr},
+                        A, st, S)))
+      return rc;
+    const oz::Sliced &B = *m->ozS[v][s];
+    const int slots = B.RP / 16;
+    if ((rc = erows.ensure(sizeof(double) * (size_t)Ms * slots))) return rc;
+    auto run = [&](auto sc) -> int {
+      constexpr int S_ = decltype(sc)::value;
+      oz::EpiKernel<S_> epi{nullptr, nullptr, nullptr, 0, 0,
+                            erows.as<double>(), slots,
+                            m->alpha.as<double>() + off,
+                            m->svalid.as<unsigned char>() + off, ident.as<int>(),
+                            m->snorm.as<double>() + off, sig2, m->power, Ms};
+      return oz::gemm_s<S_>(A, B, false, epi, err.as<int>(), st);
+    };
+    rc = S == 8 ? run(std::integral_constant<int, 8>{})
+                : (S == 7 ? run(std::integral_constant<int, 7>{})
+                          : run(std::integral_constant<int, oz::kS>{}));
+    if (rc) return rc;
+    oz::k_energy_final<<<ceil_div(Ms, 128), 128, 0, st>>>(
+        Ms, slots, erows.as<double>(), ident.as<int>(),
+        eout.as<double>() + off);
+    FGB_LAUNCH_CHECK("k_energy_final");
+  }
+  E.assign(M, 0.0);
+  int h = 0;
+  if (M > 0)
+    FGB_CUDA(cudaMemcpyAsync(E.data(), eout.p, sizeof(double) * M,
+                             cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    set_error("slice-count probe: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
+  return FGB_OK;
+}
+
+// Slice count of the kernel and variance GEMMs: the fewest of 7, 8, 9 for
+// which the energies of the model's own sparse environments (the atoms'
+// environments are drawn from the same training data) differ from the
+// 9-slice ones by at most kSliceErr eV/atom, a hundredth of the mixed
+// path's energy budget.  The probe is pessimistic (each sparse row meets
+// itself, c = 1, with its own, typically largest, alpha: on the alloy
+// model its 8-slice difference is 1.5e-9 eV/atom where whole structures
+// differ by 2e-11), and the margin keeps the total energy of large cells
+// smooth enough for finite differences: the rounding of 7 slices, summed
+// over a 131,072-atom cell, moved (E(x+h) - E(x-h)) / 2h by 3e-3 eV/A at
+// h = 1e-4 A.  Measured once per model, before its first mixed prediction.
+int choose_kernel_slices(fgb_model_s *m, cudaStream_t st) {
+  constexpr double kSliceErr = 1e-8;   // eV/atom
+  m->oz_S = oz::kS;
+  m->oz_err_est = 0.0;
+  m->slices_chosen = true;
+  if (m->M == 0) return FGB_OK;
+  int rc;
+  std::vector<double> E9, Es;
+  if ((rc = probe_energies(m, oz::kS, E9, st))) return rc;
+  for (int S : {7, 8}) {
+    if ((rc = probe_energies(m, S, Es, st))) return rc;
+    double e = 0.0;
+    for (size_t i = 0; i < E9.size(); i++) e = std::max(e, std::fabs(Es[i] - E9[i]));
+    if (e <= kSliceErr) {
+      m->oz_S = S;
+      m->oz_err_est = e;
+      return FGB_OK;
+    }
+  }
+  return FGB_OK;
+}
 
 int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                     bool want_w, bool want_var, double *d_e_atom, double *d_var,
@@ -970,23 +1090,36 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
     set_error("tensor-core kernel stage: adjoint weights are not produced");
     return FGB_ENOTSUP;
   }
-  if (!m->oz_ready[0]) {
+  // the model's slice count; its two tile candidates are variants sb, sb + 1
+  const int SL = m->oz_S;
+  const int sb = oz::s_index(SL) * oz::kF64PerS;
+  if (!m->oz_ready[sb]) {
     if (fixed) {
       set_error("tensor-core kernel stage: operands not sliced before a fixed call");
       return FGB_EINVAL;
     }
-    if ((rc = build_oz_model(m, 0, st))) return rc;
+    if ((rc = build_oz_model(m, sb, st))) return rc;
   }
-  // variant v usable without preparation; prepare it (not in fixed calls)
-  auto usable = [m](int v) { return m->oz_ready[v]; };
-  auto prepare_variant = [&](int v) -> int {
-    if (m->oz_ready[v]) return FGB_OK;
+  // candidate q usable without preparation; prepare it (not in fixed calls)
+  auto usable = [m, sb](int q) { return m->oz_ready[sb + q]; };
+  auto prepare_variant = [&](int q) -> int {
+    if (m->oz_ready[sb + q]) return FGB_OK;
     if (fixed) {
       set_error("tensor-core kernel stage: tile variant not prepared");
       return FGB_EINVAL;
     }
-    return build_oz_model(m, v, st);
+    return build_oz_model(m, sb + q, st);
   };
+  // the slice count as a compile-time constant for the GEMM instantiations
+  auto with_s = [SL](auto &&f) -> int {
+    if (SL == 8) return f(std::integral_constant<int, 8>{});
+    if (SL == 7) return f(std::integral_constant<int, 7>{});
+    return f(std::integral_constant<int, oz::kS>{});
+  };
+  // descriptor rows: the model's slices, or all kS when the fold guard
+  // sends the force product through the FP64-level GEMM (the FP32-level
+  // force GEMM reads the first kSF32)
+  const int SA = m->force_f64 ? oz::kS : SL;
   const B2Params &p = m->b2;
   const int nd = p.n_d;
   const double sig2 = m->sigma * m->sigma;
@@ -1020,32 +1153,36 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
       if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * kslots)) ||
-          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, oz::kS, m->ws.ozK))))
+          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, SL, m->ws.ozK))))
         return rc;
       int vk = 0;
       {
         StageTimer _pt(kStKernelGemm, st, 2);
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
-                            m->ws.ozA, st)))
+                            m->ws.ozA, st, SA)))
           return rc;
-        auto launch = [&](int v) -> int {
+        auto launch = [&](int q) -> int {
           int r;
-          if ((r = prepare_variant(v))) return r;
-          const oz::Sliced &B = *m->ozS[v][s];
-          oz::EpiKernel epi{nullptr,
-                            var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
-                            var_oz ? m->ws.ozK.scale.as<double>() : nullptr,
-                            m->ws.ozK.KP, eK,
-                            m->ws.erows.as<double>(), B.RP / 16,
-                            m->alpha.as<double>() + m->h_offsets[s],
-                            m->svalid.as<unsigned char>() + m->h_offsets[s],
-                            perm, m->ws.norms.as<double>(), sig2, m->power, Ms};
-          return oz::gemm(m->ws.ozA, B, false, epi, m->ws.ozerr.as<int>(), st);
+          if ((r = prepare_variant(q))) return r;
+          const oz::Sliced &B = *m->ozS[sb + q][s];
+          return with_s([&](auto sc) -> int {
+            constexpr int S_ = decltype(sc)::value;
+            oz::EpiKernel<S_> epi{
+                nullptr, var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
+                var_oz ? m->ws.ozK.scale.as<double>() : nullptr, m->ws.ozK.KP,
+                eK, m->ws.erows.as<double>(), B.RP / 16,
+                m->alpha.as<double>() + m->h_offsets[s],
+                m->svalid.as<unsigned char>() + m->h_offsets[s], perm,
+                m->ws.norms.as<double>(), sig2, m->power, Ms};
+            return oz::gemm_s<S_>(m->ws.ozA, B, false, epi,
+                                  m->ws.ozerr.as<int>(), st);
+          });
         };
-        if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::kF64Variants,
+        if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::kF64PerS,
                             launch, usable, st, fixed, &vk)))
           return rc;
+        vk += sb;
       }
       {
         StageTimer _pt(kStRowEnergy, st);
@@ -1060,17 +1197,20 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
         int vv = 0;
         {
           StageTimer _pt(kStVarianceGemm, st);
-          auto launch = [&](int v) -> int {
+          auto launch = [&](int q) -> int {
             int r;
-            if ((r = prepare_variant(v))) return r;
-            const oz::Sliced &B = *m->ozL[v][s];
+            if ((r = prepare_variant(q))) return r;
+            const oz::Sliced &B = *m->ozL[sb + q][s];
             oz::EpiZsq epi{m->ws.part.as<double>(), B.RP / 16, R};
-            return oz::gemm(m->ws.ozK, B, true, epi, m->ws.ozerr.as<int>(), st);
+            return with_s([&](auto sc) -> int {
+              return oz::gemm_s<decltype(sc)::value>(
+                  m->ws.ozK, B, true, epi, m->ws.ozerr.as<int>(), st);
+            });
           };
-          if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms,
-                              oz::kF64Variants, launch, usable, st, fixed,
-                              &vv)))
+          if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms, oz::kF64PerS,
+                              launch, usable, st, fixed, &vv)))
             return rc;
+          vv += sb;
         }
         if ((rc = launch_variance_final(Mr, m->ozL[vv][s]->RP / 16,
                                         m->ws.part.as<double>(), perm,

@@ -477,6 +477,9 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   m->solved = false;
   m->bmap_ready = false;
   m->lfull_ready = false;
+  m->slices_chosen = false;
+  m->oz_S = oz::kS;
+  m->oz_err_est = 0.0;
   m->force_f64 = false;
   m->fold_max = 0.0;
   for (bool &r : m->oz_ready) r = false;

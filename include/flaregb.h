@@ -60,8 +60,9 @@ enum {
 /* prediction precision */
 enum {
   FGB_PREC_FP64 = 0,  /* FP64 adjoint path                                   */
-  FGB_PREC_MIXED = 1  /* double-float descriptors, FP64-accurate tensor-core
-                         kernel/variance GEMMs (exact slicing), FP32-level
+  FGB_PREC_MIXED = 1  /* double-float descriptors, tensor-core kernel and
+                         variance GEMMs by exact slicing to 54, 48 or 42 bits
+                         (fgb_model_mixed_plan), FP32-level
                          tensor-core force GEMM and FP32 adjoint; models
                          whose largest folded coefficient exceeds 200
                          (fgb_model_fold_guard) get the force stage at
@@ -283,6 +284,18 @@ int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream);
  * B2 adjoint) therefore run at FP64 level, 0 when they run in double-float
  * and at FP32 level.  Either may be NULL. */
 int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
+                         int *h_fp64_forces, void *stream);
+
+/* The mixed path's precision plan for a solved model: h_kernel_slices =
+ * BF16 slices of the kernel and variance GEMMs (9, 8 or 7: 54, 48 or 42
+ * bits), the fewest for which the energies of the model's own sparse
+ * environments differ from the 9-slice ones by at most 1e-8 eV/atom, and
+ * h_slice_err_est = that largest difference (measured once per model,
+ * before its first mixed prediction); h_fold_max and h_fp64_forces as
+ * fgb_model_fold_guard.  Powers other than 1 and 2 run the mixed path's
+ * kernel stages in FP64 (9 reported).  Any output may be NULL. */
+int fgb_model_mixed_plan(fgb_model_t m, int *h_kernel_slices,
+                         double *h_slice_err_est, double *h_fold_max,
                          int *h_fp64_forces, void *stream);
 
 /* Thin Q (rows x cols, column-major) of the Householder QR of A (rows x

@@ -149,3 +149,40 @@ def test_batched_environment_addition_matches_sequential():
     for s in range(S):
         np.testing.assert_array_equal(b.sparse_descriptors[0].descriptors[s],
                                       a.sparse_descriptors[0].descriptors[s])
+
+
+def test_set_hyperparameters_matches_fresh_model():
+    """ctests/test_sparse_gp.cpp:300-366 (Set_Hyps): two GPs on the same
+    data with different hyperparameters and per-structure relative noises;
+    after set_hyperparameters(hyps of the first) the second has the first's
+    Kuu, Kuf, noise vector, alpha and predictions."""
+    import flare_gb300 as fg
+    b2a = b2_args(2, 3, 2, 5.0)
+    gb2 = fg.B2(*b2a[:5])
+    gps = [fg.SparseGP([fg.NormalizedDotProduct(1.5, 2)], 1.0, 1.5, 3.0),
+           fg.SparseGP([fg.NormalizedDotProduct(2.0, 2)], 2.0, 2.5, 3.5)]
+    rel = [(0.1, 0.2, 0.3), (0.5, 0.4, 0.6)]
+    for t in range(2):
+        cell, sp, pos = random_atoms(seed=70 + t)
+        E, F, St = lj_labels(cell, sp, pos, 2)
+        for gp in gps:
+            g = fg.Structure(cell, sp, pos, 5.0, [gb2])
+            g.energy, g.forces, g.stresses = np.array([E]), F.reshape(-1), St
+            gp.add_training_structure(g, [-1], *rel[t])
+            gp.add_all_environments(g)
+    for gp in gps:
+        gp.update_matrices_QR()
+    assert not np.allclose(gps[0].alpha, gps[1].alpha)
+    gps[1].set_hyperparameters(gps[0].hyperparameters)
+    np.testing.assert_allclose(gps[1].hyperparameters, gps[0].hyperparameters)
+    np.testing.assert_allclose(gps[1].Kuu, gps[0].Kuu, rtol=1e-13, atol=1e-14)
+    np.testing.assert_allclose(gps[1].Kuf, gps[0].Kuf, rtol=1e-13, atol=1e-14)
+    np.testing.assert_allclose(gps[1].noise_vector, gps[0].noise_vector,
+                               rtol=1e-14)
+    np.testing.assert_allclose(gps[1].alpha, gps[0].alpha, rtol=1e-7,
+                               atol=1e-7 * np.abs(gps[0].alpha).max())
+    cell, sp, pos = random_atoms(seed=79)
+    r = [gp.predict_batch([fg.Structure(cell, sp, pos, 5.0, [gb2])])
+         for gp in gps]
+    np.testing.assert_allclose(r[1]["forces"], r[0]["forces"], rtol=0,
+                               atol=1e-7 * max(1, np.abs(r[0]["forces"]).max()))
