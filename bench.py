@@ -420,7 +420,7 @@ def run_ours(args, rank, world, local):
                     "traffic": (OZ_KERNEL_TRAFFIC_ALLOY1000
                                 if gemm_stage == "kernel_gemm" and
                                 WORKLOAD.startswith("alloy1000") and B == 32
-                                else None),
+                                and S_ == 8 else None),
                     "traffic_source": "ncu dram__bytes_read.sum + "
                                       "dram__bytes_write.sum, one capture",
                     "peak_source": peak_src,
@@ -496,10 +496,11 @@ def oz_eligible(gp, b2):
     return gp.kernels[0].power in (1.0, 2.0)
 
 
-# DRAM traffic of one kernel-GEMM launch (EpiKernel, one species of the
-# alloy1000 batch): dram__bytes_read.sum + dram__bytes_write.sum from one
-# ncu capture (profiles/k_oz_gemm_alloy1000.md); applies to that workload.
-OZ_KERNEL_TRAFFIC_ALLOY1000 = 474.4e6
+# DRAM traffic of one kernel-GEMM launch (EpiKernel<8>, one species of the
+# alloy1000 batch, 8 slices): dram__bytes_read.sum + dram__bytes_write.sum
+# from one ncu capture (profiles/k_oz_gemm_alloy1000.md); applies to that
+# workload.
+OZ_KERNEL_TRAFFIC_ALLOY1000 = 414.3e6
 
 
 def bf16_peak():
