@@ -11,8 +11,10 @@ from ._lib import check, lib, ptr
 
 OPS = ("kernel_gemm", "variance_gemm", "force_gemm")
 CANDIDATES = {
-    "kernel_gemm": ("B tile 48 rows", "B tile 32 rows"),
-    "variance_gemm": ("B tile 48 rows", "B tile 32 rows"),
+    "kernel_gemm": ("B tile 48 rows", "B tile 32 rows",
+                    "B tile 64 rows (8 or 7 slices)"),
+    "variance_gemm": ("B tile 48 rows", "B tile 32 rows",
+                      "B tile 64 rows (8 or 7 slices)"),
     "force_gemm": ("B tile 128 rows, 2 epilogue warps",
                    "B tile 128 rows, 4 epilogue warps",
                    "B tile 64 rows, 2 epilogue warps"),

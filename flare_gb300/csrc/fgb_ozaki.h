@@ -32,13 +32,16 @@ constexpr int kMaxKF32 = 2720;
 // The mixed path's kernel and variance GEMMs take 9, 8 or 7 slices (54, 48
 // or 42 bits), the fewest that the model's error estimate allows
 // (choose_kernel_slices); variant v = 2 x (slice set) + (tile choice).
+// Tile candidates per slice count: B tiles of 48 and 32 rows, and of 64 rows
+// where S x 64 accumulator columns fit TMEM (S <= 8).
 constexpr int kNumSF64 = 3;
 constexpr int kSF64set[kNumSF64] = {9, 8, 7};
-constexpr int kF64PerS = 2;
+constexpr int kF64PerS = 3;
 constexpr int kF64Variants = kNumSF64 * kF64PerS;
-constexpr int kTNF64v[kF64Variants] = {48, 32, 48, 32, 48, 32};
-constexpr int kSF64v[kF64Variants] = {9, 9, 8, 8, 7, 7};
+constexpr int kTNF64v[kF64Variants] = {48, 32, 48, 48, 32, 64, 48, 32, 64};
+constexpr int kSF64v[kF64Variants] = {9, 9, 9, 8, 8, 8, 7, 7, 7};
 constexpr int s_index(int S) { return S == 9 ? 0 : (S == 8 ? 1 : 2); }
+constexpr int n_cand_s(int S) { return S == 9 ? 2 : 3; }
 constexpr int kF32Variants = 3;
 constexpr int kTNF32v[kF32Variants] = {128, 128, 64};
 constexpr int kEWF32v[kF32Variants] = {2, 4, 2};

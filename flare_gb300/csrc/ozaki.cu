@@ -86,13 +86,18 @@ struct Cfg {
 };
 using CfgF64 = Cfg<kS, 48, kStages, kMaxK, 3>;
 using CfgF64n = Cfg<kS, 32, kStages, kMaxK, 2>;
-// fewer slices: smaller stages, so a five-deep ring fits
+// fewer slices: smaller stages, so a deeper ring fits; B tiles of 64 rows
+// take four epilogue warps per lane quarter (576 threads)
+constexpr int ring_depth(int S, int TN) {
+  return 5 * S * (kTM * kKC * 2 + TN * kKC * 2) + 256 <= 227 * 1024 ? 5 : 4;
+}
 template <int S, int TN>
 using CfgS = typename std::conditional<
     S == kS, typename std::conditional<TN == 48, CfgF64, CfgF64n>::type,
-    Cfg<S, TN, 5, kMaxK, TN / 16>>::type;
+    Cfg<S, TN, ring_depth(S, TN), kMaxK, TN / 16>>::type;
 static_assert(CfgS<8, 48>::EW == 3 && CfgS<8, 32>::EW == 2 &&
-                  CfgS<7, 48>::WCOLS == 16 && CfgS<7, 32>::WCOLS == 16,
+                  CfgS<8, 64>::EW == 4 && CfgS<7, 48>::WCOLS == 16 &&
+                  CfgS<7, 32>::WCOLS == 16 && CfgS<7, 64>::WCOLS == 16,
               "every FP64-level candidate: one 16-column chunk per epilogue warp");
 using CfgF32 = Cfg<kSF32, 128, 6, kMaxKF32, 2>;
 using CfgF32w = Cfg<kSF32, 128, 6, kMaxKF32, 4>;
@@ -754,6 +759,8 @@ template <int S, class Epi>
 int gemm_s(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,
            int *err, cudaStream_t st) {
   if (B.TR == 32) return gemm_c<CfgS<S, 32>>(A, B, tri, epi, err, st);
+  if constexpr (S < kS)
+    if (B.TR == 64) return gemm_c<CfgS<S, 64>>(A, B, tri, epi, err, st);
   return gemm_c<CfgS<S, 48>>(A, B, tri, epi, err, st);
 }
 
@@ -1179,7 +1186,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                                   m->ws.ozerr.as<int>(), st);
           });
         };
-        if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::kF64PerS,
+        if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::n_cand_s(SL),
                             launch, usable, st, fixed, &vk)))
           return rc;
         vk += sb;
@@ -1207,8 +1214,9 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
                   m->ws.ozK, B, true, epi, m->ws.ozerr.as<int>(), st);
             });
           };
-          if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms, oz::kF64PerS,
-                              launch, usable, st, fixed, &vv)))
+          if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms,
+                              oz::n_cand_s(SL), launch, usable, st, fixed,
+                              &vv)))
             return rc;
           vv += sb;
         }

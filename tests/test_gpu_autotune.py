@@ -55,8 +55,13 @@ def test_tuner_times_each_candidate_once_per_shape(setup):
     r1 = predict(gp, calc, items)
     table = at.table()
     assert {e["op"] for e in table} == set(at.OPS), table
+    # the 64-row tiles exist for 8 and 7 slices only
+    n64 = 0 if gp.mixed_plan()["kernel_slices"] == 9 else 1
     for e in table:
-        assert len(e["ms"]) == len(at.CANDIDATES[e["op"]])
+        expect = len(at.CANDIDATES[e["op"]])
+        if e["op"] in ("kernel_gemm", "variance_gemm"):
+            expect = 2 + n64
+        assert len(e["ms"]) == expect, e
         assert all(x > 0 for x in e["ms"]), e
         assert e["choice"] == int(np.argmin(e["ms"])), e
     r2 = predict(gp, calc, items)
