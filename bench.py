@@ -679,6 +679,7 @@ def run_serve(args):
                    "atoms_total": int(atoms.sum()),
                    "atoms_mean": float(atoms.mean())},
         "saturation": sat, "poisson_sweep": sweep,
+        "mixed_plan": gp.mixed_plan() if args.precision == "mixed" else None,
         "setup_s": {"train_fp64": round(train_s, 1),
                     "request_generation": round(gen_s, 1)},
         "clocks": clocks.summary(),
@@ -874,6 +875,9 @@ def run_md(args):
             "max_abs": float(np.max(np.abs(drift)) / c["n_atoms"])},
         "sparse_update": grow,
         "ms_per_step_after_update": ms_after,
+        # the grown model's plan (the timed steps ran the 8,000-env model)
+        "mixed_plan_after_update": (gp.mixed_plan()
+                                    if args.precision == "mixed" else None),
         "autotune": autotune_table(),
         "setup_s": {"train_fp64": round(train_s, 1),
                     "replica_generation": round(gen_s, 1)},
