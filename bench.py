@@ -78,9 +78,16 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def rank_seeds(seed0, rank, n):
+    """Seeds of one rank's n structures: disjoint across ranks, so every
+    rank predicts its own units with no exchange (weak scaling)."""
+    return [seed0 + rank * 100000 + i for i in range(n)]
 
 
 # ------------------------------------------------------------ CPU oracle
@@ -257,8 +264,8 @@ def run_ours(args, rank, world, local):
     train_s = time.time() - t_setup
 
     B = args.batch
-    structs = [wl.alloy_structure(c["test_seed0"] + rank * 100000 + i)
-               for i in range(B)]
+    structs = [wl.alloy_structure(sd)
+               for sd in rank_seeds(c["test_seed0"], rank, B)]
     offsets = np.zeros(B + 1, dtype=np.int32)
     for i, s in enumerate(structs):
         offsets[i + 1] = offsets[i] + len(s[1])
