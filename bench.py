@@ -406,9 +406,9 @@ def run_ours(args, rank, world, local):
     tensor = args.precision == "mixed" and oz_eligible(gp, b2)
     gemm_stage = max(fp64_flops, key=lambda s_: stage.get(s_, (0, 0))[0])
     st_ms, st_n = stage[gemm_stage]
-    # launches counted per stage: the tensor-core kernel stage counts slice +
-    # GEMM, its variance stage the GEMM alone
-    per_stage_launch = 2 if tensor and gemm_stage == "kernel_gemm" else 1
+    # launches counted per stage: the tensor-core kernel stage counts row
+    # scales + slices + GEMM, its variance stage the GEMM alone
+    per_stage_launch = 3 if tensor and gemm_stage == "kernel_gemm" else 1
     launches_per_step = st_n / per_stage_launch / args.steps
     avg_ms = st_ms / (st_n / per_stage_launch)
     alg = fp64_flops[gemm_stage] / max(launches_per_step, 1)

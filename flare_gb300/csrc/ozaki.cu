@@ -299,26 +299,65 @@ __device__ __forceinline__ void store_digits8(long long (&X)[8],
   }
 }
 
-// Row slicing: scale each row to (-1, 1) by a power of two 2^e (e from the
-// row's largest magnitude), take the scaled value y as the integer
-// X = rn(y 2^(6S)) (exact for |y| >= 2^-1 of the row's top binade, rounded
-// at 2^(-6S) below that) and store its S balanced base-64 digits
-// (store_digits8).  A warp takes 8 rows (one core-matrix row group) and 32
-// consecutive k at a time, lane = row + 8 x (k group of 8), so that the
-// 16-byte row pieces a store instruction writes for one slice are two
-// contiguous 256-byte blocks (one 16-k chunk each) rather than 32 scattered
-// pieces.  Row maxima: a first pass over the row, reduced over the 4 lanes
-// of each row.
+// Row scales: 2^e with e from the row's largest magnitude (after the
+// optional division by the row norm), one warp per row; rows past R and
+// empty rows get 2^0.  Written to `scale` for k_oz_slice8.
+__global__ void __launch_bounds__(256)
+k_oz_rowscale(int R, int K, int RP, const double *__restrict__ src,
+              long long ld, const int *__restrict__ perm,
+              const double *__restrict__ rownorm, double thresh,
+              double *__restrict__ scale) {
+  const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (m >= RP) return;
+  bool valid = m < R;
+  long long row = 0;
+  double inv = 1.0;
+  if (valid) {
+    row = perm ? (long long)perm[m] : (long long)m;
+    if (rownorm) {
+      const double n = rownorm[row];
+      if (n >= thresh) inv = 1.0 / n;
+      else valid = false;
+    }
+  }
+  unsigned long long mb = 0;
+  if (valid) {
+    const double *sr = src + row * ld;
+    for (int k = lane; k < K; k += 32)
+      mb = max(mb, (unsigned long long)__double_as_longlong(sr[k]) &
+                       0x7FFFFFFFFFFFFFFFULL);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, off));
+  const double mx = __longlong_as_double((long long)mb) * inv;
+  const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  if (lane == 0) scale[m] = ldexp(1.0, e);
+}
+
+// Row slicing: each row scaled to (-1, 1) by its power of two 2^e
+// (k_oz_rowscale), the scaled value y taken as the integer X = rn(y 2^(6S))
+// (exact for |y| >= 2^-1 of the row's top binade, rounded at 2^(-6S) below
+// that) and its S balanced base-64 digits stored (store_digits8).  A warp
+// takes 8 rows (one core-matrix row group) and one part of kSlicePart
+// columns, 32 consecutive k at a time, lane = row + 8 x (k group of 8), so
+// that the 16-byte row pieces a store instruction writes for one slice are
+// two contiguous 256-byte blocks (one 16-k chunk each) rather than 32
+// scattered pieces; the parts let a few thousand rows fill the GPU.
+constexpr int kSlicePart = 128;
+static_assert(kSlicePart % 32 == 0, "a part is whole 32-column steps");
 template <int S>
 __global__ void __launch_bounds__(256)
-k_oz_slice8(int R, int K, int RP, int KP, int TR,
+k_oz_slice8(int R, int K, int RP, int KP, int TR, int nparts,
             const double *__restrict__ src, long long ld,
             const int *__restrict__ perm, const double *__restrict__ rownorm,
             double thresh, __nv_bfloat16 *__restrict__ out,
-            double *__restrict__ scale) {
-  const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+            const double *__restrict__ scale) {
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  const int m0 = warp * 8;
+  const int part = (int)(gw % nparts);
+  const int m0 = (int)(gw / nparts) * 8;
   if (m0 >= RP) return;
   const int r = lane & 7, g = lane >> 3;
   const int m = m0 + r;
@@ -334,21 +373,10 @@ k_oz_slice8(int R, int K, int RP, int KP, int TR,
     }
   }
   const double *sr = src + row * ld;
-  unsigned long long mb = 0;
-  if (valid)
-    for (int k0 = g * 8; k0 < K; k0 += 32)
-#pragma unroll
-      for (int j = 0; j < 8; j++)
-        if (k0 + j < K)
-          mb = max(mb, (unsigned long long)__double_as_longlong(sr[k0 + j]) &
-                           0x7FFFFFFFFFFFFFFFULL);
-  mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, 8));
-  mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mb, 16));
-  const double mx = __longlong_as_double((long long)mb) * inv;
-  const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
-  if (g == 0) scale[m] = ldexp(1.0, e);
+  const int e = pow2_exp(scale[m]);
   const size_t stride = (size_t)TR * kKC;
-  for (int k0 = g * 8; k0 < KP; k0 += 32) {
+  const int kend = min(KP, (part + 1) * kSlicePart);
+  for (int k0 = part * kSlicePart + g * 8; k0 < kend; k0 += 32) {
     long long X[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
@@ -709,9 +737,14 @@ template <int S>
 static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   int rc;
   if ((rc = prepare(sp.rows, sp.K, sp.TR, S, out))) return rc;
-  const long long threads = (long long)(out.RP / 8) * 32;   // RP % 8 == 0
+  k_oz_rowscale<<<ceil_div((long long)out.RP * 32, 256), 256, 0, st>>>(
+      sp.rows, sp.K, out.RP, sp.src, sp.ld, sp.perm, sp.rownorm,
+      kEmptyThresh, out.scale.as<double>());
+  FGB_LAUNCH_CHECK("k_oz_rowscale");
+  const int nparts = ceil_div(out.KP, kSlicePart);
+  const long long threads = (long long)(out.RP / 8) * nparts * 32;  // RP % 8 == 0
   k_oz_slice8<S><<<ceil_div(threads, 256), 256, 0, st>>>(
-      sp.rows, sp.K, out.RP, out.KP, sp.TR, sp.src, sp.ld, sp.perm,
+      sp.rows, sp.K, out.RP, out.KP, sp.TR, nparts, sp.src, sp.ld, sp.perm,
       sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
       out.scale.as<double>());
   FGB_LAUNCH_CHECK("k_oz_slice8");
@@ -1164,7 +1197,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
         return rc;
       int vk = 0;
       {
-        StageTimer _pt(kStKernelGemm, st, 2);
+        StageTimer _pt(kStKernelGemm, st, 3);   // row scales, slices, GEMM
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
                             m->ws.ozA, st, SA)))

@@ -367,3 +367,35 @@ def test_radial_bases_predict_matches_oracle(basis, rh):
     b = gpu_predict(ggp, calc, [(cell, sp, pos)], precision="mixed")
     assert abs(b["energy"][0] - E) <= 1e-6 * len(sp) + 1e-11 * abs(E)
     assert np.abs(b["forces"] - F).mean() <= 1e-4 + 1e-9 * Fs
+
+
+def test_structure_kernels_with_isolated_atom():
+    """self_kernel_struc, struc_struc and predict_DTC when one atom has no
+    neighbours (descriptor norm below 1e-8: its rows are skipped, as in the
+    reference's empty-environment tests) against the oracle."""
+    import flare_gb300 as fg
+    ogp, b2a = small_two_species(seed=5, n_train=2)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    ggp.R_inv = ogp.R_inv
+    rng_ = np.random.Generator(np.random.PCG64(91))
+    cell = np.eye(3) * 20.0
+    pos = np.vstack([rng_.uniform(0, 4.0, size=(9, 3)) + 2.0, [[14, 14, 14]]])
+    sp = np.array([0, 1] * 5)
+    ob2 = oracle.B2Settings(*b2a)
+    o = oracle.Structure(cell, sp, pos, 5.0, [ob2])
+    assert o.descriptors[0].atom_norms.min() < 1e-8
+    k = fg.NormalizedDotProduct(ogp.kernels[0].sigma, 2)
+    g = fg.Structure(cell, sp, pos, 5.0, [calc])
+    ref = ogp.kernels[0].self_kernel_struc(o.descriptors[0])
+    np.testing.assert_allclose(k.self_kernel_struc(g), ref, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())
+    c2, s2, p2 = random_atoms(seed=92)
+    o2 = oracle.Structure(c2, s2, p2, 5.0, [ob2])
+    ref2 = ogp.kernels[0].struc_struc(o.descriptors[0], o2.descriptors[0])
+    got2 = k.struc_struc(g, fg.Structure(c2, s2, p2, 5.0, [calc]))
+    np.testing.assert_allclose(got2, ref2, rtol=0,
+                               atol=1e-10 * np.abs(ref2).max())
+    ogp.predict_DTC(o)
+    ggp.predict_DTC(g)
+    np.testing.assert_allclose(g.variance_efs, o.variance_efs, rtol=0,
+                               atol=1e-10 * np.abs(ref).max())
