@@ -89,18 +89,27 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   const int nh = LC > 0 ? (LC + 1) * (LC + 1) : p.n_harm;
   const int nm = NC > 0 ? NC : p.n_max;
   const int nA = p.n_species * nm * nh;
+  constexpr bool kFixed = NC > 0 && LC > 0;
+  // fixed sizes with at most one (species, lm) per thread: A stays in
+  // registers over the pair chunks and is laid over the end of the Y
+  // buffer for the contraction (b2_forward_smem leaves A out)
+  const bool regA = kFixed && p.n_species * nh <= kChunk &&
+                    p.n_species * nm <= kChunk;
   T *A = reinterpret_cast<T *>(smem_raw);
-  T *sg = A + nA;
+  T *sg = regA ? A : A + nA;
   T *sy = sg + kChunk * nm;
   int *ssp = (int *)(sy + kChunk * nh);
   T *red = (T *)(ssp + kChunk);
   int *sord = (int *)(red + kChunk);      // chunk pairs, sorted by species
   int *scnt = sord + kChunk;              // [warp][species] counts
   int *sbeg = scnt + 2 * kMaxSpecies;     // species starts in sord
-  constexpr bool kFixed = NC > 0 && LC > 0;
   const int t = threadIdx.x;
   const int si = species[i];
-  for (int e = t; e < nA; e += blockDim.x) A[e] = T(0);
+  T areg[NC > 0 ? NC : 1];
+#pragma unroll
+  for (int n = 0; n < (NC > 0 ? NC : 1); n++) areg[n] = T(0);
+  if (!regA)
+    for (int e = t; e < nA; e += blockDim.x) A[e] = T(0);
   const long long b = offsets[i], e_ = offsets[i + 1];
   for (long long c0 = b; c0 < e_; c0 += kChunk) {
     long long pp = c0 + t;
@@ -157,8 +166,13 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
 #pragma unroll
           for (int n = 0; n < NC; n++) mac(acc[n], sg[pq * NC + n], y);
         }
+        if (regA) {
 #pragma unroll
-        for (int n = 0; n < NC; n++) A[(s * NC + n) * NH + lm] += finish(acc[n]);
+          for (int n = 0; n < NC; n++) areg[n] += finish(acc[n]);
+        } else {
+#pragma unroll
+          for (int n = 0; n < NC; n++) A[(s * NC + n) * NH + lm] += finish(acc[n]);
+        }
       }
     } else {
       const int cnt = (int)min((long long)kChunk, e_ - c0);
@@ -174,6 +188,20 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     }
     __syncthreads();
   }
+  if (regA) {
+    // the Y buffer is free after the last chunk (synchronised above); A
+    // takes its end, clear of the B2 row staged from the start of g
+    A = sy + (kChunk * nh - nA);
+    if constexpr (kFixed) {
+      constexpr int NH = (LC + 1) * (LC + 1);
+      if (t < p.n_species * NH) {
+        const int s = t / NH, lm = t % NH;
+#pragma unroll
+        for (int n = 0; n < NC; n++) A[(s * NC + n) * NH + lm] = areg[n];
+      }
+    }
+    __syncthreads();
+  }
   if (A_out)
     for (int e = t; e < nA; e += blockDim.x)
       A_out[(long long)i * nA + e] = to_double(A[e]);
@@ -185,7 +213,7 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     // decoding per value); the row is staged in the basis-value buffers and
     // written with coalesced stores when it fits there.
     constexpr int L1c = LC + 1, NH = (LC + 1) * (LC + 1);
-    const bool stage = nd <= kChunk * (nm + nh);
+    const bool stage = nd <= kChunk * (nm + nh) - (regA ? nA : 0);
     T *out_s = sg;
     const int npair = nr * (nr + 1) / 2;
     for (int pi = t; pi < npair; pi += blockDim.x) {
@@ -415,10 +443,12 @@ __global__ void k_struct_reduce(int n_struc, const int *__restrict__ atom_off,
 
 }  // namespace
 
-size_t b2_forward_smem(const B2Params &p) {
-  // A | g | Y | pair species | reduction | species-sorted pair order and
-  // per-warp species counts (2 x kMaxSpecies) and starts (kMaxSpecies + 1)
-  return sizeof(double) * (p.n_A + (size_t)kChunk * (p.n_max + p.n_harm)) +
+size_t b2_forward_smem(const B2Params &p, bool regA) {
+  // A (unless it stays in registers and is laid over Y) | g | Y | pair
+  // species | reduction | species-sorted pair order and per-warp species
+  // counts (2 x kMaxSpecies) and starts (kMaxSpecies + 1)
+  return sizeof(double) * ((regA ? 0 : p.n_A) +
+                           (size_t)kChunk * (p.n_max + p.n_harm)) +
          sizeof(int) * kChunk + sizeof(double) * kChunk +
          sizeof(int) * (kChunk + 3 * kMaxSpecies + 1);
 }
@@ -442,6 +472,7 @@ static void dispatch_nl(const B2Params &p, F &&f) {
 template <typename T, int NC, int LC>
 struct FwdK {
   static constexpr auto fn = k_b2_forward<T, NC, LC>;
+  static constexpr bool kFixed = NC > 0 && LC > 0;
 };
 template <typename T, int NC, int LC>
 struct AdjK {
@@ -453,14 +484,19 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       double *d_norms, cudaStream_t st, bool dfloat) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
-  size_t sm = b2_forward_smem(p);   // sizeof(df) == sizeof(double)
-  if (sm > 200 * 1024) {
-    set_error("B2 settings need %zu bytes of shared memory", sm);
+  const size_t sm_full = b2_forward_smem(p, false);   // sizeof(df) == 8
+  if (sm_full > 200 * 1024) {
+    set_error("B2 settings need %zu bytes of shared memory", sm_full);
     return FGB_EINVAL;
   }
   cudaError_t e = cudaSuccess;
   auto go = [&](auto k) {
     auto fn = decltype(k)::fn;
+    // the specialised kernels keep A in registers when one (species, lm)
+    // per thread covers it (the same test as in the kernel)
+    const bool regA = decltype(k)::kFixed && p.n_species * p.n_harm <= kChunk &&
+                      p.n_species * p.n_max <= kChunk;
+    const size_t sm = b2_forward_smem(p, regA);
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
     if (e != cudaSuccess) return;
