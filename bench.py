@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--replicas", type=int, default=0,
                     help="md workload: number of replicas (default 256)")
     ap.add_argument("--workload", default="alloy1000",
-                    choices=["alloy1000", "fcc1m", "md", "serve", "mapped"],
+                    choices=["alloy1000", "fcc256", "fcc1m", "md", "serve",
+                             "mapped"],
                     help="fcc1m: one 1,048,576-atom structure, E+F+virial, "
                          "peak device memory (reported as a side record)")
     return ap.parse_args()
@@ -562,6 +563,97 @@ def time_plain(L, _lib, model, structs, b2, c, torch):
             "sample": f"{len(times)} structure(s) after 1 warm-up, wall clock"}
 
 
+def run_fcc256(args):
+    """fcc256, the reference's small CPU-runnable case: energy, forces,
+    stress and local variance of 256-atom FCC cells in FP64 through
+    SparseGP.predict_batch (host arrays in and out, so this is end to end),
+    64 cells per call and one per call; the mixed path on the same calls;
+    the plain FP64 GPU form; and the FP64 CPU oracle on the host cores, with
+    the GPU's FP64 results checked against it."""
+    import torch
+    import flare_gb300 as fg
+    from flare_gb300 import _lib
+    from flare_gb300 import synthetic as syn
+    from flare_gb300 import workloads as wl
+    L = _lib.lib()
+    c = wl.FCC256
+    t0 = time.time()
+    gp, b2, k = wl.build_fcc256_model()
+    train_s = time.time() - t0
+    B = 64
+    structs = [wl.fcc256_structure(c["test_seed0"] + i) for i in range(B)]
+    fgs = [fg.Structure(cl, sp, ps, c["rc"], [b2]) for cl, sp, ps in structs]
+
+    def timed(batch, prec):
+        for _ in range(max(args.warmup, 1)):
+            gp.predict_batch(batch, precision=prec)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            r = gp.predict_batch(batch, precision=prec)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t1) / args.steps
+        return dt, r
+
+    f64_b, r64 = timed(fgs, "fp64")
+    f64_1, _ = timed(fgs[:1], "fp64")
+    mix_b, rmx = timed(fgs, "mixed")
+    plain = time_plain(L, _lib, gp._device_model([b2]), structs[:3], b2, c,
+                       torch)
+    # FP64 CPU oracle: the same model trained on the host
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    ob2 = oracle.B2Settings("chebyshev", "quadratic", [0.0, c["rc"]], [],
+                            [1, c["n_max"], c["l_max"]])
+    ogp = oracle.SparseGP([oracle.NormalizedDotProduct(c["sigma"], c["power"])],
+                          c["sigma_e"], c["sigma_f"], c["sigma_s"])
+    sparse = wl.fcc256_sparse_choice()
+    for t in range(c["n_train"]):
+        cell, sp, pos = wl.fcc256_structure(c["train_seed0"] + t)
+        st = oracle.Structure(cell, sp, pos, c["rc"], [ob2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, [0.4], [2.6], c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        ogp.add_training_structure(st)
+        ogp.add_specific_environments(st, sparse[t])
+    ogp.update_matrices_QR()
+    cpu_t = []
+    for i in range(3):
+        cell, sp, pos = structs[i]
+        t1 = time.perf_counter()
+        st = oracle.Structure(cell, sp, pos, c["rc"], [ob2])
+        ogp.predict_local_uncertainties(st)
+        cpu_t.append(time.perf_counter() - t1)
+        if i == 0:
+            ref_e, ref_f = st.mean_efs[0], st.mean_efs[1:-6].reshape(-1, 3)
+    cpu_v = 256 * 2 / sum(cpu_t[1:])
+    print(json.dumps({
+        "metric": "atoms/s (E+F+S+local std) in FP64, 256-atom FCC",
+        "value": B * 256 / f64_b, "unit": "atoms/s",
+        "config": {"workload": "fcc256: 4x4x4 FCC cells, a 4.05, sigma 0.05; "
+                               "B2 [1,8,3] rc 5.0; NormalizedDotProduct sigma 2 "
+                               "power 2; 20 LJ-labelled training cells, 200 "
+                               "sparse envs", "structures_per_call": B,
+                   "calls": args.steps, "timing": "wall clock around "
+                   "SparseGP.predict_batch (host arrays in and out)"},
+        "fp64_ms_per_call": 1e3 * f64_b,
+        "fp64_one_structure_ms": 1e3 * f64_1,
+        "mixed": {"value": B * 256 / mix_b, "ms_per_call": 1e3 * mix_b,
+                  "energy_ev_per_atom_max":
+                      float(np.max(np.abs(rmx["energy"] - r64["energy"])) / 256),
+                  "force_mae_ev_per_a":
+                      float(np.mean(np.abs(rmx["forces"] - r64["forces"])))},
+        "fp64_plain": plain,
+        "cpu_oracle": {"value": cpu_v, "unit": "atoms/s", "cores": cpu_cores(),
+                       "sample": "2 structures after 1 warm-up"},
+        "fp64_vs_oracle": {
+            "energy_ev": float(abs(r64["energy"][0] - ref_e)),
+            "force_max_ev_per_a": float(np.max(np.abs(
+                r64["forces"][:256] - ref_f)))},
+        "train_setup_s": round(train_s, 1),
+    }), flush=True)
+
+
 def run_fcc1m(args):
     """One 1,048,576-atom FCC structure: energy, forces and virial through
     the reverse-mode adjoint (mixed and FP64), device memory, and the
@@ -900,6 +992,9 @@ def main():
         return
     if args.workload == "fcc1m":
         run_fcc1m(args)
+        return
+    if args.workload == "fcc256":
+        run_fcc256(args)
         return
     if args.workload == "md":
         run_md(args)

@@ -82,6 +82,55 @@ def build_alloy_model(n_train=None, per_species=None, verbose=False):
 # Gaussian displacements sigma = 0.08 A (seed 3000); B2 n_max = 10, l_max = 6,
 # rc = 5.0 A; model: 4,000 sparse environments from 16 seeded 256-atom FCC
 # structures at sigma = 0.08 (seeds 3001-3016), LJ energy and force labels.
+# ``fcc256``: the reference's small, CPU-runnable case: 4 x 4 x 4 FCC cells
+# (256 atoms, a = 4.05 A), Gaussian displacements sigma 0.05 A; B2
+# chebyshev/quadratic [1, 8, 3], rc 5.0 A; NormalizedDotProduct sigma 2,
+# power 2; 20 training cells (seeds 1000-1019) with truncated LJ energies and
+# forces (eps 0.4 eV, sigma 2.6 A); 200 sparse environments drawn without
+# replacement from the 20 x 256 pool (seed 1200); noise sigma_E 1e-3
+# eV/atom (0.256 eV per structure), sigma_F 0.05 eV/A, no stress labels;
+# test cells from seeds 1100, 1101, ...
+FCC256 = dict(n_cells=4, a=4.05, sigma_disp=0.05, rc=5.0, n_max=8, l_max=3,
+              sigma=2.0, power=2, n_train=20, train_seed0=1000, n_sparse=200,
+              sparse_seed=1200, test_seed0=1100, sigma_e=0.256, sigma_f=0.05,
+              sigma_s=1.0)
+
+
+def fcc256_structure(seed):
+    c = FCC256
+    return syn.fcc_al(n_cells=c["n_cells"], a=c["a"], sigma=c["sigma_disp"],
+                      seed=seed)
+
+
+def fcc256_sparse_choice():
+    c = FCC256
+    chosen = syn.rng(c["sparse_seed"]).choice(c["n_train"] * 256,
+                                              size=c["n_sparse"], replace=False)
+    return [sorted(int(q) - 256 * t for q in chosen if q // 256 == t)
+            for t in range(c["n_train"])]
+
+
+def build_fcc256_model():
+    """Train the fcc256 model on the GPU (FP64)."""
+    import flare_gb300 as fg
+    c = FCC256
+    b2 = fg.B2("chebyshev", "quadratic", [0.0, c["rc"]], [],
+               [1, c["n_max"], c["l_max"]])
+    k = fg.NormalizedDotProduct(c["sigma"], c["power"])
+    gp = fg.SparseGP([k], c["sigma_e"], c["sigma_f"], c["sigma_s"])
+    sparse = fcc256_sparse_choice()
+    for t in range(c["n_train"]):
+        cell, sp, pos = fcc256_structure(c["train_seed0"] + t)
+        st = fg.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, [0.4], [2.6], c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(st, sparse[t])
+    gp.update_matrices_QR()
+    return gp, b2, k
+
+
 FCC1M = dict(n_cells=64, a=4.05, sigma_disp=0.08, seed=3000, rc=5.0, n_max=10,
              l_max=6, sigma=2.0, power=2, n_train=16, train_seed0=3001,
              n_sparse=4000, sparse_seed=3200, sigma_e_per_atom=1e-3,
