@@ -485,9 +485,15 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
 
   // row and column tile of tile t; chunks of a tile (triangular B: columns
   // n0 .. n0+TN-1 need k < n0 + TN)
+  // Tiles row-major (a row tile's column tiles run together and share its A
+  // operand in L2), with the column order rotated by the row tile: a
+  // persistent CTA's tiles t, t + grid, ... then visit every column tile
+  // instead of a few (with a triangular B the column tiles differ in cost).
   auto tile_rc = [&](int t, int &mt, int &nt) {
     mt = fdiv(t, divNT);
-    nt = t - mt * NTt;
+    const int rot = mt - fdiv(mt, divNT) * NTt;
+    nt = t - mt * NTt + rot;
+    if (nt >= NTt) nt -= NTt;
   };
   auto tile_nch = [&](int nt) {
     const int n0 = nt * TN;
