@@ -609,8 +609,6 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (N > 0) {
     FGB_CUDA(cudaMemsetAsync(m->ws.e_atom.p, 0, sizeof(double) * N, st));
     FGB_CUDA(cudaMemsetAsync(m->ws.var.p, 0, sizeof(double) * N, st));
-    if (want_grad)
-      FGB_CUDA(cudaMemsetAsync(m->ws.gB2.p, 0, sizeof(double) * (size_t)N * p.n_d, st));
   }
   // the fold guard is known before the descriptor: models with large folded
   // coefficients take the descriptor, force product and adjoint at FP64
@@ -631,6 +629,16 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     StageTimer _pt(kStSpeciesPerm, st, 2 + 5 * p.n_species);
     if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
     m->last_species_counts = counts;
+  }
+  // dE/dB2 rows: the kernel stages write every row of a species with sparse
+  // environments; rows of species without any stay zero
+  if (want_grad && N > 0) {
+    bool zero = false;
+    for (int s = 0; s < p.n_species; s++)
+      zero |= counts[s] > 0 && m->h_counts[s] == 0;
+    if (zero)
+      FGB_CUDA(cudaMemsetAsync(m->ws.gB2.p, 0,
+                               sizeof(double) * (size_t)N * p.n_d, st));
   }
   if (precision == FGB_PREC_MIXED) {
     if ((rc = kernel_stage_mixed(m, N, counts, want_grad, want_v,
