@@ -182,6 +182,15 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------- GPU arm
+def clocks_path(name):
+    """Where a run's nvidia-smi clock samples go: $FGB_CLOCKS_DIR (created
+    if needed) or the temporary directory."""
+    import tempfile
+    d = os.environ.get("FGB_CLOCKS_DIR") or tempfile.gettempdir()
+    os.makedirs(d, exist_ok=True)
+    return os.path.join(d, name)
+
+
 class Clocks:
     def __init__(self, path):
         self.path = path
@@ -298,9 +307,7 @@ def run_ours(args, rank, world, local):
     # ---- timed region: device-resident inputs
     L.fgb_profile_reset()
     L.fgb_profile_enable(1)
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
-                    if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                    else f"/tmp/fgb_clocks_{rank}.csv")
+    clocks = Clocks(clocks_path(f"clocks_rank{rank}.csv"))
     per = []
     barrier(world)
     torch.cuda.synchronize()
@@ -753,8 +760,7 @@ def run_serve(args):
                 "p99_ms": float(np.percentile(lat, 99)),
                 "batches": srv.stats()["batches"] - b0}
 
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with Clocks(os.path.join(ROOT, "gpurun_out", "clocks_serve.csv")) as clocks:
+    with Clocks(clocks_path("clocks_serve.csv")) as clocks:
         sat = run(np.zeros(n_req))
         lam = sat["requests_per_s"]
         sweep = []
@@ -863,7 +869,7 @@ def run_mapped(args):
             per.append(e0.elapsed_time(e1))
         return float(np.median(per))
 
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_mapped.csv"))
+    clocks = Clocks(clocks_path("clocks_mapped.csv"))
     os.makedirs(os.path.dirname(clocks.path), exist_ok=True)
     with clocks:
         ms_map = timed(mapped_step)
@@ -922,7 +928,7 @@ def run_md(args):
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks_md.csv"))
+    clocks = Clocks(clocks_path("clocks_md.csv"))
     os.makedirs(os.path.dirname(clocks.path), exist_ok=True)
     with clocks:
         ev0.record()

@@ -171,7 +171,7 @@ def fcc_structure(n_cells=None, seed=None):
                       sigma=c["sigma_disp"], seed=seed or c["seed"])
 
 
-# ``md3`` (SURVEY C5): an ensemble of 2,000-atom 3-species cubic cells at
+# ``md3``: an ensemble of 2,000-atom 3-species cubic cells at
 # 0.06 atoms/A^3 (species fractions 0.5/0.3/0.2, masses 27/58/1 amu), filled
 # by random sequential addition with a 1.8 A minimum distance (replica r:
 # seed 5000 + r), Maxwell-Boltzmann velocities at 1,200 K (seed 5500 + r),
@@ -236,7 +236,7 @@ def build_md_model(n_train=None):
     return gp, b2, k
 
 
-# ``serve3`` (SURVEY C4): prediction requests of uneven size and species mix.
+# ``serve3``: prediction requests of uneven size and species mix.
 # Request q (seed 4000 + q): N = floor(exp(U[ln 32, ln 4096])) atoms, a
 # uniformly drawn number (1-3) of the 3 species with fractions uniform on the
 # simplex, density U[0.05, 0.09] atoms/A^3, random sequential addition with a
