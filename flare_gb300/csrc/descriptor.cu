@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 8 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
-             const double *__restrict__ gB2, double3 *__restrict__ pair_grad,
+             const T *__restrict__ gB2, double3 *__restrict__ pair_grad,
              int w_in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
@@ -305,7 +305,7 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       A[e] = as_compute(A_in[i * nA + e], T(0));
     if (W)
       for (int q = t; q < nd; q += blockDim.x)
-        W[q] = as_compute(gB2[i * nd + q], T(0));
+        W[q] = gB2[i * nd + q];
   }
   __syncthreads();
   // u = dE/dA: u[c][lm] = sum_b (1 + [b == c]) w((c,b), l) A[b][lm], a
@@ -315,7 +315,7 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     const T *A = smem + (size_t)a * per + nA;
     T *u = smem + (size_t)a * per;
     const T *W = w_in_smem ? A + nA : nullptr;
-    const double *w = gB2 + (long long)(i0 + a) * nd;
+    const T *w = gB2 + (long long)(i0 + a) * nd;
     const int c = e / nh, lm = e % nh;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
@@ -323,7 +323,7 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     for (int bb = 0; bb < nr; bb++) {
       const int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
       const int wi = pair_index(lo, hi, nr) * L1 + l;
-      const T wv = W ? W[wi] : as_compute(w[wi], T(0));
+      const T wv = W ? W[wi] : w[wi];
       const T f = (bb == c) ? T(2) : T(1);
       acc += f * wv * A[bb * nh + lm];
     }
@@ -477,6 +477,7 @@ struct FwdK {
 template <typename T, int NC, int LC>
 struct AdjK {
   static constexpr auto fn = k_b2_adjoint<T, NC, LC>;
+  using type = T;
 };
 
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
@@ -513,7 +514,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
 
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
-                      const double *d_gB2, double3 *d_pair_grad,
+                      const void *d_gB2, double3 *d_pair_grad,
                       cudaStream_t st, bool fp32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
@@ -533,10 +534,11 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
     if (e != cudaSuccess) return;
+    using G = typename decltype(k)::type;   // dE/dB2 in the compute type
     fn<<<ceil_div(N, kAdjAtoms), kAdjThreads, sm, st>>>(
         p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
-        nl->nbr_rel.as<double4_16a>(), d_species, d_A, d_gB2, d_pair_grad,
-        w_in_smem);
+        nl->nbr_rel.as<double4_16a>(), d_species, d_A,
+        static_cast<const G *>(d_gB2), d_pair_grad, w_in_smem);
   };
   if (fp32) dispatch_nl<AdjK, float>(p, go);
   else dispatch_nl<AdjK, double>(p, go);

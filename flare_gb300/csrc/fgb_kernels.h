@@ -10,9 +10,11 @@ size_t b2_adjoint_smem(const B2Params &p);
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
                       double *d_norms, cudaStream_t st, bool dfloat = false);
+// d_gB2: dE/dB2 rows [N, n_d] in the compute type (float when fp32, else
+// double)
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
-                      const double *d_gB2, double3 *d_pair_grad,
+                      const void *d_gB2, double3 *d_pair_grad,
                       cudaStream_t st, bool fp32 = false);
 int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
                   double *d_forces, double *d_virial, cudaStream_t st);

@@ -20,6 +20,7 @@
 #include <memory>
 #include <vector>
 
+#include "fgb_df.cuh"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 #include "fgb_model.h"
@@ -48,12 +49,18 @@ __device__ __forceinline__ void row_dots(int lane, int nd,
   }
 }
 
+// dE/dB2 in the adjoint's compute type (FP32: the mantissa cut the FP32
+// adjoint applies to FP64 inputs)
+__device__ __forceinline__ void put_g(double *g, double x) { *g = x; }
+__device__ __forceinline__ void put_g(float *g, double x) { *g = trunc_float(x); }
+
 // Power 2: warp per row m (atom perm[m]); Y row m = beta_s B2_atom.
+template <typename G>
 __global__ void k_mapped_pow2(int Mr, int nd, const int *__restrict__ perm,
                               const double *__restrict__ B2,
                               const double *__restrict__ Y, int normalized,
                               double *__restrict__ e_atom,
-                              double *__restrict__ gB2) {
+                              G *__restrict__ gB2) {
   const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (m >= Mr) return;
@@ -62,24 +69,25 @@ __global__ void k_mapped_pow2(int Mr, int nd, const int *__restrict__ perm,
   const double *y = Y + (long long)m * nd;
   double n2, dot;
   row_dots(lane, nd, b, y, n2, dot);
-  double *g = gB2 + (long long)atom * nd;
+  G *g = gB2 + (long long)atom * nd;
   if (n2 < kEmptySq) {
-    for (int k = lane; k < nd; k += 32) g[k] = 0.0;
+    for (int k = lane; k < nd; k += 32) put_g(g + k, 0.0);
     if (lane == 0) e_atom[atom] = 0.0;
     return;
   }
   const double e = normalized ? dot / n2 : dot;
   for (int k = lane; k < nd; k += 32)
-    g[k] = normalized ? 2.0 * (y[k] - e * b[k]) / n2 : 2.0 * y[k];
+    put_g(g + k, normalized ? 2.0 * (y[k] - e * b[k]) / n2 : 2.0 * y[k]);
   if (lane == 0) e_atom[atom] = e;
 }
 
 // Power 1: warp per row; beta_s a vector.
+template <typename G>
 __global__ void k_mapped_pow1(int Mr, int nd, const int *__restrict__ perm,
                               const double *__restrict__ B2,
                               const double *__restrict__ beta, int normalized,
                               double *__restrict__ e_atom,
-                              double *__restrict__ gB2) {
+                              G *__restrict__ gB2) {
   const int m = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (m >= Mr) return;
@@ -87,16 +95,16 @@ __global__ void k_mapped_pow1(int Mr, int nd, const int *__restrict__ perm,
   const double *b = B2 + (long long)atom * nd;
   double n2, dot;
   row_dots(lane, nd, b, beta, n2, dot);
-  double *g = gB2 + (long long)atom * nd;
+  G *g = gB2 + (long long)atom * nd;
   if (n2 < kEmptySq) {
-    for (int k = lane; k < nd; k += 32) g[k] = 0.0;
+    for (int k = lane; k < nd; k += 32) put_g(g + k, 0.0);
     if (lane == 0) e_atom[atom] = 0.0;
     return;
   }
   const double nrm = sqrt(n2);
   const double e = normalized ? dot / nrm : dot;
   for (int k = lane; k < nd; k += 32)
-    g[k] = normalized ? beta[k] / nrm - e * b[k] / n2 : beta[k];
+    put_g(g + k, normalized ? beta[k] / nrm - e * b[k] / n2 : beta[k]);
   if (lane == 0) e_atom[atom] = e;
 }
 
@@ -252,6 +260,8 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   // mixed: the descriptor in double-float and the adjoint in FP32, as in
   // the prediction pipeline; Y = B2 beta stays FP64-level (exact slicing)
   const bool mixed = precision == FGB_PREC_MIXED;
+  // FP32 adjoint (and dE/dB2 rows in FP32) unless the coefficients are large
+  const bool adj32 = mixed && !m->adjoint_f64;
   if ((want & FGB_WANT_LOCAL_VAR) && !m->has_var) {
     set_error("fgb_mapped_predict: no variance map loaded");
     return FGB_EINVAL;
@@ -318,15 +328,27 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
         if ((rc = oz::gemm_store(ws.ozA, *m->ozBeta[s], ws.kmat.as<double>(),
                                  nd, ws.ozerr.as<int>(), st)))
           return rc;
-        k_mapped_pow2<<<blocks, 256, 0, st>>>(
-            Mr, nd, perm, ws.B2.as<double>(), ws.kmat.as<double>(),
-            m->normalized ? 1 : 0, ws.e_atom.as<double>(), ws.gB2.as<double>());
+        if (adj32)
+          k_mapped_pow2<<<blocks, 256, 0, st>>>(
+              Mr, nd, perm, ws.B2.as<double>(), ws.kmat.as<double>(),
+              m->normalized ? 1 : 0, ws.e_atom.as<double>(), ws.gB2.as<float>());
+        else
+          k_mapped_pow2<<<blocks, 256, 0, st>>>(
+              Mr, nd, perm, ws.B2.as<double>(), ws.kmat.as<double>(),
+              m->normalized ? 1 : 0, ws.e_atom.as<double>(),
+              ws.gB2.as<double>());
         FGB_LAUNCH_CHECK("k_mapped_pow2");
       } else {
-        k_mapped_pow1<<<blocks, 256, 0, st>>>(
-            Mr, nd, perm, ws.B2.as<double>(),
-            m->beta.as<double>() + (size_t)s * nd, m->normalized ? 1 : 0,
-            ws.e_atom.as<double>(), ws.gB2.as<double>());
+        if (adj32)
+          k_mapped_pow1<<<blocks, 256, 0, st>>>(
+              Mr, nd, perm, ws.B2.as<double>(),
+              m->beta.as<double>() + (size_t)s * nd, m->normalized ? 1 : 0,
+              ws.e_atom.as<double>(), ws.gB2.as<float>());
+        else
+          k_mapped_pow1<<<blocks, 256, 0, st>>>(
+              Mr, nd, perm, ws.B2.as<double>(),
+              m->beta.as<double>() + (size_t)s * nd, m->normalized ? 1 : 0,
+              ws.e_atom.as<double>(), ws.gB2.as<double>());
         FGB_LAUNCH_CHECK("k_mapped_pow1");
       }
       if (want_v) {
@@ -342,8 +364,8 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   }
   if (want_grad) {
     if ((rc = launch_b2_adjoint(p, &m->nl, d_species, ws.A.as<double>(),
-                                ws.gB2.as<double>(), ws.pair_grad.as<double3>(),
-                                st, mixed && !m->adjoint_f64)) ||
+                                ws.gB2.p, ws.pair_grad.as<double3>(), st,
+                                adj32)) ||
         (rc = launch_forces(&m->nl, ws.pair_grad.as<double3>(),
                             ws.forces.as<double>(), ws.virial.as<double>(),
                             st)))

@@ -97,13 +97,14 @@ __global__ void k_fold_vec(int M, int nd, const double *__restrict__ S,
 
 // dE/dB2 rows from g = dE/dd^ (power 2: g = 2 sig2 Y; power 1: g = sig2 beta)
 // warp per row: d^ = B2 / |d| in FP32 (mantissa cut, no FP64 arithmetic),
-// q = d^ . g, dE/dB2 = (g - q d^) / |d|.
+// q = d^ . g, dE/dB2 = (g - q d^) / |d|, written in FP32 for the FP32
+// adjoint.
 __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
                               const double *__restrict__ norms,
                               const double *__restrict__ B2,
                               const float *__restrict__ Y,
                               const float *__restrict__ beta, float scale,
-                              double *__restrict__ gB2) {
+                              float *__restrict__ gB2) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= Mr) return;
@@ -121,7 +122,7 @@ __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
   for (int k = lane; k < nd; k += 32) {
     const float d = trunc_float(b[k]) * inv;
     const float g = scale * (y ? y[k] : beta[k]);
-    gB2[(long long)atom * nd + k] = f2d_exact((g - scale * q * d) * inv);
+    gB2[(long long)atom * nd + k] = (g - scale * q * d) * inv;
   }
 }
 
@@ -348,7 +349,7 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
         Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
         quad ? m->ws.yf.as<float>() : nullptr,
         quad ? nullptr : m->Bmap.as<float>() + per * s,
-        quad ? 2.f * sig2 : sig2, d_gB2);
+        quad ? 2.f * sig2 : sig2, reinterpret_cast<float *>(d_gB2));
     FGB_LAUNCH_CHECK("k_mapped_grad");
     return FGB_OK;
   };

@@ -656,12 +656,14 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (want_grad) {
     {
       StageTimer _pt(kStB2Adjoint, st);
-      // FP32 adjoint in the mixed path, unless the fold guard asked for
-      // FP64-level forces
+      // FP32 adjoint in the mixed path (dE/dB2 written in FP32 by the
+      // mapped gradient), unless the fold guard asked for FP64-level forces
+      // or the power has no folded form (FP64 kernel stage)
+      const bool adj32 = mixed && !m->force_f64 &&
+                         (m->power == 2.0 || m->power == 1.0);
       if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
-                                  m->ws.gB2.as<double>(),
-                                  m->ws.pair_grad.as<double3>(), st,
-                                  precision == FGB_PREC_MIXED && !m->force_f64)))
+                                  m->ws.gB2.p, m->ws.pair_grad.as<double3>(),
+                                  st, adj32)))
         return rc;
     }
     {
