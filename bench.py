@@ -511,11 +511,11 @@ def oz_eligible(gp, b2):
     return gp.kernels[0].power in (1.0, 2.0)
 
 
-# DRAM traffic of one kernel-GEMM launch (EpiKernel<8>, one species of the
-# alloy1000 batch, 8 slices): dram__bytes_read.sum + dram__bytes_write.sum
-# from one ncu capture (profiles/k_oz_gemm_alloy1000.md); applies to that
-# workload.
-OZ_KERNEL_TRAFFIC_ALLOY1000 = 414.3e6
+# DRAM traffic of one kernel-GEMM launch (EpiKernel<8>, 64-row B tiles, one
+# species of the alloy1000 batch, 8 slices): dram__bytes_read.sum +
+# dram__bytes_write.sum from one ncu capture
+# (profiles/k_oz_gemm_alloy1000.md); applies to that workload.
+OZ_KERNEL_TRAFFIC_ALLOY1000 = 422.4e6
 
 
 def bf16_peak():
