@@ -48,3 +48,12 @@ def test_load_ring_chunk_major(tmp_path):
 def test_tmem_drain(tmp_path):
     out = run_probe("tmem_drain", tmp_path)
     assert "mode 0:" in out and "mode 2:" in out
+
+
+def test_fp32_and_double_float_throughput(tmp_path):
+    """FP32 FMA and double-float multiply-accumulate throughput of the SMs:
+    the bounds the double-float descriptor stage is measured against."""
+    out = run_probe("fp32_peak", tmp_path)
+    m = re.search(r"fp32_tflops=([\d.]+) dfmac_gops=([\d.]+)", out)
+    fp32, dfmac = float(m.group(1)), float(m.group(2))
+    assert fp32 > 30.0 and dfmac > 500.0, out
