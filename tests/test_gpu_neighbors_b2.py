@@ -92,3 +92,40 @@ def test_b2_per_pair_cutoff_matrix():
     B, _ = g.b2_values()
     np.testing.assert_allclose(B.cpu().numpy(), o.descriptors[0].atom_B2,
                                rtol=1e-11, atol=1e-13)
+
+
+def test_b2_stored_gradients_match_oracle():
+    """fgb_b2_forward_dervs, the reference's stored forward-mode gradients
+    (compute_b2, b2.cpp:181-242): dB2/dr per neighbour pair and component
+    and force_dots = dB2/dr . B2, against the oracle's
+    descriptor_force_dervs / descriptor_force_dots (one species, so the
+    oracle's species blocks are in atom order)."""
+    import torch
+    import flare_gb300 as fg
+    from flare_gb300._lib import check, lib, ptr, stream_ptr
+    b2a = b2_args(1, 6, 3, 4.5)
+    cell, sp, pos = syn.fcc_al(n_cells=2, seed=5)
+    o = oracle.Structure(cell, sp, pos, 4.5, [oracle.B2Settings(*b2a)])
+    calc = fg.B2(*b2a[:5], cutoffs=b2a[5])
+    g = fg.Structure(cell, sp, pos, 4.5, [calc])
+    N, nd, P = len(sp), calc.n_descriptors, g.n_neighbors
+    dev = "cuda"
+    B2 = torch.zeros((N, nd), dtype=torch.float64, device=dev)
+    nrm = torch.zeros(N, dtype=torch.float64, device=dev)
+    dB2 = torch.zeros((3 * P, nd), dtype=torch.float64, device=dev)
+    fdot = torch.zeros(3 * P, dtype=torch.float64, device=dev)
+    d = g._inputs()
+    check(lib().fgb_b2_forward_dervs(calc.handle, g.nlist().h,
+                                     ptr(d["species"]), ptr(B2), ptr(nrm),
+                                     ptr(dB2), ptr(fdot), stream_ptr()),
+          "b2_forward_dervs")
+    ov = o.descriptors[0]
+    ref = ov.descriptor_force_dervs[0]
+    assert ref.shape == (3 * P, nd)
+    np.testing.assert_allclose(dB2.cpu().numpy(), ref, rtol=0,
+                               atol=1e-11 * np.abs(ref).max())
+    np.testing.assert_allclose(fdot.cpu().numpy(), ov.descriptor_force_dots[0],
+                               rtol=0, atol=1e-11 * np.abs(
+                                   ov.descriptor_force_dots[0]).max())
+    np.testing.assert_allclose(B2.cpu().numpy(), ov.atom_B2, rtol=1e-11,
+                               atol=1e-12 * np.abs(ov.atom_B2).max())
