@@ -77,7 +77,7 @@ __device__ __forceinline__ df finish(df a) {
 // in the compute type T: double (FP64 path) or df (double-float, the
 // mixed-precision path; the pair geometry arrives in FP64 and is split).
 template <typename T, int NC, int LC>
-__global__ void __launch_bounds__(kChunk)
+__global__ void __launch_bounds__(kChunk, 12)
 k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, double *__restrict__ A_out,
@@ -498,6 +498,11 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
     const bool regA = decltype(k)::kFixed && p.n_species * p.n_harm <= kChunk &&
                       p.n_species * p.n_max <= kChunk;
     const size_t sm = b2_forward_smem(p, regA);
+    // all of the SM's unified memory as shared memory: twelve blocks of
+    // ~19 KB each
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return;
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
     if (e != cudaSuccess) return;
