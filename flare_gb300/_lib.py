@@ -77,6 +77,7 @@ SIGNATURES = {
     "fgb_model_mapping": (_i, [_vp, _vp, _vp]),
     "fgb_model_fold_guard": (_i, [_vp, _vp, _vp, _vp]),
     "fgb_model_mixed_plan": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_wait_expiry_check": (_i, [ctypes.c_longlong, _vp, _vp]),
     "fgb_qr_thin_q": (_i, [_i, _i, _vp, _vp, _vp]),
     "fgb_mapped_create": (_i, [_pvp, _vp, _i, _i, _vp, _vp]),
     "fgb_mapped_destroy": (_i, [_vp]),

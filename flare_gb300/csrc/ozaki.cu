@@ -404,15 +404,45 @@ __device__ __forceinline__ int fdiv(int n, FastDiv f) {
   return f.d == 1 ? n : (int)__umul64hi((unsigned long long)(unsigned)n, f.m);
 }
 
-// Wait for a phase, giving up when `abort_flag` is raised or after
-// kWaitLimit polls: 0 done, 1 aborted elsewhere, 2 timed out.
+// Wait for a phase, giving up when `abort_flag` is raised or after `limit`
+// polls: 0 done, 1 aborted elsewhere, 2 timed out.
 __device__ __forceinline__ int wait_or_abort(uint64_t *bar, uint32_t phase,
-                                             volatile int *abort_flag) {
-  for (long long i = 0; i < kWaitLimit; i++) {
+                                             volatile int *abort_flag,
+                                             long long limit = kWaitLimit) {
+  for (long long i = 0; i < limit; i++) {
     if (tc::mbar_try_wait(bar, phase)) return 0;
     if (*abort_flag) return 1;
   }
   return 2;
+}
+
+// The GEMMs' give-up path on a barrier that nothing arrives at: warp 0
+// waits (bounded by `limit` polls) for a phase that never completes, raises
+// the CTA's abort flag and reports the time-out in *err, as a GEMM's
+// producer does; warp 1 waits on the same barrier and leaves through the
+// abort flag.  Nothing faults and every wait ends.
+__global__ void k_wait_expiry(long long limit, int *__restrict__ err,
+                              int *__restrict__ how) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_flag = 0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (lane == 0) {
+    const int w = wait_or_abort(&bar, 0, &abort_flag,
+                                warp == 0 ? limit : 64 * limit);
+    if (w == 2) {
+      abort_flag = 1;
+      atomicExch(err, 1);
+    }
+    how[warp] = w;
+  }
+  __syncthreads();
 }
 
 // Persistent, warp-specialised GEMM: one CTA per SM walks the tiles
@@ -893,6 +923,35 @@ extern "C" int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A,
   FGB_CUDA(cudaStreamSynchronize(st));
   if (h) {
     set_error("fgb_oz_sgemm_nt: a bounded device wait ran out");
+    return FGB_ETIMEOUT;
+  }
+  return FGB_OK;
+}
+
+extern "C" int fgb_wait_expiry_check(long long polls, int *h_how,
+                                     void *stream) {
+  if (polls < 1 || polls > oz::kWaitLimit) {
+    set_error("fgb_wait_expiry_check: polls must be in [1, %lld]",
+              oz::kWaitLimit);
+    return FGB_EINVAL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf err, how;
+  int rc;
+  if ((rc = err.ensure(sizeof(int))) || (rc = how.ensure(2 * sizeof(int))))
+    return rc;
+  FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  FGB_CUDA(cudaMemsetAsync(how.p, 0, 2 * sizeof(int), st));
+  oz::k_wait_expiry<<<1, 64, 0, st>>>(polls, err.as<int>(), how.as<int>());
+  FGB_LAUNCH_CHECK("k_wait_expiry");
+  int h = 0, hw[2] = {0, 0};
+  FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  FGB_CUDA(cudaMemcpyAsync(hw, how.p, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                           st));
+  FGB_CUDA(cudaStreamSynchronize(st));
+  if (h_how) { h_how[0] = hw[0]; h_how[1] = hw[1]; }
+  if (h) {
+    set_error("fgb_wait_expiry_check: a bounded device wait ran out");
     return FGB_ETIMEOUT;
   }
   return FGB_OK;

@@ -298,6 +298,14 @@ int fgb_model_mixed_plan(fgb_model_t m, int *h_kernel_slices,
                          double *h_slice_err_est, double *h_fold_max,
                          int *h_fp64_forces, void *stream);
 
+/* Self-check of the tensor-core GEMMs' give-up path: one CTA waits (at
+ * most `polls` polls, 1 <= polls <= 2^22) on a barrier that nothing arrives
+ * at, raises its abort flag and reports the time-out as a GEMM does; a
+ * second warp on the same barrier leaves through the abort flag.  Returns
+ * FGB_ETIMEOUT (the expected outcome; h_how[2] = 2 and 1: timed out, left on
+ * abort) with the context still usable, or another status on failure. */
+int fgb_wait_expiry_check(long long polls, int *h_how, void *stream);
+
 /* Thin Q (rows x cols, column-major) of the Householder QR of A (rows x
  * cols, column-major, rows >= cols), device buffers; the varmap
  * coefficients (normalized_dot_product.cpp:769-830) are its leading rows. */
