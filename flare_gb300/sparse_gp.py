@@ -4,10 +4,15 @@
 Same constructor, properties, ``update_db`` modes and JSON round trip
 (``as_dict``/``from_dict``/``write_model``/``from_file``: the model is
 rebuilt by replaying ``update_db`` on the stored training structures, then
-``update_matrices_QR``).  Training structures are stored as plain dicts
-(cell, numbers, positions, energy, forces, stress, rel_efs_noise) because
-ASE is optional here.  Hyperparameter optimisation (``train``) is outside
-the prediction path and raises NotImplementedError.
+``update_matrices_QR``).  Training structures are written in the layout
+the reference writes them in: ASE's ``Atoms.todict()`` (numbers, positions,
+cell, pbc, info with rel_efs_noise) with the labels under ``results``
+(energy as a list of zero or one totals, forces N x 3, stress as six values
+or an empty list), which ``FLARE_Atoms.from_dict`` reads
+(flare/atoms.py:162-183, flare/bffs/sgp/sparse_gp.py:190-211, 273-309).
+ASE itself is optional here: the records are plain dicts.  Hyperparameter
+optimisation (``train``) is outside the prediction path and raises
+NotImplementedError.
 """
 import json
 import warnings
@@ -178,15 +183,9 @@ class SGP_Wrapper:
         out["Kuu_jitter"] = self.sparse_gp.Kuu_jitter
         out["kernels"] = [("NormalizedDotProduct", k.sigma, k.power)
                           for k in self.sparse_gp.kernels]
-        out["training_structures"] = []
-        for d in self._training_dicts:
-            out["training_structures"].append({
-                "cell": d["cell"], "numbers": d["numbers"],
-                "positions": d["positions"], "energy": d["energy"],
-                "forces": d["forces"],
-                "stress": None if d["stress"] is None else
-                [None if v is None else float(v) for v in np.ravel(d["stress"])],
-                "info": {"rel_efs_noise": d["rel_efs_noise"]}})
+        out["training_structures"] = [
+            _training_record(d, self.energy_training, self.stress_training)
+            for d in self._training_dicts]
         out["sparse_indice"] = self.sparse_gp.sparse_indices
         return out
 
@@ -220,12 +219,11 @@ class SGP_Wrapper:
             custom_range = in_dict["sparse_indice"][0][s]
             atom_indices = in_dict["atom_indices"][s] if "atom_indices" in in_dict \
                 else [-1]
-            rel = td.get("info", {}).get("rel_efs_noise", [1, 1, 1])
-            stress = td.get("stress")
-            if not in_dict["stress_training"] or stress is None:
+            forces, energy, stress, rel = _read_training_record(td)
+            if not in_dict["stress_training"]:
                 stress = None
-            gp.update_db(_Atoms(td), td["forces"], custom_range=custom_range,
-                         energy=td["energy"], stress=stress, mode="specific",
+            gp.update_db(_Atoms(td), forces, custom_range=custom_range,
+                         energy=energy, stress=stress, mode="specific",
                          sgp=None, update_qr=False, atom_indices=atom_indices,
                          rel_e_noise=rel[0], rel_f_noise=rel[1],
                          rel_s_noise=rel[2])
@@ -247,6 +245,60 @@ class SGP_Wrapper:
     def __deepcopy__(self, memo):
         return SGP_Wrapper.from_dict(json.loads(json.dumps(
             self.as_dict(), cls=_NumpyEncoder)))[0]
+
+
+def _training_record(d, energy_training, stress_training):
+    """One training structure in the reference's file layout: ASE's
+    ``Atoms.todict()`` plus ``results`` (sparse_gp.py:190-211).  The energy
+    is the total as labelled (single-atom energies included); an energy or
+    stress that is not trained on is written as an empty list, as the
+    reference's empty label vectors are.  Structures given without forces
+    carry zeros (the reference's reader needs the key) and
+    ``info["has_forces"] = False``, so that a reload does not train on
+    them."""
+    n = len(d["numbers"])
+    energy = [] if d["energy"] is None or not energy_training \
+        else [float(d["energy"])]
+    stress = []
+    if d["stress"] is not None and stress_training:
+        st = [None if v is None else float(v) for v in np.ravel(d["stress"])]
+        if st and all(v is not None for v in st):
+            stress = st
+    info = {"rel_efs_noise": [float(v) for v in d["rel_efs_noise"]]}
+    if d["forces"] is None:
+        forces = np.zeros((n, 3))
+        info["has_forces"] = False
+    else:
+        forces = np.asarray(d["forces"], np.float64).reshape(n, 3)
+    return {"numbers": [int(z) for z in d["numbers"]],
+            "positions": np.asarray(d["positions"], np.float64).tolist(),
+            "cell": np.asarray(d["cell"], np.float64).tolist(),
+            "pbc": [True, True, True], "info": info,
+            "results": {"energy": energy, "forces": forces.tolist(),
+                        "stress": stress}}
+
+
+def _read_training_record(td):
+    """(forces, energy, stress, rel_efs_noise) of one stored training
+    structure, as the reference's reader takes them (sparse_gp.py:273-309):
+    labels from ``results`` (the reference's layout), or from the top level
+    (the flat layout earlier versions of this package wrote)."""
+    info = td.get("info") or {}
+    rel = list(info.get("rel_efs_noise", [1, 1, 1]))
+    if "results" in td:
+        res = td["results"]
+        e = res.get("energy")
+        e = np.ravel(np.asarray([] if e is None else e, np.float64))
+        energy = float(e[0]) if e.size else None
+        forces = res.get("forces")
+        if not info.get("has_forces", True):
+            forces = None
+        st = res.get("stress")
+        stress = None if st is None or np.size(st) == 0 else st
+    else:
+        energy, forces, stress = td.get("energy"), td.get("forces"), \
+            td.get("stress")
+    return forces, energy, stress, rel
 
 
 class _Atoms:
