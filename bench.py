@@ -225,7 +225,14 @@ class Clocks:
             rows = [l.split(",") for l in open(self.path).read().splitlines()]
         except Exception:
             return None
+        def numeric(r):
+            try:
+                float(r[1]), float(r[2])
+                return True
+            except ValueError:
+                return False
         rows = [[x.strip() for x in r] for r in rows if len(r) >= 9]
+        rows = [r for r in rows if numeric(r)]       # "[N/A]" samples
         rows = [r for r in rows if r[0] == str(dev_index)] or rows
         if not rows:
             return None
