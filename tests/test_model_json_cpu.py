@@ -95,3 +95,27 @@ def test_reads_flat_record():
     forces, energy, stress, rel = _read_training_record(rec)
     assert energy == -1.0 and stress is None and rel == [2, 1, 1]
     assert np.array_equal(forces, FORCES)
+
+
+def test_model_dict_has_every_key_the_reference_reads():
+    """The keys SGP_Wrapper.from_dict reads (sparse_gp.py:215-313) are all
+    written, and the dict survives JSON (an empty model: no GPU needed)."""
+    import flare_gb300 as fg
+    from flare_gb300.sparse_gp import SGP_Wrapper
+    b2 = fg.B2("chebyshev", "quadratic", [0, 5], [], [2, 4, 3])
+    w = SGP_Wrapper([fg.NormalizedDotProduct(2.0, 2)], [b2], 5.0, 0.01, 0.1,
+                    0.001, {13: 0, 29: 1}, single_atom_energies={0: -1.5, 1: 2})
+    d = json.loads(json.dumps(w.as_dict(), cls=_NumpyEncoder))
+    for key in ("kernels", "descriptor_calculators", "single_atom_energies",
+                "species_map", "cutoff", "hyps", "variance_type",
+                "energy_training", "force_training", "stress_training",
+                "max_iterations", "opt_method", "bounds", "Kuu_jitter",
+                "training_structures", "sparse_indice"):
+        assert key in d, key
+    assert d["kernels"] == [["NormalizedDotProduct", 2.0, 2]]
+    assert d["hyps"][-3:] == [0.01, 0.1, 0.001] and d["hyps"][0] == 2.0
+    bd = d["descriptor_calculators"][0]
+    assert bd["type"] == "B2" and bd["radial_basis"] == "chebyshev"
+    assert bd["cutoff_hyps"] == [] and bd["cutoffs"] == [[5.0, 5.0]] * 2
+    assert {int(k): v for k, v in d["species_map"].items()} == {13: 0, 29: 1}
+    assert d["training_structures"] == []
