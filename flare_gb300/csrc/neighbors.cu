@@ -23,7 +23,6 @@
 // checks that its FP64 decisions agree with the count pass.  One warp
 // serves one atom, a lane per bin image.
 #include <limits>
-#include <mutex>
 
 #include "fgb_internal.h"
 
@@ -862,9 +861,12 @@ extern "C" int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
 // the heap between steps.
 //
 // The array's name, used in host code, is only a host-side stand-in for the
-// symbol; the kernels need its device address, which is looked up once per
-// device with cudaGetSymbolAddress (on the first call made with that device
-// current) and cached.  Every call on a device shares the one array and
+// symbol; the kernels need its device address, which every call looks up
+// with cudaGetSymbolAddress for the device current at the call (an address
+// belongs to one context, so none is cached across calls: a context made
+// again after cudaDeviceReset gets a fresh one).  The first lookup on a
+// device loads the library's module into that context, so the first call
+// on each device should come before any stream capture.  Every call on a device shares the one array and
 // leaves its contents behind; each call clears what must start at zero (bin
 // counts, error flags, the structure index of each atom), so calls that run
 // one after another are independent, but calls that overlap on the GPU (for
@@ -875,29 +877,14 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = FGB_NOALLOC_SCRATCH_BYTES;  // 24 MiB
 static __device__ __align__(256) unsigned char g_nlist_scratch[kNoAllocScratchBytes];
 
-std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[64] = {nullptr};
-
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Device address of g_nlist_scratch on the current device (set-up on the
-// first call per device).
+// Device address of g_nlist_scratch in the current device's context.
 int noalloc_scratch(unsigned char **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
-  if (dev < 0 || dev >= 64) {
-    set_error("fgb_nlist_build_noalloc: device ordinal %d out of range", dev);
-    return FGB_EINVAL;
-  }
-  std::lock_guard<std::mutex> g(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_nlist_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_nlist_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
+  *out = static_cast<unsigned char *>(p);
   return FGB_OK;
 }
 
@@ -953,6 +940,14 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
     return FGB_EINVAL;
   }
   const long long nbins = (long long)geom.nb[0] * geom.nb[1] * geom.nb[2];
+  // two int arrays of nbins + 1 entries must fit the scratch; bounding the
+  // bin count first also keeps every size below in range
+  if (nbins < 1 ||
+      nbins > (long long)(kNoAllocScratchBytes / (2 * sizeof(int)))) {
+    set_error("fgb_nlist_build_noalloc: %lld cell-list bins exceed the "
+              "%zu-byte no-allocation scratch", nbins, kNoAllocScratchBytes);
+    return FGB_EINVAL;
+  }
   unsigned char *base = nullptr;
   int rc;
   if ((rc = noalloc_scratch(&base))) return rc;
@@ -963,7 +958,7 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
     off += align256(bytes);
     return p;
   };
-  const int nsum = (int)std::max<long long>(N, nbins) / 1024 + 2;
+  const int nsum = (int)(std::max<long long>(N, nbins) / 1024 + 2);
   StrucGeom *d_geom = (StrucGeom *)take(sizeof(StrucGeom));
   int *atom_struct = (int *)take(sizeof(int) * (N + 1));
   double *wrapped = (double *)take(sizeof(double) * 3 * (N + 1));

@@ -253,9 +253,10 @@ def _training_record(d, energy_training, stress_training):
     is the total as labelled (single-atom energies included); an energy or
     stress that is not trained on is written as an empty list, as the
     reference's empty label vectors are.  Structures given without forces
-    carry zeros (the reference's reader needs the key) and
-    ``info["has_forces"] = False``, so that a reload does not train on
-    them."""
+    carry an empty force list: the reference's reader passes it on as an
+    empty label vector (``FLARE_Atoms.from_dict`` then ``update_db``,
+    sparse_gp.py:273-309), so neither reader trains on force labels that
+    were never given."""
     n = len(d["numbers"])
     energy = [] if d["energy"] is None or not energy_training \
         else [float(d["energy"])]
@@ -266,8 +267,7 @@ def _training_record(d, energy_training, stress_training):
             stress = st
     info = {"rel_efs_noise": [float(v) for v in d["rel_efs_noise"]]}
     if d["forces"] is None:
-        forces = np.zeros((n, 3))
-        info["has_forces"] = False
+        forces = np.zeros((0,))
     else:
         forces = np.asarray(d["forces"], np.float64).reshape(n, 3)
     return {"numbers": [int(z) for z in d["numbers"]],
@@ -291,6 +291,10 @@ def _read_training_record(td):
         e = np.ravel(np.asarray([] if e is None else e, np.float64))
         energy = float(e[0]) if e.size else None
         forces = res.get("forces")
+        # an empty list is the reference's empty force-label vector;
+        # has_forces marks the zero-filled records older versions wrote
+        if forces is not None and np.size(forces) == 0:
+            forces = None
         if not info.get("has_forces", True):
             forces = None
         st = res.get("stress")

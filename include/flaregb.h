@@ -129,9 +129,13 @@ int fgb_nlist_export(fgb_nlist_t nl, int *d_neighbor_count,
  * message.  Outputs as in fgb_nlist_export (d_shifts may be NULL;
  * d_relative_positions 16-byte aligned); *h_n_pairs receives the pair count
  * (also when it exceeds max_pairs, so the caller can grow its buffers).
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture.  Calls share the array, so
- * calls that overlap on the GPU race; calls in sequence are independent. */
+ * Each call looks up the array's device address in the current context;
+ * the first call on each device also loads the module, so make that first
+ * call before any stream capture.  The call synchronises `stream` twice (to
+ * read the pair count, and to read the consistency flags at the end), so
+ * it returns with its outputs complete.  Calls share the array, so calls
+ * that overlap on the GPU race and must be serialised (for example on one
+ * stream); calls in sequence are independent. */
 #define FGB_NOALLOC_MAX_ATOMS 8192
 #define FGB_NOALLOC_MAX_PAIRS 262144
 #define FGB_NOALLOC_SCRATCH_BYTES (24u << 20)

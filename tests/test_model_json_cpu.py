@@ -61,10 +61,19 @@ def test_untrained_and_missing_labels():
         _stored(energy=None, forces=None,
                 stress=np.array([1.0, None, 2.0, 3.0, 4.0, 5.0], dtype=object)),
         True, True))
-    assert rec["results"]["forces"] == np.zeros((3, 3)).tolist()
-    assert rec["info"]["has_forces"] is False
+    # no fake labels: the force list is empty, and read the way the
+    # reference reads it (np.array of the list, reshape(-1)) it gives no
+    # force label at all
+    assert rec["results"]["forces"] == []
+    assert "has_forces" not in rec["info"]
+    assert np.array(rec["results"]["forces"]).reshape(-1).size == 0
     forces, energy, stress, _ = _read_training_record(rec)
     assert forces is None and energy is None and stress is None
+    # records older versions wrote: zero forces marked has_forces = False
+    rec["results"]["forces"] = np.zeros((3, 3)).tolist()
+    rec["info"]["has_forces"] = False
+    forces, _, _, _ = _read_training_record(rec)
+    assert forces is None
 
 
 def test_reads_reference_written_record():
