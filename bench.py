@@ -46,6 +46,9 @@ def parse():
                     help="structures (1000 atoms each) per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true")
+    ap.add_argument("--oracle-weights", default=None,
+                    help=argparse.SUPPRESS)
     ap.add_argument("--requests", type=int, default=0,
                     help="serve workload: number of requests (default 4096)")
     ap.add_argument("--replicas", type=int, default=0,
@@ -131,6 +134,27 @@ def oracle_step(oracle, gp, b2, seed):
     return len(sp)
 
 
+def oracle_reference(gp, b2, struct):
+    """E, F [N, 3], stress [6] and local variances (input order) of one
+    structure from the FP64 CPU oracle carrying the GPU model's sparse set,
+    alpha and L_inv (no training on the host)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from flare_gb300 import workloads as wl
+    k = gp.kernels[0]
+    ogp = oracle.SparseGP.from_weights(
+        [oracle.NormalizedDotProduct(k.sigma, k.power)],
+        gp.sparse_descriptors, gp.alpha, gp.L_inv)
+    ob2 = oracle.B2Settings("chebyshev", "quadratic", [0.0, wl.ALLOY["rc"]],
+                            [], [2, wl.ALLOY["n_max"], wl.ALLOY["l_max"]])
+    cell, sp, pos = struct
+    st = oracle.Structure(cell, sp, pos, wl.ALLOY["rc"], [ob2])
+    ogp.predict_local_uncertainties(st)
+    m = st.mean_efs
+    return (m[0], m[1:-6].reshape(-1, 3), m[-6:],
+            oracle.sort_variances(st, st.local_uncertainties[0]))
+
+
 def cpu_cores():
     return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
@@ -145,14 +169,69 @@ def time_oracle(n_structures, warm=1):
         t0 = time.perf_counter()
         atoms += oracle_step(oracle, gp, b2, 2100 + k)
         times.append(time.perf_counter() - t0)
-    return atoms / sum(times), times
+    sd = gp.sparse_descriptors[0]
+    weights = {"alpha": gp.alpha, "L_inv": gp.L_inv}
+    for s_ in range(sd.n_types):
+        weights[f"desc{s_}"] = sd.descriptors[s_]
+        weights[f"norm{s_}"] = sd.descriptor_norms[s_]
+    return atoms / sum(times), times, weights
+
+
+def oracle_model_from_weights(path):
+    """The oracle model from saved weights (no training)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from types import SimpleNamespace
+    from flare_gb300 import workloads as wl
+    c = wl.ALLOY
+    z = np.load(path)
+    nt = 2
+    sd = SimpleNamespace(n_types=nt, n_descriptors=z["desc0"].shape[1],
+                         descriptors=[z[f"desc{s}"] for s in range(nt)],
+                         descriptor_norms=[z[f"norm{s}"] for s in range(nt)])
+    gp = oracle.SparseGP.from_weights(
+        [oracle.NormalizedDotProduct(c["sigma"], c["power"])], [sd],
+        z["alpha"], z["L_inv"])
+    b2 = oracle.B2Settings("chebyshev", "quadratic", [0.0, c["rc"]], [],
+                           [2, c["n_max"], c["l_max"]])
+    return oracle, gp, b2
+
+
+def time_oracle_one_thread(weights):
+    """The oracle on one host thread (OpenMP and BLAS pinned to 1 in a child
+    process that loads the model's weights): one structure after one
+    warm-up."""
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "oracle_weights.npz")
+        np.savez(path, **weights)
+        env = dict(os.environ)
+        for k_ in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS",
+                   "MKL_NUM_THREADS", "BLIS_NUM_THREADS"):
+            env[k_] = "1"
+        r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"),
+                            "--impl", "reference", "--steps", "1",
+                            "--warmup", "1", "--oracle-weights", path],
+                           env=env, capture_output=True, text=True,
+                           timeout=600)
+    for line in r.stdout.splitlines():
+        if line.startswith("{"):
+            d = json.loads(line)
+            return {"value": d["value"], "unit": "atoms/s", "cores": 1,
+                    "sample": "one 1000-atom alloy structure after one "
+                              "warm-up, OMP and BLAS threads 1"}
+    return {"error": (r.stderr or r.stdout)[-300:]}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     cores = cpu_cores()
-    oracle, gp, b2 = oracle_model()
+    if args.oracle_weights:
+        oracle, gp, b2 = oracle_model_from_weights(args.oracle_weights)
+    else:
+        oracle, gp, b2 = oracle_model()
     for w in range(args.warmup):
         oracle_step(oracle, gp, b2, 2100 + w)
     times, atoms = [], 0
@@ -182,6 +261,36 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------- GPU arm
+def timed_steps(torch, stream, flush, step, steps):
+    """Per-step milliseconds from CUDA events on the launching stream; L2 is
+    flushed (a 256 MiB write) before every step, outside the events."""
+    per = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        torch.cuda.nvtx.range_push("timed_step")
+        step()
+        torch.cuda.nvtx.range_pop()
+        s1.record(stream)
+        s1.synchronize()
+        per.append(s0.elapsed_time(s1))
+    return per
+
+
+def read_stages(L):
+    """{stage name: (total ms, launches)} from the library's stage profiler."""
+    import ctypes
+    nst = L.fgb_profile_n_stages()
+    ms = ctypes_array("d", nst)
+    ln = ctypes_array("q", nst)
+    L.fgb_profile_read(ctypes.cast(ms, ctypes.c_void_p),
+                       ctypes.cast(ln, ctypes.c_void_p), nst)
+    return {L.fgb_profile_stage_name(i).decode(): (ms[i], ln[i])
+            for i in range(nst)}
+
+
 def clocks_path(name):
     """Where a run's nvidia-smi clock samples go: $FGB_CLOCKS_DIR (created
     if needed) or the temporary directory."""
@@ -311,36 +420,15 @@ def run_ours(args, rank, world, local):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    # ---- timed region: device-resident inputs
-    L.fgb_profile_reset()
-    L.fgb_profile_enable(1)
+    # ---- timed region: device-resident inputs, stage profiler off
+    L.fgb_profile_enable(0)
     clocks = Clocks(clocks_path(f"clocks_rank{rank}.csv"))
-    per = []
     barrier(world)
     torch.cuda.synchronize()
     with clocks:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            s0 = torch.cuda.Event(enable_timing=True)
-            s1 = torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            torch.cuda.nvtx.range_push("timed_step")
-            step()
-            torch.cuda.nvtx.range_pop()
-            s1.record(stream)
-            s1.synchronize()
-            per.append(s0.elapsed_time(s1))
+        per = timed_steps(torch, stream, flush, step, args.steps)
     torch.cuda.synchronize()
     barrier(world)
-    L.fgb_profile_enable(0)
-    nst = L.fgb_profile_n_stages()
-    ms = (ctypes_array("d", nst))
-    ln = (ctypes_array("q", nst))
-    import ctypes
-    L.fgb_profile_read(ctypes.cast(ms, ctypes.c_void_p),
-                       ctypes.cast(ln, ctypes.c_void_p), nst)
-    stage = {L.fgb_profile_stage_name(i).decode(): (ms[i], ln[i])
-             for i in range(nst)}
     total_ms = sum(per)
     total_ms_max = max_over_ranks(total_ms, world)
     atoms_all = N * args.steps * world
@@ -350,25 +438,65 @@ def run_ours(args, rank, world, local):
     res_s = out["s"].cpu().numpy().copy()
     res_v = out["v"].cpu().numpy().copy()
 
-    # ---- errors of this precision against the FP64 path, same batch
+    # ---- stage split: the same steps again with the per-stage CUDA-event
+    # profiler on (events on the launching stream); not part of `value`
+    L.fgb_profile_reset()
+    L.fgb_profile_enable(1)
+    prof_per = timed_steps(torch, stream, flush, step, args.steps)
+    torch.cuda.synchronize()
+    L.fgb_profile_enable(0)
+    stage = read_stages(L)
+
+    # ---- errors of this precision against the FP64 path (same batch), and
+    # the fused FP64 path's own throughput on it (CUDA events, same flush)
     errors = None
+    fp64_fused = None
+    nat = np.diff(offsets)
+    std = lambda v: np.where(v > 0, np.sqrt(np.abs(v)),
+                             -np.sqrt(np.abs(v))) / c["sigma"]
     if args.precision != "fp64":
         step(_lib.FGB_PREC_FP64)
         torch.cuda.synchronize()
+        k64 = max(3, min(args.steps, 5))
+        per64 = timed_steps(torch, stream, flush,
+                            lambda: step(_lib.FGB_PREC_FP64), k64)
+        fp64_fused = {"value": N * k64 / (sum(per64) * 1e-3),
+                      "unit": "atoms/s", "steps": k64,
+                      "sample": f"the same {B}-structure batch through the "
+                                "fused FP64 path (neighbours, FP64 B2, FP64 "
+                                "SIMT GEMMs, FP64 adjoint), CUDA events"}
         e64 = out["e"].cpu().numpy()
         f64 = out["f"].cpu().numpy()
         s64 = out["s"].cpu().numpy()
         v64 = out["v"].cpu().numpy()
-        nat = np.diff(offsets)
-        std = lambda v: np.where(v > 0, np.sqrt(np.abs(v)), -np.sqrt(np.abs(v))) / c["sigma"]
         errors = {
             "energy_ev_per_atom_max": float(np.max(np.abs(res_e - e64) / nat)),
             "force_mae_ev_per_a": float(np.mean(np.abs(res_f - f64))),
             "force_max_ev_per_a": float(np.max(np.abs(res_f - f64))),
             "stress_max_ev_per_a3": float(np.max(np.abs(res_s - s64))),
             "local_std_max_abs": float(np.max(np.abs(std(res_v) - std(v64)))),
-            "reference": "FP64 path of this library on the same batch "
-                         "(itself checked against the FP64 CPU oracle)"}
+            "reference": "FP64 path of this library on the same batch"}
+    # against the FP64 CPU oracle carrying this model's weights, on the
+    # batch's first structure (rank 0)
+    errors_oracle = None
+    if rank == 0 and not args.no_oracle_check:
+        n0 = int(nat[0])
+        E, F, Sg, V = oracle_reference(gp, b2, structs[0])
+        errors_oracle = {
+            "structure": "batch structure 0 (seed %d, %d atoms)"
+                         % (c["test_seed0"], n0),
+            "energy_ev_per_atom": float(abs(res_e[0] - E) / n0),
+            "force_mae_ev_per_a": float(np.mean(np.abs(res_f[:3 * n0] -
+                                                       F.reshape(-1)))),
+            "force_max_ev_per_a": float(np.max(np.abs(res_f[:3 * n0] -
+                                                      F.reshape(-1)))),
+            "stress_max_ev_per_a3": float(np.max(np.abs(res_s[:6] - Sg))),
+            "local_var_max_abs": float(np.max(np.abs(res_v[:n0] - V))),
+            "local_std_max_abs": float(np.max(np.abs(std(res_v[:n0]) -
+                                                     std(V)))),
+            "reference": "FP64 CPU oracle (restatement of flare_pp's "
+                         "predict_local_uncertainties) with this model's "
+                         "sparse set, alpha and L_inv"}
 
     # ---- e2e through the host-buffer C ABI (pinned buffers)
     h_pos = torch.from_numpy(pos).pin_memory()
@@ -411,7 +539,11 @@ def run_ours(args, rank, world, local):
                  "force_stage": "fp64-level" if f64.value else "fp32-level",
                  "fold_threshold": 200.0}
 
-    # ---- dominant kernel roofline
+    # ---- dominant kernel roofline.  Algorithmic FLOP per launch: the
+    # kernel GEMM c = d^ . s^ is 2 M_s n_d per atom of species s (one launch
+    # per species and row chunk), counted once whatever precision scheme
+    # carries it; the time is the GEMM kernel's own launches (the row
+    # slicing is a stage of its own).
     sizes = species_sizes(sp, offsets, gp)
     nd_ = b2.n_descriptors
     fp64_flops = {"kernel_gemm": sum(2.0 * n_s * m_s * nd_ for n_s, m_s in sizes),
@@ -421,48 +553,51 @@ def run_ours(args, rank, world, local):
     tensor = args.precision == "mixed" and oz_eligible(gp, b2)
     gemm_stage = max(fp64_flops, key=lambda s_: stage.get(s_, (0, 0))[0])
     st_ms, st_n = stage[gemm_stage]
-    # launches counted per stage: the tensor-core kernel stage counts row
-    # scales + slices + GEMM, its variance stage the GEMM alone
-    per_stage_launch = 3 if tensor and gemm_stage == "kernel_gemm" else 1
-    launches_per_step = st_n / per_stage_launch / args.steps
-    avg_ms = st_ms / (st_n / per_stage_launch)
+    launches_per_step = st_n / args.steps
+    avg_ms = st_ms / st_n
     alg = fp64_flops[gemm_stage] / max(launches_per_step, 1)
+    achieved = alg / (avg_ms * 1e-3) / 1e12
     fp64_peak = measure_fp64_peak(torch)
     if tensor:
-        # the algorithm executed on the tensor pipe: S(S+1)/2 BF16 slice
-        # products per FP64 product (S slices of 6 bits, a + b <= S + 1)
+        # executed on the tensor pipe: S(S+1)/2 BF16 slice products per
+        # FP64-level product (S slices of 6 bits, a + b <= S + 1)
         S_ = guard["kernel_slices"] if guard else 9
         products = S_ * (S_ + 1) // 2
-        flop = products * alg
         peak, peak_src = bf16_peak()
-        roofline = {"kernel": gemm_stage + " (tcgen05, exact BF16 slicing)",
-                    "bound": "tensor", "achieved": flop / (avg_ms * 1e-3) / 1e12,
+        roofline = {"kernel": gemm_stage + " (k_oz_gemm, tcgen05, exact BF16 "
+                              "slicing)",
+                    "bound": "tensor", "achieved": achieved,
                     "peak": peak, "unit": "TFLOP/s",
-                    "frac": flop / (avg_ms * 1e-3) / 1e12 / peak,
-                    "traffic": (OZ_KERNEL_TRAFFIC_ALLOY1000
-                                if gemm_stage == "kernel_gemm" and
-                                WORKLOAD.startswith("alloy1000") and B == 32
-                                and S_ == 8 else None),
-                    "traffic_source": "ncu dram__bytes_read.sum + "
-                                      "dram__bytes_write.sum, one capture",
+                    "frac": achieved / peak,
+                    "traffic": None,
+                    "traffic_note": "DRAM bytes are not measured in this run; "
+                                    "the ncu capture of this kernel is "
+                                    "summarised under profiles/",
                     "peak_source": peak_src,
-                    "flop_per_launch": flop, "avg_launch_ms": avg_ms,
-                    "fp64_equivalent_tflops": alg / (avg_ms * 1e-3) / 1e12,
-                    "fp64_dgemm_measured_tflops": fp64_peak,
+                    "flop_per_launch_algorithmic": alg,
+                    "avg_launch_ms": avg_ms,
+                    "launches_per_step": launches_per_step,
                     "slices": S_, "products_per_fp64_product": products,
-                    "note": "achieved counts the BF16 slice products the "
-                            "kernel executes per FP64 product; the stage time "
-                            "includes the row-slicing kernel"}
+                    "slice_products_tflops": products * achieved,
+                    "slice_products_frac": products * achieved / peak,
+                    "fp64_dgemm_measured_tflops": fp64_peak,
+                    "vs_fp64_dgemm": achieved / fp64_peak,
+                    "note": "achieved = algorithmic FLOP (2 M_s n_d per atom, "
+                            "counted once) / the GEMM kernel's mean launch "
+                            "time; the kernel carries it at FP64-level "
+                            "accuracy as products_per_fp64_product BF16 "
+                            "slice products (slice_products_frac = tensor "
+                            "pipe work against the same peak)"}
     else:
         roofline = {"kernel": gemm_stage, "bound": "tensor",
-                    "achieved": alg / (avg_ms * 1e-3) / 1e12, "peak": fp64_peak,
-                    "unit": "TFLOP/s",
-                    "frac": alg / (avg_ms * 1e-3) / 1e12 / fp64_peak,
+                    "achieved": achieved, "peak": fp64_peak,
+                    "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                     "traffic": None,
                     "peak_source": "FP64 cuBLAS DGEMM 8192^3 measured in this "
                                    "run (FP64 has no entry in the measured-peaks "
                                    "file)",
-                    "flop_per_launch": alg, "avg_launch_ms": avg_ms}
+                    "flop_per_launch_algorithmic": alg, "avg_launch_ms": avg_ms,
+                    "launches_per_step": launches_per_step}
     gpu_launches = int(sum(v[1] for v in stage.values()))
 
     result = {
@@ -486,6 +621,10 @@ def run_ours(args, rank, world, local):
         "roofline": roofline,
         "stages_ms_per_step": {k_: round(v[0] / args.steps, 4)
                                for k_, v in stage.items() if v[1]},
+        "stage_split": {"source": "a second pass of the same steps with the "
+                                  "per-stage CUDA-event profiler on",
+                        "ms_per_step": sum(prof_per) / args.steps},
+        "errors_vs_oracle": errors_oracle,
         "gpu_launches": gpu_launches,
         "errors_vs_fp64": errors,
         "mixed_plan": guard,
@@ -493,17 +632,25 @@ def run_ours(args, rank, world, local):
         "autotune": autotune_table(),
     }
     if rank == 0 and not args.no_plain:
-        result["fp64_plain"] = time_plain(L, _lib, model, structs[:2], b2, c,
+        result["fp64_plain"] = time_plain(L, _lib, model, structs[:6], b2, c,
                                           torch)
+        if result["fp64_plain"] and fp64_fused:
+            result["fp64_plain"]["mixed_over_plain"] = \
+                value / world / result["fp64_plain"]["value"]
+    if fp64_fused:
+        fp64_fused["mixed_over_fused_fp64"] = value / world / fp64_fused["value"]
+        result["fp64_fused"] = fp64_fused
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            v, ts = time_oracle(2)
+            v, ts, weights = time_oracle(2)
             result["cpu_baseline"] = {
                 "value": v, "unit": "atoms/s", "cores": cpu_cores(),
                 "kind": "port",
                 "sample": "2 alloy structures (2000 atoms) through the FP64 "
                           "CPU oracle (brute-force neighbours, stored-gradient "
                           "B2, envs_struc, local variance), after 1 warm-up"}
+            result["cpu_baseline"]["one_thread"] = time_oracle_one_thread(
+                weights)
         except Exception as ex:  # report, never hide
             result["cpu_baseline"] = {"error": repr(ex)}
     if rank == 0:
@@ -518,11 +665,6 @@ def oz_eligible(gp, b2):
     return gp.kernels[0].power in (1.0, 2.0)
 
 
-# DRAM traffic of one kernel-GEMM launch (EpiKernel<8>, 64-row B tiles, one
-# species of the alloy1000 batch, 8 slices): dram__bytes_read.sum +
-# dram__bytes_write.sum from one ncu capture
-# (profiles/k_oz_gemm_alloy1000.md); applies to that workload.
-OZ_KERNEL_TRAFFIC_ALLOY1000 = 422.4e6
 
 
 def bf16_peak():
@@ -550,9 +692,14 @@ def species_sizes(sp, offsets, gp):
 
 
 def time_plain(L, _lib, model, structs, b2, c, torch):
-    """The plain FP64 GPU form (reference algorithm: stored gradients,
-    envs_struc GEMM + scatter, K^T alpha, variance) per structure."""
+    """The plain FP64 GPU form of the reference algorithm (stored forward
+    gradients, envs_struc GEMM + scatter, K^T alpha, variance), one
+    structure per call: the first structure warms up, the others are timed
+    with CUDA events on the launching stream (the neighbour list is built
+    outside the events, as the reference's Structure does before
+    prediction)."""
     import flare_gb300 as fg
+    stream = torch.cuda.current_stream()
     times, atoms = [], 0
     for i, (cell, sp, pos) in enumerate(structs):
         st = fg.Structure(cell, sp, pos, c["rc"], [b2])
@@ -562,19 +709,21 @@ def time_plain(L, _lib, model, structs, b2, c, torch):
         mean = torch.zeros(1 + 3 * N + 6, dtype=torch.float64, device="cuda")
         var = torch.zeros(N, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
         _lib.check(L.fgb_predict_plain(model.h, nl.h, _lib.ptr(d["species"]),
                                        _lib.ptr(mean), _lib.ptr(var),
-                                       _lib.stream_ptr()))
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
+                                       _lib.stream_ptr(stream)))
+        s1.record(stream)
+        s1.synchronize()
         if i > 0:            # first one warms up
-            times.append(dt)
+            times.append(s0.elapsed_time(s1) * 1e-3)
             atoms += N
     if not times:
         return None
     return {"value": atoms / sum(times), "unit": "atoms/s",
-            "sample": f"{len(times)} structure(s) after 1 warm-up, wall clock"}
+            "sample": f"{len(times)} structures after 1 warm-up, CUDA events"}
 
 
 def run_fcc256(args):

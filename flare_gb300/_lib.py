@@ -67,6 +67,8 @@ SIGNATURES = {
     "fgb_struc_struc": (_i, [_vp, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_predict_plain": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "fgb_oz_dgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
+    "fgb_oz_dgemm_nt_slices": (_i, [_i, _i, _i, _i, _vp, _ll, _vp, _ll, _vp,
+                                    _ll, _vp]),
     "fgb_oz_sgemm_nt": (_i, [_i, _i, _i, _vp, _ll, _vp, _ll, _vp, _ll, _vp]),
     "fgb_md_create": (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _d, _i]),
     "fgb_md_destroy": (_i, [_vp]),

@@ -20,6 +20,7 @@ enum Stage {
   kStPlainDervs,
   kStPlainEnvsStruc,
   kStOther,
+  kStRowSlice,
   kNumStages
 };
 

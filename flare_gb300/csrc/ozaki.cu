@@ -860,7 +860,17 @@ using namespace fgb;
 extern "C" int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A,
                                long long lda, const double *d_B, long long ldb,
                                double *d_C, long long ldc, void *stream) {
-  if (M < 0 || N < 0 || K < 0 || (M && N && (!d_A || !d_B || !d_C))) {
+  return fgb_oz_dgemm_nt_slices(oz::kS, M, N, K, d_A, lda, d_B, ldb, d_C, ldc,
+                                stream);
+}
+
+extern "C" int fgb_oz_dgemm_nt_slices(int slices, int M, int N, int K,
+                                      const double *d_A, long long lda,
+                                      const double *d_B, long long ldb,
+                                      double *d_C, long long ldc,
+                                      void *stream) {
+  if (M < 0 || N < 0 || K < 0 || (M && N && (!d_A || !d_B || !d_C)) ||
+      (slices != 9 && slices != 8 && slices != 7)) {
     set_error("fgb_oz_dgemm_nt: invalid arguments");
     return FGB_EINVAL;
   }
@@ -877,11 +887,16 @@ extern "C" int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A,
   int rc;
   if ((rc = err.ensure(sizeof(int)))) return rc;
   FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-  if ((rc = oz::slice({M, K, oz::kTM, d_A, lda, nullptr, nullptr}, A, st)) ||
-      (rc = oz::slice({N, K, oz::kTN, d_B, ldb, nullptr, nullptr}, B, st)))
+  if ((rc = oz::slice({M, K, oz::kTM, d_A, lda, nullptr, nullptr}, A, st,
+                      slices)) ||
+      (rc = oz::slice({N, K, oz::kTN, d_B, ldb, nullptr, nullptr}, B, st,
+                      slices)))
     return rc;
-  if ((rc = oz::gemm(A, B, false, oz::EpiStore{d_C, ldc, N}, err.as<int>(), st)))
-    return rc;
+  const oz::EpiStore epi{d_C, ldc, N};
+  rc = slices == 9 ? oz::gemm_s<9>(A, B, false, epi, err.as<int>(), st)
+       : slices == 8 ? oz::gemm_s<8>(A, B, false, epi, err.as<int>(), st)
+                     : oz::gemm_s<7>(A, B, false, epi, err.as<int>(), st);
+  if (rc) return rc;
   int h = 0;
   FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
@@ -1262,11 +1277,14 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
         return rc;
       int vk = 0;
       {
-        StageTimer _pt(kStKernelGemm, st, 3);   // row scales, slices, GEMM
+        StageTimer _pt(kStRowSlice, st, 2);   // row scales, slices
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
                              m->ws.norms.as<double>()},
                             m->ws.ozA, st, SA)))
           return rc;
+      }
+      {
+        StageTimer _pt(kStKernelGemm, st, 1);
         auto launch = [&](int q) -> int {
           int r;
           if ((r = prepare_variant(q))) return r;

@@ -13,7 +13,7 @@ const char *kNames[kNumStages] = {
     "neighbors",      "b2_forward",     "species_perm",  "kernel_gemm",
     "row_energy",     "adjoint_gemm",   "variance_gemm", "variance_final",
     "b2_adjoint",     "forces",         "struct_reduce", "mapped_gemm",
-    "plain_dervs",    "plain_envs_struc", "other"};
+    "plain_dervs",    "plain_envs_struc", "other",       "row_slice"};
 
 struct Pending {
   int stage;

@@ -455,6 +455,13 @@ int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl, const int *d_species,
 int fgb_oz_dgemm_nt(int M, int N, int K, const double *d_A, long long lda,
                     const double *d_B, long long ldb, double *d_C,
                     long long ldc, void *stream);
+/* The same product at `slices` = 9, 8 or 7 BF16 slices per operand (54,
+ * 48 or 42 bits: the precisions the mixed path's kernel and variance GEMMs
+ * run at); the dropped digit products and slice residuals stay below
+ * 2^(-6 slices) of the row maxima.  No reference counterpart. */
+int fgb_oz_dgemm_nt_slices(int slices, int M, int N, int K, const double *d_A,
+                           long long lda, const double *d_B, long long ldb,
+                           double *d_C, long long ldc, void *stream);
 
 /* C = A B^T in FP32 accuracy on the same tensor-core kernel with 4 slices
  * (10 slice products, exact accumulation), FP64 inputs, FP32 output

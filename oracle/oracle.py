@@ -482,6 +482,34 @@ class SparseGP:
         self.n_strucs = 0
         self.L_inv = None
 
+    @staticmethod
+    def from_weights(kernels, sparse_descriptors, alpha, L_inv):
+        """A solved model carrying given weights (no training data): per
+        kernel a ClusterDescriptor-like object (n_types, n_descriptors,
+        descriptors, descriptor_norms, n_clusters_by_type), alpha [M] and
+        L_inv [M x M].  Prediction then follows sparse_gp.cpp:643-757 with
+        exactly these weights, so another implementation's model can be
+        checked against this oracle."""
+        gp = SparseGP(kernels, 1.0, 1.0, 1.0)
+        for i, sd in enumerate(sparse_descriptors):
+            cd = ClusterDescriptor(sd.n_types, sd.n_descriptors)
+            cd.descriptors = [np.asarray(d, np.float64).reshape(
+                -1, sd.n_descriptors) for d in sd.descriptors]
+            cd.descriptor_norms = [np.asarray(d, np.float64)
+                                   for d in sd.descriptor_norms]
+            cd.n_clusters_by_type = [len(d) for d in cd.descriptor_norms]
+            for s in range(1, cd.n_types):
+                cd.cumulative_type_count[s] = (cd.cumulative_type_count[s - 1]
+                                               + cd.n_clusters_by_type[s - 1])
+            cd.n_clusters = sum(cd.n_clusters_by_type)
+            gp.sparse_descriptors.append(cd)
+            gp.Kuu_kernels[i] = np.zeros((cd.n_clusters, cd.n_clusters))
+        gp.n_sparse = sum(cd.n_clusters for cd in gp.sparse_descriptors)
+        gp._stack_Kuu()
+        gp.alpha = np.asarray(alpha, np.float64).copy()
+        gp.L_inv = np.asarray(L_inv, np.float64).copy()
+        return gp
+
     def initialize_sparse_descriptors(self, structure):
         if self.sparse_descriptors:
             return

@@ -109,3 +109,27 @@ def c1_model(n_train=20, n_sparse=200, power=2):
     gp, b2 = oracle_model(strucs, labels, sparse, b2a, sigma=2.0, power=power,
                           noise=(0.256, 0.05, 1.0))
     return gp, b2a
+
+
+def alloy_oracle_model(n_train=2):
+    """Oracle SparseGP of the alloy1000 workload (flare_gb300.workloads):
+    2 species, B2 [2, 8, 4], rc 5.5 A, NormalizedDotProduct sigma 2 power
+    2, trained on the first ``n_train`` training structures with LJ energy
+    and force labels and the workload's sparse choice (about 1,000 sparse
+    environments per species)."""
+    from flare_gb300 import workloads as wl
+    c = wl.ALLOY
+    b2a = b2_args(2, c["n_max"], c["l_max"], c["rc"])
+    data = [wl.alloy_structure(c["train_seed0"] + t) for t in range(n_train)]
+    sparse = wl.alloy_sparse_choice(n_train, [d[1] for d in data],
+                                    c["sparse_per_species"], c["sparse_seed"])
+    labels = []
+    for cell, sp, pos in data:
+        E, F, _ = wl.alloy_labels(cell, sp, pos)
+        labels.append((E, F, None))
+    gp, _ = oracle_model(data, labels, sparse, b2a, sigma=c["sigma"],
+                         power=c["power"],
+                         noise=(c["sigma_e_per_atom"] * c["n_atoms"],
+                                c["sigma_f"], c["sigma_s"]),
+                         cutoff=c["rc"])
+    return gp, b2a

@@ -102,6 +102,95 @@ def test_extreme_row_scales(sa, sb):
     assert np.all(err <= 2e-15 * bound + 1e-300), float((err / bound).max())
 
 
+def oz_s(A, B, slices):
+    import torch
+    from flare_gb300 import _lib
+    M, K = A.shape
+    N = B.shape[0]
+    dA = torch.from_numpy(np.ascontiguousarray(A)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+    dC = torch.full((max(M, 1), max(N, 1)), np.nan, dtype=torch.float64,
+                    device="cuda")
+    _lib.check(_lib.lib().fgb_oz_dgemm_nt_slices(
+        slices, M, N, K, _lib.ptr(dA), K, _lib.ptr(dB), K, _lib.ptr(dC),
+        max(N, 1), _lib.stream_ptr()))
+    torch.cuda.synchronize()
+    return dC.cpu().numpy()[:M, :N]
+
+
+def emulate(A, B, S):
+    """Exact emulation of the S-slice product: per-row power-of-two scales,
+    X = rn(y 2^(6S)), balanced base-64 digits, the digit products with
+    a + b <= S + 1 summed exactly (integers below 2^53 in FP64), one final
+    rounding."""
+    from fractions import Fraction
+
+    def digits(X):
+        e = np.frexp(np.abs(X).max(1))[1].astype(np.int64)
+        Y = np.rint(np.ldexp(X, (6 * S - e)[:, None])).astype(np.int64)
+        bias = sum(32 << (6 * (S - a)) for a in range(2, S + 1))
+        U = Y + bias
+        d = [(U >> (6 * (S - 1))).astype(np.float64)]
+        for a in range(2, S + 1):
+            d.append((((U >> (6 * (S - a))) & 63) - 32).astype(np.float64))
+        return d, e
+
+    da, ea = digits(A)
+    db, eb = digits(B)
+    G = []
+    for t in range(2, S + 2):
+        g = np.zeros((A.shape[0], B.shape[0]))
+        for a in range(1, S + 1):
+            if 1 <= t - a <= S:
+                g += da[a - 1] @ db[t - a - 1].T
+        G.append(g)
+    out = np.zeros((A.shape[0], B.shape[0]))
+    for i in range(A.shape[0]):
+        for j in range(B.shape[0]):
+            v = sum(Fraction(int(G[t - 2][i, j])) / (1 << (6 * t))
+                    for t in range(2, S + 2))
+            out[i, j] = float(v * Fraction(2) ** int(ea[i] + eb[j]))
+    return out
+
+
+@pytest.mark.parametrize("S", [8, 7])
+def test_fewer_slices_match_exact_emulation(S):
+    """8 and 7 slices (the mixed path's kernel and variance GEMMs): the
+    result is the exactly rounded value of the truncated digit sum, so it
+    equals an exact CPU emulation bit for bit."""
+    r = np.random.Generator(np.random.PCG64(100 + S))
+    A = r.normal(size=(40, 96)) * np.exp(r.uniform(-4, 1, size=(40, 96)))
+    B = r.normal(size=(24, 96)) * np.exp(r.uniform(-4, 1, size=(24, 96)))
+    np.testing.assert_array_equal(oz_s(A, B, S), emulate(A, B, S))
+
+
+@pytest.mark.parametrize("S", [8, 7])
+@pytest.mark.parametrize("M,N,K", [(300, 130, 680), (257, 1000, 1000)])
+def test_fewer_slices_error_bound(S, M, N, K):
+    """At S slices the dropped digit products and the slice residuals stay
+    below 2^(-6S) (2^-48, 2^-42) of the row maxima: |C - A B^T| <=
+    2 2^(-6S) (max|A_i| sum|B_j| + sum|A_i| max|B_j|)."""
+    r = np.random.Generator(np.random.PCG64(M + N + S))
+    A = r.normal(size=(M, K)) * np.exp(r.uniform(-6, 2, size=(M, K)))
+    B = r.normal(size=(N, K)) * np.exp(r.uniform(-6, 2, size=(N, K)))
+    C = oz_s(A, B, S)
+    ref = A @ B.T
+    bound = np.abs(A).max(1)[:, None] * np.abs(B).sum(1)[None, :] + \
+        np.abs(A).sum(1)[:, None] * np.abs(B).max(1)[None, :]
+    err = np.abs(C - ref)
+    assert np.all(err <= 2.0 ** (1 - 6 * S) * bound + 2e-16 * np.abs(ref)), \
+        float((err / bound).max())
+    # and the error is not far below the bound: the slices are really cut
+    assert (err / bound).max() > 2.0 ** (-6 * S - 12)
+
+
+def test_slices_9_equals_default_entry():
+    r = np.random.Generator(np.random.PCG64(9))
+    A = r.normal(size=(130, 200))
+    B = r.normal(size=(70, 200))
+    np.testing.assert_array_equal(oz_s(A, B, 9), oz(A, B))
+
+
 def oz32(A, B):
     import torch
     from flare_gb300 import _lib

@@ -154,6 +154,22 @@ def test_local_variances_nonnegative_and_sparse_points_small():
     assert np.all(v > -1e-8)
 
 
+def test_model_from_weights_predicts_the_same():
+    """SparseGP.from_weights (the oracle carrying another model's weights)
+    predicts exactly what the trained model predicts."""
+    gp, b2a = small_two_species(seed=4, n_train=2)
+    twin = oracle.SparseGP.from_weights(gp.kernels, gp.sparse_descriptors,
+                                        gp.alpha, gp.L_inv)
+    cell, sp, pos = random_atoms(seed=77)
+    a = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    b = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    gp.predict_local_uncertainties(a)
+    twin.predict_local_uncertainties(b)
+    np.testing.assert_array_equal(a.mean_efs, b.mean_efs)
+    np.testing.assert_array_equal(a.local_uncertainties[0],
+                                  b.local_uncertainties[0])
+
+
 def _unit_rows(st):
     dv = st.descriptors[0]
     out = []
