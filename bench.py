@@ -533,8 +533,13 @@ def run_ours(args, rank, world, local):
         _lib.check(L.fgb_model_mixed_plan(model.h, ctypes.byref(sl),
                                           ctypes.byref(est), ctypes.byref(fmax),
                                           ctypes.byref(f64), sptr))
+        slv, vest = ctypes.c_int(0), ctypes.c_double(0.0)
+        _lib.check(L.fgb_model_slice_plan(model.h, None, ctypes.byref(slv),
+                                          None, ctypes.byref(vest), sptr))
         guard = {"kernel_slices": sl.value,
                  "slice_err_ev_per_atom": est.value,
+                 "variance_slices": slv.value,
+                 "variance_slice_err": vest.value,
                  "fold_max": fmax.value,
                  "force_stage": "fp64-level" if f64.value else "fp32-level",
                  "fold_threshold": 200.0}
@@ -561,7 +566,8 @@ def run_ours(args, rank, world, local):
     if tensor:
         # executed on the tensor pipe: S(S+1)/2 BF16 slice products per
         # FP64-level product (S slices of 6 bits, a + b <= S + 1)
-        S_ = guard["kernel_slices"] if guard else 9
+        S_ = (guard["variance_slices"] if gemm_stage == "variance_gemm"
+              else guard["kernel_slices"]) if guard else 9
         products = S_ * (S_ + 1) // 2
         peak, peak_src = bf16_peak()
         roofline = {"kernel": gemm_stage + " (k_oz_gemm, tcgen05, exact BF16 "

@@ -79,6 +79,8 @@ SIGNATURES = {
     "fgb_model_mapping": (_i, [_vp, _vp, _vp]),
     "fgb_model_fold_guard": (_i, [_vp, _vp, _vp, _vp]),
     "fgb_model_mixed_plan": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_model_slice_plan": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fgb_model_set_slices": (_i, [_vp, _i, _i]),
     "fgb_wait_expiry_check": (_i, [ctypes.c_longlong, _vp, _vp]),
     "fgb_qr_thin_q": (_i, [_i, _i, _vp, _vp, _vp]),
     "fgb_mapped_create": (_i, [_pvp, _vp, _i, _i, _vp, _vp]),

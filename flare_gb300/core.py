@@ -965,6 +965,9 @@ class SparseGP(_Training):
             if self.R_inv is not None:
                 R = np.ascontiguousarray(self.R_inv[:M, :M], np.float64)
                 check(lib().fgb_model_set_R_inv(m.h, ptr(R)), "SparseGP")
+            slices = getattr(self, "_slices", None)
+            if slices:
+                check(lib().fgb_model_set_slices(m.h, *slices), "set_slices")
             self._model = m
         return self._model
 
@@ -1062,19 +1065,34 @@ class SparseGP(_Training):
 
     def mixed_plan(self):
         """The mixed path's precision plan for this model: slices of the
-        kernel and variance GEMMs (9, 8 or 7) with the largest energy
-        difference to 9 slices measured on the sparse set when they were
-        chosen, and the fold guard (largest folded coefficient, whether the
-        descriptor and forces run at FP64 level)."""
+        kernel GEMM (9, 8 or 7) and of the variance GEMM (9, 8, 7 or 6)
+        with the largest energy (eV/atom) and local-variance differences to
+        9 slices measured on the sparse set when they were chosen, and the
+        fold guard (largest folded coefficient, whether the descriptor and
+        forces run at FP64 level)."""
         m = self._device_model()
-        S, fp64 = ctypes.c_int(0), ctypes.c_int(0)
-        est, fmax = ctypes.c_double(0.0), ctypes.c_double(0.0)
-        check(lib().fgb_model_mixed_plan(m.h, ctypes.byref(S),
-                                         ctypes.byref(est), ctypes.byref(fmax),
+        S, Sv, fp64 = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        est, vest = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        fmax = ctypes.c_double(0.0)
+        check(lib().fgb_model_mixed_plan(m.h, None, None, ctypes.byref(fmax),
                                          ctypes.byref(fp64), stream_ptr()),
               "mixed_plan")
-        return {"kernel_slices": S.value, "slice_err_ev_per_atom": est.value,
+        check(lib().fgb_model_slice_plan(m.h, ctypes.byref(S),
+                                         ctypes.byref(Sv), ctypes.byref(est),
+                                         ctypes.byref(vest), stream_ptr()),
+              "mixed_plan")
+        return {"kernel_slices": S.value, "variance_slices": Sv.value,
+                "slice_err_ev_per_atom": est.value,
+                "variance_slice_err": vest.value,
                 "fold_max": fmax.value, "fp64_forces": bool(fp64.value)}
+
+    def set_slices(self, kernel=0, variance=0):
+        """Force the mixed path's slice counts (kernel GEMM 7-9, variance
+        GEMM 6-9; 0 = the fewest the model's error probes allow)."""
+        self._slices = (int(kernel), int(variance))
+        if self._model is not None:
+            check(lib().fgb_model_set_slices(self._model.h, *self._slices),
+                  "set_slices")
 
     # -------------------------------------------------- mapped models
     def write_mapping_coefficients(self, file_name, contributor,

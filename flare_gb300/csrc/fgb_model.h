@@ -55,15 +55,22 @@ struct fgb_model_s {
   bool force_f64 = false;
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozB64;   // FP64-level B_s rows
   // mixed path: sliced sparse set and L_inv panels per species (tensor
-  // cores), one set per B tile width of the autotuner's candidates
+  // cores), one set per variant (slice count x B tile width of the
+  // autotuner's candidates), each sliced the first time it runs
   std::vector<std::unique_ptr<fgb::oz::Sliced>> ozS[fgb::oz::kF64Variants],
       ozL[fgb::oz::kF64Variants];
-  bool oz_ready[fgb::oz::kF64Variants] = {};
-  // slices of the kernel and variance GEMMs (9, 8 or 7) and the largest
-  // energy difference to 9 slices measured on the sparse set when they
-  // were chosen (choose_kernel_slices)
+  bool ozS_ready[fgb::oz::kF64Variants] = {};
+  bool ozL_ready[fgb::oz::kF64Variants] = {};
+  // slices of the kernel GEMM (9, 8 or 7) and of the variance GEMM (9, 8,
+  // 7 or 6) with the largest energy (eV/atom) and local-variance
+  // differences to 9 slices measured on the sparse set when they were
+  // chosen (choose_kernel_slices); forced counts (fgb_model_set_slices,
+  // 0 = chosen by the probes) outlive new weights
   int oz_S = fgb::oz::kS;
+  int oz_Sv = fgb::oz::kS;
   double oz_err_est = 0.0;
+  double oz_var_err_est = 0.0;
+  int oz_S_forced = 0, oz_Sv_forced = 0;
   bool slices_chosen = false;
   fgb_nlist_s nl;
   fgb_workspace ws;

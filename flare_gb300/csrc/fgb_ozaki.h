@@ -29,19 +29,24 @@ constexpr int kMaxKF32 = 2720;
 // sums land in the same 16-column slots whatever the tile.  FP32 level: B
 // tiles of kTNF32v[v] rows drained by kEWF32v[v] epilogue warps per TMEM
 // lane quarter.  All candidates give the same results bit for bit.
-// The mixed path's kernel and variance GEMMs take 9, 8 or 7 slices (54, 48
-// or 42 bits), the fewest that the model's error estimate allows
-// (choose_kernel_slices); variant v = 2 x (slice set) + (tile choice).
-// Tile candidates per slice count: B tiles of 48 and 32 rows, and of 64 rows
-// where S x 64 accumulator columns fit TMEM (S <= 8).
-constexpr int kNumSF64 = 3;
-constexpr int kSF64set[kNumSF64] = {9, 8, 7};
+// The mixed path's kernel GEMM takes 9, 8 or 7 slices (54, 48 or 42 bits)
+// and its variance GEMM 9, 8, 7 or 6 (36 bits), each the fewest that the
+// model's error probes allow (choose_kernel_slices); variant v =
+// kF64PerS x (slice set) + (tile choice).  Tile candidates per slice count:
+// B tiles of 48 and 32 rows, and of 64 rows where S x 64 accumulator
+// columns fit TMEM (S <= 8).
+constexpr int kNumSF64 = 4;
+constexpr int kSF64set[kNumSF64] = {9, 8, 7, 6};
 constexpr int kF64PerS = 3;
 constexpr int kF64Variants = kNumSF64 * kF64PerS;
-constexpr int kTNF64v[kF64Variants] = {48, 32, 48, 48, 32, 64, 48, 32, 64};
-constexpr int kSF64v[kF64Variants] = {9, 9, 9, 8, 8, 8, 7, 7, 7};
-constexpr int s_index(int S) { return S == 9 ? 0 : (S == 8 ? 1 : 2); }
+constexpr int kTNF64v[kF64Variants] = {48, 32, 48, 48, 32, 64,
+                                       48, 32, 64, 48, 32, 64};
+constexpr int kSF64v[kF64Variants] = {9, 9, 9, 8, 8, 8, 7, 7, 7, 6, 6, 6};
+constexpr int s_index(int S) { return 9 - S; }
 constexpr int n_cand_s(int S) { return S == 9 ? 2 : 3; }
+// slice counts each GEMM may take
+constexpr int kMinKernelSlices = 7;
+constexpr int kMinVarianceSlices = 6;
 constexpr int kF32Variants = 3;
 constexpr int kTNF32v[kF32Variants] = {128, 128, 64};
 constexpr int kEWF32v[kF32Variants] = {2, 4, 2};
@@ -67,11 +72,11 @@ struct Sliced {
 int pad_to(int x, int m);
 // Size `out` for rows x K in S slices (no conversion).
 int prepare(int rows, int K, int TR, int S, Sliced &out);
-// Slice rows into S = kS (FP64-level), 8 or 7 (the mixed path's kernel
+// Slice rows into S = kS (FP64-level), 8, 7 or 6 (the mixed path's kernel
 // and variance GEMMs) or kSF32 (FP32-level) digits.
 int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S = kS);
 
-// Product of S-slice operands (S = 9, 8 or 7; B.S == S, A.S >= S); the
+// Product of S-slice operands (S = 9, 8, 7 or 6; B.S == S, A.S >= S); the
 // tile shape follows B.TR (one of kTNF64v).
 template <int S, class Epi>
 int gemm_s(const Sliced &A, const Sliced &B, bool tri, const Epi &epi,

@@ -409,6 +409,46 @@ extern "C" int fgb_model_mixed_plan(fgb_model_t m, int *h_kernel_slices,
   return FGB_OK;
 }
 
+extern "C" int fgb_model_slice_plan(fgb_model_t m, int *h_kernel_slices,
+                                    int *h_variance_slices,
+                                    double *h_energy_err_est,
+                                    double *h_var_err_est, void *stream) {
+  if (!m) {
+    set_error("fgb_model_slice_plan: invalid arguments");
+    return FGB_EINVAL;
+  }
+  if (!m->solved) {
+    set_error("L_inv must be up to date to make predictions. Please call "
+              "update_matrices_QR and try again.");
+    return FGB_ESTALE;
+  }
+  int rc;
+  if ((rc = prepare_mixed(m, (cudaStream_t)stream))) return rc;
+  if (h_kernel_slices) *h_kernel_slices = m->oz_S;
+  if (h_variance_slices) *h_variance_slices = m->oz_Sv;
+  if (h_energy_err_est) *h_energy_err_est = m->oz_err_est;
+  if (h_var_err_est) *h_var_err_est = m->oz_var_err_est;
+  return FGB_OK;
+}
+
+extern "C" int fgb_model_set_slices(fgb_model_t m, int kernel_slices,
+                                    int variance_slices) {
+  if (!m || !(kernel_slices == 0 || (kernel_slices >= oz::kMinKernelSlices &&
+                                     kernel_slices <= oz::kS)) ||
+      !(variance_slices == 0 ||
+        (variance_slices >= oz::kMinVarianceSlices &&
+         variance_slices <= oz::kS))) {
+    set_error("fgb_model_set_slices: kernel slices must be 0 (chosen) or "
+              "%d..%d, variance slices 0 or %d..%d", oz::kMinKernelSlices,
+              oz::kS, oz::kMinVarianceSlices, oz::kS);
+    return FGB_EINVAL;
+  }
+  m->oz_S_forced = kernel_slices;
+  m->oz_Sv_forced = variance_slices;
+  m->slices_chosen = false;   // chosen again before the next mixed call
+  return FGB_OK;
+}
+
 extern "C" int fgb_model_mapping(fgb_model_t m, double *h_beta, void *stream) {
   if (!m || !h_beta || (m->power != 1.0 && m->power != 2.0)) {
     set_error("fgb_model_mapping: invalid arguments (power 1 or 2 models)");

@@ -791,6 +791,7 @@ int slice(const SliceSpec &sp, Sliced &out, cudaStream_t st, int S) {
   if (S == kS) return slice_s<kS>(sp, out, st);
   if (S == 8) return slice_s<8>(sp, out, st);
   if (S == 7) return slice_s<7>(sp, out, st);
+  if (S == 6) return slice_s<6>(sp, out, st);
   if (S == kSF32) return slice_s<kSF32>(sp, out, st);
   set_error("ozaki slice: unsupported slice count %d", S);
   return FGB_EINVAL;
@@ -984,13 +985,30 @@ namespace fgb {
 namespace oz {
 namespace {
 
+// k (16 values of one row) as SO BF16 slices at a fixed scale 2^eK, stored
+// at (m, n0) of a 128-row-tile operand of K extent KPv.
+template <int SO>
+__device__ __forceinline__ void store_k_slices(const double (&k)[16], int eK,
+                                               __nv_bfloat16 *Ksl, int m,
+                                               int n0, int KPv) {
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    long long X[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], kBeta * SO - eK);
+    store_digits8<SO>(X, Ksl + tiled_index<SO>(m, n0 + 8 * h, KPv, kTM),
+                      (size_t)kTM * kKC);
+  }
+}
+
 // Kernel GEMM epilogue: c = d^ . s^ -> k = sig^2 c^xi, zero for empty
 // environments and invalid sparse rows (the same expressions as the FP64
 // path).  Per row and tile it keeps sum_n alpha_n k_n (the energy partial,
 // finished in a fixed order by k_energy_final) and, for the variance GEMM,
-// writes k directly as S BF16 slices (A operand layout, 128-row tiles, K = N
-// padded to 16) under the fixed scale 2^eK > sig^2 >= |k|; the FP64 matrix
-// is written only when the variance runs in FP64.
+// writes k directly as SO BF16 slices (the variance GEMM's slice count; A
+// operand layout, 128-row tiles, K = N padded to 16) under the fixed scale
+// 2^eK > sig^2 >= |k|; the FP64 matrix is written only when the variance
+// runs in FP64.
 template <int S>
 struct EpiKernel {
   using Value = double;
@@ -999,6 +1017,7 @@ struct EpiKernel {
   __nv_bfloat16 *Ksl;         // optional slices of K (variance A operand)
   double *Kscale;             // their row scales (all 2^eK)
   int KPv, eK;
+  int SO;                     // slices of K written (9, 8, 7 or 6)
   double *epart;              // M x nslots energy partials
   int nslots;                 // B tiles x epilogue warps per quarter
   const double *alpha;
@@ -1021,14 +1040,12 @@ struct EpiKernel {
     }
     if (Ksl && n0 < KPv) {
       // 16 columns = one k chunk of the variance operand: two core-matrix
-      // rows of 8
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        long long X[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) X[j] = fixed_rn(k[8 * h + j], kBeta * S - eK);
-        store_digits8<S>(X, Ksl + tiled_index<S>(m, n0 + 8 * h, KPv, kTM),
-                         (size_t)kTM * kKC);
+      // rows of 8 (SO is uniform across the launch)
+      switch (SO) {
+        case 9: store_k_slices<9>(k, eK, Ksl, m, n0, KPv); break;
+        case 8: store_k_slices<8>(k, eK, Ksl, m, n0, KPv); break;
+        case 7: store_k_slices<7>(k, eK, Ksl, m, n0, KPv); break;
+        default: store_k_slices<6>(k, eK, Ksl, m, n0, KPv); break;
       }
     }
     return acc;
@@ -1073,19 +1090,17 @@ __global__ void k_energy_final(int M, int ntiles, const double *__restrict__ par
 }  // namespace oz
 
 
-// Slice the model operands for variant v (slice count and B tile height):
-// normalised sparse rows (B of the kernel GEMM) and the L_inv panels (B of
-// the variance GEMM), per species.  Done once per variant, the first time
-// the variant runs.
-static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
+// Slice the model operands for variant v (slice count and B tile height),
+// per species: the normalised sparse rows (B of the kernel GEMM) or the
+// L_inv panels (B of the variance GEMM).  Each is done once per variant,
+// the first time the variant runs.
+static int build_oz_S(fgb_model_s *m, int v, cudaStream_t st) {
   const int S = m->b2.n_species, nd = m->b2.n_d, TN = oz::kTNF64v[v];
   const int SL = oz::kSF64v[v];
   m->ozS[v].clear();
-  m->ozL[v].clear();
   int rc;
   for (int s = 0; s < S; s++) {
     m->ozS[v].emplace_back(new oz::Sliced());
-    m->ozL[v].emplace_back(new oz::Sliced());
     const int Ms = m->h_counts[s];
     if (Ms == 0) continue;
     if ((rc = oz::slice({Ms, nd, TN,
@@ -1093,73 +1108,125 @@ static int build_oz_model(fgb_model_s *m, int v, cudaStream_t st) {
                          nullptr, nullptr},
                         *m->ozS[v][s], st, SL)))
       return rc;
+  }
+  m->ozS_ready[v] = true;
+  return FGB_OK;
+}
+
+static int build_oz_L(fgb_model_s *m, int v, cudaStream_t st) {
+  const int S = m->b2.n_species, TN = oz::kTNF64v[v];
+  const int SL = oz::kSF64v[v];
+  m->ozL[v].clear();
+  int rc;
+  for (int s = 0; s < S; s++) {
+    m->ozL[v].emplace_back(new oz::Sliced());
+    const int Ms = m->h_counts[s];
+    if (Ms == 0) continue;
     if ((rc = oz::slice({m->h_panel_rows[s], Ms, TN,
                          m->Lp.as<double>() + m->h_panel_off[s], Ms, nullptr,
                          nullptr},
                         *m->ozL[v][s], st, SL)))
       return rc;
   }
-  m->oz_ready[v] = true;
+  m->ozL_ready[v] = true;
   return FGB_OK;
 }
 
+// The slice count as a compile-time constant.
+template <class F>
+static int with_slices(int S, F &&f) {
+  if (S == 8) return f(std::integral_constant<int, 8>{});
+  if (S == 7) return f(std::integral_constant<int, 7>{});
+  if (S == 6) return f(std::integral_constant<int, 6>{});
+  return f(std::integral_constant<int, oz::kS>{});
+}
 
-// Per-environment energies sum_t alpha_t k(s_i, s_t) of the sparse set's own
-// environments with S-slice operands (48-row B tiles), one per sparse row.
-static int probe_energies(fgb_model_s *m, int S, std::vector<double> &E,
-                          cudaStream_t st) {
-  const int v = oz::s_index(S) * oz::kF64PerS;
+// The sparse set's own environments through the mixed path's kernel and
+// variance GEMMs (48-row B tiles), one row per sparse environment: energies
+// sum_t alpha_t k(s_i, s_t) with the kernel GEMM at Sk slices and, when
+// Sv > 0, local variances k_self - |L_inv k_i|^2 with k written as Sv
+// slices and the variance GEMM at Sv slices.  Every sparse row meets
+// itself (c = 1, its own alpha), and its variance is the smallest the
+// model gives (about the jitter): the largest cancellation.
+static int probe_sparse(fgb_model_s *m, int Sk, int Sv, std::vector<double> &E,
+                        std::vector<double> &V, cudaStream_t st) {
+  const int vk = oz::s_index(Sk) * oz::kF64PerS;
+  const int vv = oz::s_index(Sv > 0 ? Sv : oz::kS) * oz::kF64PerS;
   int rc;
-  if (!m->oz_ready[v] && (rc = build_oz_model(m, v, st))) return rc;
-  const int nd = m->b2.n_d, M = m->M;
+  if (!m->ozS_ready[vk] && (rc = build_oz_S(m, vk, st))) return rc;
+  if (Sv > 0 && !m->ozL_ready[vv] && (rc = build_oz_L(m, vv, st))) return rc;
+  const int M = m->M, nd = m->b2.n_d;
   int maxMs = 0;
   for (int s = 0; s < m->b2.n_species; s++) maxMs = std::max(maxMs, m->h_counts[s]);
   std::vector<int> id(maxMs);
   for (int i = 0; i < maxMs; i++) id[i] = i;
-  DevBuf ident, erows, eout, err;
-  oz::Sliced A;
+  DevBuf ident, erows, eout, vout, part, err;
+  oz::Sliced A, Ksl;
   if ((rc = ident.ensure(sizeof(int) * (maxMs + 1))) ||
       (rc = eout.ensure(sizeof(double) * (M + 1))) ||
+      (rc = vout.ensure(sizeof(double) * (M + 1))) ||
       (rc = err.ensure(sizeof(int))))
     return rc;
   FGB_CUDA(cudaMemcpyAsync(ident.p, id.data(), sizeof(int) * maxMs,
                            cudaMemcpyHostToDevice, st));
   FGB_CUDA(cudaMemsetAsync(eout.p, 0, sizeof(double) * (M + 1), st));
+  FGB_CUDA(cudaMemsetAsync(vout.p, 0, sizeof(double) * (M + 1), st));
   FGB_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
   const double sig2 = m->sigma * m->sigma;
+  const int eK = std::ilogb(sig2) + 1;
   for (int s = 0; s < m->b2.n_species; s++) {
     const int Ms = m->h_counts[s], off = m->h_offsets[s];
     if (Ms == 0) continue;
     if ((rc = oz::slice({Ms, nd, oz::kTM, m->S.as<double>() + (size_t)off * nd,
                          nd, nullptr, nullptr},
-                        A, st, S)))
+                        A, st, Sk)))
       return rc;
-    const oz::Sliced &B = *m->ozS[v][s];
+    if (Sv > 0 && (rc = oz::prepare(Ms, Ms, oz::kTM, Sv, Ksl))) return rc;
+    const oz::Sliced &B = *m->ozS[vk][s];
     const int slots = B.RP / 16;
     if ((rc = erows.ensure(sizeof(double) * (size_t)Ms * slots))) return rc;
-    auto run = [&](auto sc) -> int {
+    rc = with_slices(Sk, [&](auto sc) -> int {
       constexpr int S_ = decltype(sc)::value;
-      oz::EpiKernel<S_> epi{nullptr, nullptr, nullptr, 0, 0,
-                            erows.as<double>(), slots,
+      oz::EpiKernel<S_> epi{nullptr,
+                            Sv > 0 ? Ksl.q.as<__nv_bfloat16>() : nullptr,
+                            Sv > 0 ? Ksl.scale.as<double>() : nullptr,
+                            Ksl.KP, eK, Sv, erows.as<double>(), slots,
                             m->alpha.as<double>() + off,
                             m->svalid.as<unsigned char>() + off, ident.as<int>(),
                             m->snorm.as<double>() + off, sig2, m->power, Ms};
       return oz::gemm_s<S_>(A, B, false, epi, err.as<int>(), st);
-    };
-    rc = S == 8 ? run(std::integral_constant<int, 8>{})
-                : (S == 7 ? run(std::integral_constant<int, 7>{})
-                          : run(std::integral_constant<int, oz::kS>{}));
+    });
     if (rc) return rc;
     oz::k_energy_final<<<ceil_div(Ms, 128), 128, 0, st>>>(
         Ms, slots, erows.as<double>(), ident.as<int>(),
         eout.as<double>() + off);
     FGB_LAUNCH_CHECK("k_energy_final");
+    if (Sv > 0) {
+      const oz::Sliced &L = *m->ozL[vv][s];
+      const int vslots = L.RP / 16;
+      if ((rc = part.ensure(sizeof(double) * (size_t)Ms * vslots))) return rc;
+      oz::EpiZsq zepi{part.as<double>(), vslots, m->h_panel_rows[s]};
+      rc = with_slices(Sv, [&](auto sc) -> int {
+        return oz::gemm_s<decltype(sc)::value>(Ksl, L, true, zepi,
+                                               err.as<int>(), st);
+      });
+      if (rc) return rc;
+      if ((rc = launch_variance_final(Ms, vslots, part.as<double>(),
+                                      ident.as<int>(),
+                                      m->snorm.as<double>() + off, sig2,
+                                      m->power, vout.as<double>() + off, st)))
+        return rc;
+    }
   }
   E.assign(M, 0.0);
+  V.assign(M, 0.0);
   int h = 0;
-  if (M > 0)
+  if (M > 0) {
     FGB_CUDA(cudaMemcpyAsync(E.data(), eout.p, sizeof(double) * M,
                              cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaMemcpyAsync(V.data(), vout.p, sizeof(double) * M,
+                             cudaMemcpyDeviceToHost, st));
+  }
   FGB_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
   if (h) {
@@ -1169,34 +1236,63 @@ static int probe_energies(fgb_model_s *m, int S, std::vector<double> &E,
   return FGB_OK;
 }
 
-// Slice count of the kernel and variance GEMMs: the fewest of 7, 8, 9 for
-// which the energies of the model's own sparse environments (the atoms'
-// environments are drawn from the same training data) differ from the
-// 9-slice ones by at most kSliceErr eV/atom, a hundredth of the mixed
-// path's energy budget.  The probe is pessimistic (each sparse row meets
-// itself, c = 1, with its own, typically largest, alpha: on the alloy
-// model its 8-slice difference is 1.5e-9 eV/atom where whole structures
-// differ by 2e-11), and the margin keeps the total energy of large cells
-// smooth enough for finite differences: the rounding of 7 slices, summed
-// over a 131,072-atom cell, moved (E(x+h) - E(x-h)) / 2h by 3e-3 eV/A at
-// h = 1e-4 A.  Measured once per model, before its first mixed prediction.
+static double max_abs_diff(const std::vector<double> &a,
+                           const std::vector<double> &b) {
+  double e = 0.0;
+  for (size_t i = 0; i < a.size(); i++) e = std::max(e, std::fabs(a[i] - b[i]));
+  return e;
+}
+
+// Slice counts of the kernel and variance GEMMs, chosen per model from the
+// sparse set's own environments (probe_sparse) against 9 slices:
+//   kernel GEMM: the fewest of 7, 8, 9 whose energies differ by at most
+//     kEnergyProbe = 1e-7 eV/atom, a tenth of the mixed path's energy
+//     budget of 1e-6 eV/atom;
+//   variance GEMM: the fewest of 6, 7, 8, 9 whose local variances differ
+//     by at most kVarProbe sigma^2 = 5e-9 sigma^2, half the stated
+//     local-variance budget of 1e-8 sigma^2 (local std sqrt|var| / sigma
+//     then errs by under 1e-4 anywhere, 1e-7 at std 0.05).
+// On held-out structures of the 2-species alloy model the errors track
+// these probes to within a factor of two (exact CPU emulation of the
+// slicing: energy 4.7e-8 eV/atom at 7 slices against a probe of 6.6e-8;
+// variance 9.4e-9 at 6 slices against 1.4e-8), the variance error coming
+// almost entirely from the variance GEMM's own slicing.  Forced counts
+// (fgb_model_set_slices) skip the probes.  Measured once per model, before
+// its first mixed prediction.
 int choose_kernel_slices(fgb_model_s *m, cudaStream_t st) {
-  constexpr double kSliceErr = 1e-8;   // eV/atom
-  m->oz_S = oz::kS;
+  constexpr double kEnergyProbe = 1e-7;   // eV/atom
+  constexpr double kVarProbe = 5e-9;      // x sigma^2
+  m->oz_S = m->oz_S_forced ? m->oz_S_forced : oz::kS;
+  m->oz_Sv = m->oz_Sv_forced ? m->oz_Sv_forced : oz::kS;
   m->oz_err_est = 0.0;
+  m->oz_var_err_est = 0.0;
   m->slices_chosen = true;
   if (m->M == 0) return FGB_OK;
   int rc;
-  std::vector<double> E9, Es;
-  if ((rc = probe_energies(m, oz::kS, E9, st))) return rc;
-  for (int S : {7, 8}) {
-    if ((rc = probe_energies(m, S, Es, st))) return rc;
-    double e = 0.0;
-    for (size_t i = 0; i < E9.size(); i++) e = std::max(e, std::fabs(Es[i] - E9[i]));
-    if (e <= kSliceErr) {
-      m->oz_S = S;
-      m->oz_err_est = e;
-      return FGB_OK;
+  std::vector<double> E9, V9, E, V;
+  if (!m->oz_S_forced) {
+    if ((rc = probe_sparse(m, oz::kS, 0, E9, V9, st))) return rc;
+    for (int S = oz::kMinKernelSlices; S < oz::kS; S++) {
+      if ((rc = probe_sparse(m, S, 0, E, V, st))) return rc;
+      const double e = max_abs_diff(E, E9);
+      if (e <= kEnergyProbe) {
+        m->oz_S = S;
+        m->oz_err_est = e;
+        break;
+      }
+    }
+  }
+  if (!m->oz_Sv_forced) {
+    const double vmax = kVarProbe * m->sigma * m->sigma;
+    if ((rc = probe_sparse(m, m->oz_S, oz::kS, E9, V9, st))) return rc;
+    for (int S = oz::kMinVarianceSlices; S < oz::kS; S++) {
+      if ((rc = probe_sparse(m, m->oz_S, S, E, V, st))) return rc;
+      const double e = max_abs_diff(V, V9);
+      if (e <= vmax) {
+        m->oz_Sv = S;
+        m->oz_var_err_est = e;
+        break;
+      }
     }
   }
   return FGB_OK;
@@ -1210,35 +1306,43 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
     set_error("tensor-core kernel stage: adjoint weights are not produced");
     return FGB_ENOTSUP;
   }
-  // the model's slice count; its two tile candidates are variants sb, sb + 1
-  const int SL = m->oz_S;
+  // the model's slice counts; each GEMM's tile candidates are variants
+  // sb + q (kernel GEMM, sparse rows at SL slices) and vb + q (variance
+  // GEMM, L_inv panels at SV slices)
+  const int SL = m->oz_S, SV = m->oz_Sv;
   const int sb = oz::s_index(SL) * oz::kF64PerS;
-  if (!m->oz_ready[sb]) {
+  const int vb = oz::s_index(SV) * oz::kF64PerS;
+  if (!m->ozS_ready[sb] || (want_var && !m->ozL_ready[vb])) {
     if (fixed) {
       set_error("tensor-core kernel stage: operands not sliced before a fixed call");
       return FGB_EINVAL;
     }
-    if ((rc = build_oz_model(m, sb, st))) return rc;
+    if (!m->ozS_ready[sb] && (rc = build_oz_S(m, sb, st))) return rc;
+    if (want_var && !m->ozL_ready[vb] && (rc = build_oz_L(m, vb, st)))
+      return rc;
   }
   // candidate q usable without preparation; prepare it (not in fixed calls)
-  auto usable = [m, sb](int q) { return m->oz_ready[sb + q]; };
-  auto prepare_variant = [&](int q) -> int {
-    if (m->oz_ready[sb + q]) return FGB_OK;
+  auto usable_k = [m, sb](int q) { return m->ozS_ready[sb + q]; };
+  auto usable_v = [m, vb](int q) { return m->ozL_ready[vb + q]; };
+  auto prepare_k = [&](int q) -> int {
+    if (m->ozS_ready[sb + q]) return FGB_OK;
     if (fixed) {
       set_error("tensor-core kernel stage: tile variant not prepared");
       return FGB_EINVAL;
     }
-    return build_oz_model(m, sb + q, st);
+    return build_oz_S(m, sb + q, st);
   };
-  // the slice count as a compile-time constant for the GEMM instantiations
-  auto with_s = [SL](auto &&f) -> int {
-    if (SL == 8) return f(std::integral_constant<int, 8>{});
-    if (SL == 7) return f(std::integral_constant<int, 7>{});
-    return f(std::integral_constant<int, oz::kS>{});
+  auto prepare_v = [&](int q) -> int {
+    if (m->ozL_ready[vb + q]) return FGB_OK;
+    if (fixed) {
+      set_error("tensor-core kernel stage: tile variant not prepared");
+      return FGB_EINVAL;
+    }
+    return build_oz_L(m, vb + q, st);
   };
-  // descriptor rows: the model's slices, or all kS when the fold guard
-  // sends the force product through the FP64-level GEMM (the FP32-level
-  // force GEMM reads the first kSF32)
+  // descriptor rows: the kernel GEMM's slices, or all kS when the fold
+  // guard sends the force product through the FP64-level GEMM (the
+  // FP32-level force GEMM reads the first kSF32)
   const int SA = m->force_f64 ? oz::kS : SL;
   const B2Params &p = m->b2;
   const int nd = p.n_d;
@@ -1273,7 +1377,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       const int Mr = std::min(kRows, Ns - r0);
       const int *perm = perm_s + r0;
       if ((rc = m->ws.erows.ensure(sizeof(double) * (size_t)Mr * kslots)) ||
-          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, SL, m->ws.ozK))))
+          (var_oz && (rc = oz::prepare(Mr, Ms, oz::kTM, SV, m->ws.ozK))))
         return rc;
       int vk = 0;
       {
@@ -1287,14 +1391,14 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
         StageTimer _pt(kStKernelGemm, st, 1);
         auto launch = [&](int q) -> int {
           int r;
-          if ((r = prepare_variant(q))) return r;
+          if ((r = prepare_k(q))) return r;
           const oz::Sliced &B = *m->ozS[sb + q][s];
-          return with_s([&](auto sc) -> int {
+          return with_slices(SL, [&](auto sc) -> int {
             constexpr int S_ = decltype(sc)::value;
             oz::EpiKernel<S_> epi{
                 nullptr, var_oz ? m->ws.ozK.q.as<__nv_bfloat16>() : nullptr,
                 var_oz ? m->ws.ozK.scale.as<double>() : nullptr, m->ws.ozK.KP,
-                eK, m->ws.erows.as<double>(), B.RP / 16,
+                eK, SV, m->ws.erows.as<double>(), B.RP / 16,
                 m->alpha.as<double>() + m->h_offsets[s],
                 m->svalid.as<unsigned char>() + m->h_offsets[s], perm,
                 m->ws.norms.as<double>(), sig2, m->power, Ms};
@@ -1303,7 +1407,7 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
           });
         };
         if ((rc = tune::run(tune::kOpKernelGemm, Mr, Ms, nd, oz::n_cand_s(SL),
-                            launch, usable, st, fixed, &vk)))
+                            launch, usable_k, st, fixed, &vk)))
           return rc;
         vk += sb;
       }
@@ -1322,19 +1426,19 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
           StageTimer _pt(kStVarianceGemm, st);
           auto launch = [&](int q) -> int {
             int r;
-            if ((r = prepare_variant(q))) return r;
-            const oz::Sliced &B = *m->ozL[sb + q][s];
+            if ((r = prepare_v(q))) return r;
+            const oz::Sliced &B = *m->ozL[vb + q][s];
             oz::EpiZsq epi{m->ws.part.as<double>(), B.RP / 16, R};
-            return with_s([&](auto sc) -> int {
+            return with_slices(SV, [&](auto sc) -> int {
               return oz::gemm_s<decltype(sc)::value>(
                   m->ws.ozK, B, true, epi, m->ws.ozerr.as<int>(), st);
             });
           };
           if ((rc = tune::run(tune::kOpVarianceGemm, Mr, R, Ms,
-                              oz::n_cand_s(SL), launch, usable, st, fixed,
+                              oz::n_cand_s(SV), launch, usable_v, st, fixed,
                               &vv)))
             return rc;
-          vv += sb;
+          vv += vb;
         }
         if ((rc = launch_variance_final(Mr, m->ozL[vv][s]->RP / 16,
                                         m->ws.part.as<double>(), perm,

@@ -479,10 +479,13 @@ extern "C" int fgb_model_set(fgb_model_t m, const int *h_counts,
   m->lfull_ready = false;
   m->slices_chosen = false;
   m->oz_S = oz::kS;
+  m->oz_Sv = oz::kS;
   m->oz_err_est = 0.0;
+  m->oz_var_err_est = 0.0;
   m->force_f64 = false;
   m->fold_max = 0.0;
-  for (bool &r : m->oz_ready) r = false;
+  for (bool &r : m->ozS_ready) r = false;
+  for (bool &r : m->ozL_ready) r = false;
   for (bool &r : m->ozB_ready) r = false;
   if (!h_alpha || !h_L_inv) return FGB_OK;
   if ((rc = m->alpha.ensure(sizeof(double) * (M + 1)))) return rc;

@@ -61,8 +61,8 @@ enum {
 enum {
   FGB_PREC_FP64 = 0,  /* FP64 adjoint path                                   */
   FGB_PREC_MIXED = 1  /* double-float descriptors, tensor-core kernel and
-                         variance GEMMs by exact slicing to 54, 48 or 42 bits
-                         (fgb_model_mixed_plan), FP32-level
+                         variance GEMMs by exact slicing to 54 down to 42
+                         and 36 bits (fgb_model_slice_plan), FP32-level
                          tensor-core force GEMM and FP32 adjoint; models
                          whose largest folded coefficient exceeds 200
                          (fgb_model_fold_guard) get the force stage at
@@ -291,16 +291,33 @@ int fgb_model_fold_guard(fgb_model_t m, double *h_fold_max,
                          int *h_fp64_forces, void *stream);
 
 /* The mixed path's precision plan for a solved model: h_kernel_slices =
- * BF16 slices of the kernel and variance GEMMs (9, 8 or 7: 54, 48 or 42
- * bits), the fewest for which the energies of the model's own sparse
- * environments differ from the 9-slice ones by at most 1e-8 eV/atom, and
- * h_slice_err_est = that largest difference (measured once per model,
- * before its first mixed prediction); h_fold_max and h_fp64_forces as
- * fgb_model_fold_guard.  Powers other than 1 and 2 run the mixed path's
- * kernel stages in FP64 (9 reported).  Any output may be NULL. */
+ * BF16 slices of the kernel GEMM (9, 8 or 7: 54, 48 or 42 bits) and
+ * h_slice_err_est = the largest energy difference to 9 slices measured on
+ * the model's sparse environments (fgb_model_slice_plan gives the variance
+ * GEMM's count too); h_fold_max and h_fp64_forces as fgb_model_fold_guard.
+ * Powers other than 1 and 2 run the mixed path's kernel stages in FP64 (9
+ * reported).  Any output may be NULL. */
 int fgb_model_mixed_plan(fgb_model_t m, int *h_kernel_slices,
                          double *h_slice_err_est, double *h_fold_max,
                          int *h_fp64_forces, void *stream);
+
+/* The mixed path's slice counts for a solved model: h_kernel_slices (9, 8
+ * or 7: the kernel GEMM c = d^ . s^, whose energies must stay within 1e-6
+ * eV/atom) and h_variance_slices (9, 8, 7 or 6: the variance GEMM
+ * z = L_inv k, whose local variances must stay within 1e-8 sigma^2), each
+ * the fewest for which the model's own sparse environments differ from 9
+ * slices by at most a tenth of the energy budget (1e-7 eV/atom) and half
+ * the variance budget (5e-9 sigma^2), with those largest differences in
+ * h_energy_err_est and h_var_err_est (measured once per model, before its
+ * first mixed prediction; 0 when a count is forced).  Any output may be
+ * NULL.  No reference counterpart. */
+int fgb_model_slice_plan(fgb_model_t m, int *h_kernel_slices,
+                         int *h_variance_slices, double *h_energy_err_est,
+                         double *h_var_err_est, void *stream);
+/* Force the slice counts (kernel 7..9, variance 6..9; 0 = chosen by the
+ * probes above); kept across new weights.  No reference counterpart. */
+int fgb_model_set_slices(fgb_model_t m, int kernel_slices,
+                         int variance_slices);
 
 /* Self-check of the tensor-core GEMMs' give-up path: one CTA waits (at
  * most `polls` polls, 1 <= polls <= 2^22) on a barrier that nothing arrives

@@ -99,13 +99,21 @@ def test_alloy_fp64_matches_oracle(alloy):
         np.testing.assert_allclose(v, V, rtol=0, atol=V64_TOL)
 
 
-def test_alloy_mixed_matches_oracle(alloy):
+@pytest.mark.parametrize("slices", [None, (8, 8), (7, 6)])
+def test_alloy_mixed_matches_oracle(alloy, slices):
     """The mixed path (double-float descriptor, exact-slicing tensor-core
     kernel and variance GEMMs, FP32-level force GEMM, FP32 adjoint)
-    against the oracle itself, not against this library's FP64 path."""
+    against the oracle itself, not against this library's FP64 path: at the
+    slice counts the probes choose (None) and forced to 8/8 and to the
+    fewest the path takes, 7 for the kernel GEMM and 6 for the variance."""
     ogp, b2a, ggp, calc, tests, ref = alloy
+    ggp.set_slices(*(slices or (0, 0)))
     plan = ggp.mixed_plan()
-    assert plan["kernel_slices"] in (7, 8, 9), plan
+    if slices:
+        assert (plan["kernel_slices"], plan["variance_slices"]) == slices
+    else:
+        assert plan["kernel_slices"] in (7, 8, 9), plan
+        assert plan["variance_slices"] in (6, 7, 8, 9), plan
     assert not plan["fp64_forces"], plan   # alloy folds stay below the guard
     got = _split(_predict(ggp, calc, tests, "mixed"), tests)
     for (E, F, S, V), (e, f, s, v), (_, sp, _) in zip(ref, got, tests):
@@ -125,6 +133,7 @@ def test_alloy_calculator_matches_oracle(alloy):
     import flare_gb300 as fg
     from flare_gb300.sparse_gp import SGP_Wrapper
     ogp, b2a, ggp, calc, tests, ref = alloy
+    ggp.set_slices(0, 0)
     cell, sp, pos = tests[0]
     st = oracle.Structure(cell, sp, pos, RC, [oracle.B2Settings(*b2a)])
     ogp.predict_local_uncertainties(st)

@@ -25,6 +25,11 @@ def _predict(gp, b2, cell, sp, pos, precision):
 def test_directional_finite_differences(fcc_model, precision):
     from flare_gb300 import workloads as wl
     gp, b2 = fcc_model
+    # the mixed path's kernel GEMM at 9 slices: the energy then resolves
+    # h F (its rounding at 7 slices, summed over the atoms near the moved
+    # ones, moves a central difference by ~1e-3 eV/A); the forces are the
+    # mixed path's own (FP32-level fold GEMM, FP32 adjoint)
+    gp.set_slices(9, 0)
     cell, sp, pos = wl.fcc_structure(n_cells=32, seed=3100)
     r = _predict(gp, b2, cell, sp, pos, precision)
     F = r["forces"]

@@ -159,21 +159,37 @@ def test_autograd_energy_gradient_is_minus_forces(c1):
                                atol=0)
 
 
+@pytest.mark.parametrize("slices", [None, (9, 9), (8, 8), (7, 6)])
 @pytest.mark.parametrize("power", [2, 1])
-def test_mixed_precision_within_budget(power):
+def test_mixed_precision_within_budget(power, slices):
     """Mixed path against the FP64 path on an FCC model (|alpha| ~ 1e4):
     energy and local variance come from the tensor-core GEMMs with exact
-    integer slicing (FP64-level: energy <= 1e-8 eV/atom, variance <= 1e-11);
-    forces from the alpha-folded FP32 GEMM and the FP32 adjoint must stay
-    within the stated budget, MAE <= 1e-4 eV/A; stress within 1e-5 eV/A^3."""
+    integer slicing, forces from the alpha-folded FP32 GEMM and the FP32
+    adjoint.  At every slice count the model may run (the probes' choice
+    when `slices` is None; forced otherwise) the stated budget holds:
+    energy <= 1e-6 eV/atom, local variance <= 1e-8 sigma^2, force MAE <=
+    1e-4 eV/A, stress 1e-5 eV/A^3; at 9 slices (54 bits) energy and
+    variance are FP64-level (1e-8 eV/atom, 1e-11)."""
     ogp, b2a = c1_model(n_train=8, n_sparse=120, power=power)
     ggp, calc = to_gpu_sgp(ogp, b2a)
+    if slices:
+        ggp.set_slices(*slices)
+    plan = ggp.mixed_plan()
+    sig2 = ogp.kernels[0].sigma ** 2
+    if slices:
+        assert (plan["kernel_slices"], plan["variance_slices"]) == slices
+    else:
+        assert plan["kernel_slices"] in (7, 8, 9), plan
+        assert plan["variance_slices"] in (6, 7, 8, 9), plan
+        assert plan["slice_err_ev_per_atom"] <= 1e-7, plan
+        assert plan["variance_slice_err"] <= 5e-9 * sig2, plan
     items = [syn.fcc_al(seed=1120 + k) for k in range(3)]
     a = gpu_predict(ggp, calc, items, precision="fp64")
     b = gpu_predict(ggp, calc, items, precision="mixed")
-    assert np.max(np.abs(a["energy"] - b["energy"])) / 256 <= 1e-8
+    e_tol, v_tol = (1e-8, 1e-11) if slices == (9, 9) else (1e-6, 1e-8 * sig2)
+    assert np.max(np.abs(a["energy"] - b["energy"])) / 256 <= e_tol
     np.testing.assert_allclose(b["local_var"], a["local_var"], rtol=0,
-                               atol=1e-11)
+                               atol=v_tol)
     mae = np.abs(a["forces"] - b["forces"]).mean()
     assert mae <= 1e-4, mae
     np.testing.assert_allclose(b["stress"], a["stress"], atol=1e-5)
