@@ -100,6 +100,9 @@ SIGNATURES = {
     "fgb_serve_stop": (_i, [_vp]),
     "fgb_solve_qr": (_i, [_i, _i, _vp, _vp, _vp, _vp, _d, _vp, _vp, _vp,
                           _vp]),
+    "fgb_cholesky": (_i, [_i, _vp, _vp]),
+    "fgb_trtri_lower": (_i, [_i, _vp, _vp, _vp]),
+    "fgb_solve_products": (_i, [_i, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -165,12 +165,13 @@ class NormalizedDotProduct:
               "struc_struc")
         return out.cpu().numpy()
 
-    def self_kernel_struc(self, struc, hyps=None):
+    def self_kernel_struc(self, struc, hyps=None, kernel_index=0):
         """Prior variances of a structure's energy, forces and stress
         [1 + 3N + 6] (normalized_dot_product.cpp:450-586; the C++ method
-        behind predict_DTC); ``struc`` is a Structure (FP64 on the GPU)."""
+        behind predict_DTC); ``struc`` is a Structure (FP64 on the GPU) and
+        ``kernel_index`` picks its descriptor calculator."""
         sig = self.sigma if hyps is None else float(np.asarray(hyps)[0])
-        calc = struc.descriptor_calculators[0]
+        calc = struc.descriptor_calculators[kernel_index]
         out = torch.zeros(1 + 3 * struc.noa + 6, dtype=torch.float64,
                           device=_device())
         d = struc._inputs()
@@ -462,24 +463,31 @@ class _KernelBlock:
         return out
 
 
-def envs_struc_gpu(envs, struc, sigma, power, k=0):
+def _envs_struc_device(envs, struc, sigma, power, k=0):
     """envs_struc (normalized_dot_product.cpp:117-214) in FP64 on the GPU,
-    stored-gradient form; ``struc`` is a Structure."""
+    stored-gradient form, as a device tensor; ``struc`` is a Structure and
+    ``k`` the index of its descriptor calculator."""
     calc = struc.descriptor_calculators[k]
     counts, rows = envs.stacked()
     M = int(counts.sum())
     ncol = 1 + 3 * struc.noa + 6
-    if M == 0:
-        return np.zeros((0, ncol))
     dev = _device()
-    d_rows = torch.from_numpy(rows).to(dev)
     out = torch.zeros((M, ncol), dtype=torch.float64, device=dev)
+    if M == 0:
+        return out
+    d_rows = torch.from_numpy(rows).to(dev)
     d = struc._inputs()
     check(lib().fgb_envs_struc(calc.handle, float(sigma), float(power),
                                ptr(counts), ptr(d_rows), struc.nlist().h,
                                ptr(d["species"]), ptr(out), stream_ptr()),
           "envs_struc")
-    return out.cpu().numpy()
+    return out
+
+
+def envs_struc_gpu(envs, struc, sigma, power, k=0):
+    """envs_struc (normalized_dot_product.cpp:117-214) in FP64 on the GPU,
+    stored-gradient form; ``struc`` is a Structure."""
+    return _envs_struc_device(envs, struc, sigma, power, k).cpu().numpy()
 
 
 
@@ -860,9 +868,48 @@ class _Training:
         self.alpha = alpha.cpu().numpy()
         self.L_inv = Li.cpu().numpy()
         self.R_inv = Ri.cpu().numpy()
-        self.Kuu_inverse = self.L_inv.T @ self.L_inv
-        self.Sigma = self.R_inv @ self.R_inv.T
+        # Kuu_inverse = L_inv^T L_inv and Sigma = R_inv R_inv^T
+        # (sparse_gp.cpp:619, 640) are formed on the GPU when first read
+        self._Kuu_inverse = None
+        self._Sigma = None
         self._model = None
+
+    def _solve_product(self, which):
+        dev = _device()
+        src = self.L_inv if which == "Kuu_inverse" else self.R_inv
+        Li = torch.from_numpy(np.ascontiguousarray(src, np.float64)).to(dev)
+        Ri = Li
+        M = Li.shape[0]
+        out = torch.empty((M, M), dtype=torch.float64, device=dev)
+        check(lib().fgb_solve_products(
+            M, ptr(Li), ptr(Ri), ptr(out) if which == "Kuu_inverse" else None,
+            ptr(out) if which == "Sigma" else None, stream_ptr()),
+            which)
+        return out.cpu().numpy()
+
+    @property
+    def Kuu_inverse(self):
+        """L_inv^T L_inv (sparse_gp.cpp:619), formed on the GPU at FP64
+        level when first read after a solve."""
+        if self._Kuu_inverse is None and self.L_inv is not None:
+            self._Kuu_inverse = self._solve_product("Kuu_inverse")
+        return self._Kuu_inverse
+
+    @Kuu_inverse.setter
+    def Kuu_inverse(self, v):
+        self._Kuu_inverse = v
+
+    @property
+    def Sigma(self):
+        """R_inv R_inv^T (sparse_gp.cpp:640), formed on the GPU at FP64
+        level when first read after a solve."""
+        if self._Sigma is None and self.R_inv is not None:
+            self._Sigma = self._solve_product("Sigma")
+        return self._Sigma
+
+    @Sigma.setter
+    def Sigma(self, v):
+        self._Sigma = v
 
 
 # -------------------------------------------------------------- model
@@ -924,8 +971,8 @@ class SparseGP(_Training):
         self.alpha = None
         self.L_inv = None
         self.R_inv = None
-        self.Sigma = None
-        self.Kuu_inverse = None
+        self._Sigma = None
+        self._Kuu_inverse = None
         self._model = None
         self._model_key = None
 
@@ -942,67 +989,111 @@ class SparseGP(_Training):
         self.sparse_descriptors = list(sparse_descriptors)
         self.alpha = np.asarray(alpha, np.float64)
         self.L_inv = np.asarray(L_inv, np.float64)
+        self._Kuu_inverse = None
+        self._Sigma = None
         self._calculators = list(calculators)
         self._model = None
 
-    def _device_model(self, structure_calcs=None):
+    def _kernel_blocks(self):
+        """(first row, rows) of each kernel's sparse set in alpha and L_inv
+        (sparse_gp.cpp:94-139, 643-665: kernels are stacked in order)."""
+        out, c = [], 0
+        for cd in self.sparse_descriptors[:self.n_kernels]:
+            n = int(np.sum(cd.n_clusters_by_type))
+            out.append((c, n))
+            c += n
+        return out
+
+    def _device_models(self, structure_calcs=None):
+        """One device model per kernel: its descriptor calculator, sparse
+        set, alpha segment and L_inv diagonal block.  The mean is the sum
+        of the kernels' terms and each kernel's local variance uses its own
+        diagonal block, exactly as predict_mean and
+        compute_cluster_uncertainties do (sparse_gp.cpp:94-139, 643-665)."""
         if self.alpha is None or self.L_inv is None:
             raise RuntimeError(
                 "L_inv must be up to date to make predictions. Please call "
                 "update_matrices_QR and try again.")
+        if self._model is None:
+            calcs = list(structure_calcs or self._calculators)
+            if len(calcs) < self.n_kernels:
+                raise ValueError("a structure needs one descriptor calculator "
+                                 "per kernel")
+            models = []
+            for i, ((c0, n), k) in enumerate(zip(self._kernel_blocks(),
+                                                 self.kernels)):
+                m = _Model(calcs[i], k.sigma, k.power)
+                counts, desc = self.sparse_descriptors[i].stacked()
+                m.set(counts, desc, self.alpha[c0:c0 + n],
+                      self.L_inv[c0:c0 + n, c0:c0 + n])
+                if self.R_inv is not None and self.n_kernels == 1:
+                    R = np.ascontiguousarray(self.R_inv[:n, :n], np.float64)
+                    check(lib().fgb_model_set_R_inv(m.h, ptr(R)), "SparseGP")
+                slices = getattr(self, "_slices", None)
+                if slices:
+                    check(lib().fgb_model_set_slices(m.h, *slices),
+                          "set_slices")
+                models.append(m)
+            self._model = models
+        return self._model
+
+    def _device_model(self, structure_calcs=None):
+        """The device model of a single-kernel SparseGP (the mapped,
+        MD-ensemble, serving and autograd front-ends take one kernel)."""
         if self.n_kernels != 1:
             raise NotImplementedError(
-                "GPU prediction supports one kernel / descriptor (the "
-                "reference's local variance makes the same restriction, "
-                "calculator.py:105-108)")
-        if self._model is None:
-            calc = (structure_calcs or self._calculators)[0]
-            k = self.kernels[0]
-            m = _Model(calc, k.sigma, k.power)
-            counts, desc = self.sparse_descriptors[0].stacked()
-            M = desc.shape[0]
-            m.set(counts, desc, self.alpha[:M], self.L_inv[:M, :M])
-            if self.R_inv is not None:
-                R = np.ascontiguousarray(self.R_inv[:M, :M], np.float64)
-                check(lib().fgb_model_set_R_inv(m.h, ptr(R)), "SparseGP")
-            slices = getattr(self, "_slices", None)
-            if slices:
-                check(lib().fgb_model_set_slices(m.h, *slices), "set_slices")
-            self._model = m
-        return self._model
+                "this operation takes a single-kernel SparseGP; prediction "
+                "(predict_mean / predict_local_uncertainties / predict_SOR / "
+                "predict_DTC / predict_batch) takes any number of kernels")
+        return self._device_models(structure_calcs)[0]
 
     def predict_batch(self, structures, want=0xF, precision=None,
                       stream=None):
         """Batched prediction on the GPU.  Returns dict of numpy arrays:
         energy [S], forces [N, 3], stress [S, 6] (flare order), local_var
-        [N] (atom order)."""
+        [N] (atom order; the first kernel's) and local_vars (one [N] array
+        per kernel).  With several kernels each runs the fused pipeline on
+        its own descriptor and the mean terms are summed."""
         if not structures:
             return {}
         calcs = structures[0].descriptor_calculators
-        m = self._device_model(calcs)
+        models = self._device_models(calcs)
         offsets, cells, pos, sp = pack_structures(structures)
         dev = _device()
         N = int(offsets[-1])
         S = len(structures)
         d_pos = torch.from_numpy(pos).to(dev)
         d_sp = torch.from_numpy(sp).to(dev)
-        e = torch.zeros(S, dtype=torch.float64, device=dev)
-        f = torch.zeros((max(N, 1), 3), dtype=torch.float64, device=dev)
-        st = torch.zeros((S, 6), dtype=torch.float64, device=dev)
-        v = torch.zeros(max(N, 1), dtype=torch.float64, device=dev)
         prec = _prec[precision or _default_precision[0]]
         cutoff = structures[0].cutoff
         for s in structures:
             if s.cutoff != cutoff:
                 raise ValueError("a batch must share one structure cutoff")
-        check(lib().fgb_predict(m.h, S, ptr(offsets), ptr(cells), ptr(d_pos),
-                                ptr(d_sp), cutoff, int(want), prec, ptr(e),
-                                ptr(f), ptr(st), ptr(v), stream_ptr(stream)),
-              "predict")
+        out = None
+        local_vars = []
+        for m in models:
+            e = torch.zeros(S, dtype=torch.float64, device=dev)
+            f = torch.zeros((max(N, 1), 3), dtype=torch.float64, device=dev)
+            st = torch.zeros((S, 6), dtype=torch.float64, device=dev)
+            v = torch.zeros(max(N, 1), dtype=torch.float64, device=dev)
+            check(lib().fgb_predict(m.h, S, ptr(offsets), ptr(cells),
+                                    ptr(d_pos), ptr(d_sp), cutoff, int(want),
+                                    prec, ptr(e), ptr(f), ptr(st), ptr(v),
+                                    stream_ptr(stream)),
+                  "predict")
+            if out is None:
+                out = [e, f, st]
+            else:
+                out[0] += e
+                out[1] += f
+                out[2] += st
+            local_vars.append(v)
         torch.cuda.current_stream().synchronize()
-        return {"energy": e.cpu().numpy(), "forces": f.cpu().numpy()[:N],
-                "stress": st.cpu().numpy(), "local_var": v.cpu().numpy()[:N],
-                "offsets": offsets}
+        lv = [v.cpu().numpy()[:N] for v in local_vars]
+        return {"energy": out[0].cpu().numpy(),
+                "forces": out[1].cpu().numpy()[:N],
+                "stress": out[2].cpu().numpy(), "local_var": lv[0],
+                "local_vars": lv, "offsets": offsets}
 
     def _predict_one(self, structure, want):
         r = self.predict_batch([structure], want)
@@ -1016,21 +1107,48 @@ class SparseGP(_Training):
                           _lib.FGB_WANT_FORCES | _lib.FGB_WANT_STRESS)
 
     def predict_local_uncertainties(self, structure):
-        """sparse_gp.cpp:731-757: mean_efs plus per-atom local variances
-        (stored in species-sorted order, as the reference does)."""
+        """sparse_gp.cpp:731-757: mean_efs plus per-atom local variances,
+        one array per kernel (each stored in its descriptor's
+        species-sorted order, as the reference does)."""
         r = self._predict_one(structure, 0xF)
         sp = np.asarray(structure.species)
-        S = structure.descriptor_calculators[0].descriptor_settings[0]
-        order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
-        structure.local_uncertainties = [r["local_var"][order]]
+        out = []
+        for i, v in enumerate(r["local_vars"]):
+            S = structure.descriptor_calculators[i].descriptor_settings[0]
+            order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
+            out.append(v[order])
+        structure.local_uncertainties = out
 
-    def predict_SOR(self, structure):
-        """sparse_gp.cpp:667-692: mean_efs and the SOR variances
-        diag(K^T R_inv R_inv^T K) over all 1 + 3N + 6 outputs (FP64)."""
+    def _stacked_kernel_matrix(self, structure):
+        """The kernels' envs_struc blocks stacked in kernel order on the
+        device, [n_sparse x (1 + 3N + 6)] (sparse_gp.cpp:667-692)."""
+        blocks = []
+        for i, k in enumerate(self.kernels):
+            blocks.append(_envs_struc_device(self.sparse_descriptors[i],
+                                             structure, k.sigma, k.power, i))
+        return torch.cat(blocks, 0)
+
+    def _check_solved(self):
         if self.R_inv is None:
             raise RuntimeError(
                 "L_inv must be up to date to make predictions. Please call "
                 "update_matrices_QR and try again.")
+
+    def predict_SOR(self, structure):
+        """sparse_gp.cpp:667-692: mean_efs and the SOR variances
+        diag(K^T R_inv R_inv^T K) over all 1 + 3N + 6 outputs (FP64).  One
+        kernel: the fused fgb_predict_sor.  Several: K stacked over the
+        kernels (each block from the GPU envs_struc), then K^T alpha and
+        the rows of K^T R_inv as plain FP64 GEMMs (cuBLAS)."""
+        self._check_solved()
+        if self.n_kernels != 1:
+            K = self._stacked_kernel_matrix(structure)
+            alpha = torch.from_numpy(np.asarray(self.alpha)).to(K.device)
+            Ri = torch.from_numpy(np.ascontiguousarray(self.R_inv)).to(K.device)
+            vs = K.T @ Ri
+            structure.mean_efs = (K.T @ alpha).cpu().numpy()
+            structure.variance_efs = (vs * vs).sum(1).cpu().numpy()
+            return
         m = self._device_model(structure.descriptor_calculators)
         dev = _device()
         n_out = 1 + 3 * structure.noa + 6
@@ -1046,11 +1164,26 @@ class SparseGP(_Training):
     def predict_DTC(self, structure):
         """sparse_gp.cpp:694-729: mean_efs and the DTC variances K_self -
         diag(K^T Kuu^-1 K) + diag(K^T Sigma K) over all 1 + 3N + 6 outputs
-        (FP64; K_self is NormalizedDotProduct::self_kernel_struc)."""
-        if self.R_inv is None:
-            raise RuntimeError(
-                "L_inv must be up to date to make predictions. Please call "
-                "update_matrices_QR and try again.")
+        (FP64; K_self is NormalizedDotProduct::self_kernel_struc, summed
+        over the kernels).  Several kernels: K stacked as in predict_SOR,
+        diag(K^T Kuu^-1 K) = |L_inv K|^2 and diag(K^T Sigma K) = |R_inv^T
+        K|^2 per column."""
+        self._check_solved()
+        if self.n_kernels != 1:
+            K = self._stacked_kernel_matrix(structure)
+            dev = K.device
+            alpha = torch.from_numpy(np.asarray(self.alpha)).to(dev)
+            Li = torch.from_numpy(np.ascontiguousarray(self.L_inv)).to(dev)
+            Ri = torch.from_numpy(np.ascontiguousarray(self.R_inv)).to(dev)
+            kself = sum(torch.from_numpy(k.self_kernel_struc(structure,
+                                                             kernel_index=i))
+                        for i, k in enumerate(self.kernels)).to(dev)
+            q = Li @ K
+            v = Ri.T @ K
+            structure.mean_efs = (K.T @ alpha).cpu().numpy()
+            structure.variance_efs = (kself - (q * q).sum(0) +
+                                      (v * v).sum(0)).cpu().numpy()
+            return
         m = self._device_model(structure.descriptor_calculators)
         dev = _device()
         n_out = 1 + 3 * structure.noa + 6
@@ -1063,14 +1196,14 @@ class SparseGP(_Training):
         structure.mean_efs = mean.cpu().numpy()
         structure.variance_efs = var.cpu().numpy()
 
-    def mixed_plan(self):
-        """The mixed path's precision plan for this model: slices of the
-        kernel GEMM (9, 8 or 7) and of the variance GEMM (9, 8, 7 or 6)
-        with the largest energy (eV/atom) and local-variance differences to
-        9 slices measured on the sparse set when they were chosen, and the
-        fold guard (largest folded coefficient, whether the descriptor and
-        forces run at FP64 level)."""
-        m = self._device_model()
+    def mixed_plan(self, kernel_index=0):
+        """The mixed path's precision plan for one kernel of this model:
+        slices of the kernel GEMM (9, 8 or 7) and of the variance GEMM (9,
+        8, 7 or 6) with the largest energy (eV/atom) and local-variance
+        differences to 9 slices measured on the sparse set when they were
+        chosen, and the fold guard (largest folded coefficient, whether the
+        descriptor and forces run at FP64 level)."""
+        m = self._device_models()[kernel_index]
         S, Sv, fp64 = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
         est, vest = ctypes.c_double(0.0), ctypes.c_double(0.0)
         fmax = ctypes.c_double(0.0)
@@ -1090,8 +1223,8 @@ class SparseGP(_Training):
         """Force the mixed path's slice counts (kernel GEMM 7-9, variance
         GEMM 6-9; 0 = the fewest the model's error probes allow)."""
         self._slices = (int(kernel), int(variance))
-        if self._model is not None:
-            check(lib().fgb_model_set_slices(self._model.h, *self._slices),
+        for m in self._model or []:
+            check(lib().fgb_model_set_slices(m.h, *self._slices),
                   "set_slices")
 
     # -------------------------------------------------- mapped models
@@ -1123,6 +1256,9 @@ class SparseGP(_Training):
         """sparse_gp.cpp:94-139 (species-sorted variances)."""
         r = self.predict_batch([structure], _lib.FGB_WANT_LOCAL_VAR)
         sp = np.asarray(structure.species)
-        S = structure.descriptor_calculators[0].descriptor_settings[0]
-        order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
-        return [r["local_var"][order]]
+        out = []
+        for i, v in enumerate(r["local_vars"]):
+            S = structure.descriptor_calculators[i].descriptor_settings[0]
+            order = np.concatenate([np.nonzero(sp == s)[0] for s in range(S)])
+            out.append(v[order])
+        return out

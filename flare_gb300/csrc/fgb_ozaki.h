@@ -90,6 +90,10 @@ int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
 // one rounding.
 int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
                int *err, cudaStream_t st);
+// C = a (A B^T) + b C in FP64 from kS-slice operands (b = 0: C is only
+// written), the same exact integer sums and one rounding of the product.
+int gemm_axpby(const Sliced &A, const Sliced &B, double *C, long long ldc,
+               double a, double b, int *err, cudaStream_t st);
 // Y (A.rows x B.rows, leading dimension ldy) = A B^T rounded to FP32, from
 // kSF32-slice operands (A tiles of kTM rows, B tiles of 128 or 64 rows;
 // `ew` epilogue warps per lane quarter, 2 or 4 for 128-row tiles).  A may

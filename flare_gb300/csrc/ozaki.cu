@@ -731,6 +731,31 @@ struct EpiStore {
   __device__ void finish(int, bool, int, double) const {}
 };
 
+// C = a (A B^T) + b C (b = 0: C is not read), FP64; the dense
+// factorizations' updates (C -= L21 L21^T, X21 = -X22 T, ...).
+struct EpiAxpby {
+  using Value = double;
+  static constexpr bool kFloat = false;
+  double *C;
+  long long ldc;
+  int N;
+  double a, b;
+  __device__ double chunk(int m, bool row_ok, int n0, const double (&v)[16],
+                          double acc) const {
+    if (!row_ok) return acc;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int n = n0 + j;
+      if (n < N) {
+        double *c = C + (long long)m * ldc + n;
+        *c = b == 0.0 ? a * v[j] : fma(b, *c, a * v[j]);
+      }
+    }
+    return acc;
+  }
+  __device__ void finish(int, bool, int, double) const {}
+};
+
 // Plain product Y = A B^T rounded to FP32.
 struct EpiStoreF32 {
   using Value = float;
@@ -843,6 +868,11 @@ int gemm(const Sliced &A, const Sliced &B, bool tri, const Epi &epi, int *err,
 int gemm_store(const Sliced &A, const Sliced &B, double *C, long long ldc,
                int *err, cudaStream_t st) {
   return gemm(A, B, false, EpiStore{C, ldc, B.rows}, err, st);
+}
+
+int gemm_axpby(const Sliced &A, const Sliced &B, double *C, long long ldc,
+               double a, double b, int *err, cudaStream_t st) {
+  return gemm(A, B, false, EpiAxpby{C, ldc, B.rows, a, b}, err, st);
 }
 
 int gemm_f32(const Sliced &A, const Sliced &B, float *Y, long long ldy,

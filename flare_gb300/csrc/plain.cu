@@ -1,9 +1,9 @@
 // Plain FP64 form: the reference's algorithm on the GPU (stored
 // forward-mode descriptor gradients, envs_struc GEMM + scatter), envs_envs,
 // and the FP64 QR solve.
-#include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include "fgb_dense.h"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
 #include "fgb_model.h"
@@ -545,21 +545,11 @@ __global__ void k_add_diag(int M, double *A, double v) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < M) A[(long long)i * M + i] += v;
 }
-__global__ void k_zero_upper(int M, double *L) {  // column-major
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)M * M) return;
-  int c = (int)(idx / M), r = (int)(idx % M);
-  if (r < c) L[idx] = 0.0;
-}
-__global__ void k_eye(int M, double *X) {
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)M * M) return;
-  int c = (int)(idx / M), r = (int)(idx % M);
-  X[idx] = r == c ? 1.0 : 0.0;
-}
-__global__ void k_build_A(int M, int nl, const double *Kuf, const double *noise,
-                          const double *y, const double *L, double *A,
-                          double *b) {
+// A = [sqrt(noise) Kuf^T; L^T] column-major (rows = n_labels + M) with L
+// row-major lower (L^T(i, c) = L(c, i)), and b = [sqrt(noise) y; 0].
+__global__ void k_build_A_rm(int M, int nl, const double *Kuf,
+                             const double *noise, const double *y,
+                             const double *L, double *A, double *b) {
   long long rows = (long long)nl + M;
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= rows * M) return;
@@ -567,9 +557,30 @@ __global__ void k_build_A(int M, int nl, const double *Kuf, const double *noise,
   long long r = idx % rows;
   double v;
   if (r < nl) v = sqrt(noise[r]) * Kuf[(long long)c * nl + r];
-  else v = L[(long long)(r - nl) * M + c];   // L^T(i, c) = L(c, i)
+  else v = L[(long long)c * M + (r - nl)];
   A[idx] = v;
   if (c == 0) b[r] = r < nl ? sqrt(noise[r]) * y[r] : 0.0;
+}
+// R^T row-major lower from the QR factor held in the first M rows of the
+// column-major A (ld rows): R^T(j, i) = R(i, j) = A[j rows + i], i <= j.
+__global__ void k_rt_from_qr(int M, long long rows, const double *A,
+                             double *Rt) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)M * M) return;
+  int j = (int)(idx / M), i = (int)(idx % M);
+  Rt[idx] = i <= j ? A[(long long)j * rows + i] : 0.0;
+}
+// alpha = R_inv Qb (R_inv row-major upper): a warp per row, lanes over
+// columns, fixed-order shuffle tree.
+__global__ void k_upper_gemv(int M, const double *R, const double *x,
+                             double *y) {
+  const int row = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= M) return;
+  double s = 0.0;
+  for (int j = row + lane; j < M; j += 32) s += R[(long long)row * M + j] * x[j];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if (lane == 0) y[row] = s;
 }
 __global__ void k_transpose(int M, const double *in, double *out) {
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -590,6 +601,12 @@ __global__ void k_transpose(int M, const double *in, double *out) {
     }                                                                   \
   } while (0)
 
+// SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) on the GPU in FP64:
+// L = chol(Kuu + jitter I) and L_inv = L^-1 by the blocked kernels of
+// dense.cu (diagonal blocks in shared memory, O(M^3) updates as FP64-level
+// tensor-core products), the Householder QR of A = [sqrt(noise) Kuf^T;
+// L^T] and Q^T b by cuSOLVER (geqrf, ormqr), R_inv = (R^T)^-1^T by
+// dense.cu, alpha = R_inv (Q^T b)[:M] (the reference's R_inv * Q_b).
 extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
                             const double *d_Kuf, const double *d_y,
                             const double *d_noise, double jitter,
@@ -604,10 +621,9 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
   const long long rows = (long long)n_labels + M;
   int rc = FGB_OK;
   cusolverDnHandle_t sol = nullptr;
-  cublasHandle_t blas = nullptr;
-  DevBuf L, X, A, b, tau, work, info;
+  DevBuf L, X, A, b, tau, work, info, Rinv;
   int lwork = 0, lw2 = 0, hinfo = 0;
-  const double one = 1.0;
+  double *R_inv = d_R_inv;
   if ((rc = L.ensure(sizeof(double) * (size_t)M * M)) ||
       (rc = X.ensure(sizeof(double) * (size_t)M * M)) ||
       (rc = A.ensure(sizeof(double) * (size_t)rows * M)) ||
@@ -615,19 +631,21 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
       (rc = tau.ensure(sizeof(double) * (size_t)M)) ||
       (rc = info.ensure(sizeof(int))))
     return rc;
-  FGB_SOLVER(cusolverDnCreate(&sol), "cusolverDnCreate");
-  FGB_SOLVER(cublasCreate(&blas), "cublasCreate");
-  FGB_SOLVER(cusolverDnSetStream(sol, st), "cusolverDnSetStream");
-  FGB_SOLVER(cublasSetStream(blas, st), "cublasSetStream");
-  FGB_SOLVER(cudaMemcpyAsync(L.p, d_Kuu, sizeof(double) * (size_t)M * M,
-                             cudaMemcpyDeviceToDevice, st), "copy Kuu");
+  if (!R_inv) {
+    if ((rc = Rinv.ensure(sizeof(double) * (size_t)M * M))) return rc;
+    R_inv = Rinv.as<double>();
+  }
+  FGB_CUDA(cudaMemcpyAsync(L.p, d_Kuu, sizeof(double) * (size_t)M * M,
+                           cudaMemcpyDeviceToDevice, st));
   k_add_diag<<<ceil_div(M, 256), 256, 0, st>>>(M, L.as<double>(), jitter);
-  FGB_SOLVER(cusolverDnDpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, M,
-                                         L.as<double>(), M, &lwork),
-             "potrf_bufferSize");
+  FGB_LAUNCH_CHECK("k_add_diag");
+  if ((rc = dense::cholesky(M, L.as<double>(), M, st))) return rc;
+  if ((rc = dense::trtri_lower(M, L.as<double>(), M, d_L_inv, M, st)))
+    return rc;
+  FGB_SOLVER(cusolverDnCreate(&sol), "cusolverDnCreate");
+  FGB_SOLVER(cusolverDnSetStream(sol, st), "cusolverDnSetStream");
   FGB_SOLVER(cusolverDnDgeqrf_bufferSize(sol, (int)rows, M, A.as<double>(),
-                                         (int)rows, &lw2), "geqrf_bufferSize");
-  lwork = std::max(lwork, lw2);
+                                         (int)rows, &lwork), "geqrf_bufferSize");
   FGB_SOLVER(cusolverDnDormqr_bufferSize(sol, CUBLAS_SIDE_LEFT, CUBLAS_OP_T,
                                          (int)rows, 1, M, A.as<double>(),
                                          (int)rows, tau.as<double>(),
@@ -635,28 +653,10 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
              "ormqr_bufferSize");
   lwork = std::max(lwork, lw2);
   if ((rc = work.ensure(sizeof(double) * ((size_t)lwork + 1)))) goto done;
-  FGB_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, M, L.as<double>(),
-                              M, work.as<double>(), lwork, info.as<int>()),
-             "potrf");
-  FGB_SOLVER(cudaMemcpyAsync(&hinfo, info.p, sizeof(int),
-                             cudaMemcpyDeviceToHost, st), "info");
-  FGB_SOLVER(cudaStreamSynchronize(st), "sync");
-  if (hinfo != 0) {
-    set_error("Cholesky of Kuu + jitter failed (leading minor %d not "
-              "positive definite)", hinfo);
-    rc = FGB_EINVAL;
-    goto done;
-  }
-  k_zero_upper<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(M, L.as<double>());
-  k_eye<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(M, X.as<double>());
-  FGB_SOLVER(cublasDtrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER,
-                         CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, M, M, &one,
-                         L.as<double>(), M, X.as<double>(), M), "trsm L");
-  k_transpose<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
-      M, X.as<double>(), d_L_inv);
-  k_build_A<<<ceil_div(rows * M, 256), 256, 0, st>>>(
+  k_build_A_rm<<<ceil_div(rows * M, 256), 256, 0, st>>>(
       M, n_labels, d_Kuf, d_noise, d_y, L.as<double>(), A.as<double>(),
       b.as<double>());
+  FGB_SOLVER(cudaGetLastError(), "k_build_A_rm");
   FGB_SOLVER(cusolverDnDgeqrf(sol, (int)rows, M, A.as<double>(), (int)rows,
                               tau.as<double>(), work.as<double>(), lwork,
                               info.as<int>()), "geqrf");
@@ -664,25 +664,28 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
                               M, A.as<double>(), (int)rows, tau.as<double>(),
                               b.as<double>(), (int)rows, work.as<double>(),
                               lwork, info.as<int>()), "ormqr");
-  FGB_SOLVER(cublasDtrsv(blas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                         CUBLAS_DIAG_NON_UNIT, M, A.as<double>(), (int)rows,
-                         b.as<double>(), 1), "trsv");
-  FGB_SOLVER(cudaMemcpyAsync(d_alpha, b.p, sizeof(double) * M,
-                             cudaMemcpyDeviceToDevice, st), "copy alpha");
-  if (d_R_inv) {
-    k_eye<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(M, X.as<double>());
-    FGB_SOLVER(cublasDtrsm(blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER,
-                           CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, M, M, &one,
-                           A.as<double>(), (int)rows, X.as<double>(), M),
-               "trsm R");
-    k_transpose<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
-        M, X.as<double>(), d_R_inv);
+  FGB_SOLVER(cudaMemcpyAsync(&hinfo, info.p, sizeof(int),
+                             cudaMemcpyDeviceToHost, st), "info");
+  FGB_SOLVER(cudaStreamSynchronize(st), "sync");
+  if (hinfo != 0) {
+    set_error("fgb_solve_qr: QR failed (info %d)", hinfo);
+    rc = FGB_ECUDA;
+    goto done;
   }
+  // R^T (lower) into X, its inverse into L, R_inv = that inverse transposed
+  k_rt_from_qr<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
+      M, rows, A.as<double>(), X.as<double>());
+  FGB_SOLVER(cudaGetLastError(), "k_rt_from_qr");
+  if ((rc = dense::trtri_lower(M, X.as<double>(), M, L.as<double>(), M, st)))
+    goto done;
+  k_transpose<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
+      M, L.as<double>(), R_inv);
+  k_upper_gemv<<<ceil_div((long long)M * 32, 256), 256, 0, st>>>(
+      M, R_inv, b.as<double>(), d_alpha);
   FGB_SOLVER(cudaStreamSynchronize(st), "sync");
   FGB_SOLVER(cudaGetLastError(), "solve kernels");
 done:
   if (sol) cusolverDnDestroy(sol);
-  if (blas) cublasDestroy(blas);
   return rc;
 }
 

@@ -25,6 +25,7 @@ struct Request {
   std::vector<int> species;
   long long bytes;
   Clock::time_point t_submit, t_done;
+  int passed_over = 0;   // batches admitted past this request
   bool done = false;
   int status = FGB_OK;
   std::string error;
@@ -44,6 +45,38 @@ long long footprint_per_atom(const fgb_model_s *m) {
   b += 9LL * 2 * (p.n_d + mmax) + 8LL * mmax;     // tensor-core slices and K rows
   return b;
 }
+
+// Page-locked host staging buffer of a worker: host<->device copies of a
+// batch's inputs and results run asynchronously on the worker's stream
+// (from pageable memory they would be staged and synchronous).
+template <typename T>
+struct Pinned {
+  T *p = nullptr;
+  size_t n = 0;
+  int ensure(size_t want) {
+    if (want <= n) return FGB_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    if (cudaHostAlloc((void **)&p, sizeof(T) * want, cudaHostAllocDefault) !=
+        cudaSuccess) {
+      p = nullptr;
+      set_error("serving: page-locked staging buffer of %zu bytes",
+                sizeof(T) * want);
+      return FGB_ENOMEM;
+    }
+    n = want;
+    return FGB_OK;
+  }
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
+// A queued request passed over this many times (because it did not fit the
+// memory left while later, smaller ones did) blocks the requests behind it
+// until it is admitted.
+constexpr int kMaxPassOvers = 4;
 
 }  // namespace
 }  // namespace fgb
@@ -65,33 +98,61 @@ struct fgb_server_s {
 };
 
 
+// Admission: scan the queue in arrival order and take every request that
+// fits the memory budget left (in-flight bytes of all workers) until the
+// batch holds max_structures; a request that does not fit is passed over,
+// at most kMaxPassOvers times, after which nothing behind it is taken
+// before it.  Returns the batch's bytes (0: nothing fits now).
+static long long admit(fgb_server_s *s, std::vector<Request *> &batch) {
+  long long bytes = 0;
+  bool blocked = false;
+  for (auto it = s->queue.begin();
+       it != s->queue.end() && (int)batch.size() < s->max_structures;) {
+    Request *r = *it;
+    if (s->in_flight_bytes + bytes + r->bytes <= s->budget) {
+      bytes += r->bytes;
+      batch.push_back(r);
+      it = s->queue.erase(it);
+      continue;
+    }
+    if (r->passed_over >= kMaxPassOvers) blocked = true;
+    if (blocked) break;
+    ++it;
+  }
+  if (!batch.empty())
+    for (Request *r : s->queue) {
+      if (r->t_submit > batch.back()->t_submit) break;
+      r->passed_over++;
+    }
+  return bytes;
+}
+
+static bool any_fits(const fgb_server_s *s) {
+  for (const Request *r : s->queue) {
+    if (s->in_flight_bytes + r->bytes <= s->budget) return true;
+    if (r->passed_over >= kMaxPassOvers) return false;
+  }
+  return false;
+}
+
 static void worker_loop(fgb_server_s *s, int w) {
   cudaSetDevice(s->device);
   cudaStream_t st;
   cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   fgb_model_s *m = s->replicas[w];
   std::vector<int> offsets;
-  std::vector<double> cells, pos, energy, forces, stress, var;
-  std::vector<int> species;
+  std::vector<double> cells;
+  Pinned<double> pos, energy, forces, stress, var;
+  Pinned<int> species;
   for (;;) {
     std::vector<Request *> batch;
     long long bytes = 0;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      s->cv_work.wait(lk, [&] {
-        if (s->stop) return true;
-        return !s->queue.empty() &&
-               s->in_flight_bytes + s->queue.front()->bytes <= s->budget;
-      });
-      if (s->stop && s->queue.empty()) break;
+      s->cv_work.wait(lk, [&] { return s->stop || any_fits(s); });
       if (s->stop) break;
-      // admit the longest FIFO prefix that fits the remaining budget
-      while (!s->queue.empty() && (int)batch.size() < s->max_structures &&
-             s->in_flight_bytes + bytes + s->queue.front()->bytes <= s->budget) {
-        bytes += s->queue.front()->bytes;
-        batch.push_back(s->queue.front());
-        s->queue.pop_front();
-      }
+      bytes = admit(s, batch);
+      if (batch.empty()) continue;
       s->in_flight_bytes += bytes;
       s->batches++;
     }
@@ -99,22 +160,28 @@ static void worker_loop(fgb_server_s *s, int w) {
     offsets.assign(S + 1, 0);
     for (int k = 0; k < S; k++) offsets[k + 1] = offsets[k] + batch[k]->n;
     const int N = offsets[S];
-    cells.resize(9 * S);
-    pos.resize(3 * (size_t)N);
-    species.resize(N);
-    for (int k = 0; k < S; k++) {
-      std::copy(batch[k]->cell, batch[k]->cell + 9, cells.begin() + 9 * k);
-      std::copy(batch[k]->pos.begin(), batch[k]->pos.end(), pos.begin() + 3 * (size_t)offsets[k]);
-      std::copy(batch[k]->species.begin(), batch[k]->species.end(), species.begin() + offsets[k]);
+    int rc = FGB_OK;
+    if ((rc = pos.ensure(3 * (size_t)N + 1)) ||
+        (rc = species.ensure((size_t)N + 1)) ||
+        (rc = energy.ensure((size_t)S + 1)) ||
+        (rc = forces.ensure(3 * (size_t)N + 1)) ||
+        (rc = stress.ensure(6 * (size_t)S + 1)) ||
+        (rc = var.ensure((size_t)N + 1))) {
+    } else {
+      cells.resize(9 * S);
+      for (int k = 0; k < S; k++) {
+        std::copy(batch[k]->cell, batch[k]->cell + 9, cells.begin() + 9 * k);
+        std::copy(batch[k]->pos.begin(), batch[k]->pos.end(),
+                  pos.p + 3 * (size_t)offsets[k]);
+        std::copy(batch[k]->species.begin(), batch[k]->species.end(),
+                  species.p + offsets[k]);
+      }
+      std::fill(energy.p, energy.p + S, 0.0);
+      std::fill(stress.p, stress.p + 6 * (size_t)S, 0.0);
+      rc = fgb_predict_host(m, S, offsets.data(), cells.data(), pos.p,
+                            species.p, s->cutoff, s->want, s->precision,
+                            energy.p, forces.p, stress.p, var.p, st);
     }
-    energy.assign(S, 0);
-    forces.assign(3 * (size_t)N, 0);
-    stress.assign(6 * (size_t)S, 0);
-    var.assign(N, 0);
-    int rc = fgb_predict_host(m, S, offsets.data(), cells.data(), pos.data(),
-                              species.data(), s->cutoff, s->want, s->precision,
-                              energy.data(), forces.data(), stress.data(),
-                              var.data(), st);
     std::string err = rc ? fgb_last_error() : "";
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -124,11 +191,11 @@ static void worker_loop(fgb_server_s *s, int w) {
         r->status = rc;
         r->error = err;
         if (!rc) {
-          r->energy = energy[k];
-          std::copy(stress.begin() + 6 * k, stress.begin() + 6 * k + 6, r->stress);
-          r->forces.assign(forces.begin() + 3 * (size_t)offsets[k],
-                           forces.begin() + 3 * (size_t)offsets[k + 1]);
-          r->var.assign(var.begin() + offsets[k], var.begin() + offsets[k + 1]);
+          r->energy = energy.p[k];
+          std::copy(stress.p + 6 * k, stress.p + 6 * k + 6, r->stress);
+          r->forces.assign(forces.p + 3 * (size_t)offsets[k],
+                           forces.p + 3 * (size_t)offsets[k + 1]);
+          r->var.assign(var.p + offsets[k], var.p + offsets[k + 1]);
         }
         r->t_done = now;
         r->done = true;

@@ -489,14 +489,36 @@ int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A, long long lda,
                     long long ldc, void *stream);
 
 /* SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 on the GPU:
- * Cholesky of Kuu + jitter I, L_inv, QR of [diag(sqrt(noise)) Kuf^T ; L^T],
- * alpha = R^-1 Q^T b.  All device pointers, row-major.
+ * Cholesky of Kuu + jitter I and L_inv (fgb_cholesky, fgb_trtri_lower), the
+ * Householder QR of [diag(sqrt(noise)) Kuf^T ; L^T] and Q^T b (cuSOLVER),
+ * R_inv, alpha = R_inv (Q^T b)[:M].  All device pointers, row-major.
  * d_Kuu[M*M], d_Kuf[M*n_labels], d_y[n_labels], d_noise[n_labels] ->
- * d_alpha[M], d_L_inv[M*M], d_R_inv[M*M] (may be NULL). */
+ * d_alpha[M], d_L_inv[M*M], d_R_inv[M*M] (may be NULL).  A Kuu + jitter
+ * that is not positive definite returns FGB_EINVAL with the reference's
+ * kind of message. */
 int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
                  const double *d_Kuf, const double *d_y,
                  const double *d_noise, double jitter, double *d_alpha,
                  double *d_L_inv, double *d_R_inv, void *stream);
+
+/* The LLT step of update_matrices_QR (sparse_gp.cpp:610-615, Eigen's LLT in
+ * the reference): d_A (M x M, row-major, symmetric; the lower triangle is
+ * read) is replaced by its lower Cholesky factor, strict upper part zeroed.
+ * Blocked: 128 x 128 diagonal blocks factored in shared memory, the panel
+ * and trailing updates as FP64-level tensor-core products.  FGB_EINVAL if a
+ * leading minor is not positive definite. */
+int fgb_cholesky(int M, double *d_A, void *stream);
+/* Inverse of a lower-triangular M x M matrix (row-major; the reference's
+ * triangularView<Lower>().solve(Kuu_eye), sparse_gp.cpp:616-618, and the
+ * R_inv solve through R^T, :636-638), recursive over diagonal halves with
+ * FP64-level tensor-core products; d_X's strict upper part zeroed; d_L and
+ * d_X distinct. */
+int fgb_trtri_lower(int M, const double *d_L, double *d_X, void *stream);
+/* Kuu_inverse = L_inv^T L_inv and Sigma = R_inv R_inv^T (sparse_gp.cpp:619,
+ * 640) as FP64-level tensor-core products (M x M, row-major; either output
+ * may be NULL). */
+int fgb_solve_products(int M, const double *d_L_inv, const double *d_R_inv,
+                       double *d_Kuu_inverse, double *d_Sigma, void *stream);
 
 #ifdef __cplusplus
 }
