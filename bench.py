@@ -155,6 +155,86 @@ def oracle_reference(gp, b2, struct):
             oracle.sort_variances(st, st.local_uncertainties[0]))
 
 
+def _oracle_3species_model(cells, per_cell_sparse, lj_eps, lj_sigma, seed):
+    """FP64 CPU oracle model with the 3-species descriptor of the serving
+    and MD workloads (B2 [3, 8, 4], rc 5.5 A, n_d 1,500): LJ-labelled
+    training cells and `per_cell_sparse` seeded sparse atoms per cell."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from flare_gb300 import synthetic as syn
+    from flare_gb300 import workloads as wl
+    c = wl.MD3
+    b2 = oracle.B2Settings("chebyshev", "quadratic", [0.0, c["rc"]], [],
+                           [3, c["n_max"], c["l_max"]])
+    gp = oracle.SparseGP([oracle.NormalizedDotProduct(c["sigma"], c["power"])],
+                         c["sigma_e_per_atom"] * len(cells[0][1]),
+                         c["sigma_f"], c["sigma_s"])
+    r = syn.rng(seed)
+    for cell, sp, pos in cells:
+        st = oracle.Structure(cell, sp, pos, c["rc"], [b2])
+        E, F, _ = syn.lennard_jones(cell, sp, pos, lj_eps, lj_sigma, c["rc"])
+        st.energy = np.array([E])
+        st.forces = F.reshape(-1)
+        gp.add_training_structure(st)
+        gp.add_specific_environments(
+            st, sorted(r.choice(len(sp), size=per_cell_sparse,
+                                replace=False).tolist()))
+    gp.update_matrices_QR()
+    return oracle, gp, b2
+
+
+def cpu_serve_sweep(sizes=(32, 64, 128, 256, 512, 1024)):
+    """The FP64 CPU oracle on one request per size (E + F + stress + local
+    std, as the server answers), with a 3-species model of 600 sparse
+    environments (the served model has 3,000: the oracle's stored-gradient
+    envs_struc scales with M x 3P)."""
+    from flare_gb300 import synthetic as syn
+    from flare_gb300 import workloads as wl
+    cells = [syn.rsa_alloy(500, density=0.07, fractions=(1 / 3,) * 3,
+                           dmin=1.8, seed=4700 + t) for t in range(2)]
+    oracle, gp, b2 = _oracle_3species_model(cells, 300, wl.MD3["eps"],
+                                            wl.MD3["lj_sigma"], 4710)
+    out = []
+    for k, n in enumerate((sizes[0],) + tuple(sizes)):
+        cell, sp, pos = syn.rsa_alloy(n, density=0.07, fractions=(1 / 3,) * 3,
+                                      dmin=1.8, seed=4800 + k)
+        t0 = time.perf_counter()
+        st = oracle.Structure(cell, sp, pos, wl.MD3["rc"], [b2])
+        gp.predict_local_uncertainties(st)
+        oracle.calculator_results(st, "local", wl.MD3["sigma"])
+        dt = time.perf_counter() - t0
+        if k > 0:           # the first request warms up
+            out.append({"atoms": n, "ms": 1e3 * dt, "atoms_per_s": n / dt})
+    return {"kind": "port", "cores": cpu_cores(), "sparse_envs": gp.n_sparse,
+            "sample": "one request per size after one warm-up; FP64 CPU "
+                      "oracle (brute-force neighbours, stored-gradient B2, "
+                      "envs_struc, K^T alpha, local variance)",
+            "requests": out}
+
+
+def cpu_md_step():
+    """The FP64 CPU oracle's prediction for one md3 replica (2,000 atoms, 3
+    species; forces and local variance are what a step needs) with a model
+    of 1,000 sparse environments (the ensemble's has 8,000)."""
+    from flare_gb300 import workloads as wl
+    c = wl.MD3
+    cells = [wl.md_cell(c["train_seed0"])]
+    oracle, gp, b2 = _oracle_3species_model(cells, 1000, c["eps"],
+                                            c["lj_sigma"], 5610)
+    cell, sp, pos = wl.md_cell(c["replica_seed0"])
+    times = []
+    for _ in range(2):      # the first warms up
+        t0 = time.perf_counter()
+        st = oracle.Structure(cell, sp, pos, c["rc"], [b2])
+        gp.predict_local_uncertainties(st)
+        times.append(time.perf_counter() - t0)
+    return {"kind": "port", "cores": cpu_cores(), "sparse_envs": gp.n_sparse,
+            "replica_step_ms": 1e3 * times[-1],
+            "atom_steps_per_s": c["n_atoms"] / times[-1],
+            "sample": "one 2,000-atom replica's forces and local variance "
+                      "after one warm-up, FP64 CPU oracle"}
+
+
 def cpu_cores():
     return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
 
@@ -933,6 +1013,12 @@ def run_serve(args):
             r["offered_rate_x_saturation"] = f
             sweep.append(r)
     srv.close()
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_serve_sweep()
+        except Exception as ex:  # report, never hide
+            cpu = {"error": repr(ex)}
     print(json.dumps({
         "metric": "serving atoms/s (E+F+stress+local std per request) with "
                   "p50/p99 latency",
@@ -945,7 +1031,7 @@ def run_serve(args):
                                "<= 64 structures per batch" % n_req,
                    "atoms_total": int(atoms.sum()),
                    "atoms_mean": float(atoms.mean())},
-        "saturation": sat, "poisson_sweep": sweep,
+        "saturation": sat, "poisson_sweep": sweep, "cpu_baseline": cpu,
         "mixed_plan": gp.mixed_plan() if args.precision == "mixed" else None,
         "setup_s": {"train_fp64": round(train_s, 1),
                     "request_generation": round(gen_s, 1)},
@@ -1149,6 +1235,12 @@ def run_md(args):
     torch.cuda.synchronize()
     ms_after = ev0.elapsed_time(ev1)
     flag_after = float((ens.state()["flagged"] - before["flagged"]).sum() / N)
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = cpu_md_step()
+        except Exception as ex:  # report, never hide
+            cpu = {"error": repr(ex)}
     print(json.dumps({
         "metric": "MD ensemble atom-steps/s (forces + local std every step)",
         "value": N * args.steps / (ms * 1e-3), "unit": "atom-steps/s",
@@ -1176,6 +1268,7 @@ def run_md(args):
         "flagged_fraction_step_before_update": flag_before,
         "flagged_fraction_step_after_update": flag_after,
         "ms_per_step_after_update": ms_after,
+        "cpu_baseline": cpu,
         # the grown model's plan (the timed steps ran the 8,000-env model)
         "mixed_plan_after_update": (gp.mixed_plan()
                                     if args.precision == "mixed" else None),

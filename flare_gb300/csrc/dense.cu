@@ -17,6 +17,8 @@
 // Operation orders differ from Eigen's (the reference's LLT and triangular
 // solves), so results agree with it to FP64 rounding, not bit for bit.
 #include <cmath>
+#include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "fgb_dense.h"
@@ -133,6 +135,78 @@ __global__ void k_zero_strict_upper(int M, double *__restrict__ A, long long lda
   if (idx >= (long long)M * M) return;
   const int i = (int)(idx / M), j = (int)(idx - (long long)i * M);
   if (j > i) A[(long long)i * lda + j] = 0.0;
+}
+
+// At (M x (nl + M), row-major) = [Kuf diag(sqrt(noise)) | L]: the
+// transpose of the reference's A = [sqrt(noise) Kuf^T ; L^T]
+// (sparse_gp.cpp:621-630), built without a transpose (Kuf is M x nl
+// row-major, L lower row-major); b = [sqrt(noise) y ; 0].
+__global__ void k_build_At(int M, int nl, const double *__restrict__ Kuf,
+                           const double *__restrict__ noise,
+                           const double *__restrict__ y,
+                           const double *__restrict__ L, double *__restrict__ At,
+                           double *__restrict__ b) {
+  const long long n = (long long)nl + M;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)M * n) return;
+  const int c = (int)(idx / n);
+  const long long r = idx - (long long)c * n;
+  At[idx] = r < nl ? sqrt(noise[r]) * Kuf[(long long)c * nl + r]
+                   : L[(long long)c * M + (r - nl)];
+  if (c == 0) b[r] = r < nl ? sqrt(noise[r]) * y[r] : 0.0;
+}
+
+// Per-block partial sums of squares (fixed order), then one block adds them.
+__global__ void k_sumsq_part(long long n, const double *__restrict__ x,
+                             double *__restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * 256 + threadIdx.x; i < n;
+       i += (long long)gridDim.x * 256)
+    s += x[i] * x[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// A += s I (M x M, row-major) with s = kShift * part sum (the shifted
+// Cholesky QR's shift from the squared Frobenius norm).
+__global__ void k_add_shift(int M, double *__restrict__ A, long long lda,
+                            const double *__restrict__ part, int nparts,
+                            double factor) {
+  __shared__ double tot;
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < nparts; k++) t += part[k];
+    tot = t * factor;
+  }
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M;
+       i += gridDim.x * blockDim.x)
+    A[(long long)i * lda + i] += tot;
+}
+
+// y[j] = sum_r Q[r][j] b[r] for Q (n x M, row-major): 32 columns per block
+// (lane = column), 8 row groups, fixed-order sums.
+__global__ void k_gemv_t(long long n, int M, const double *__restrict__ Q,
+                         const double *__restrict__ b, double *__restrict__ y) {
+  __shared__ double red[8][33];
+  const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  double s = 0.0;
+  if (j < M)
+    for (long long r = g; r < n; r += 8) s += Q[r * M + j] * b[r];
+  red[g][lane] = s;
+  __syncthreads();
+  if (g == 0 && j < M) {
+    double t = 0.0;
+    for (int k = 0; k < 8; k++) t += red[k][lane];
+    y[j] = t;
+  }
 }
 
 int transpose(int rows, int cols, const double *in, long long ldi, double *out,
@@ -302,6 +376,101 @@ int sym_product(int M, const double *A, bool transpose_first, double *C,
   }
   if ((rc = gemm_nt(M, M, M, op, M, op, M, C, M, 1.0, 0.0, w, st))) return rc;
   return finish(w, st, "symmetric product");
+}
+
+// The factor R (returned as R_inv = R^-1, row-major upper) and Q^T b of the
+// Householder QR in update_matrices_QR (sparse_gp.cpp:621-640), by shifted
+// Cholesky QR with two refinement passes: pass 0 factors A^T A + s I (s =
+// 11 (n M + M (M + 1)) u |A|_F^2), Q0 = A R0^-1; passes 1 and 2 factor
+// Q^T Q without shift, Q <- Q R_k^-1; R = R2 R1 R0 and Q^T b = Q2^T b.
+// That is backward stable like Householder QR for condition numbers below
+// 1/u; A here = [sqrt(noise) Kuf^T; L^T] has sigma_min >= sqrt(jitter).
+// Every O(n M^2) product is an FP64-level tensor-core product.  R agrees
+// with a Householder R up to the signs of its rows, so alpha = R^-1 Q^T b
+// and Sigma = R^-1 R^-T are the same quantities.  At (M x n, row-major) is
+// read; b has n entries.
+int cholqr_solve(int M, long long n, double *At, const double *b,
+                 double *R_inv, double *Qtb, cudaStream_t st) {
+  Work w;
+  DevBuf G, X[3], A0, Q, Qt, part, P;
+  int rc;
+  const size_t MM = (size_t)M * M, nM = (size_t)n * M;
+  if ((rc = w.err.ensure(sizeof(int))) || (rc = G.ensure(sizeof(double) * MM)) ||
+      (rc = X[0].ensure(sizeof(double) * MM)) ||
+      (rc = X[1].ensure(sizeof(double) * MM)) ||
+      (rc = X[2].ensure(sizeof(double) * MM)) ||
+      (rc = P.ensure(sizeof(double) * MM)) ||
+      (rc = A0.ensure(sizeof(double) * nM)) ||
+      (rc = Q.ensure(sizeof(double) * nM)) ||
+      (rc = part.ensure(sizeof(double) * 1024)))
+    return rc;
+  FGB_CUDA(cudaMemsetAsync(w.err.p, 0, sizeof(int), st));
+  if (n > (long long)INT32_MAX) {
+    set_error("update_matrices_QR: %lld rows exceed the product kernels' "
+              "limit", n);
+    return FGB_EINVAL;
+  }
+  const int ni = (int)n;
+  const double u = std::ldexp(1.0, -53);
+  const double shift = 11.0 * ((double)n * M + (double)M * (M + 1)) * u;
+  // the rows of A (n x M) for the products Q = A R^-1
+  if ((rc = transpose(M, ni, At, n, A0.as<double>(), M, st))) return rc;
+  const double *Qprev = A0.as<double>();
+  const double *Tprev = At;   // Q_prev^T (M x n)
+  for (int pass = 0; pass < 3; pass++) {
+    if ((rc = gemm_nt(M, M, ni, Tprev, n, Tprev, n, G.as<double>(), M, 1.0,
+                      0.0, w, st)))
+      return rc;
+    if (pass == 0) {
+      const int nparts = 1024;
+      k_sumsq_part<<<nparts, 256, 0, st>>>((long long)M * n, At,
+                                          part.as<double>());
+      FGB_LAUNCH_CHECK("k_sumsq_part");
+      k_add_shift<<<ceil_div(M, 256), 256, 0, st>>>(
+          M, G.as<double>(), M, part.as<double>(), nparts, shift);
+      FGB_LAUNCH_CHECK("k_add_shift");
+    }
+    if ((rc = cholesky(M, G.as<double>(), M, st)) ||
+        (rc = trtri_lower(M, G.as<double>(), M, X[pass].as<double>(), M, st)))
+      return rc;
+    // Q_pass = Q_prev R_pass^-1 = Q_prev X_pass^T (X = L^-1, R = L^T)
+    if ((rc = gemm_nt(ni, M, M, Qprev, M, X[pass].as<double>(), M,
+                      Q.as<double>(), M, 1.0, 0.0, w, st)))
+      return rc;
+    if (pass < 2) {
+      // Q becomes the next pass's input (A0's storage is free after pass 0)
+      std::swap(Q.p, A0.p);
+      std::swap(Q.bytes, A0.bytes);
+      Qprev = A0.as<double>();
+      if ((rc = Qt.ensure(sizeof(double) * nM))) return rc;
+      if ((rc = transpose(ni, M, Qprev, M, Qt.as<double>(), n, st))) return rc;
+      Tprev = Qt.as<double>();
+    }
+  }
+  // Q^T b with the final Q
+  k_gemv_t<<<ceil_div(M, 32), 256, 0, st>>>(n, M, Q.as<double>(), b, Qtb);
+  FGB_LAUNCH_CHECK("k_gemv_t");
+  // R^-1 = R0^-1 R1^-1 R2^-1 = (X2 X1 X0)^T
+  double *T1 = G.as<double>();
+  if ((rc = transpose(M, M, X[1].as<double>(), M, T1, M, st)) ||
+      (rc = gemm_nt(M, M, M, X[2].as<double>(), M, T1, M, P.as<double>(), M,
+                    1.0, 0.0, w, st)) ||
+      (rc = transpose(M, M, X[0].as<double>(), M, T1, M, st)) ||
+      (rc = gemm_nt(M, M, M, P.as<double>(), M, T1, M, X[1].as<double>(), M,
+                    1.0, 0.0, w, st)) ||
+      (rc = transpose(M, M, X[1].as<double>(), M, R_inv, M, st)))
+    return rc;
+  return finish(w, st, "Cholesky QR");
+}
+
+int build_At(int M, int nl, const double *Kuf, const double *noise,
+             const double *y, const double *L, double *At, double *b,
+             cudaStream_t st) {
+  const long long n = (long long)nl + M;
+  k_build_At<<<ceil_div((long long)M * n, 256), 256, 0, st>>>(M, nl, Kuf, noise,
+                                                             y, L, At, b);
+  FGB_LAUNCH_CHECK("k_build_At");
+  return FGB_OK;
 }
 
 }  // namespace dense

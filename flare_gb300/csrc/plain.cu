@@ -534,41 +534,16 @@ extern "C" int fgb_predict_plain(fgb_model_t m, fgb_nlist_t nl,
 }
 
 // ------------------------------------------------------------ QR solve
-// SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 with
-// cuSOLVER/cuBLAS (column-major internally):
+// SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64:
 //   L = chol(Kuu + jitter I);  L_inv = L^-1
 //   A = [diag(sqrt(noise)) Kuf^T ; L^T],  b = [sqrt(noise) y ; 0]
 //   A = QR;  alpha = R^-1 (Q^T b)[:M];  R_inv = R^-1
+// (dense.cu holds the factorisations)
 namespace fgb {
 namespace {
 __global__ void k_add_diag(int M, double *A, double v) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < M) A[(long long)i * M + i] += v;
-}
-// A = [sqrt(noise) Kuf^T; L^T] column-major (rows = n_labels + M) with L
-// row-major lower (L^T(i, c) = L(c, i)), and b = [sqrt(noise) y; 0].
-__global__ void k_build_A_rm(int M, int nl, const double *Kuf,
-                             const double *noise, const double *y,
-                             const double *L, double *A, double *b) {
-  long long rows = (long long)nl + M;
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= rows * M) return;
-  int c = (int)(idx / rows);
-  long long r = idx % rows;
-  double v;
-  if (r < nl) v = sqrt(noise[r]) * Kuf[(long long)c * nl + r];
-  else v = L[(long long)c * M + (r - nl)];
-  A[idx] = v;
-  if (c == 0) b[r] = r < nl ? sqrt(noise[r]) * y[r] : 0.0;
-}
-// R^T row-major lower from the QR factor held in the first M rows of the
-// column-major A (ld rows): R^T(j, i) = R(i, j) = A[j rows + i], i <= j.
-__global__ void k_rt_from_qr(int M, long long rows, const double *A,
-                             double *Rt) {
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)M * M) return;
-  int j = (int)(idx / M), i = (int)(idx % M);
-  Rt[idx] = i <= j ? A[(long long)j * rows + i] : 0.0;
 }
 // alpha = R_inv Qb (R_inv row-major upper): a warp per row, lanes over
 // columns, fixed-order shuffle tree.
@@ -581,12 +556,6 @@ __global__ void k_upper_gemv(int M, const double *R, const double *x,
   for (int j = row + lane; j < M; j += 32) s += R[(long long)row * M + j] * x[j];
   for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   if (lane == 0) y[row] = s;
-}
-__global__ void k_transpose(int M, const double *in, double *out) {
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)M * M) return;
-  int c = (int)(idx / M), r = (int)(idx % M);
-  out[(long long)r * M + c] = in[idx];
 }
 }  // namespace
 }  // namespace fgb
@@ -601,12 +570,11 @@ __global__ void k_transpose(int M, const double *in, double *out) {
     }                                                                   \
   } while (0)
 
-// SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) on the GPU in FP64:
-// L = chol(Kuu + jitter I) and L_inv = L^-1 by the blocked kernels of
-// dense.cu (diagonal blocks in shared memory, O(M^3) updates as FP64-level
-// tensor-core products), the Householder QR of A = [sqrt(noise) Kuf^T;
-// L^T] and Q^T b by cuSOLVER (geqrf, ormqr), R_inv = (R^T)^-1^T by
-// dense.cu, alpha = R_inv (Q^T b)[:M] (the reference's R_inv * Q_b).
+// SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) on the GPU in FP64,
+// by the kernels of dense.cu: L = chol(Kuu + jitter I), L_inv = L^-1, the
+// QR of A = [sqrt(noise) Kuf^T; L^T] by shifted Cholesky QR (R_inv and
+// Q^T b; every O(n M^2) and O(M^3) product an FP64-level tensor-core
+// product), alpha = R_inv (Q^T b)[:M] (the reference's R_inv * Q_b).
 extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
                             const double *d_Kuf, const double *d_y,
                             const double *d_noise, double jitter,
@@ -620,16 +588,12 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
   cudaStream_t st = (cudaStream_t)stream;
   const long long rows = (long long)n_labels + M;
   int rc = FGB_OK;
-  cusolverDnHandle_t sol = nullptr;
-  DevBuf L, X, A, b, tau, work, info, Rinv;
-  int lwork = 0, lw2 = 0, hinfo = 0;
+  DevBuf L, At, b, Qtb, Rinv;
   double *R_inv = d_R_inv;
   if ((rc = L.ensure(sizeof(double) * (size_t)M * M)) ||
-      (rc = X.ensure(sizeof(double) * (size_t)M * M)) ||
-      (rc = A.ensure(sizeof(double) * (size_t)rows * M)) ||
+      (rc = At.ensure(sizeof(double) * (size_t)rows * M)) ||
       (rc = b.ensure(sizeof(double) * (size_t)rows)) ||
-      (rc = tau.ensure(sizeof(double) * (size_t)M)) ||
-      (rc = info.ensure(sizeof(int))))
+      (rc = Qtb.ensure(sizeof(double) * (size_t)M)))
     return rc;
   if (!R_inv) {
     if ((rc = Rinv.ensure(sizeof(double) * (size_t)M * M))) return rc;
@@ -639,54 +603,18 @@ extern "C" int fgb_solve_qr(int M, int n_labels, const double *d_Kuu,
                            cudaMemcpyDeviceToDevice, st));
   k_add_diag<<<ceil_div(M, 256), 256, 0, st>>>(M, L.as<double>(), jitter);
   FGB_LAUNCH_CHECK("k_add_diag");
-  if ((rc = dense::cholesky(M, L.as<double>(), M, st))) return rc;
-  if ((rc = dense::trtri_lower(M, L.as<double>(), M, d_L_inv, M, st)))
+  if ((rc = dense::cholesky(M, L.as<double>(), M, st)) ||
+      (rc = dense::trtri_lower(M, L.as<double>(), M, d_L_inv, M, st)) ||
+      (rc = dense::build_At(M, n_labels, d_Kuf, d_noise, d_y, L.as<double>(),
+                            At.as<double>(), b.as<double>(), st)) ||
+      (rc = dense::cholqr_solve(M, rows, At.as<double>(), b.as<double>(),
+                                R_inv, Qtb.as<double>(), st)))
     return rc;
-  FGB_SOLVER(cusolverDnCreate(&sol), "cusolverDnCreate");
-  FGB_SOLVER(cusolverDnSetStream(sol, st), "cusolverDnSetStream");
-  FGB_SOLVER(cusolverDnDgeqrf_bufferSize(sol, (int)rows, M, A.as<double>(),
-                                         (int)rows, &lwork), "geqrf_bufferSize");
-  FGB_SOLVER(cusolverDnDormqr_bufferSize(sol, CUBLAS_SIDE_LEFT, CUBLAS_OP_T,
-                                         (int)rows, 1, M, A.as<double>(),
-                                         (int)rows, tau.as<double>(),
-                                         b.as<double>(), (int)rows, &lw2),
-             "ormqr_bufferSize");
-  lwork = std::max(lwork, lw2);
-  if ((rc = work.ensure(sizeof(double) * ((size_t)lwork + 1)))) goto done;
-  k_build_A_rm<<<ceil_div(rows * M, 256), 256, 0, st>>>(
-      M, n_labels, d_Kuf, d_noise, d_y, L.as<double>(), A.as<double>(),
-      b.as<double>());
-  FGB_SOLVER(cudaGetLastError(), "k_build_A_rm");
-  FGB_SOLVER(cusolverDnDgeqrf(sol, (int)rows, M, A.as<double>(), (int)rows,
-                              tau.as<double>(), work.as<double>(), lwork,
-                              info.as<int>()), "geqrf");
-  FGB_SOLVER(cusolverDnDormqr(sol, CUBLAS_SIDE_LEFT, CUBLAS_OP_T, (int)rows, 1,
-                              M, A.as<double>(), (int)rows, tau.as<double>(),
-                              b.as<double>(), (int)rows, work.as<double>(),
-                              lwork, info.as<int>()), "ormqr");
-  FGB_SOLVER(cudaMemcpyAsync(&hinfo, info.p, sizeof(int),
-                             cudaMemcpyDeviceToHost, st), "info");
-  FGB_SOLVER(cudaStreamSynchronize(st), "sync");
-  if (hinfo != 0) {
-    set_error("fgb_solve_qr: QR failed (info %d)", hinfo);
-    rc = FGB_ECUDA;
-    goto done;
-  }
-  // R^T (lower) into X, its inverse into L, R_inv = that inverse transposed
-  k_rt_from_qr<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
-      M, rows, A.as<double>(), X.as<double>());
-  FGB_SOLVER(cudaGetLastError(), "k_rt_from_qr");
-  if ((rc = dense::trtri_lower(M, X.as<double>(), M, L.as<double>(), M, st)))
-    goto done;
-  k_transpose<<<ceil_div((long long)M * M, 256), 256, 0, st>>>(
-      M, L.as<double>(), R_inv);
   k_upper_gemv<<<ceil_div((long long)M * 32, 256), 256, 0, st>>>(
-      M, R_inv, b.as<double>(), d_alpha);
-  FGB_SOLVER(cudaStreamSynchronize(st), "sync");
-  FGB_SOLVER(cudaGetLastError(), "solve kernels");
-done:
-  if (sol) cusolverDnDestroy(sol);
-  return rc;
+      M, R_inv, Qtb.as<double>(), d_alpha);
+  FGB_LAUNCH_CHECK("k_upper_gemv");
+  FGB_CUDA(cudaStreamSynchronize(st));
+  return FGB_OK;
 }
 
 // Thin Q of a Householder QR (cuSOLVER geqrf + orgqr): A and Q column-major

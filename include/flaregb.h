@@ -490,8 +490,11 @@ int fgb_oz_sgemm_nt(int M, int N, int K, const double *d_A, long long lda,
 
 /* SparseGP::update_matrices_QR (sparse_gp.cpp:607-641) in FP64 on the GPU:
  * Cholesky of Kuu + jitter I and L_inv (fgb_cholesky, fgb_trtri_lower), the
- * Householder QR of [diag(sqrt(noise)) Kuf^T ; L^T] and Q^T b (cuSOLVER),
- * R_inv, alpha = R_inv (Q^T b)[:M].  All device pointers, row-major.
+ * QR of [diag(sqrt(noise)) Kuf^T ; L^T] by shifted Cholesky QR with two
+ * refinement passes (R_inv and Q^T b; R agrees with the reference's
+ * Householder R up to row signs, so alpha and Sigma are the same
+ * quantities), alpha = R_inv (Q^T b)[:M]; the O(n M^2) and O(M^3) products
+ * as FP64-level tensor-core products.  All device pointers, row-major.
  * d_Kuu[M*M], d_Kuf[M*n_labels], d_y[n_labels], d_noise[n_labels] ->
  * d_alpha[M], d_L_inv[M*M], d_R_inv[M*M] (may be NULL).  A Kuu + jitter
  * that is not positive definite returns FGB_EINVAL with the reference's

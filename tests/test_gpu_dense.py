@@ -105,3 +105,56 @@ def test_training_products_match_oracle():
                                atol=1e-7 * np.abs(ogp.Kuu_inverse).max())
     np.testing.assert_allclose(ggp.Sigma, ogp.Sigma, rtol=0,
                                atol=1e-7 * np.abs(ogp.Sigma).max())
+
+
+@pytest.mark.parametrize("M,nl,cond,rank,scale", [(300, 2000, 1e6, 300, 1.0),
+                                                  (700, 5000, 1e10, 350, 1e-3)])
+def test_solve_qr_matches_householder(M, nl, cond, rank, scale):
+    """fgb_solve_qr (Cholesky, triangular inverses, shifted Cholesky QR)
+    against numpy's Householder QR of the same A = [sqrt(noise) Kuf^T;
+    L^T]: alpha, L_inv and Sigma = R_inv R_inv^T (R agrees up to row
+    signs, so R_inv is compared through Sigma).  Kuf of rank `rank` scaled
+    by `scale` leaves the small singular values to L^T: cond(A) = 1.9e4
+    and 5.5e4."""
+    import scipy.linalg as sla
+    import torch
+    from flare_gb300 import _lib
+    r = np.random.Generator(np.random.PCG64(M + nl))
+    Kuu = 4.0 * _spd(M, M + 1, cond=cond)
+    Kuf = (r.normal(size=(M, rank)) @ r.normal(size=(rank, nl))) * scale / \
+        np.sqrt(rank)
+    y = r.normal(size=nl)
+    noise = np.where(r.uniform(size=nl) < 0.1, 1e6, 400.0)
+    jitter = 1e-8
+    d = {k: _dev(v) for k, v in (("Kuu", Kuu), ("Kuf", Kuf), ("y", y),
+                                   ("noise", noise))}
+    alpha = torch.zeros(M, dtype=torch.float64, device="cuda")
+    Li = torch.zeros((M, M), dtype=torch.float64, device="cuda")
+    Ri = torch.zeros((M, M), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().fgb_solve_qr(
+        M, nl, _lib.ptr(d["Kuu"]), _lib.ptr(d["Kuf"]), _lib.ptr(d["y"]),
+        _lib.ptr(d["noise"]), jitter, _lib.ptr(alpha), _lib.ptr(Li),
+        _lib.ptr(Ri), _lib.stream_ptr()), "solve")
+    torch.cuda.synchronize()
+    Lc = np.linalg.cholesky(Kuu + jitter * np.eye(M))
+    Lref = sla.solve_triangular(Lc, np.eye(M), lower=True)
+    A = np.vstack([np.sqrt(noise)[:, None] * Kuf.T, Lc.T])
+    b = np.concatenate([np.sqrt(noise) * y, np.zeros(M)])
+    Q, R = np.linalg.qr(A)
+    Rinv = sla.solve_triangular(R, np.eye(M), lower=False)
+    aref = Rinv @ (Q.T @ b)
+    Sref = Rinv @ Rinv.T
+    Ri_ = Ri.cpu().numpy()
+    # two backward-stable computations differ by up to about the problem's
+    # condition number x u: cond(Kuu + jitter) for L_inv, cond(A)^2 for
+    # alpha and Sigma = (A^T A)^-1
+    ev = np.linalg.eigvalsh(Kuu + jitter * np.eye(M))
+    tol_L = max(1e-9, 4 * (ev[-1] / ev[0]) * 2.0 ** -53)
+    tol_a = max(1e-8, 10 * np.linalg.cond(A) ** 2 * 2.0 ** -53)
+    np.testing.assert_allclose(Li.cpu().numpy(), Lref, rtol=0,
+                               atol=tol_L * np.abs(Lref).max())
+    np.testing.assert_allclose(alpha.cpu().numpy(), aref, rtol=0,
+                               atol=tol_a * np.abs(aref).max())
+    np.testing.assert_allclose(Ri_ @ Ri_.T, Sref, rtol=0,
+                               atol=tol_a * np.abs(Sref).max())
+    assert np.all(np.tril(Ri_, -1) == 0.0)
