@@ -79,6 +79,41 @@ static __constant__ float c_ylm_norm_lo[(kMaxL + 1) * (kMaxL + 1)] = {
 __device__ __forceinline__ void ylm_norm(int i, double &k) { k = c_ylm_norm[i]; }
 __device__ __forceinline__ void ylm_norm(int i, float &k) { k = c_ylm_norm_f[i]; }
 
+// The double factorials (2m - 1)!! (m = 0 .. kMaxL, exact in FP64 and as
+// FP32 head + FP32 tail) and the reciprocals 1/k (k = 1 .. 2 kMaxL + 1,
+// FP32 nearest and its FP32 remainder): the associated-Legendre recurrence
+// multiplies by these instead of dividing (a double-float or FP32 division
+// costs tens of instructions; the FP64 evaluation keeps its divisions).
+constexpr int kNumInv = 2 * kMaxL + 2;
+__host__ __device__ constexpr double dfact_value(int m) {
+  double v = 1.0;
+  for (int k = 1; k <= m; k++) v *= (double)(2 * k - 1);
+  return v;
+}
+#define FGB_DFACT(X) X(dfact_value(0)) X(dfact_value(1)) X(dfact_value(2)) \
+  X(dfact_value(3)) X(dfact_value(4)) X(dfact_value(5)) X(dfact_value(6)) \
+  X(dfact_value(7)) X(dfact_value(8)) X(dfact_value(9)) X(dfact_value(10))
+#define FGB_INV(X) X(0.0) X(1.0) X(1.0 / 2) X(1.0 / 3) X(1.0 / 4) X(1.0 / 5) \
+  X(1.0 / 6) X(1.0 / 7) X(1.0 / 8) X(1.0 / 9) X(1.0 / 10) X(1.0 / 11) \
+  X(1.0 / 12) X(1.0 / 13) X(1.0 / 14) X(1.0 / 15) X(1.0 / 16) X(1.0 / 17) \
+  X(1.0 / 18) X(1.0 / 19) X(1.0 / 20) X(1.0 / 21)
+static_assert(kMaxL == 10, "the double-factorial and reciprocal tables");
+static __constant__ double c_dfact[kMaxL + 1] = {FGB_DFACT(FGB_AS_F64)};
+static __constant__ float c_dfact_f[kMaxL + 1] = {FGB_DFACT(FGB_AS_F32)};
+static __constant__ float c_dfact_lo[kMaxL + 1] = {FGB_DFACT(FGB_AS_F32_LO)};
+static __constant__ float c_inv_f[kNumInv] = {FGB_INV(FGB_AS_F32)};
+static __constant__ float c_inv_lo[kNumInv] = {FGB_INV(FGB_AS_F32_LO)};
+
+__device__ __forceinline__ void dfact_const(int m, double &v) { v = c_dfact[m]; }
+__device__ __forceinline__ void dfact_const(int m, float &v) { v = c_dfact_f[m]; }
+// x / k for a small positive integer k
+__device__ __forceinline__ double div_int(double x, int k) {
+  return x / (double)k;
+}
+__device__ __forceinline__ float div_int(float x, int k) {
+  return x * c_inv_f[k];
+}
+
 // ------------------------------------------------------------ cutoff
 // cutoffs.cpp:7-85.  Returns value and derivative w.r.t. r.
 template <typename T>
@@ -305,20 +340,19 @@ __device__ __forceinline__ void ylm_visit(int Lrt, T x, T y, T z, Fn &&fn) {
 #pragma unroll
   for (int l = 0; l <= L + 1; l++) qnext[l] = T(0);
   // (2m-1)!! for m = L
-  T dfact = T(1);
-#pragma unroll
-  for (int k = 1; k <= L; k++) dfact *= T(2 * k - 1);
 #pragma unroll
   for (int m = L; m >= 0; m--) {
-    if (m < L) dfact /= T(2 * m + 1);       // (2m-1)!!
+    T dfact;
+    dfact_const(m, dfact);                  // (2m-1)!!
 #pragma unroll
     for (int l = 0; l <= L; l++) qcur[l] = T(0);
     qcur[m] = dfact;
     if (m + 1 <= L) qcur[m + 1] = T(2 * m + 1) * uz * dfact;
 #pragma unroll
     for (int l = m + 2; l <= L; l++)
-      qcur[l] = (T(2 * l - 1) * uz * qcur[l - 1] - T(l + m - 1) * qcur[l - 2]) /
-                T(l - m);
+      qcur[l] = div_int(T(2 * l - 1) * uz * qcur[l - 1] -
+                            T(l + m - 1) * qcur[l - 2],
+                        l - m);
 #pragma unroll
     for (int l = m; l <= L; l++) {
       T K;

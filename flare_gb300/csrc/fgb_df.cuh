@@ -171,6 +171,12 @@ __device__ __forceinline__ double to_double(df a) {
 __device__ __forceinline__ void ylm_norm(int i, df &k) {
   k = df(c_ylm_norm_f[i], c_ylm_norm_lo[i]);
 }
+__device__ __forceinline__ void dfact_const(int m, df &v) {
+  v = df(c_dfact_f[m], c_dfact_lo[m]);
+}
+__device__ __forceinline__ df div_int(df x, int k) {
+  return x * df(c_inv_f[k], c_inv_lo[k]);
+}
 
 // Rare-path functions (cutoffs other than quadratic and hard): evaluated in
 // FP64 and split back.
