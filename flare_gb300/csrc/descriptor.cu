@@ -22,10 +22,6 @@ namespace {
 
 constexpr int kChunk = 64;      // pairs per shared-memory chunk = block size
 
-__device__ __forceinline__ int pair_index(int n1, int n2, int nr) {
-  return n1 * nr - n1 * (n1 - 1) / 2 + (n2 - n1);
-}
-
 __device__ __forceinline__ void decode_b2(int q, int L1, int nr, int &n1,
                                           int &n2, int &l) {
   l = q % L1;
@@ -309,23 +305,30 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   }
   __syncthreads();
   // u = dE/dA: u[c][lm] = sum_b (1 + [b == c]) w((c,b), l) A[b][lm], a
-  // thread per (atom, entry)
+  // thread per (atom, entry), b ascending.  The B2 index of the radial
+  // pair (min(b,c), max(b,c)) advances by nr - b - 1 while b < c and by 1
+  // after it, so the loop carries it instead of recomputing it.
   for (int it = t; it < na * nA; it += blockDim.x) {
-    const int a = it / nA, e = it % nA;
+    const int a = it / nA, e = it - a * nA;
     const T *A = smem + (size_t)a * per + nA;
     T *u = smem + (size_t)a * per;
-    const T *W = w_in_smem ? A + nA : nullptr;
-    const T *w = gB2 + (long long)(i0 + a) * nd;
-    const int c = e / nh, lm = e % nh;
+    const T *wsrc = w_in_smem ? A + nA : gB2 + (long long)(i0 + a) * nd;
+    const int c = e / nh, lm = e - c * nh;
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) l++;
+    const T *Acol = A + lm;
+    const T *wl = wsrc + l;
     T acc = T(0);
-    for (int bb = 0; bb < nr; bb++) {
-      const int lo = c < bb ? c : bb, hi = c < bb ? bb : c;
-      const int wi = pair_index(lo, hi, nr) * L1 + l;
-      const T wv = W ? W[wi] : w[wi];
-      const T f = (bb == c) ? T(2) : T(1);
-      acc += f * wv * A[bb * nh + lm];
+    int pidx = c;   // radial pair (0, c)
+    for (int bb = 0; bb < c; bb++) {
+      acc += wl[pidx * L1] * Acol[bb * nh];
+      pidx += nr - bb - 1;
+    }
+    // pidx is now the pair (c, c)
+    acc += T(2) * wl[pidx * L1] * Acol[c * nh];
+    for (int bb = c + 1; bb < nr; bb++) {
+      pidx++;
+      acc += wl[pidx * L1] * Acol[bb * nh];
     }
     u[e] = acc;
   }
