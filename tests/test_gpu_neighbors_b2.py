@@ -26,6 +26,15 @@ def cases():
     out.append(("unwrapped", c, s, p, 5.0))
     out.append(("sparse_gas", np.eye(3) * 30.0, np.zeros(3, int),
                 np.array([[0, 0, 0], [1, 1, 1], [15, 15, 15.]]), 5.0))
+    # fractional coordinates that wrap to exactly 1.0 (a tiny negative
+    # coordinate): the atom's raw bin is the top one, in a cell whose bins
+    # are staged per bin and in a tiny cell searched atom by atom
+    for name, (c, s, p) in (("face_rounding", syn.random_alloy(300, seed=9)),
+                            ("face_rounding_tiny", random_atoms(seed=12))):
+        p = p.copy()
+        p[0] = [-1e-18, 0.5 * c[1, 1], -1e-17]
+        p[1] = [0.25 * c[0, 0], -3e-18, 0.5 * c[2, 2]]
+        out.append((name, c, s, p, 5.0))
     return out
 
 
