@@ -31,19 +31,12 @@ __device__ __forceinline__ void decode_b2(int q, int L1, int nr, int &n1,
   n2 = n1 + pidx;
 }
 
-template <typename T>
-__device__ T block_sum(T v, T *red) {
-  // fixed-order tree reduction over the block (blockDim.x == kChunk)
-  int t = threadIdx.x;
-  red[t] = v;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (t < s) red[t] += red[t + s];
-    __syncthreads();
-  }
-  T r = red[0];
-  __syncthreads();
-  return r;
+__device__ __forceinline__ double shfl_down(double v, int o) {
+  return __shfl_down_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ df shfl_down(df v, int o) {
+  return df(__shfl_down_sync(0xffffffffu, v.hi, o),
+            __shfl_down_sync(0xffffffffu, v.lo, o));
 }
 
 // acc += a b.  FP64: one fused multiply-add.  Double-float: the exact
@@ -77,8 +70,18 @@ __global__ void __launch_bounds__(kChunk, 12)
 k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, double *__restrict__ A_out,
-             double *__restrict__ B2, double *__restrict__ norms) {
+             double *__restrict__ B2, double *__restrict__ norms,
+             double *__restrict__ rowmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // largest |B2| of the row as written (the bits of |x| order as the
+  // values do), for the tensor-core row scales: no second pass over B2
+  __shared__ unsigned long long s_max[kChunk / 32];
+  unsigned long long lmax = 0;
+  const auto track = [&lmax](double x) {
+    const unsigned long long a =
+        (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFULL;
+    lmax = a > lmax ? a : lmax;
+  };
   const int i = blockIdx.x;
   if (i >= n_atoms) return;
   // NC / LC > 0: n_max / l_max fixed at compile time
@@ -223,14 +226,22 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
         for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[l * l + m], a2[l * l + m]);
         v = finish(v);
         if (stage) out_s[pi * L1c + l] = v;
-        else B2[(long long)i * nd + pi * L1c + l] = to_double(v);
+        else {
+          const double x = to_double(v);
+          B2[(long long)i * nd + pi * L1c + l] = x;
+          track(x);
+        }
         mac(nrm, v, v);
       }
     }
     if (stage) {
       __syncthreads();
       for (int q = t; q < nd; q += blockDim.x)
-        B2[(long long)i * nd + q] = to_double(out_s[q]);
+      {
+        const double x = to_double(out_s[q]);
+        B2[(long long)i * nd + q] = x;
+        track(x);
+      }
     }
   } else {
     for (int q = t; q < nd; q += blockDim.x) {
@@ -240,12 +251,35 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       T v = T(0);
       for (int m = 0; m < 2 * l + 1; m++) mac(v, a1[m], a2[m]);
       v = finish(v);
-      B2[(long long)i * nd + q] = to_double(v);
+      const double x = to_double(v);
+      B2[(long long)i * nd + q] = x;
+      track(x);
       mac(nrm, v, v);
     }
   }
-  nrm = block_sum(finish(nrm), red);
-  if (t == 0) norms[i] = to_double(sqrt(nrm));
+  // norm and row maximum: shuffles down each warp (fixed order), then
+  // thread 0 adds the warps' partials in warp order -- one barrier
+  nrm = finish(nrm);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nrm = nrm + shfl_down(nrm, o);
+    const unsigned long long m =
+        (unsigned long long)__shfl_down_sync(0xffffffffu, (long long)lmax, o);
+    lmax = m > lmax ? m : lmax;
+  }
+  if ((t & 31) == 0) {
+    red[t >> 5] = nrm;
+    s_max[t >> 5] = lmax;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int w = 1; w < kChunk / 32; w++) {
+      nrm = nrm + red[w];
+      lmax = s_max[w] > lmax ? s_max[w] : lmax;
+    }
+    norms[i] = to_double(sqrt(nrm));
+    if (rowmax) rowmax[i] = __longlong_as_double((long long)lmax);
+  }
 }
 
 // Shared memory: u[nA] | A[nA] (compute type T: double, or float in the
@@ -485,7 +519,8 @@ struct AdjK {
 
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
-                      double *d_norms, cudaStream_t st, bool dfloat) {
+                      double *d_norms, cudaStream_t st, bool dfloat,
+                      double *d_rowmax) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
   const size_t sm_full = b2_forward_smem(p, false);   // sizeof(df) == 8
@@ -511,7 +546,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
     if (e != cudaSuccess) return;
     fn<<<N, kChunk, sm, st>>>(p, N, nl->offsets.as<long long>(),
                               nl->nbr_j.as<int>(), nl->nbr_rel.as<double4_16a>(),
-                              d_species, d_A, d_B2, d_norms);
+                              d_species, d_A, d_B2, d_norms, d_rowmax);
   };
   if (dfloat) dispatch_nl<FwdK, df>(p, go);
   else dispatch_nl<FwdK, double>(p, go);

@@ -6,10 +6,12 @@ namespace fgb {
 
 size_t b2_forward_smem(const B2Params &p, bool regA = false);
 size_t b2_adjoint_smem(const B2Params &p);
-// dfloat: compute in double-float (mixed-precision path) instead of FP64
+// dfloat: compute in double-float (mixed-precision path) instead of FP64;
+// d_rowmax (optional): each row's largest |B2| as written
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
-                      double *d_norms, cudaStream_t st, bool dfloat = false);
+                      double *d_norms, cudaStream_t st, bool dfloat = false,
+                      double *d_rowmax = nullptr);
 // d_gB2: dE/dB2 rows [N, n_d] in the compute type (float when fp32, else
 // double)
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,

@@ -10,6 +10,7 @@
 struct fgb_workspace {
   fgb::DevBuf perm, flags, pos, scal, scan_tmp, flag;
   fgb::DevBuf A, B2, norms, e_atom, var, volume, atom_off;
+  fgb::DevBuf rowmax;   // largest |B2| per row (tensor-core row scales)
   fgb::DevBuf gB2, pair_grad, forces, virial;
   fgb::DevBuf kmat, wmat, erows, part;
   fgb::DevBuf b2f, yf;           // mixed path: FP32 normalised rows, D^ B

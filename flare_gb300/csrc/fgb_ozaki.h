@@ -61,6 +61,9 @@ struct SliceSpec {
   long long ld;
   const int *perm;         // optional row gather
   const double *rownorm;   // optional: divide row by its norm (0 if < 1e-8)
+  // optional: each source row's largest |value| (indexed like src rows);
+  // the row scales then come from it instead of a pass over the rows
+  const double *rowmax = nullptr;
 };
 
 struct Sliced {

@@ -126,6 +126,57 @@ __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
   }
 }
 
+// The same for power 2 with rows of n_d = 4 t <= 1024 values: a lane takes
+// four consecutive columns at a time (two double2 loads of B2, one float4
+// of Y, one float4 store), keeps d^ and g in registers between the dot
+// product and the update, and the row's bytes are read once.
+constexpr int kGradV4It = 8;   // 8 x 32 lanes x 4 columns = 1024
+__global__ void __launch_bounds__(256)
+k_mapped_grad_v4(int Mr, int nd, const int *__restrict__ perm,
+                 const double *__restrict__ norms,
+                 const double *__restrict__ B2, const float *__restrict__ Y,
+                 float scale, float *__restrict__ gB2) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= Mr) return;
+  const int atom = perm[warp];
+  const double n = norms[atom];
+  const bool ok = n >= kEmptyThresh;
+  const float inv = ok ? __frcp_rn(trunc_float(n)) : 0.f;
+  const int n4 = nd >> 2;
+  const double2 *b = reinterpret_cast<const double2 *>(B2 + (long long)atom * nd);
+  const float4 *y = reinterpret_cast<const float4 *>(Y + (long long)warp * nd);
+  float4 dv[kGradV4It], yv[kGradV4It];
+  float q = 0.f;
+#pragma unroll
+  for (int it = 0; it < kGradV4It; it++) {
+    const int k4 = lane + 32 * it;
+    if (k4 < n4) {
+      const double2 b0 = b[2 * k4], b1 = b[2 * k4 + 1];
+      dv[it] = make_float4(trunc_float(b0.x) * inv, trunc_float(b0.y) * inv,
+                           trunc_float(b1.x) * inv, trunc_float(b1.y) * inv);
+      yv[it] = y[k4];
+      q = __fmaf_rn(dv[it].x, yv[it].x, q);
+      q = __fmaf_rn(dv[it].y, yv[it].y, q);
+      q = __fmaf_rn(dv[it].z, yv[it].z, q);
+      q = __fmaf_rn(dv[it].w, yv[it].w, q);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+  const float sq = scale * q;
+  float4 *out = reinterpret_cast<float4 *>(gB2 + (long long)atom * nd);
+#pragma unroll
+  for (int it = 0; it < kGradV4It; it++) {
+    const int k4 = lane + 32 * it;
+    if (k4 < n4)
+      out[k4] = make_float4((scale * yv[it].x - sq * dv[it].x) * inv,
+                            (scale * yv[it].y - sq * dv[it].y) * inv,
+                            (scale * yv[it].z - sq * dv[it].z) * inv,
+                            (scale * yv[it].w - sq * dv[it].w) * inv);
+  }
+}
+
 // The same in FP64, for the guarded path (large folded coefficients):
 // Y = D^ B_s from the FP64-level product, or the FP64 fold vector.
 __global__ void k_mapped_grad64(int Mr, int nd, const int *__restrict__ perm,
@@ -345,12 +396,19 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                          launch, usable, st, fixed, &v)))
         return r;
     }
-    k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
-        Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
-        quad ? m->ws.yf.as<float>() : nullptr,
-        quad ? nullptr : m->Bmap.as<float>() + per * s,
-        quad ? 2.f * sig2 : sig2, reinterpret_cast<float *>(d_gB2));
-    FGB_LAUNCH_CHECK("k_mapped_grad");
+    if (quad && nd % 4 == 0 && nd <= 4 * 32 * kGradV4It) {
+      k_mapped_grad_v4<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+          m->ws.yf.as<float>(), 2.f * sig2, reinterpret_cast<float *>(d_gB2));
+      FGB_LAUNCH_CHECK("k_mapped_grad_v4");
+    } else {
+      k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
+          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+          quad ? m->ws.yf.as<float>() : nullptr,
+          quad ? nullptr : m->Bmap.as<float>() + per * s,
+          quad ? 2.f * sig2 : sig2, reinterpret_cast<float *>(d_gB2));
+      FGB_LAUNCH_CHECK("k_mapped_grad");
+    }
     return FGB_OK;
   };
   // Kernel and variance GEMMs on the tensor cores, FP64-accurate by exact

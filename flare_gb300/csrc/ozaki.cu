@@ -336,6 +336,31 @@ k_oz_rowscale(int R, int K, int RP, const double *__restrict__ src,
   if (lane == 0) scale[m] = ldexp(1.0, e);
 }
 
+// The same scales from each source row's largest |value| given up front
+// (`rowmax`, indexed like the source rows): a thread per row.
+__global__ void k_oz_scale_from_max(int R, int RP, const int *__restrict__ perm,
+                                    const double *__restrict__ rownorm,
+                                    double thresh,
+                                    const double *__restrict__ rowmax,
+                                    double *__restrict__ scale) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= RP) return;
+  double mx = 0.0;
+  if (m < R) {
+    const long long row = perm ? (long long)perm[m] : (long long)m;
+    double inv = 1.0;
+    bool valid = true;
+    if (rownorm) {
+      const double n = rownorm[row];
+      if (n >= thresh) inv = 1.0 / n;
+      else valid = false;
+    }
+    if (valid) mx = rowmax[row] * inv;
+  }
+  const int e = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  scale[m] = ldexp(1.0, e);
+}
+
 // Row slicing: each row scaled to (-1, 1) by its power of two 2^e
 // (k_oz_rowscale), the scaled value y taken as the integer X = rn(y 2^(6S))
 // (exact for |y| >= 2^-1 of the row's top binade, rounded at 2^(-6S) below
@@ -798,10 +823,17 @@ template <int S>
 static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   int rc;
   if ((rc = prepare(sp.rows, sp.K, sp.TR, S, out))) return rc;
-  k_oz_rowscale<<<ceil_div((long long)out.RP * 32, 256), 256, 0, st>>>(
-      sp.rows, sp.K, out.RP, sp.src, sp.ld, sp.perm, sp.rownorm,
-      kEmptyThresh, out.scale.as<double>());
-  FGB_LAUNCH_CHECK("k_oz_rowscale");
+  if (sp.rowmax) {
+    k_oz_scale_from_max<<<ceil_div(out.RP, 256), 256, 0, st>>>(
+        sp.rows, out.RP, sp.perm, sp.rownorm, kEmptyThresh, sp.rowmax,
+        out.scale.as<double>());
+    FGB_LAUNCH_CHECK("k_oz_scale_from_max");
+  } else {
+    k_oz_rowscale<<<ceil_div((long long)out.RP * 32, 256), 256, 0, st>>>(
+        sp.rows, sp.K, out.RP, sp.src, sp.ld, sp.perm, sp.rownorm,
+        kEmptyThresh, out.scale.as<double>());
+    FGB_LAUNCH_CHECK("k_oz_rowscale");
+  }
   const int nparts = ceil_div(out.KP, kSlicePart);
   const long long threads = (long long)(out.RP / 8) * nparts * 32;  // RP % 8 == 0
   k_oz_slice8<S><<<ceil_div(threads, 256), 256, 0, st>>>(
@@ -1413,7 +1445,8 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       {
         StageTimer _pt(kStRowSlice, st, 2);   // row scales, slices
         if ((rc = oz::slice({Mr, nd, oz::kTM, m->ws.B2.as<double>(), nd, perm,
-                             m->ws.norms.as<double>()},
+                             m->ws.norms.as<double>(),
+                             m->ws.rowmax.as<double>()},
                             m->ws.ozA, st, SA)))
           return rc;
       }

@@ -592,6 +592,7 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       (rc = m->ws.norms.ensure(sizeof(double) * (N + 1))) ||
       (rc = m->ws.e_atom.ensure(sizeof(double) * (N + 1))) ||
       (rc = m->ws.var.ensure(sizeof(double) * (N + 1))) ||
+      (rc = m->ws.rowmax.ensure(sizeof(double) * (N + 1))) ||
       (rc = m->ws.volume.ensure(sizeof(double) * (n_struc + 1))) ||
       (rc = m->ws.atom_off.ensure(sizeof(int) * (n_struc + 1))))
     return rc;
@@ -622,7 +623,8 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     // mixed precision: the descriptor in double-float (about 46 bits)
     if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
                                 m->ws.B2.as<double>(), m->ws.norms.as<double>(),
-                                st, mixed && !m->force_f64)))
+                                st, mixed && !m->force_f64,
+                                mixed ? m->ws.rowmax.as<double>() : nullptr)))
       return rc;
   }
   std::vector<int> counts;
