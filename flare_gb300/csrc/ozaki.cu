@@ -669,27 +669,34 @@ k_oz_gemm(int M, int N, int K, int KP, int MT, int NTt, FastDiv divNT,
           break;
         }
         tc::fence_after_sync();
+        // (chunk, group) loads in sequence, two register buffers: the load
+        // of the next pair is in flight while this one is added up, and the
+        // accumulator is released as soon as the last load has landed
+        uint32_t rb[2][16];
+        tc::tmem_ld16(trow + c_lo, rb[0]);
+        tc::tmem_ld_wait(rb[0]);
 #pragma unroll
-        for (int ch = 0; ch < NCH; ch++) {
-#pragma unroll
-          for (int g = 0; g < S; g++) {
-            uint32_t r[16];
-            tc::tmem_ld16(trow + g * TN + c_lo + ch * 16, r);
-            tc::tmem_ld_wait();
-            const int tg = g + 2;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const long long qv =
-                  (long long)__float2int_rn(__uint_as_float(r[j]));
-              if (tg <= C::TSPLIT) hi[ch][j] += qv << (6 * (C::TSPLIT - tg));
-              else lo[ch][j] += qv << (6 * (S + 1 - tg));
-            }
+        for (int it = 0; it < NCH * S; it++) {
+          const int ch = it / S, g = it % S, cur = it & 1;
+          if (it + 1 < NCH * S) {
+            const int ch1 = (it + 1) / S, g1 = (it + 1) % S;
+            tc::tmem_ld16(trow + g1 * TN + c_lo + ch1 * 16, rb[cur ^ 1]);
+          } else {
+            // the accumulator may now take the next segment or tile
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(acc_empty);
           }
+          const int tg = g + 2;
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const long long qv =
+                (long long)__float2int_rn(__uint_as_float(rb[cur][j]));
+            if (tg <= C::TSPLIT) hi[ch][j] += qv << (6 * (C::TSPLIT - tg));
+            else lo[ch][j] += qv << (6 * (S + 1 - tg));
+          }
+          if (it + 1 < NCH * S) tc::tmem_ld_wait(rb[cur ^ 1]);
         }
-        // the accumulator may now take the next segment or tile
-        tc::fence_before_sync();
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(acc_empty);
       }
       if (!alive) break;
       // C = (hi 2^(-6 TSPLIT) + lo 2^(-6(S+1))) 2^(e_row + e_col): exact
@@ -791,11 +798,18 @@ struct EpiStoreF32 {
   __device__ double chunk(int m, bool row_ok, int n0, const float (&v)[16],
                           double acc) const {
     if (!row_ok) return acc;
+    float *y = Y + (long long)m * ldy + n0;
+    if (n0 + 16 <= N && (reinterpret_cast<uintptr_t>(y) & 15) == 0) {
+      // a full chunk on a 16-byte boundary: four vector stores
+      float4 *y4 = reinterpret_cast<float4 *>(y);
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      int n = n0 + j;
-      if (n < N) Y[(long long)m * ldy + n] = v[j];
+      for (int q = 0; q < 4; q++)
+        y4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      return acc;
     }
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      if (n0 + j < N) y[j] = v[j];
     return acc;
   }
   __device__ void finish(int, bool, int, double) const {}
