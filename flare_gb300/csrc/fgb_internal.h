@@ -66,12 +66,21 @@ int scan_int_to_ll_raw(const int *d_in, long long *d_out, int n,
 
 struct fgb_nlist_s;
 namespace fgb {
-// fgb_nlist_build on a stream; with `check` false the fill and twin
-// consistency flags (flag[1], flag[2]) are left on the device for the
-// caller, so the build synchronises once (the pair count).
+// fgb_nlist_build on a stream.  With `check` false the device flags
+// (non-finite positions, fill and twin consistency, single-pass overflow)
+// are left for the caller, who reads them after its own synchronisation
+// and passes them to nlist_finish; a single-pass build then does not
+// synchronise at all, and n_pairs is an upper bound until nlist_finish.
 int nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
                 const double *h_cells, const double *d_positions,
                 double cutoff, cudaStream_t st, bool check);
+// The deferred checks of a build with `check` false, from its four device
+// flags read after the stream synchronised: FGB_OK (and the exact pair
+// count in n_pairs), an error, or kNlistRetry when an atom had more pairs
+// than its single-pass slots (the caller repeats its work with
+// count_pass set).
+constexpr int kNlistRetry = 1000;
+int nlist_finish(fgb_nlist_s *nl, const int *hflag);
 // Per-pair buffers for at least `cap` pairs (neighbors.cu).
 int nlist_reserve(fgb_nlist_s *nl, long long cap);
 // The list of the last full build's structures (same atoms, cells, bins) at
@@ -114,6 +123,21 @@ struct fgb_nlist_s {
                              // capacity exceeded (fixed rebuild)
   fgb::DevBuf scan_tmp;
   fgb::DevBuf scalars;       // long long[4]
+  // single-pass builds: slots per atom of the last one and the least the
+  // next may take (raised after an overflow), the pinned pair total the
+  // build copies back, whether n_pairs still waits for it, and a request
+  // for a count pass (set by callers repeating a build that overflowed)
+  long long last_slots = 0, min_slots = 0;
+  int last_launches = 0;     // kernels the last build or rebuild launched
+  long long *h_total = nullptr;
+  bool total_pending = false;
+  bool count_pass = false;
+  fgb_nlist_s() = default;
+  fgb_nlist_s(const fgb_nlist_s &) = delete;
+  fgb_nlist_s &operator=(const fgb_nlist_s &) = delete;
+  ~fgb_nlist_s() {
+    if (h_total) cudaFreeHost(h_total);
+  }
 };
 
 struct fgb_b2_s {

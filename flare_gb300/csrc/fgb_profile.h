@@ -32,6 +32,8 @@ class StageTimer {
   ~StageTimer();
   StageTimer(const StageTimer &) = delete;
   StageTimer &operator=(const StageTimer &) = delete;
+  // the stage's kernel count when it is known only after its launches
+  void set_launches(int n) { launches_ = n; }
 
  private:
   int stage_;

@@ -393,11 +393,19 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   FGB_CUDA(cudaMemcpyAsync(h + 4, ws.ozerr.p, sizeof(int),
                            cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
-  if (h[1] || h[2]) {
-    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
-              h[1], h[2]);
-    return FGB_ECUDA;
+  rc = nlist_finish(&m->nl, h);
+  if (rc == kNlistRetry) {
+    // an atom had more pairs than its single-pass slots: again, with a
+    // count pass
+    m->nl.count_pass = true;
+    rc = fgb_mapped_predict(m, n_struc, h_atom_offsets, h_cells, d_positions,
+                            d_species, cutoff, want, d_energy, d_forces,
+                            d_stress, d_atom_energy, d_local_var, precision,
+                            stream);
+    m->nl.count_pass = false;
+    return rc;
   }
+  if (rc) return rc;
   if (h[4]) {
     set_error("mapped evaluation: a bounded tensor-core wait ran out");
     return FGB_ETIMEOUT;

@@ -266,19 +266,23 @@ constexpr int kQueue = 64;      // per-warp candidate queue
 
 // Warp per atom: write the pairs (key = local j, packed shift; FP64
 // relative vector and distance) into the atom's segment; the rank sort that
-// follows puts them in canonical order.  The lanes advance through their
-// candidate streams in lockstep; candidates that pass the FP32 filter are
-// compacted into a shared-memory queue and evaluated in FP64 32 at a time,
-// so the FP64 work runs on full warps.  flag[1] is set when the FP64
-// decisions disagree with the count pass or with a certain-inside class.
+// follows puts them in canonical order.  Segments are either the exact CSR
+// segments of a count pass (cap = 0) or fixed slots [i cap, (i + 1) cap)
+// of a single pass (cap > 0), whose pair counts go to counts_out; a
+// single-pass atom with more than cap pairs sets flag[3] and keeps cap.
+// The lanes advance through their candidate streams in lockstep;
+// candidates that pass the FP32 filter are compacted into a shared-memory
+// queue and evaluated in FP64 32 at a time, so the FP64 work runs on full
+// warps.  flag[1] is set when the FP64 decisions disagree with the count
+// pass or with a certain-inside class.
 __global__ void __launch_bounds__(32 * kFillWarps)
 k_fill(int n, const int *__restrict__ atom_struct,
        const StrucGeom *__restrict__ geom, const double *__restrict__ wrapped,
        const float4 *__restrict__ w32, const int *__restrict__ raw,
        const int *__restrict__ bin_start, const int *__restrict__ bin_atoms,
-       double cutoff, const long long *__restrict__ offsets,
-       unsigned long long *__restrict__ key, double4_16a *__restrict__ rel,
-       int *__restrict__ flag) {
+       double cutoff, const long long *__restrict__ offsets, long long cap,
+       int *__restrict__ counts_out, unsigned long long *__restrict__ key,
+       double4_16a *__restrict__ rel, int *__restrict__ flag) {
   __shared__ int2 queue[kFillWarps][kQueue];
   const int wib = threadIdx.x >> 5;
   const int i = blockIdx.x * kFillWarps + wib;
@@ -290,13 +294,14 @@ k_fill(int n, const int *__restrict__ atom_struct,
                wi2 = wrapped[3 * i + 2];
   const float4 wi = w32[i];
   const int b0 = raw[3 * i], b1 = raw[3 * i + 1], b2 = raw[3 * i + 2];
-  const long long seg = offsets[i], seg_end = offsets[i + 1];
+  const long long seg = cap ? (long long)i * cap : offsets[i];
+  const long long seg_end = cap ? seg + cap : offsets[i + 1];
   const unsigned lt = (1u << lane) - 1u;
   LaneCursor c{lane, 0, 0, 0, 0, 0};
   cursor_seek(c, g, b0, b1, b2, bin_start);
   int queued = 0;            // warp-uniform
   long long written = 0;     // warp-uniform
-  bool bad = false;
+  bool bad = false, over = false;
   // evaluate queue entries [0, m) in FP64, one per lane, and write the pairs
   auto drain = [&](int m) {
     bool in = false, certain = false;
@@ -322,6 +327,8 @@ k_fill(int n, const int *__restrict__ atom_struct,
                  ((unsigned long long)(s1 + 128) << 8) |
                  (unsigned long long)(s2 + 128);
         rel[p] = make_double4_16a(d, x, y, z);
+      } else if (cap) {
+        over = true;
       } else {
         bad = true;
       }
@@ -377,15 +384,23 @@ k_fill(int n, const int *__restrict__ atom_struct,
     }
   }
   if (queued > 0) drain(queued);
-  if (seg + written != seg_end) bad = true;
+  if (cap) {
+    if (lane == 0) counts_out[i] = (int)(written < cap ? written : cap);
+    if (__any_sync(0xffffffffu, over) && lane == 0) atomicExch(flag + 3, 1);
+  } else if (seg + written != seg_end) {
+    bad = true;
+  }
   if (__any_sync(0xffffffffu, bad) && lane == 0) atomicExch(flag + 1, 1);
 }
 
 // Warp per atom: rank each key within the atom's segment (keys are unique),
-// scatter into canonical (j, s1, s2, s3) order.
+// scatter into canonical (j, s1, s2, s3) order at the atom's CSR segment.
+// The source segment is the CSR one (cap = 0) or the single pass's slots
+// from i cap (the CSR segment's length).
 __global__ void k_rank_scatter(int n, const int *__restrict__ atom_struct,
                                const StrucGeom *__restrict__ geom,
                                const long long *__restrict__ offsets,
+                               long long cap,
                                const unsigned long long *__restrict__ key,
                                const double4_16a *__restrict__ rel_in,
                                int *__restrict__ nbr_j,
@@ -394,12 +409,13 @@ __global__ void k_rank_scatter(int n, const int *__restrict__ atom_struct,
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= n) return;
-  long long b = offsets[warp], e = offsets[warp + 1];
+  const long long b = offsets[warp], e = offsets[warp + 1];
+  const long long sb = cap ? (long long)warp * cap : b, se = sb + (e - b);
   int atom0 = geom[atom_struct[warp]].atom0;
-  for (long long p = b + lane; p < e; p += 32) {
+  for (long long p = sb + lane; p < se; p += 32) {
     unsigned long long k = key[p];
     long long r = 0;
-    for (long long q = b; q < e; q++) r += key[q] < k ? 1 : 0;
+    for (long long q = sb; q < se; q++) r += key[q] < k ? 1 : 0;
     long long dst = b + r;
     nbr_j[dst] = atom0 + (int)(k >> 24);
     nbr_shift[dst] = (int)(k & 0xFFFFFFull);
@@ -575,6 +591,46 @@ extern "C" int fgb_nlist_build(fgb_nlist_t nl, int n_struc,
                      cutoff, (cudaStream_t)stream, true);
 }
 
+namespace fgb {
+
+// Slots per atom of a single-pass build: twice the expected neighbour
+// count of the densest structure (density x the cutoff sphere) plus 32, in
+// multiples of 32, and at least twice the slots of the last build that
+// overflowed; 0 (count pass) when that would take more than 2^26 slots.
+static long long single_pass_slots(const fgb_nlist_s *nl, double density,
+                                   double cutoff, int n_atoms) {
+  const double r = cutoff * (1.0 + 1e-9);
+  const double expect = density * (4.0 / 3.0) * 3.14159265358979324 * r * r * r;
+  const double c = 2.0 * expect + 32.0;
+  if (!(c < 65536.0)) return 0;
+  long long C = ((long long)std::ceil(c) + 31) / 32 * 32;
+  C = std::max(C, nl->min_slots);
+  return (long long)n_atoms * C > (1LL << 26) ? 0 : C;
+}
+
+int nlist_finish(fgb_nlist_s *nl, const int *hflag) {
+  if (hflag[0]) {
+    set_error("fgb_nlist_build: non-finite atomic positions");
+    return FGB_EINVAL;
+  }
+  if (nl->total_pending) {
+    nl->total_pending = false;
+    if (hflag[3]) {   // an atom had more pairs than its slots
+      nl->min_slots = 2 * nl->last_slots;
+      return kNlistRetry;
+    }
+    nl->n_pairs = *nl->h_total;
+  }
+  if (hflag[1] || hflag[2]) {
+    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
+              hflag[1], hflag[2]);
+    return FGB_ECUDA;
+  }
+  return FGB_OK;
+}
+
+}  // namespace fgb
+
 int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
                      const double *h_cells, const double *d_positions,
                      double cutoff, cudaStream_t st, bool check) {
@@ -608,6 +664,7 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
   std::vector<StrucGeom> geom(n_struc);
   std::vector<int> atom_struct(N);
   long long nbins = 0;
+  double dmax = 0.0;   // atoms per unit volume, densest structure
   for (int s = 0; s < n_struc; s++) {
     double sweep_cut;
     const double *c = h_cells + 9 * s;
@@ -629,6 +686,7 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
       return FGB_EINVAL;
     }
     nl->h_volume[s] = geom[s].volume;
+    dmax = std::max(dmax, geom[s].natoms / geom[s].volume);
     nbins += (long long)geom[s].nb[0] * geom[s].nb[1] * geom[s].nb[2];
     for (int a = h_atom_offsets[s]; a < h_atom_offsets[s + 1]; a++)
       atom_struct[a] = s;
@@ -663,6 +721,8 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
   const int T = 128;
   if (N == 0) {
     nl->n_pairs = 0;
+    nl->total_pending = false;
+    nl->last_launches = 0;
     FGB_CUDA(cudaMemsetAsync(nl->offsets.p, 0, sizeof(long long), st));
     return FGB_OK;
   }
@@ -681,19 +741,80 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
       nl->bin_start.as<int>(), nl->bin_atoms.as<int>());
   FGB_LAUNCH_CHECK("k_bin_fill");
   const long long NW = (long long)N * 32;   // warp per atom
+  nl->n_bins = nbins;
+  // offsets[N] receives the total pair count
+  long long *d_total = nl->offsets.as<long long>() + N;
+  int hflag[4];
+  // Single pass: every atom's pairs go to its own slots [i C, (i + 1) C),
+  // C about twice the densest structure's expected neighbour count, so no
+  // count pass and no synchronisation are needed; the CSR list is then
+  // gathered by the rank sort.  An atom with more than C pairs sets flag[3]
+  // and the list is rebuilt with a count pass (below when checking here,
+  // by the caller through nlist_finish otherwise), and later builds take
+  // at least 2 C slots.
+  const long long C = nl->count_pass ? 0 : single_pass_slots(nl, dmax, cutoff, N);
+  if (C > 0) {
+    const long long slots = (long long)N * C;
+    nl->last_slots = C;
+    if ((rc = nl->tmp_key.ensure(sizeof(unsigned long long) * (slots + 1))) ||
+        (rc = nl->tmp_rel.ensure(sizeof(double4_16a) * (slots + 1))) ||
+        (rc = nl->nbr_j.ensure(sizeof(int) * (slots + 1))) ||
+        (rc = nl->nbr_shift.ensure(sizeof(int) * (slots + 1))) ||
+        (rc = nl->nbr_rel.ensure(sizeof(double4_16a) * (slots + 1))) ||
+        (rc = nl->nbr_twin.ensure(sizeof(long long) * (slots + 1))))
+      return rc;
+    if (!nl->h_total) {
+      void *h = nullptr;
+      FGB_CUDA(cudaMallocHost(&h, sizeof(long long)));
+      nl->h_total = static_cast<long long *>(h);
+    }
+    k_fill<<<ceil_div(N, kFillWarps), 32 * kFillWarps, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
+        nl->raw_bin.as<int>(), nl->bin_start.as<int>(),
+        nl->bin_atoms.as<int>(), cutoff, nl->offsets.as<long long>(), C,
+        nl->counts.as<int>(), nl->tmp_key.as<unsigned long long>(),
+        nl->tmp_rel.as<double4_16a>(), nl->flag.as<int>());
+    FGB_LAUNCH_CHECK("k_fill");
+    if ((rc = scan_int_to_ll(nl->counts.as<int>(), nl->offsets.as<long long>(),
+                             N, d_total, nl->scan_tmp, st)))
+      return rc;
+    k_rank_scatter<<<ceil_div(NW, T), T, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->offsets.as<long long>(), C, nl->tmp_key.as<unsigned long long>(),
+        nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(),
+        nl->nbr_shift.as<int>(), nl->nbr_rel.as<double4_16a>());
+    FGB_LAUNCH_CHECK("k_rank_scatter");
+    k_twin<<<ceil_div(NW, T), T, 0, st>>>(
+        N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
+        nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
+        nl->nbr_shift.as<int>(), nl->nbr_twin.as<long long>(),
+        nl->flag.as<int>());
+    FGB_LAUNCH_CHECK("k_twin");
+    FGB_CUDA(cudaMemcpyAsync(nl->h_total, d_total, sizeof(long long),
+                             cudaMemcpyDeviceToHost, st));
+    nl->n_pairs = slots;   // an upper bound until nlist_finish reads the count
+    nl->total_pending = true;
+    nl->last_launches = 11;
+    if (!check) return FGB_OK;
+    FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
+                             cudaMemcpyDeviceToHost, st));
+    FGB_CUDA(cudaStreamSynchronize(st));
+    rc = nlist_finish(nl, hflag);
+    if (rc != kNlistRetry) return rc;
+    // too many pairs for the slots: the count pass, on the same bins
+    FGB_CUDA(cudaMemsetAsync(nl->flag.p, 0, sizeof(int) * 4, st));
+  }
   k_count<<<ceil_div(NW, T), T, 0, st>>>(
       N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
       nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
       nl->raw_bin.as<int>(), nl->bin_start.as<int>(),
       nl->bin_atoms.as<int>(), cutoff, nl->counts.as<int>());
   FGB_LAUNCH_CHECK("k_count");
-  // offsets[N] receives the total pair count
-  long long *d_total = nl->offsets.as<long long>() + N;
   if ((rc = scan_int_to_ll(nl->counts.as<int>(), nl->offsets.as<long long>(), N,
                            d_total, nl->scan_tmp, st)))
     return rc;
   long long P = 0;
-  int hflag[4];
   FGB_CUDA(cudaMemcpyAsync(&P, d_total, sizeof(long long),
                            cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
@@ -704,7 +825,10 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
     return FGB_EINVAL;
   }
   nl->n_pairs = P;
-  nl->n_bins = nbins;
+  nl->total_pending = false;
+  // wrap, bin scan (3), bin fill, count, pair scan (3), then fill, rank and
+  // twin when there are pairs; after an overflowed single pass its 6 more
+  nl->last_launches = 9 + (P > 0 ? 3 : 0) + (C > 0 ? 6 : 0);
   if ((rc = nl->tmp_key.ensure(sizeof(unsigned long long) * (P + 1))) ||
       (rc = nl->tmp_rel.ensure(sizeof(double4_16a) * (P + 1))) ||
       (rc = nl->nbr_j.ensure(sizeof(int) * (P + 1))) ||
@@ -718,12 +842,13 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
         nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
         nl->raw_bin.as<int>(),
         nl->bin_start.as<int>(), nl->bin_atoms.as<int>(), cutoff,
-        nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
-        nl->tmp_rel.as<double4_16a>(), nl->flag.as<int>());
+        nl->offsets.as<long long>(), 0LL, nullptr,
+        nl->tmp_key.as<unsigned long long>(), nl->tmp_rel.as<double4_16a>(),
+        nl->flag.as<int>());
     FGB_LAUNCH_CHECK("k_fill");
     k_rank_scatter<<<ceil_div((long long)N * 32, T), T, 0, st>>>(
         N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
-        nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
+        nl->offsets.as<long long>(), 0LL, nl->tmp_key.as<unsigned long long>(),
         nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(), nl->nbr_shift.as<int>(),
         nl->nbr_rel.as<double4_16a>());
     FGB_LAUNCH_CHECK("k_rank_scatter");
@@ -738,12 +863,7 @@ int fgb::nlist_build(fgb_nlist_s *nl, int n_struc, const int *h_atom_offsets,
   FGB_CUDA(cudaMemcpyAsync(hflag, nl->flag.p, sizeof(int) * 4,
                            cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
-  if (hflag[1] || hflag[2]) {
-    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
-              hflag[1], hflag[2]);
-    return FGB_ECUDA;
-  }
-  return FGB_OK;
+  return nlist_finish(nl, hflag);
 }
 
 namespace fgb {
@@ -768,6 +888,7 @@ int nlist_rebuild_fixed(fgb_nlist_s *nl, const double *d_positions,
   int rc;
   FGB_CUDA(cudaMemsetAsync(nl->bin_count.p, 0, sizeof(int) * (nbins + 1), st));
   FGB_CUDA(cudaMemsetAsync(nl->flag.p, 0, sizeof(int) * 4, st));
+  nl->last_launches = 0;
   if (N == 0) return FGB_OK;
   k_wrap_bin<<<ceil_div(N, T), T, 0, st>>>(
       N, d_positions, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
@@ -801,13 +922,13 @@ int nlist_rebuild_fixed(fgb_nlist_s *nl, const double *d_positions,
       N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
       nl->wrapped.as<double>(), nl->wrapped32.as<float4>(),
       nl->raw_bin.as<int>(), nl->bin_start.as<int>(), nl->bin_atoms.as<int>(),
-      cutoff, nl->offsets.as<long long>(),
+      cutoff, nl->offsets.as<long long>(), 0LL, nullptr,
       nl->tmp_key.as<unsigned long long>(), nl->tmp_rel.as<double4_16a>(),
       nl->flag.as<int>());
   FGB_LAUNCH_CHECK("k_fill");
   k_rank_scatter<<<ceil_div(NW, T), T, 0, st>>>(
       N, nl->atom_struct.as<int>(), nl->geom.as<StrucGeom>(),
-      nl->offsets.as<long long>(), nl->tmp_key.as<unsigned long long>(),
+      nl->offsets.as<long long>(), 0LL, nl->tmp_key.as<unsigned long long>(),
       nl->tmp_rel.as<double4_16a>(), nl->nbr_j.as<int>(),
       nl->nbr_shift.as<int>(), nl->nbr_rel.as<double4_16a>());
   FGB_LAUNCH_CHECK("k_rank_scatter");
@@ -818,6 +939,7 @@ int nlist_rebuild_fixed(fgb_nlist_s *nl, const double *d_positions,
       nl->flag.as<int>());
   FGB_LAUNCH_CHECK("k_twin");
   nl->n_pairs = cap;   // an upper bound; the device offsets hold the count
+  nl->last_launches = 13;
   return FGB_OK;
 }
 
@@ -1040,10 +1162,12 @@ extern "C" int fgb_nlist_build_noalloc(const double *h_cell,
   double4_16a *nbr_rel = (double4_16a *)take(sizeof(double4_16a) * (P + 1));
   k_fill<<<ceil_div(N, kFillWarps), 32 * kFillWarps, 0, st>>>(N, atom_struct, d_geom, wrapped, w32,
                                         raw, bin_start, bin_atoms, cutoff,
-                                        offsets, key, tmp_rel, flag);
+                                        offsets, 0LL, nullptr, key, tmp_rel,
+                                        flag);
   FGB_LAUNCH_CHECK("k_fill");
   k_rank_scatter<<<ceil_div((long long)N * 32, T), T, 0, st>>>(
-      N, atom_struct, d_geom, offsets, key, tmp_rel, nbr_j, nbr_shift, nbr_rel);
+      N, atom_struct, d_geom, offsets, 0LL, key, tmp_rel, nbr_j, nbr_shift,
+      nbr_rel);
   FGB_LAUNCH_CHECK("k_rank_scatter");
   k_export<<<ceil_div(N, T), T, 0, st>>>(N, offsets, atom_struct, d_geom, nbr_j,
                                          nbr_shift, nbr_rel, d_neighbor_count,

@@ -568,11 +568,12 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     return FGB_EINVAL;
   }
   {
-    StageTimer _pt(kStNeighbors, st, 11);
+    StageTimer _pt(kStNeighbors, st);
     rc = fixed ? nlist_rebuild_fixed(&m->nl, d_positions, cutoff,
                                      fixed->pair_cap, st)
                : nlist_build(&m->nl, n_struc, h_atom_offsets, h_cells,
                              d_positions, cutoff, st, false);
+    _pt.set_launches(m->nl.last_launches);
     if (rc) return rc;
   }
   const B2Params &p = m->b2;
@@ -703,11 +704,18 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     FGB_CUDA(cudaMemcpyAsync(h + 4, m->ws.ozerr.p, sizeof(int),
                              cudaMemcpyDeviceToHost, st));
   FGB_CUDA(cudaStreamSynchronize(st));
-  if (h[1] || h[2]) {
-    set_error("fgb_nlist_build: internal consistency check failed (%d %d)",
-              h[1], h[2]);
-    return FGB_ECUDA;
+  rc = nlist_finish(&m->nl, h);
+  if (rc == kNlistRetry) {
+    // an atom had more pairs than its single-pass slots: the whole call
+    // again, its list built with a count pass
+    m->nl.count_pass = true;
+    rc = predict_impl(m, n_struc, h_atom_offsets, h_cells, d_positions,
+                      d_species, cutoff, want, precision, d_energy, d_forces,
+                      d_stress, d_local_var, st, nullptr);
+    m->nl.count_pass = false;
+    return rc;
   }
+  if (rc) return rc;
   if (h[4]) {
     set_error("tensor-core stage: a bounded device wait ran out");
     return FGB_ETIMEOUT;

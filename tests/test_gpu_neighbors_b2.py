@@ -35,7 +35,17 @@ def cases():
         p[0] = [-1e-18, 0.5 * c[1, 1], -1e-17]
         p[1] = [0.25 * c[0, 0], -3e-18, 0.5 * c[2, 2]]
         out.append((name, c, s, p, 5.0))
+    out.append(("cluster_in_vacuum", *dense_cluster(), 5.0))
     return out
+
+
+def dense_cluster(seed=13):
+    """120 atoms at 0.2 atoms/A^3 in the middle of a 40 A cell: about 100
+    neighbours per atom where the cell's mean density suggests one, so a
+    single-pass build overflows its per-atom slots and the list is built
+    again with a count pass."""
+    c, s, p = syn.random_alloy(120, density=0.2, dmin=1.2, seed=seed)
+    return np.eye(3) * 40.0, s, p + 16.0
 
 
 @pytest.mark.parametrize("case", cases(), ids=lambda c: c[0])
@@ -138,3 +148,26 @@ def test_b2_stored_gradients_match_oracle():
                                    ov.descriptor_force_dots[0]).max())
     np.testing.assert_allclose(B2.cpu().numpy(), ov.atom_B2, rtol=1e-11,
                                atol=1e-12 * np.abs(ov.atom_B2).max())
+
+
+def test_prediction_after_slot_overflow():
+    """The prediction path builds its list without a count pass; on the
+    dense cluster an atom overflows its slots, the call is repeated with a
+    count pass, and energy, forces and stress match the oracle."""
+    import flare_gb300 as fg
+    from helpers import small_two_species, to_gpu_sgp
+    ogp, b2a = small_two_species(seed=4)
+    ggp, calc = to_gpu_sgp(ogp, b2a)
+    cell, sp, pos = dense_cluster()
+    o = oracle.Structure(cell, sp, pos, 5.0, [oracle.B2Settings(*b2a)])
+    ogp.predict_mean(o)
+    m = o.mean_efs
+    E, F, S = m[0], m[1:-6].reshape(-1, 3), m[-6:]
+    for _ in range(2):   # the second call starts from the doubled slots
+        r = ggp.predict_batch([fg.Structure(cell, sp, pos, 5.0, [calc])],
+                              precision="fp64")
+        assert abs(r["energy"][0] - E) <= 1e-9 * max(1.0, abs(E))
+        np.testing.assert_allclose(r["forces"], F, rtol=0,
+                                   atol=1e-8 * max(1.0, np.abs(F).max()))
+        np.testing.assert_allclose(r["stress"][0], S, rtol=0,
+                                   atol=1e-10 * max(1.0, np.abs(S).max()))
