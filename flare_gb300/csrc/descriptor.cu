@@ -291,11 +291,15 @@ __device__ __forceinline__ double as_compute(double x, double) { return x; }
 __device__ __forceinline__ float as_compute(double x, float) {
   return trunc_float(x);
 }
+// Pair gradients in the adjoint's compute type: the FP32 adjoint writes
+// float3 (half the bytes, and the force sums then run in FP32).
+template <typename T> struct PairGrad { using type = double3; };
+template <> struct PairGrad<float> { using type = float3; };
 __device__ __forceinline__ double3 pair_out(double x, double y, double z) {
   return make_double3(x, y, z);
 }
-__device__ __forceinline__ double3 pair_out(float x, float y, float z) {
-  return make_double3(f2d_exact(x), f2d_exact(y), f2d_exact(z));
+__device__ __forceinline__ float3 pair_out(float x, float y, float z) {
+  return make_float3(x, y, z);
 }
 
 // Atoms per block of the adjoint and its block size: ~42 pairs per atom,
@@ -313,7 +317,8 @@ __global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 8 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
-             const T *__restrict__ gB2, double3 *__restrict__ pair_grad,
+             const T *__restrict__ gB2,
+             typename PairGrad<T>::type *__restrict__ pair_grad,
              int w_in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *smem = reinterpret_cast<T *>(smem_raw);
@@ -377,40 +382,36 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     double4_16a r = rel[pp];
     int sj = species[j];
     double rc = p.cutoffs[si * kMaxSpecies + sj];
-    double3 out = make_double3(0.0, 0.0, 0.0);
+    typename PairGrad<T>::type out = pair_out(T(0), T(0), T(0));
     if (r.x <= rc) {
-      // dE/dr = sum_{n,lm} u[n][lm] (dg_n/dr e Y_lm + g_n dY_lm/dr), the
-      // harmonics contracted as the recurrence produces them
+      // dE/dr = sum_{n,lm} u[n][lm] (dg_n/dr e Y_lm + g_n dY_lm/dr)
+      //       = e sum_lm d_lm Y_lm + sum_lm c_lm dY_lm/dr, with
+      // c_lm = sum_n u[n][lm] g_n and d_lm = sum_n u[n][lm] dg_n/dr formed
+      // as the recurrence produces each harmonic (20 multiply-adds per
+      // harmonic instead of 4 n_max)
       T g[NA], dg[NA];
       const T rx = as_compute(r.x, T(0)), ry = as_compute(r.y, T(0)),
               rz = as_compute(r.z, T(0)), rw = as_compute(r.w, T(0));
       radial_eval<T, NC>(p, rx, as_compute(rc, T(0)), g, dg);
       const T *us = u + sj * nm * nh;
-      T t1[NA], tx[NA], ty[NA], tz[NA];
-#pragma unroll
-      for (int n = 0; n < nm; n++) { t1[n] = tx[n] = ty[n] = tz[n] = T(0); }
+      T orad = T(0), ox = T(0), oy = T(0), oz = T(0);
       ylm_visit<T, LC, true>(p.l_max, ry, rz, rw,
                              [&](int idx, T v, T gx, T gy, T gz) {
+        T c = T(0), d = T(0);
 #pragma unroll
         for (int n = 0; n < nm; n++) {
           const T uv = us[n * nh + idx];
-          t1[n] += uv * v;
-          tx[n] += uv * gx;
-          ty[n] += uv * gy;
-          tz[n] += uv * gz;
+          c += uv * g[n];
+          d += uv * dg[n];
         }
+        orad += d * v;
+        ox += c * gx;
+        oy += c * gy;
+        oz += c * gz;
       });
       const T ir = T(1) / rx;
-      const T ex = ry * ir, ey = rz * ir, ez = rw * ir;
-      T ox = T(0), oy = T(0), oz = T(0);
-#pragma unroll
-      for (int n = 0; n < nm; n++) {
-        const T dgr = dg[n];
-        ox += dgr * ex * t1[n] + g[n] * tx[n];
-        oy += dgr * ey * t1[n] + g[n] * ty[n];
-        oz += dgr * ez * t1[n] + g[n] * tz[n];
-      }
-      out = pair_out(ox, oy, oz);
+      out = pair_out(orad * (ry * ir) + ox, orad * (rz * ir) + oy,
+                     orad * (rw * ir) + oz);
     }
     pair_grad[pp] = out;
   }
@@ -418,32 +419,53 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
 
 // F_i = sum_{p in out(i)} (g_p - g_twin(p)); per-atom virial partials
 // v_i[ab] = sum_{p in out(i)} g_p,a r_p,b (flare order xx xy xz yy yz zz).
+// kForceLanes lanes per atom take its pairs lane, lane + kForceLanes, ...
+// (enough threads to hide the dependent twin loads), then a fixed-order
+// butterfly over those lanes sums them (each level is 9 FP64 additions per
+// lane, so the group stays small: FP64 is scarce on this GPU).
+// Sums in the pair gradients' type (FP32 after the FP32 adjoint).
+constexpr int kForceLanes = 4;
+template <typename T>
 __global__ void k_forces(int n_atoms, const long long *__restrict__ offsets,
                          const long long *__restrict__ twin,
                          const double4_16a *__restrict__ rel,
-                         const double3 *__restrict__ pg,
+                         const typename PairGrad<T>::type *__restrict__ pg,
                          double *__restrict__ forces,
                          double *__restrict__ virial) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = (int)(gt % kForceLanes);
+  // whole groups of kForceLanes lanes leave together (n_atoms is uniform)
+  const int i = (int)(gt / kForceLanes);
   if (i >= n_atoms) return;
-  double fx = 0, fy = 0, fz = 0;
-  double v[6] = {0, 0, 0, 0, 0, 0};
-  for (long long q = offsets[i]; q < offsets[i + 1]; q++) {
-    double3 g = pg[q];
-    long long tw = twin[q];
-    double3 h = tw >= 0 ? pg[tw] : make_double3(0, 0, 0);
-    fx += g.x - h.x;
-    fy += g.y - h.y;
-    fz += g.z - h.z;
-    double4_16a r = rel[q];
-    v[0] += g.x * r.y; v[1] += g.x * r.z; v[2] += g.x * r.w;
-    v[3] += g.y * r.z; v[4] += g.y * r.w; v[5] += g.z * r.w;
+  T a[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+  const long long e = offsets[i + 1];   // a: F (3), virial (6)
+  for (long long q = offsets[i] + lane; q < e; q += kForceLanes) {
+    const auto g = pg[q];
+    const long long tw = twin[q];
+    const auto h = tw >= 0 ? pg[tw] : pair_out(T(0), T(0), T(0));
+    a[0] += g.x - h.x;
+    a[1] += g.y - h.y;
+    a[2] += g.z - h.z;
+    const double4_16a r = rel[q];
+    const T ry = as_compute(r.y, T(0)), rz = as_compute(r.z, T(0)),
+            rw = as_compute(r.w, T(0));
+    a[3] += g.x * ry; a[4] += g.x * rz; a[5] += g.x * rw;
+    a[6] += g.y * rz; a[7] += g.y * rw; a[8] += g.z * rw;
   }
-  if (forces) {
-    forces[3 * i] = fx; forces[3 * i + 1] = fy; forces[3 * i + 2] = fz;
+  // the group's lanes are consecutive lanes of one warp; groups past
+  // n_atoms returned as a whole, so the mask names the live lanes
+  const unsigned gmask = ((1u << kForceLanes) - 1u)
+                         << ((threadIdx.x & 31) & ~(kForceLanes - 1));
+#pragma unroll
+  for (int off = kForceLanes / 2; off > 0; off >>= 1)
+#pragma unroll
+    for (int k = 0; k < 9; k++) a[k] += __shfl_xor_sync(gmask, a[k], off);
+  if (lane == 0) {
+    if (forces)
+      for (int k = 0; k < 3; k++) forces[3 * i + k] = (double)a[k];
+    if (virial)
+      for (int k = 0; k < 6; k++) virial[6 * i + k] = (double)a[3 + k];
   }
-  if (virial)
-    for (int k = 0; k < 6; k++) virial[6 * i + k] = v[k];
 }
 
 // Per-structure energy and stress: fixed-order tree sums over the
@@ -557,7 +579,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
 
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
-                      const void *d_gB2, double3 *d_pair_grad,
+                      const void *d_gB2, void *d_pair_grad,
                       cudaStream_t st, bool fp32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
@@ -581,7 +603,8 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
     fn<<<ceil_div(N, kAdjAtoms), kAdjThreads, sm, st>>>(
         p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
         nl->nbr_rel.as<double4_16a>(), d_species, d_A,
-        static_cast<const G *>(d_gB2), d_pair_grad, w_in_smem);
+        static_cast<const G *>(d_gB2),
+        static_cast<typename PairGrad<G>::type *>(d_pair_grad), w_in_smem);
   };
   if (fp32) dispatch_nl<AdjK, float>(p, go);
   else dispatch_nl<AdjK, double>(p, go);
@@ -590,13 +613,21 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
   return FGB_OK;
 }
 
-int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
+int launch_forces(const fgb_nlist_s *nl, const void *d_pair_grad, bool fp32,
                   double *d_forces, double *d_virial, cudaStream_t st) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
-  k_forces<<<ceil_div(N, 128), 128, 0, st>>>(
-      N, nl->offsets.as<long long>(), nl->nbr_twin.as<long long>(),
-      nl->nbr_rel.as<double4_16a>(), d_pair_grad, d_forces, d_virial);
+  const unsigned nb = (unsigned)ceil_div((long long)N * kForceLanes, 256);
+  if (fp32)
+    k_forces<float><<<nb, 256, 0, st>>>(
+        N, nl->offsets.as<long long>(), nl->nbr_twin.as<long long>(),
+        nl->nbr_rel.as<double4_16a>(), static_cast<const float3 *>(d_pair_grad),
+        d_forces, d_virial);
+  else
+    k_forces<double><<<nb, 256, 0, st>>>(
+        N, nl->offsets.as<long long>(), nl->nbr_twin.as<long long>(),
+        nl->nbr_rel.as<double4_16a>(),
+        static_cast<const double3 *>(d_pair_grad), d_forces, d_virial);
   FGB_LAUNCH_CHECK("k_forces");
   return FGB_OK;
 }

@@ -12,13 +12,14 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
                       double *d_norms, cudaStream_t st, bool dfloat = false,
                       double *d_rowmax = nullptr);
-// d_gB2: dE/dB2 rows [N, n_d] in the compute type (float when fp32, else
-// double)
+// d_gB2: dE/dB2 rows [N, n_d] and d_pair_grad: pair gradients [P], both in
+// the compute type (float / float3 when fp32, else double / double3)
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
-                      const void *d_gB2, double3 *d_pair_grad,
+                      const void *d_gB2, void *d_pair_grad,
                       cudaStream_t st, bool fp32 = false);
-int launch_forces(const fgb_nlist_s *nl, const double3 *d_pair_grad,
+// d_pair_grad as the adjoint wrote it (fp32: float3)
+int launch_forces(const fgb_nlist_s *nl, const void *d_pair_grad, bool fp32,
                   double *d_forces, double *d_virial, cudaStream_t st);
 int launch_struct_reduce(int n_struc, const int *d_atom_off,
                          const double *d_volume, const double *d_e_atom,

@@ -364,9 +364,8 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
   }
   if (want_grad) {
     if ((rc = launch_b2_adjoint(p, &m->nl, d_species, ws.A.as<double>(),
-                                ws.gB2.p, ws.pair_grad.as<double3>(), st,
-                                adj32)) ||
-        (rc = launch_forces(&m->nl, ws.pair_grad.as<double3>(),
+                                ws.gB2.p, ws.pair_grad.p, st, adj32)) ||
+        (rc = launch_forces(&m->nl, ws.pair_grad.p, adj32,
                             ws.forces.as<double>(), ws.virial.as<double>(),
                             st)))
       return rc;

@@ -198,28 +198,93 @@ __global__ void k_kt_alpha(int M, long long ncol, const double *__restrict__ KT,
   out[o] = acc;
 }
 
-__global__ void k_species_flags(int n, const int *__restrict__ species, int s,
-                                int *__restrict__ flags) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) flags[i] = species[i] == s ? 1 : 0;
-}
-
-// totals[q] = atoms of species q < s (already counted on the stream)
-__global__ void k_species_scatter(int n, const int *__restrict__ species, int s,
-                                  const int *__restrict__ pos,
-                                  const int *__restrict__ totals,
-                                  int *__restrict__ perm) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || species[i] != s) return;
-  int base = 0;
-  for (int q = 0; q < s; q++) base += totals[q];
-  perm[base + pos[i]] = i;
-}
-
 __global__ void k_check_species(int n, const int *__restrict__ species, int ns,
                                 int *__restrict__ flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && (species[i] < 0 || species[i] >= ns)) atomicExch(flag, 1);
+}
+
+// Species permutation as a counting sort over blocks of kPermBlock atoms
+// (n_species <= kMaxSpecies): per-block histograms, one block of offsets,
+// then a stable scatter (atoms of a species keep their index order).
+constexpr int kPermBlock = 1024;
+
+// hist[s * nb + b] = atoms of species s in block b; flag: a species out of
+// [0, ns)
+__global__ void __launch_bounds__(kPermBlock)
+k_species_hist(int n, const int *__restrict__ species, int ns,
+               int *__restrict__ hist, int *__restrict__ flag) {
+  __shared__ int cnt[kMaxSpecies];
+  const int t = threadIdx.x, b = blockIdx.x, nb = gridDim.x;
+  if (t < kMaxSpecies) cnt[t] = 0;
+  __syncthreads();
+  const int i = b * kPermBlock + t;
+  if (i < n) {
+    const int sp = species[i];
+    if (sp < 0 || sp >= ns) atomicExch(flag, 1);
+    else atomicAdd(&cnt[sp], 1);
+  }
+  __syncthreads();
+  if (t < ns) hist[t * nb + b] = cnt[t];
+}
+
+// In place: hist becomes the exclusive prefix over (species, block) in
+// species-major order, i.e. the first perm slot of each (species, block);
+// totals[s] = atoms of species s.  One block; each thread scans a
+// contiguous run, then the runs' sums are scanned.
+__global__ void __launch_bounds__(kPermBlock)
+k_species_offsets(int nb, int ns, int *__restrict__ hist,
+                  int *__restrict__ totals) {
+  __shared__ int run[kPermBlock];
+  __shared__ int grand;
+  const int t = threadIdx.x, L = ns * nb;
+  const int per = (L + kPermBlock - 1) / kPermBlock;
+  const int lo = min(L, t * per), hi = min(L, lo + per);
+  int sum = 0;
+  for (int k = lo; k < hi; k++) sum += hist[k];
+  run[t] = sum;
+  __syncthreads();
+  if (t == 0) {
+    int acc = 0;
+    for (int k = 0; k < kPermBlock; k++) {
+      const int v = run[k];
+      run[k] = acc;
+      acc += v;
+    }
+    grand = acc;
+  }
+  __syncthreads();
+  int acc = run[t];
+  for (int k = lo; k < hi; k++) {
+    const int v = hist[k];
+    hist[k] = acc;
+    acc += v;
+  }
+  __syncthreads();
+  if (t < ns) totals[t] = (t + 1 < ns ? hist[(t + 1) * nb] : grand) - hist[t * nb];
+}
+
+// perm[first(s, b) + rank of atom i among block b's species-s atoms] = i
+__global__ void __launch_bounds__(kPermBlock)
+k_species_scatter(int n, const int *__restrict__ species, int ns,
+                  const int *__restrict__ first, int *__restrict__ perm) {
+  __shared__ int wc[kPermBlock / 32][kMaxSpecies];   // per-warp counts
+  const int t = threadIdx.x, b = blockIdx.x, nb = gridDim.x;
+  const int w = t >> 5, lane = t & 31;
+  const int i = b * kPermBlock + t;
+  int sp = i < n ? species[i] : -1;
+  if (sp >= ns) sp = -1;
+  const unsigned same = __match_any_sync(0xffffffffu, sp);
+  const int rank = __popc(same & ((1u << lane) - 1u));
+  if (lane < kMaxSpecies) wc[w][lane] = 0;
+  __syncwarp();
+  if (sp >= 0 && rank == 0) wc[w][sp] = __popc(same);
+  __syncthreads();
+  if (sp >= 0) {
+    int before = 0;
+    for (int q = 0; q < w; q++) before += wc[q][sp];
+    perm[first[sp * nb + b] + before + rank] = i;
+  }
 }
 
 }  // namespace
@@ -284,28 +349,27 @@ int species_permutation(fgb_model_s *m, const int *d_species, int N,
 int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st) {
   counts.assign(S, 0);
+  if (S < 1 || S > kMaxSpecies) {
+    set_error("species permutation: %d species (at most %d)", S, kMaxSpecies);
+    return FGB_EINVAL;
+  }
+  const int nb = ceil_div(std::max(N, 1), kPermBlock);
   int rc;
   if ((rc = ws.perm.ensure(sizeof(int) * (N + 1))) ||
-      (rc = ws.flags.ensure(sizeof(int) * (N + 1))) ||
-      (rc = ws.pos.ensure(sizeof(int) * (N + 1))) ||
+      (rc = ws.flags.ensure(sizeof(int) * ((size_t)S * nb + 1))) ||
       (rc = ws.scal.ensure(sizeof(int) * (S + 2))))
     return rc;
   if (N == 0) return FGB_OK;
   int *tot = ws.scal.as<int>();   // [0, S): counts; [S]: range flag
+  int *hist = ws.flags.as<int>();
   FGB_CUDA(cudaMemsetAsync(tot + S, 0, sizeof(int), st));
-  k_check_species<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, S, tot + S);
-  FGB_LAUNCH_CHECK("k_check_species");
-  for (int s = 0; s < S; s++) {
-    k_species_flags<<<ceil_div(N, 256), 256, 0, st>>>(N, d_species, s,
-                                                      ws.flags.as<int>());
-    FGB_LAUNCH_CHECK("k_species_flags");
-    if ((rc = scan_int_to_int(ws.flags.as<int>(), ws.pos.as<int>(), N,
-                              tot + s, ws.scan_tmp, st)))
-      return rc;
-    k_species_scatter<<<ceil_div(N, 256), 256, 0, st>>>(
-        N, d_species, s, ws.pos.as<int>(), tot, ws.perm.as<int>());
-    FGB_LAUNCH_CHECK("k_species_scatter");
-  }
+  k_species_hist<<<nb, kPermBlock, 0, st>>>(N, d_species, S, hist, tot + S);
+  FGB_LAUNCH_CHECK("k_species_hist");
+  k_species_offsets<<<1, kPermBlock, 0, st>>>(nb, S, hist, tot);
+  FGB_LAUNCH_CHECK("k_species_offsets");
+  k_species_scatter<<<nb, kPermBlock, 0, st>>>(N, d_species, S, hist,
+                                               ws.perm.as<int>());
+  FGB_LAUNCH_CHECK("k_species_scatter");
   std::vector<int> h(S + 1);
   FGB_CUDA(cudaMemcpyAsync(h.data(), tot, sizeof(int) * (S + 1),
                            cudaMemcpyDeviceToHost, st));
@@ -632,7 +696,7 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (fixed) {
     counts = fixed->counts;
   } else {
-    StageTimer _pt(kStSpeciesPerm, st, 2 + 5 * p.n_species);
+    StageTimer _pt(kStSpeciesPerm, st, 3);
     if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
     m->last_species_counts = counts;
   }
@@ -660,21 +724,21 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       return rc;
   }
   if (want_grad) {
+    // FP32 adjoint (and FP32 pair gradients and force sums) in the mixed
+    // path (dE/dB2 written in FP32 by the mapped gradient), unless the fold
+    // guard asked for FP64-level forces or the power has no folded form
+    // (FP64 kernel stage)
+    const bool adj32 = mixed && !m->force_f64 &&
+                       (m->power == 2.0 || m->power == 1.0);
     {
       StageTimer _pt(kStB2Adjoint, st);
-      // FP32 adjoint in the mixed path (dE/dB2 written in FP32 by the
-      // mapped gradient), unless the fold guard asked for FP64-level forces
-      // or the power has no folded form (FP64 kernel stage)
-      const bool adj32 = mixed && !m->force_f64 &&
-                         (m->power == 2.0 || m->power == 1.0);
       if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
-                                  m->ws.gB2.p, m->ws.pair_grad.as<double3>(),
-                                  st, adj32)))
+                                  m->ws.gB2.p, m->ws.pair_grad.p, st, adj32)))
         return rc;
     }
     {
       StageTimer _pt(kStForces, st);
-      if ((rc = launch_forces(&m->nl, m->ws.pair_grad.as<double3>(),
+      if ((rc = launch_forces(&m->nl, m->ws.pair_grad.p, adj32,
                               m->ws.forces.as<double>(),
                               m->ws.virial.as<double>(), st)))
         return rc;
