@@ -12,6 +12,8 @@
 // -> per pair dE/dr_ij = sum_{n,lm} u[s_j][n][lm] d(g_n Y_lm)/dr_ij, with g
 // and Y recomputed instead of stored.  Forces and the virial are assembled by
 // owner-computes over each atom's pairs and their twins (no float atomics).
+#include <type_traits>
+
 #include "fgb_df.cuh"
 #include "fgb_internal.h"
 #include "fgb_kernels.h"
@@ -304,7 +306,68 @@ __device__ __forceinline__ float3 pair_out(float x, float y, float z) {
 
 // Atoms per block of the adjoint and its block size: ~42 pairs per atom,
 // so three atoms' pairs fill the 128 threads of the pair loop.
+// The 2l + 1 entries u[c][l^2 .. l^2 + 2l] (M = 2l + 1 at compile time),
+// each summed over b in the order of the thread-per-entry form.
+template <typename T, int M>
+__device__ __forceinline__ void u_entries(const T *A, const T *wsrc, int nh,
+                                          int nr, int L1, int c, int l, T *u,
+                                          int nm, int cs, int cn) {
+  const T *wl = wsrc + l;
+  const T *Al = A + l * l;
+  T acc[M];
+#pragma unroll
+  for (int m = 0; m < M; m++) acc[m] = T(0);
+  int pidx = c;   // radial pair (0, c)
+  for (int bb = 0; bb < c; bb++) {
+    const T w = wl[pidx * L1];
+#pragma unroll
+    for (int m = 0; m < M; m++) acc[m] += w * Al[bb * nh + m];
+    pidx += nr - bb - 1;
+  }
+  {   // pidx is now the pair (c, c)
+    const T w = T(2) * wl[pidx * L1];
+#pragma unroll
+    for (int m = 0; m < M; m++) acc[m] += w * Al[c * nh + m];
+  }
+  for (int bb = c + 1; bb < nr; bb++) {
+    pidx++;
+    const T w = wl[pidx * L1];
+#pragma unroll
+    for (int m = 0; m < M; m++) acc[m] += w * Al[bb * nh + m];
+  }
+#pragma unroll
+  for (int m = 0; m < M; m++) u[(cs * nh + l * l + m) * nm + cn] = acc[m];
+}
+
+// The same for any l (run-time entry count).
+template <typename T>
+__device__ void u_entries_any(const T *A, const T *wsrc, int nh, int nr,
+                              int L1, int c, int l, T *u, int nm, int cs,
+                              int cn) {
+  const T *wl = wsrc + l;
+  for (int m = 0; m < 2 * l + 1; m++) {
+    const T *Acol = A + l * l + m;
+    T acc = T(0);
+    int pidx = c;
+    for (int bb = 0; bb < c; bb++) {
+      acc += wl[pidx * L1] * Acol[bb * nh];
+      pidx += nr - bb - 1;
+    }
+    acc += T(2) * wl[pidx * L1] * Acol[c * nh];
+    for (int bb = c + 1; bb < nr; bb++) {
+      pidx++;
+      acc += wl[pidx * L1] * Acol[bb * nh];
+    }
+    u[(cs * nh + l * l + m) * nm + cn] = acc;
+  }
+}
+
 constexpr int kAdjAtoms = 3;
+// Shared-memory values per atom of the adjoint: u and A (n_A each) and
+// optionally the dE/dB2 row, rounded up to whole groups of 4.
+__host__ __device__ constexpr int adj_atom_values(int nA, int nd_in_smem) {
+  return (2 * nA + nd_in_smem + 3) / 4 * 4;
+}
 constexpr int kAdjThreads = 128;
 
 // Shared memory, per atom of the block: u[nA] | A[nA] | w[nd] (the atom's
@@ -330,7 +393,8 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   const int nm = NC > 0 ? NC : p.n_max;
   const int nA = p.n_species * nm * nh, nr = p.n_species * nm,
             L1 = (LC > 0 ? LC : p.l_max) + 1, nd = p.n_d;
-  const int per = 2 * nA + (w_in_smem ? nd : 0);   // T values per atom
+  // T values per atom, in whole 4-value groups (16-byte aligned u rows)
+  const int per = adj_atom_values(nA, w_in_smem ? nd : 0);
   const int t = threadIdx.x;
   for (int a = 0; a < na; a++) {
     T *A = smem + (size_t)a * per + nA;
@@ -343,33 +407,58 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
         W[q] = gB2[i * nd + q];
   }
   __syncthreads();
-  // u = dE/dA: u[c][lm] = sum_b (1 + [b == c]) w((c,b), l) A[b][lm], a
-  // thread per (atom, entry), b ascending.  The B2 index of the radial
-  // pair (min(b,c), max(b,c)) advances by nr - b - 1 while b < c and by 1
-  // after it, so the loop carries it instead of recomputing it.
-  for (int it = t; it < na * nA; it += blockDim.x) {
-    const int a = it / nA, e = it - a * nA;
-    const T *A = smem + (size_t)a * per + nA;
-    T *u = smem + (size_t)a * per;
-    const T *wsrc = w_in_smem ? A + nA : gB2 + (long long)(i0 + a) * nd;
-    const int c = e / nh, lm = e - c * nh;
-    int l = 0;
-    while ((l + 1) * (l + 1) <= lm) l++;
-    const T *Acol = A + lm;
-    const T *wl = wsrc + l;
-    T acc = T(0);
-    int pidx = c;   // radial pair (0, c)
-    for (int bb = 0; bb < c; bb++) {
-      acc += wl[pidx * L1] * Acol[bb * nh];
-      pidx += nr - bb - 1;
+  // u = dE/dA: u[c][lm] = sum_b (1 + [b == c]) w((c,b), l) A[b][lm], b
+  // ascending, stored as u[s][lm][n] (c = s n_max + n) so that a pair reads
+  // a harmonic's n_max values together.  The B2 index of the radial pair
+  // (min(b,c), max(b,c)) advances by nr - b - 1 while b < c and by 1 after
+  // it, so the loop carries it instead of recomputing it.
+  if constexpr (LC > 0) {
+    // a thread per (l, atom, c) computes the 2l + 1 entries of (c, l),
+    // loading each weight w((c,b), l) once for them (l slowest, so that
+    // the threads of a warp mostly share l and its entry count)
+    const int nac = na * nr;
+    for (int it = t; it < L1 * nac; it += blockDim.x) {
+      const int l = it / nac, r2 = it - l * nac;
+      const int a = r2 / nr, c = r2 - a * nr;
+      const T *A = smem + (size_t)a * per + nA;
+      T *u = smem + (size_t)a * per;
+      const T *wsrc = w_in_smem ? A + nA : gB2 + (long long)(i0 + a) * nd;
+      const int cs = c / nm, cn = c - cs * nm;
+      switch (l) {
+        case 0: u_entries<T, 1>(A, wsrc, nh, nr, L1, c, 0, u, nm, cs, cn); break;
+        case 1: u_entries<T, 3>(A, wsrc, nh, nr, L1, c, 1, u, nm, cs, cn); break;
+        case 2: if constexpr (LC >= 2) u_entries<T, 5>(A, wsrc, nh, nr, L1, c, 2, u, nm, cs, cn); break;
+        case 3: if constexpr (LC >= 3) u_entries<T, 7>(A, wsrc, nh, nr, L1, c, 3, u, nm, cs, cn); break;
+        case 4: if constexpr (LC >= 4) u_entries<T, 9>(A, wsrc, nh, nr, L1, c, 4, u, nm, cs, cn); break;
+        default: u_entries_any<T>(A, wsrc, nh, nr, L1, c, l, u, nm, cs, cn); break;
+      }
     }
-    // pidx is now the pair (c, c)
-    acc += T(2) * wl[pidx * L1] * Acol[c * nh];
-    for (int bb = c + 1; bb < nr; bb++) {
-      pidx++;
-      acc += wl[pidx * L1] * Acol[bb * nh];
+  } else {
+    for (int it = t; it < na * nA; it += blockDim.x) {
+      const int a = it / nA, e = it - a * nA;
+      const T *A = smem + (size_t)a * per + nA;
+      T *u = smem + (size_t)a * per;
+      const T *wsrc = w_in_smem ? A + nA : gB2 + (long long)(i0 + a) * nd;
+      const int c = e / nh, lm = e - c * nh;
+      int l = 0;
+      while ((l + 1) * (l + 1) <= lm) l++;
+      const T *Acol = A + lm;
+      const T *wl = wsrc + l;
+      T acc = T(0);
+      int pidx = c;   // radial pair (0, c)
+      for (int bb = 0; bb < c; bb++) {
+        acc += wl[pidx * L1] * Acol[bb * nh];
+        pidx += nr - bb - 1;
+      }
+      // pidx is now the pair (c, c)
+      acc += T(2) * wl[pidx * L1] * Acol[c * nh];
+      for (int bb = c + 1; bb < nr; bb++) {
+        pidx++;
+        acc += wl[pidx * L1] * Acol[bb * nh];
+      }
+      const int cs = c / nm, cn = c - cs * nm;
+      u[(cs * nh + lm) * nm + cn] = acc;
     }
-    u[e] = acc;
   }
   __syncthreads();
   const long long pbeg = offsets[i0], pend = offsets[i0 + na];
@@ -398,11 +487,25 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       ylm_visit<T, LC, true>(p.l_max, ry, rz, rw,
                              [&](int idx, T v, T gx, T gy, T gz) {
         T c = T(0), d = T(0);
+        const T *ul = us + idx * nm;
+        if constexpr (std::is_same<T, float>::value && NC > 0 && NC % 4 == 0) {
+          // n_max values of the harmonic in 16-byte loads (u rows start on
+          // 16-byte boundaries: per and n_max n_harm are whole 4-groups)
 #pragma unroll
-        for (int n = 0; n < nm; n++) {
-          const T uv = us[n * nh + idx];
-          c += uv * g[n];
-          d += uv * dg[n];
+          for (int q = 0; q < NC / 4; q++) {
+            const float4 uv = reinterpret_cast<const float4 *>(ul)[q];
+            c += uv.x * g[4 * q];     d += uv.x * dg[4 * q];
+            c += uv.y * g[4 * q + 1]; d += uv.y * dg[4 * q + 1];
+            c += uv.z * g[4 * q + 2]; d += uv.z * dg[4 * q + 2];
+            c += uv.w * g[4 * q + 3]; d += uv.w * dg[4 * q + 3];
+          }
+        } else {
+#pragma unroll
+          for (int n = 0; n < nm; n++) {
+            const T uv = ul[n];
+            c += uv * g[n];
+            d += uv * dg[n];
+          }
         }
         orad += d * v;
         ox += c * gx;
@@ -512,9 +615,6 @@ size_t b2_forward_smem(const B2Params &p, bool regA) {
          sizeof(int) * (kChunk + 3 * kMaxSpecies + 1);
 }
 
-size_t b2_adjoint_smem(const B2Params &p) {
-  return sizeof(double) * 2 * (size_t)p.n_A;
-}
 
 // The descriptor sizes with compile-time specialisations (registers instead
 // of local memory for the per-pair basis values; Chebyshev basis); others
@@ -584,15 +684,15 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
   // per atom of a block: u and A, and the atom's dE/dB2 row when it fits
-  size_t sm = (fp32 ? b2_adjoint_smem(p) / 2 : b2_adjoint_smem(p)) * kAdjAtoms;
+  const size_t es = fp32 ? sizeof(float) : sizeof(double);
+  size_t sm = es * (size_t)adj_atom_values(p.n_A, 0) * kAdjAtoms;
   if (sm > 200 * 1024) {
     set_error("B2 adjoint needs %zu bytes of shared memory", sm);
     return FGB_EINVAL;
   }
-  const size_t wbytes =
-      (fp32 ? sizeof(float) : sizeof(double)) * (size_t)p.n_d * kAdjAtoms;
-  const int w_in_smem = sm + wbytes <= 96 * 1024 ? 1 : 0;
-  if (w_in_smem) sm += wbytes;
+  const size_t smw = es * (size_t)adj_atom_values(p.n_A, p.n_d) * kAdjAtoms;
+  const int w_in_smem = smw <= 96 * 1024 ? 1 : 0;
+  if (w_in_smem) sm = smw;
   cudaError_t e = cudaSuccess;
   auto go = [&](auto k) {
     auto fn = decltype(k)::fn;

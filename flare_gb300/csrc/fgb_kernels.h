@@ -5,7 +5,6 @@
 namespace fgb {
 
 size_t b2_forward_smem(const B2Params &p, bool regA = false);
-size_t b2_adjoint_smem(const B2Params &p);
 // dfloat: compute in double-float (mixed-precision path) instead of FP64;
 // d_rowmax (optional): each row's largest |B2| as written
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
