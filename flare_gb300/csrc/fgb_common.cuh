@@ -17,6 +17,25 @@ constexpr int kMaxSpecies = 8;
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEmptyThresh = 1e-8;          // normalized_dot_product.cpp:50
 
+// Row sums of GEMM partial slots (part[m * nslots + t]) by kRowLanes
+// consecutive lanes per row: lane q adds slots q, q + kRowLanes, ... and a
+// fixed butterfly joins the lanes (coalesced slot reads; launch
+// rows x kRowLanes threads in blocks of whole groups).  Every lane of the
+// group returns the sum.
+constexpr int kRowLanes = 4;
+__device__ __forceinline__ double row_slots_sum(const double *__restrict__ part,
+                                                long long m, int nslots,
+                                                int q) {
+  double s = 0.0;
+  for (int t = q; t < nslots; t += kRowLanes) s += part[m * nslots + t];
+  const unsigned gmask = ((1u << kRowLanes) - 1u)
+                         << ((threadIdx.x & 31) & ~(kRowLanes - 1));
+#pragma unroll
+  for (int off = kRowLanes / 2; off > 0; off >>= 1)
+    s += __shfl_xor_sync(gmask, s, off);
+  return s;
+}
+
 // Error state shared by the C-ABI (defined in capi.cu).
 void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *where);

@@ -1151,15 +1151,15 @@ struct EpiZsq {
   }
 };
 
-// E_atom = sum of the row's energy partials, tiles in order.
+// E_atom = sum of the row's energy partials (fixed order, row_slots_sum).
 __global__ void k_energy_final(int M, int ntiles, const double *__restrict__ part,
                                const int *__restrict__ perm,
                                double *__restrict__ e_atom) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= M) return;
-  double s = 0.0;
-  for (int t = 0; t < ntiles; t++) s += part[(long long)m * ntiles + t];
-  e_atom[perm[m]] = s;
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = (int)(gt / kRowLanes), q = (int)(gt % kRowLanes);
+  if (m >= M) return;   // whole lane groups
+  const double s = row_slots_sum(part, m, ntiles, q);
+  if (q == 0) e_atom[perm[m]] = s;
 }
 
 }  // namespace
@@ -1273,7 +1273,8 @@ static int probe_sparse(fgb_model_s *m, int Sk, int Sv, std::vector<double> &E,
       return oz::gemm_s<S_>(A, B, false, epi, err.as<int>(), st);
     });
     if (rc) return rc;
-    oz::k_energy_final<<<ceil_div(Ms, 128), 128, 0, st>>>(
+    oz::k_energy_final<<<
+        ceil_div((long long)Ms * kRowLanes, 128), 128, 0, st>>>(
         Ms, slots, erows.as<double>(), ident.as<int>(),
         eout.as<double>() + off);
     FGB_LAUNCH_CHECK("k_energy_final");
@@ -1490,7 +1491,8 @@ int kernel_stage_oz(fgb_model_s *m, int N, const std::vector<int> &counts,
       }
       {
         StageTimer _pt(kStRowEnergy, st);
-        oz::k_energy_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
+        oz::k_energy_final<<<
+            ceil_div((long long)Mr * kRowLanes, 128), 128, 0, st>>>(
             Mr, m->ozS[vk][s]->RP / 16, m->ws.erows.as<double>(), perm,
             d_e_atom);
         FGB_LAUNCH_CHECK("k_energy_final");

@@ -151,12 +151,13 @@ __global__ void k_variance_final(int M, int ntiles, const double *__restrict__ p
                                  const int *__restrict__ perm,
                                  const double *__restrict__ norms, double sig2,
                                  double xi, double *__restrict__ var) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= M) return;
+  const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = (int)(gt / kRowLanes), q = (int)(gt % kRowLanes);
+  if (m >= M) return;   // whole lane groups
+  const double s = row_slots_sum(part, m, ntiles, q);
+  if (q) return;
   int atom = perm[m];
   double nd = norms[atom];
-  double s = 0.0;
-  for (int t = 0; t < ntiles; t++) s += part[(long long)m * ntiles + t];
   // K_self = sig^2 (d.d/(|d||d|))^xi, zero for an empty environment.
   double kself = nd >= kEmptyThresh ? sig2 * powx((nd * nd) / (nd * nd), xi)
                                     : 0.0;
@@ -303,8 +304,9 @@ int launch_variance_final(int Mr, int ntiles, const double *part,
                           const int *perm, const double *norms, double sig2,
                           double xi, double *var, cudaStream_t st) {
   StageTimer _pt(kStVarianceFinal, st);
-  k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(Mr, ntiles, part, perm,
-                                                      norms, sig2, xi, var);
+  k_variance_final<<<
+      ceil_div((long long)Mr * kRowLanes, 128), 128, 0, st>>>(
+      Mr, ntiles, part, perm, norms, sig2, xi, var);
   FGB_LAUNCH_CHECK("k_variance_final");
   return FGB_OK;
 }
@@ -397,7 +399,8 @@ int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
     if (Ns > 0 && Ms == 0 && want_var) {
       // No sparse environments of this species: k = 0 and E = 0 (zero
       // filled), var = k_self.
-      k_variance_final<<<ceil_div(Ns, 128), 128, 0, st>>>(
+      k_variance_final<<<
+          ceil_div((long long)Ns * kRowLanes, 128), 128, 0, st>>>(
           Ns, 0, nullptr, perm_s, m->ws.norms.as<double>(), sig2, m->power,
           d_var);
       FGB_LAUNCH_CHECK("k_variance_final");
@@ -457,9 +460,10 @@ int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
         }
         {
           StageTimer _pt(kStVarianceFinal, st, 1);
-          k_variance_final<<<ceil_div(Mr, 128), 128, 0, st>>>(
-              Mr, ntiles, m->ws.part.as<double>(), perm, m->ws.norms.as<double>(),
-              sig2, m->power, d_var);
+          k_variance_final<<<
+              ceil_div((long long)Mr * kRowLanes, 128), 128, 0, st>>>(
+              Mr, ntiles, m->ws.part.as<double>(), perm,
+              m->ws.norms.as<double>(), sig2, m->power, d_var);
           FGB_LAUNCH_CHECK("k_variance_final");
         }
       }
