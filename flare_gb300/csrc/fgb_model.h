@@ -102,15 +102,26 @@ struct FixedPlan {
 // nullptr with rc set on failure.
 fgb_model_s *model_replicate(const fgb_model_s *src, int &rc);
 
+// Host side of a prediction whose inputs and results live in host memory
+// (fgb_predict_host): the host copy of the species (species counts without
+// a device read-back) and the result buffers, copied back on the stream
+// before the call's final synchronisation (any may be null).
+struct PredictHostIO {
+  const int *species = nullptr;
+  double *energy = nullptr, *forces = nullptr, *stress = nullptr,
+         *local_var = nullptr;
+};
+
 // One batched prediction on device positions (predict.cu): the body of
 // fgb_predict, also driven by the MD ensemble (with `fixed` for the steps
-// it replays).
+// it replays) and by fgb_predict_host (with `hio`).
 int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
                  const double *h_cells, const double *d_positions,
                  const int *d_species, double cutoff, int want, int precision,
                  double *d_energy, double *d_forces, double *d_stress,
                  double *d_local_var, cudaStream_t st,
-                 const fgb::FixedPlan *fixed = nullptr);
+                 const fgb::FixedPlan *fixed = nullptr,
+                 const PredictHostIO *hio = nullptr);
 
 namespace fgb {
 int kernel_stage_fp64(fgb_model_s *m, int N, const std::vector<int> &counts,
@@ -137,11 +148,15 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
                        double *d_gB2, double *d_var, cudaStream_t st,
                        bool fixed = false);
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
-                        std::vector<int> &counts, cudaStream_t st);
+                        std::vector<int> &counts, cudaStream_t st,
+                        const int *h_species = nullptr);
 // The same on any workspace: perm = atoms of species 0 (ascending), then
-// 1, ...; one host synchronisation (counts and the species range check).
+// 1, ...; one host synchronisation (counts and the species range check),
+// none when the host copy of the species is given (counted and checked on
+// the host).
 int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
-                        std::vector<int> &counts, cudaStream_t st);
+                        std::vector<int> &counts, cudaStream_t st,
+                        const int *h_species = nullptr);
 int envs_struc_impl(const B2Params &p, double sigma, double power,
                     const int *h_counts, const double *d_sparse,
                     fgb_nlist_s *nl, const int *d_species, double *d_kern,

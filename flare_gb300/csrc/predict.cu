@@ -344,16 +344,29 @@ int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
 // The species range check and every species count come back to the host in
 // one read (a single synchronisation).
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
-                        std::vector<int> &counts, cudaStream_t st) {
-  return species_permutation(m->b2.n_species, m->ws, d_species, N, counts, st);
+                        std::vector<int> &counts, cudaStream_t st,
+                        const int *h_species) {
+  return species_permutation(m->b2.n_species, m->ws, d_species, N, counts, st,
+                             h_species);
 }
 
 int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
-                        std::vector<int> &counts, cudaStream_t st) {
+                        std::vector<int> &counts, cudaStream_t st,
+                        const int *h_species) {
   counts.assign(S, 0);
   if (S < 1 || S > kMaxSpecies) {
     set_error("species permutation: %d species (at most %d)", S, kMaxSpecies);
     return FGB_EINVAL;
+  }
+  if (h_species) {
+    for (int i = 0; i < N; i++) {
+      const int q = h_species[i];
+      if (q < 0 || q >= S) {
+        set_error("species must lie in [0, %d)", S);
+        return FGB_EINVAL;
+      }
+      counts[q]++;
+    }
   }
   const int nb = ceil_div(std::max(N, 1), kPermBlock);
   int rc;
@@ -372,6 +385,7 @@ int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
   k_species_scatter<<<nb, kPermBlock, 0, st>>>(N, d_species, S, hist,
                                                ws.perm.as<int>());
   FGB_LAUNCH_CHECK("k_species_scatter");
+  if (h_species) return FGB_OK;   // counted and checked above
   std::vector<int> h(S + 1);
   FGB_CUDA(cudaMemcpyAsync(h.data(), tot, sizeof(int) * (S + 1),
                            cudaMemcpyDeviceToHost, st));
@@ -618,7 +632,8 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
                  const double *h_cells, const double *d_positions,
                  const int *d_species, double cutoff, int want, int precision,
                  double *d_energy, double *d_forces, double *d_stress,
-                 double *d_local_var, cudaStream_t st, const FixedPlan *fixed) {
+                 double *d_local_var, cudaStream_t st, const FixedPlan *fixed,
+                 const PredictHostIO *hio) {
   if (!m->solved) {
     set_error("L_inv must be up to date to make predictions. Please call "
               "update_matrices_QR and try again.");
@@ -701,7 +716,9 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     counts = fixed->counts;
   } else {
     StageTimer _pt(kStSpeciesPerm, st, 3);
-    if ((rc = species_permutation(m, d_species, N, counts, st))) return rc;
+    if ((rc = species_permutation(m, d_species, N, counts, st,
+                                  hio ? hio->species : nullptr)))
+      return rc;
     m->last_species_counts = counts;
   }
   // dE/dB2 rows: the kernel stages write every row of a species with sparse
@@ -764,6 +781,20 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     FGB_CUDA(cudaMemcpyAsync(d_local_var, m->ws.var.p, sizeof(double) * N,
                              cudaMemcpyDeviceToDevice, st));
   if (fixed) return FGB_OK;
+  if (hio) {   // results to the host ahead of the one synchronisation below
+    if (hio->energy && want_e)
+      FGB_CUDA(cudaMemcpyAsync(hio->energy, d_energy, sizeof(double) * n_struc,
+                               cudaMemcpyDeviceToHost, st));
+    if (hio->forces && want_f && N > 0)
+      FGB_CUDA(cudaMemcpyAsync(hio->forces, d_forces, sizeof(double) * 3 * N,
+                               cudaMemcpyDeviceToHost, st));
+    if (hio->stress && want_s)
+      FGB_CUDA(cudaMemcpyAsync(hio->stress, d_stress, sizeof(double) * 6 * n_struc,
+                               cudaMemcpyDeviceToHost, st));
+    if (hio->local_var && want_v && N > 0)
+      FGB_CUDA(cudaMemcpyAsync(hio->local_var, d_local_var,
+                               sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  }
   // deferred checks: neighbour-list consistency, tensor-core waits
   int h[5] = {0, 0, 0, 0, 0};
   FGB_CUDA(cudaMemcpyAsync(h, m->nl.flag.p, sizeof(int) * 4,
@@ -779,7 +810,7 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     m->nl.count_pass = true;
     rc = predict_impl(m, n_struc, h_atom_offsets, h_cells, d_positions,
                       d_species, cutoff, want, precision, d_energy, d_forces,
-                      d_stress, d_local_var, st, nullptr);
+                      d_stress, d_local_var, st, nullptr, hio);
     m->nl.count_pass = false;
     return rc;
   }
@@ -829,26 +860,19 @@ extern "C" int fgb_predict_host(fgb_model_t m, int n_struc,
     FGB_CUDA(cudaMemcpyAsync(m->io.species.p, h_species, sizeof(int) * N,
                              cudaMemcpyHostToDevice, st));
   }
-  rc = predict_impl(m, n_struc, h_atom_offsets, h_cells, m->io.pos.as<double>(),
-                    m->io.species.as<int>(), cutoff, want, precision,
-                    m->io.energy.as<double>(), m->io.forces.as<double>(),
-                    m->io.stress.as<double>(), m->io.var.as<double>(), st);
-  if (rc) return rc;
-  if (h_energy && (want & FGB_WANT_ENERGY))
-    FGB_CUDA(cudaMemcpyAsync(h_energy, m->io.energy.p, sizeof(double) * n_struc,
-                             cudaMemcpyDeviceToHost, st));
-  if (h_forces && (want & FGB_WANT_FORCES) && N > 0)
-    FGB_CUDA(cudaMemcpyAsync(h_forces, m->io.forces.p, sizeof(double) * 3 * N,
-                             cudaMemcpyDeviceToHost, st));
-  if (h_stress && (want & FGB_WANT_STRESS))
-    FGB_CUDA(cudaMemcpyAsync(h_stress, m->io.stress.p,
-                             sizeof(double) * 6 * n_struc, cudaMemcpyDeviceToHost,
-                             st));
-  if (h_local_var && (want & FGB_WANT_LOCAL_VAR) && N > 0)
-    FGB_CUDA(cudaMemcpyAsync(h_local_var, m->io.var.p, sizeof(double) * N,
-                             cudaMemcpyDeviceToHost, st));
-  FGB_CUDA(cudaStreamSynchronize(st));
-  return FGB_OK;
+  // species counted on the host (no read-back) and results copied back
+  // before the prediction's final synchronisation
+  PredictHostIO hio;
+  hio.species = h_species;
+  hio.energy = h_energy;
+  hio.forces = h_forces;
+  hio.stress = h_stress;
+  hio.local_var = h_local_var;
+  return predict_impl(m, n_struc, h_atom_offsets, h_cells,
+                      m->io.pos.as<double>(), m->io.species.as<int>(), cutoff,
+                      want, precision, m->io.energy.as<double>(),
+                      m->io.forces.as<double>(), m->io.stress.as<double>(),
+                      m->io.var.as<double>(), st, nullptr, &hio);
 }
 
 extern "C" int fgb_model_set_R_inv(fgb_model_t m, const double *h_R_inv) {
