@@ -105,7 +105,13 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   int *scnt = sord + kChunk;              // [warp][species] counts
   int *sbeg = scnt + 2 * kMaxSpecies;     // species starts in sord
   const int t = threadIdx.x;
-  const int si = species[i];
+  // a species outside [0, n_species) contributes nothing here (the caller
+  // rejects it before any later stage): no table or shared-memory index is
+  // formed from it
+  const int ns = p.n_species;
+  const int si_raw = species[i];
+  const bool si_ok = si_raw >= 0 && si_raw < ns;
+  const int si = si_ok ? si_raw : 0;
   T areg[NC > 0 ? NC : 1];
 #pragma unroll
   for (int n = 0; n < (NC > 0 ? NC : 1); n++) areg[n] = T(0);
@@ -119,8 +125,9 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
       int j = nbr_j[pp];
       double4_16a r = rel[pp];
       sj = species[j];
-      double rc = p.cutoffs[si * kMaxSpecies + sj];
-      if (r.x <= rc) {
+      const bool ok = si_ok && sj >= 0 && sj < ns;
+      double rc = ok ? p.cutoffs[si * kMaxSpecies + sj] : 0.0;
+      if (ok && r.x <= rc) {
         radial_eval<T, NC>(p, T(r.x), T(rc), sg + t * nm, (T *)nullptr);
         ylm_eval<T, LC>(p.l_max, T(r.y), T(r.z), T(r.w), sy + t * nh, nullptr);
       } else {

@@ -107,7 +107,10 @@ int fgb_nlist_destroy(fgb_nlist_t nl);
 int fgb_nlist_build(fgb_nlist_t nl, int n_struc, const int *h_atom_offsets,
                     const double *h_cells, const double *d_positions,
                     double cutoff, void *stream);
-/* total pairs and atoms of the last build */
+/* total pairs and atoms of the last build (fgb_nlist_build returns after
+ * its checks, so the count is exact; the build fills per-atom slots in one
+ * pass and falls back to a counting pass when an atom has more pairs than
+ * its slots) */
 int fgb_nlist_size(fgb_nlist_t nl, long long *n_pairs, int *n_atoms);
 /* Copy out in the reference's Structure layout (device pointers; any may be
  * NULL): neighbor_count[N], structure_indices[P] (index within the
@@ -221,7 +224,10 @@ int fgb_predict(fgb_model_t m, int n_struc, const int *h_atom_offsets,
                 double *d_local_var, void *stream);
 
 /* Same with HOST input/output buffers: copies in, predicts, copies out on
- * `stream` and synchronises it. */
+ * `stream` and synchronises it once (the species are counted and range-
+ * checked on the host; results are queued for copy-back before that
+ * synchronisation).  fgb_predict synchronises twice (the species counts,
+ * then the deferred checks). */
 int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
                      const double *h_cells, const double *h_positions,
                      const int *h_species, double cutoff, int want,
