@@ -253,22 +253,16 @@ __device__ __forceinline__ long long fixed_rn(double d, int sh) {
   return (bits >> 63) ? -(long long)q : (long long)q;
 }
 
-// BF16 bits of a small integer (|q| <= 256, exact): the float of q from the
-// bits of 1.5 * 2^23 + q minus 1.5 * 2^23 (one FP32 subtraction; an
-// integer-to-float conversion would run on the FP64/conversion pipe, which
-// this GPU runs slowly and which the tensor-core epilogue must leave free).
-__device__ __forceinline__ uint32_t bf16_bits(long long q) {
-  return __float_as_uint(
-             __fsub_rn(__int_as_float(0x4B400000 + (int)q), 12582912.0f)) >>
-         16;
-}
-
 // The S base-64 digits of X (|X| < 2^(6S)) for 8 consecutive k, stored as
 // 16-byte rows of the canonical layout: slice a at out + a * stride.  The
 // digits are balanced: U = X + sum_{a >= 2} 32 2^(6(S-a)) has plain base-64
 // digits u_2..u_S below its top one, d_a = u_a - 32 in [-32, 31] and d_1 =
-// U >> 6(S-1) in [-64, 64]; X = sum_a d_a 2^(6(S-a)) exactly.  A digit is a
-// bit-field extract, and its BF16 bits come from one FP32 subtraction.
+// U >> 6(S-1) in [-64, 64]; X = sum_a d_a 2^(6(S-a)) exactly.  U is held as
+// two 32-bit words, so a digit is one funnel shift (or word shift) and a
+// mask.  Its float (exact: |d| <= 64) is the bits of 1.5 * 2^23 + d minus
+// 1.5 * 2^23, one FP32 subtraction (an integer-to-float conversion would
+// run on the FP64/conversion pipe, which this GPU runs slowly); its BF16 is
+// that float's upper half, and one byte permute packs two of them.
 template <int S>
 __device__ __forceinline__ void store_digits8(long long (&X)[8],
                                               __nv_bfloat16 *out,
@@ -278,21 +272,33 @@ __device__ __forceinline__ void store_digits8(long long (&X)[8],
     for (int a = 2; a <= S; a++) b += 32LL << (kBeta * (S - a));
     return b;
   }();
-  long long U[8];
+  uint32_t lo[8], hi[8];
 #pragma unroll
-  for (int j = 0; j < 8; j++) U[j] = X[j] + kBias;
+  for (int j = 0; j < 8; j++) {
+    const unsigned long long u = (unsigned long long)(X[j] + kBias);
+    lo[j] = (uint32_t)u;
+    hi[j] = (uint32_t)(u >> 32);
+  }
 #pragma unroll
   for (int a = 1; a <= S; a++) {
     const int sh = kBeta * (S - a);
     uint32_t w[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
-      int d[2];
+      float f[2];
 #pragma unroll
-      for (int h = 0; h < 2; h++)
-        d[h] = a == 1 ? (int)(U[j + h] >> sh)
-                      : (int)((unsigned)(U[j + h] >> sh) & 63u) - 32;
-      w[j / 2] = bf16_bits(d[0]) | (bf16_bits(d[1]) << 16);
+      for (int h = 0; h < 2; h++) {
+        // bits [sh, ...) of U: the low word of U >> sh (U >> sh fits it)
+        const uint32_t v = sh >= 32 ? hi[j + h] >> (sh - 32)
+                                    : __funnelshift_r(lo[j + h], hi[j + h], sh);
+        const int q = a == 1
+                          ? (sh >= 32 ? (int)hi[j + h] >> (sh - 32) : (int)v)
+                          : (int)(v & 63u) - 32;
+        f[h] = __fsub_rn(__int_as_float(0x4B400000 + q), 12582912.0f);
+      }
+      // BF16 of each (their exact floats' upper halves), low digit first
+      w[j / 2] = __byte_perm(__float_as_uint(f[0]), __float_as_uint(f[1]),
+                             0x7632);
     }
     *reinterpret_cast<uint4 *>(out + (size_t)(a - 1) * stride) =
         make_uint4(w[0], w[1], w[2], w[3]);
