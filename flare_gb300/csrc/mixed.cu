@@ -16,6 +16,7 @@
 // then runs in FP32.  Other powers use the FP64 kernel, adjoint and variance
 // GEMMs.
 #include <cstring>
+#include <type_traits>
 
 #include "fgb_df.cuh"
 #include "fgb_internal.h"
@@ -130,7 +131,9 @@ __global__ void k_mapped_grad(int Mr, int nd, const int *__restrict__ perm,
 // four consecutive columns at a time (two double2 loads of B2, one float4
 // of Y, one float4 store), keeps d^ and g in registers between the dot
 // product and the update, and the row's bytes are read once.
+// IT: 4-column groups per lane, ceil(n_d / 128) (the row's registers)
 constexpr int kGradV4It = 8;   // 8 x 32 lanes x 4 columns = 1024
+template <int IT>
 __global__ void __launch_bounds__(256)
 k_mapped_grad_v4(int Mr, int nd, const int *__restrict__ perm,
                  const double *__restrict__ norms,
@@ -146,10 +149,10 @@ k_mapped_grad_v4(int Mr, int nd, const int *__restrict__ perm,
   const int n4 = nd >> 2;
   const double2 *b = reinterpret_cast<const double2 *>(B2 + (long long)atom * nd);
   const float4 *y = reinterpret_cast<const float4 *>(Y + (long long)warp * nd);
-  float4 dv[kGradV4It], yv[kGradV4It];
+  float4 dv[IT], yv[IT];
   float q = 0.f;
 #pragma unroll
-  for (int it = 0; it < kGradV4It; it++) {
+  for (int it = 0; it < IT; it++) {
     const int k4 = lane + 32 * it;
     if (k4 < n4) {
       const double2 b0 = b[2 * k4], b1 = b[2 * k4 + 1];
@@ -167,7 +170,7 @@ k_mapped_grad_v4(int Mr, int nd, const int *__restrict__ perm,
   const float sq = scale * q;
   float4 *out = reinterpret_cast<float4 *>(gB2 + (long long)atom * nd);
 #pragma unroll
-  for (int it = 0; it < kGradV4It; it++) {
+  for (int it = 0; it < IT; it++) {
     const int k4 = lane + 32 * it;
     if (k4 < n4)
       out[k4] = make_float4((scale * yv[it].x - sq * dv[it].x) * inv,
@@ -397,9 +400,23 @@ int kernel_stage_mixed(fgb_model_s *m, int N, const std::vector<int> &counts,
         return r;
     }
     if (quad && nd % 4 == 0 && nd <= 4 * 32 * kGradV4It) {
-      k_mapped_grad_v4<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(
-          Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
-          m->ws.yf.as<float>(), 2.f * sig2, reinterpret_cast<float *>(d_gB2));
+      const unsigned nb = (unsigned)ceil_div((long long)Mr * 32, 256);
+      const auto go = [&](auto it) {
+        k_mapped_grad_v4<decltype(it)::value><<<nb, 256, 0, st>>>(
+            Mr, nd, perm, m->ws.norms.as<double>(), m->ws.B2.as<double>(),
+            m->ws.yf.as<float>(), 2.f * sig2,
+            reinterpret_cast<float *>(d_gB2));
+      };
+      switch ((nd + 127) / 128) {   // 4-column groups per lane
+        case 1: go(std::integral_constant<int, 1>()); break;
+        case 2: go(std::integral_constant<int, 2>()); break;
+        case 3: go(std::integral_constant<int, 3>()); break;
+        case 4: go(std::integral_constant<int, 4>()); break;
+        case 5: go(std::integral_constant<int, 5>()); break;
+        case 6: go(std::integral_constant<int, 6>()); break;
+        case 7: go(std::integral_constant<int, 7>()); break;
+        default: go(std::integral_constant<int, kGradV4It>()); break;
+      }
       FGB_LAUNCH_CHECK("k_mapped_grad_v4");
     } else {
       k_mapped_grad<<<ceil_div((long long)Mr * 32, 256), 256, 0, st>>>(

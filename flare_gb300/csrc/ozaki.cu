@@ -381,7 +381,7 @@ static_assert(kSlicePart % 32 == 0, "a part is whole 32-column steps");
 template <int S>
 __global__ void __launch_bounds__(256)
 k_oz_slice8(int R, int K, int RP, int KP, int TR, int nparts,
-            const double *__restrict__ src, long long ld,
+            const double *__restrict__ src, long long ld, int vec,
             const int *__restrict__ perm, const double *__restrict__ rownorm,
             double thresh, __nv_bfloat16 *__restrict__ out,
             const double *__restrict__ scale) {
@@ -408,12 +408,26 @@ k_oz_slice8(int R, int K, int RP, int KP, int TR, int nparts,
   const size_t stride = (size_t)TR * kKC;
   const int kend = min(KP, (part + 1) * kSlicePart);
   for (int k0 = part * kSlicePart + g * 8; k0 < kend; k0 += 32) {
+    // the lane's 8 values: four 16-byte loads when the source rows allow
+    // (vec: 16-byte aligned rows) and all 8 lie inside the row
+    double v[8];
+    if (vec && valid && k0 + 8 <= K) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const double2 t = reinterpret_cast<const double2 *>(sr + k0)[q];
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; j++) v[j] = (valid && k0 + j < K) ? sr[k0 + j] : 0.0;
+    }
     long long X[8];
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int k = k0 + j;
       X[j] = (valid && k < K)
-                 ? fixed_rn(rownorm ? sr[k] * inv : sr[k], kBeta * S - e)
+                 ? fixed_rn(rownorm ? v[j] * inv : v[j], kBeta * S - e)
                  : 0;
     }
     store_digits8<S>(X, out + tiled_index<S>(m, k0, KP, TR), stride);
@@ -856,9 +870,12 @@ static int slice_s(const SliceSpec &sp, Sliced &out, cudaStream_t st) {
   }
   const int nparts = ceil_div(out.KP, kSlicePart);
   const long long threads = (long long)(out.RP / 8) * nparts * 32;  // RP % 8 == 0
+  // 16-byte loads need every row start 16-byte aligned
+  const int vec = (sp.ld % 2 == 0 &&
+                   reinterpret_cast<uintptr_t>(sp.src) % 16 == 0) ? 1 : 0;
   k_oz_slice8<S><<<ceil_div(threads, 256), 256, 0, st>>>(
-      sp.rows, sp.K, out.RP, out.KP, sp.TR, nparts, sp.src, sp.ld, sp.perm,
-      sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
+      sp.rows, sp.K, out.RP, out.KP, sp.TR, nparts, sp.src, sp.ld, vec,
+      sp.perm, sp.rownorm, kEmptyThresh, out.q.as<__nv_bfloat16>(),
       out.scale.as<double>());
   FGB_LAUNCH_CHECK("k_oz_slice8");
   return FGB_OK;
