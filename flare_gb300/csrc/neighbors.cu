@@ -17,11 +17,18 @@
 // wrapped positions and the cell.  A margin well above the FP32 rounding
 // error (set per structure in make_geom) sorts candidates into certainly
 // outside, certainly inside, or near the cutoff (or near zero distance);
-// only the last class is decided by the FP64 test in the count pass, and
-// only candidates not certainly outside are evaluated in FP64 in the fill
-// pass, whose FP64 test alone decides what is written.  The fill pass
-// checks that its FP64 decisions agree with the count pass.  One warp
-// serves one atom, a lane per bin image.
+// candidates not certainly outside are evaluated in FP64 by the fill, whose
+// FP64 test alone decides what is written, and which checks that no
+// certainly-inside candidate fails it.  One warp serves one atom, a lane
+// per bin image.
+//
+// The fill normally runs once, into per-atom slots sized from the densest
+// structure (no counting pass, no host synchronisation); the counts are
+// scanned on the device and the rank sort gathers the slots into the CSR
+// list.  An atom with more pairs than its slots flags the build, which is
+// then repeated with a counting pass (k_count: only near-cutoff candidates
+// take the FP64 test there) that sizes the CSR segments exactly; the fill
+// then also checks its counts against that pass.
 #include <limits>
 
 #include "fgb_internal.h"
