@@ -38,7 +38,7 @@ WORKLOAD = ("alloy1000: 2-species random alloy, 1000-atom cubic cell, 0.06 "
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -381,9 +381,21 @@ def clocks_path(name):
 
 
 class Clocks:
+    """nvidia-smi clock samples during a timed region: sampling starts (and
+    its first line is written) before the region, every 20 ms; the summary
+    keeps the samples taken after that first line, i.e. inside the region."""
+
     def __init__(self, path):
         self.path = path
         self.p = None
+        self.skip = 0
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return f.read().count("\n")
+        except Exception:
+            return 0
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,"
@@ -395,7 +407,11 @@ class Clocks:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=self.f, stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while self._lines() == 0 and time.time() - t0 < 5.0:
+                time.sleep(0.005)
+            self.skip = self._lines()
         except Exception:
             self.p = None
         return self
@@ -414,6 +430,10 @@ class Clocks:
             rows = [l.split(",") for l in open(self.path).read().splitlines()]
         except Exception:
             return None
+        # samples from inside the region (if none came after the ones
+        # written before it, those, and in_region says so)
+        in_region = len(rows) - self.skip
+        rows = rows[self.skip:] if in_region > 0 else rows
         def numeric(r):
             try:
                 float(r[1]), float(r[2])
@@ -432,7 +452,8 @@ class Clocks:
         reasons = sorted({names[k] for r in rows for k in range(4)
                           if r[5 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "samples_in_region": max(in_region, 0)}
 
 
 def measure_fp64_peak(torch):
