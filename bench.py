@@ -427,22 +427,26 @@ class Clocks:
 
     def summary(self, dev_index=0):
         try:
-            rows = [l.split(",") for l in open(self.path).read().splitlines()]
+            lines = open(self.path).read().splitlines()
         except Exception:
             return None
-        # samples from inside the region (if none came after the ones
-        # written before it, those, and in_region says so)
-        in_region = len(rows) - self.skip
-        rows = rows[self.skip:] if in_region > 0 else rows
+        # (line number, fields): the lines before `skip` were written before
+        # the timed region began
+        rows = [(k, [x.strip() for x in l.split(",")])
+                for k, l in enumerate(lines)]
+
         def numeric(r):
             try:
                 float(r[1]), float(r[2])
                 return True
             except ValueError:
                 return False
-        rows = [[x.strip() for x in r] for r in rows if len(r) >= 9]
-        rows = [r for r in rows if numeric(r)]       # "[N/A]" samples
-        rows = [r for r in rows if r[0] == str(dev_index)] or rows
+        rows = [(k, r) for k, r in rows if len(r) >= 9 and numeric(r)]
+        rows = [(k, r) for k, r in rows if r[0] == str(dev_index)] or rows
+        inside = [(k, r) for k, r in rows if k >= self.skip]
+        # samples from inside the region (if there are none, those written
+        # before it, and samples_in_region says so)
+        rows = [r for _, r in (inside or rows)]
         if not rows:
             return None
         sm = [float(r[1]) for r in rows]
@@ -453,7 +457,7 @@ class Clocks:
                           if r[5 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx,
                 "reasons": reasons, "samples": len(rows),
-                "samples_in_region": max(in_region, 0)}
+                "samples_in_region": len(inside)}
 
 
 def measure_fp64_peak(torch):

@@ -1,6 +1,6 @@
 """CPU: the bench's clock record — the median SM clock, the maximum and the
 throttle reasons seen while the timed region ran, from nvidia-smi's
-per-200-ms samples (bench.py Clocks.summary)."""
+per-20-ms samples (bench.py Clocks.summary)."""
 import os
 import sys
 
@@ -23,9 +23,19 @@ def test_clock_summary(tmp_path):
     c = bench.Clocks(str(path))
     s = c.summary(0)
     assert s == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0,
-                 "reasons": ["sw_power_cap"], "samples": 3}
+                 "reasons": ["sw_power_cap"], "samples": 3,
+                 "samples_in_region": 3}
     s1 = c.summary(1)
     assert s1["sm_mhz"] == 1200.0 and s1["reasons"] == ["hw_slowdown"]
+    # the first two lines written before the timed region began
+    c.skip = 2
+    s2 = c.summary(0)
+    assert s2["samples"] == 2 and s2["samples_in_region"] == 2
+    assert s2["sm_mhz"] == (1980.0 + 2055.0) / 2
+    # none inside the region: the earlier samples, flagged as such
+    c.skip = 5
+    s3 = c.summary(0)
+    assert s3["samples"] == 3 and s3["samples_in_region"] == 0
 
 
 def test_clock_summary_without_samples(tmp_path):
