@@ -73,7 +73,7 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, double *__restrict__ A_out,
              double *__restrict__ B2, double *__restrict__ norms,
-             double *__restrict__ rowmax) {
+             double *__restrict__ rowmax, float *__restrict__ A_out32) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // largest |B2| of the row as written (the bits of |x| order as the
   // values do), for the tensor-core row scales: no second pass over B2
@@ -213,6 +213,9 @@ k_b2_forward(B2Params p, int n_atoms, const long long *__restrict__ offsets,
   if (A_out)
     for (int e = t; e < nA; e += blockDim.x)
       A_out[(long long)i * nA + e] = to_double(A[e]);
+  if (A_out32)   // the FP32 adjoint's input: the nearest float, no FP64
+    for (int e = t; e < nA; e += blockDim.x)
+      A_out32[(long long)i * nA + e] = to_float(A[e]);
   const int L1 = (LC > 0 ? LC : p.l_max) + 1, nr = p.n_species * nm,
             nd = p.n_d;
   T nrm = T(0);
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 8 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
-             const T *__restrict__ gB2,
+             const float *__restrict__ A_in32, const T *__restrict__ gB2,
              typename PairGrad<T>::type *__restrict__ pair_grad,
              int w_in_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -408,7 +411,7 @@ k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
     T *W = w_in_smem ? A + nA : nullptr;
     const long long i = i0 + a;
     for (int e = t; e < nA; e += blockDim.x)
-      A[e] = as_compute(A_in[i * nA + e], T(0));
+      A[e] = A_in32 ? T(A_in32[i * nA + e]) : as_compute(A_in[i * nA + e], T(0));
     if (W)
       for (int q = t; q < nd; q += blockDim.x)
         W[q] = gB2[i * nd + q];
@@ -649,7 +652,7 @@ struct AdjK {
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
                       double *d_norms, cudaStream_t st, bool dfloat,
-                      double *d_rowmax) {
+                      double *d_rowmax, float *d_A32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
   const size_t sm_full = b2_forward_smem(p, false);   // sizeof(df) == 8
@@ -675,7 +678,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
     if (e != cudaSuccess) return;
     fn<<<N, kChunk, sm, st>>>(p, N, nl->offsets.as<long long>(),
                               nl->nbr_j.as<int>(), nl->nbr_rel.as<double4_16a>(),
-                              d_species, d_A, d_B2, d_norms, d_rowmax);
+                              d_species, d_A, d_B2, d_norms, d_rowmax, d_A32);
   };
   if (dfloat) dispatch_nl<FwdK, df>(p, go);
   else dispatch_nl<FwdK, double>(p, go);
@@ -687,7 +690,7 @@ int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
                       const void *d_gB2, void *d_pair_grad,
-                      cudaStream_t st, bool fp32) {
+                      cudaStream_t st, bool fp32, const float *d_A32) {
   const int N = nl->n_atoms;
   if (N == 0) return FGB_OK;
   // per atom of a block: u and A, and the atom's dE/dB2 row when it fits
@@ -710,7 +713,7 @@ int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
     fn<<<ceil_div(N, kAdjAtoms), kAdjThreads, sm, st>>>(
         p, N, nl->offsets.as<long long>(), nl->nbr_j.as<int>(),
         nl->nbr_rel.as<double4_16a>(), d_species, d_A,
-        static_cast<const G *>(d_gB2),
+        fp32 ? d_A32 : nullptr, static_cast<const G *>(d_gB2),
         static_cast<typename PairGrad<G>::type *>(d_pair_grad), w_in_smem);
   };
   if (fp32) dispatch_nl<AdjK, float>(p, go);

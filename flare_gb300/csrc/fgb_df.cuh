@@ -196,6 +196,10 @@ using dfm::f2d_exact;
 using dfm::two_sum;
 using dfm::fast_two_sum;
 __device__ __forceinline__ double to_double(double a) { return a; }
+// The nearest float: the high part of a normalised double-float; an FP64
+// value is rounded (a conversion on the FP64 pipe).
+__device__ __forceinline__ float to_float(df a) { return a.hi; }
+__device__ __forceinline__ float to_float(double a) { return (float)a; }
 template <> __device__ __forceinline__ df rad_from_double<df>(double x) {
   return dfm::df_from_double(x);
 }

@@ -7,16 +7,20 @@ namespace fgb {
 size_t b2_forward_smem(const B2Params &p, bool regA = false);
 // dfloat: compute in double-float (mixed-precision path) instead of FP64;
 // d_rowmax (optional): each row's largest |B2| as written
+// d_A32 (double-float forward only): A written in FP32 instead of d_A, for
+// the FP32 adjoint
 int launch_b2_forward(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, double *d_A, double *d_B2,
                       double *d_norms, cudaStream_t st, bool dfloat = false,
-                      double *d_rowmax = nullptr);
+                      double *d_rowmax = nullptr, float *d_A32 = nullptr);
 // d_gB2: dE/dB2 rows [N, n_d] and d_pair_grad: pair gradients [P], both in
 // the compute type (float / float3 when fp32, else double / double3)
+// d_A32 (fp32 only): A read in FP32 instead of from d_A
 int launch_b2_adjoint(const B2Params &p, const fgb_nlist_s *nl,
                       const int *d_species, const double *d_A,
                       const void *d_gB2, void *d_pair_grad,
-                      cudaStream_t st, bool fp32 = false);
+                      cudaStream_t st, bool fp32 = false,
+                      const float *d_A32 = nullptr);
 // d_pair_grad as the adjoint wrote it (fp32: float3)
 int launch_forces(const fgb_nlist_s *nl, const void *d_pair_grad, bool fp32,
                   double *d_forces, double *d_virial, cudaStream_t st);

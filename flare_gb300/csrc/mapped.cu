@@ -301,9 +301,12 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
     FGB_CUDA(cudaMemsetAsync(ws.e_atom.p, 0, sizeof(double) * N, st));
     FGB_CUDA(cudaMemsetAsync(ws.var.p, 0, sizeof(double) * N, st));
   }
-  if ((rc = launch_b2_forward(p, &m->nl, d_species, ws.A.as<double>(),
+  // the FP32 adjoint's A is written in FP32 by the double-float forward
+  if ((rc = launch_b2_forward(p, &m->nl, d_species,
+                              adj32 ? nullptr : ws.A.as<double>(),
                               ws.B2.as<double>(), ws.norms.as<double>(), st,
-                              mixed && !m->adjoint_f64)))
+                              mixed && !m->adjoint_f64, nullptr,
+                              adj32 ? ws.A.as<float>() : nullptr)))
     return rc;
   std::vector<int> counts;
   if ((rc = species_permutation(S, ws, d_species, N, counts, st))) return rc;
@@ -363,8 +366,10 @@ extern "C" int fgb_mapped_predict(fgb_mapped_t m, int n_struc,
     }
   }
   if (want_grad) {
-    if ((rc = launch_b2_adjoint(p, &m->nl, d_species, ws.A.as<double>(),
-                                ws.gB2.p, ws.pair_grad.p, st, adj32)) ||
+    if ((rc = launch_b2_adjoint(p, &m->nl, d_species,
+                                adj32 ? nullptr : ws.A.as<double>(), ws.gB2.p,
+                                ws.pair_grad.p, st, adj32,
+                                adj32 ? ws.A.as<float>() : nullptr)) ||
         (rc = launch_forces(&m->nl, ws.pair_grad.p, adj32,
                             ws.forces.as<double>(), ws.virial.as<double>(),
                             st)))

@@ -671,7 +671,7 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   const bool want_e = want & FGB_WANT_ENERGY, want_f = want & FGB_WANT_FORCES,
              want_s = want & FGB_WANT_STRESS, want_v = want & FGB_WANT_LOCAL_VAR;
   const bool want_grad = want_f || want_s;
-  if ((rc = m->ws.A.ensure(sizeof(double) * ((size_t)N * p.n_A + 1))) ||
+  if ((rc = m->ws.A.ensure(sizeof(float) * ((size_t)N * p.n_A + 2))) ||
       (rc = m->ws.B2.ensure(sizeof(double) * ((size_t)N * p.n_d + 1))) ||
       (rc = m->ws.norms.ensure(sizeof(double) * (N + 1))) ||
       (rc = m->ws.e_atom.ensure(sizeof(double) * (N + 1))) ||
@@ -702,13 +702,24 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   // coefficients take the descriptor, force product and adjoint at FP64
   // level (a fixed call reuses the full call's fold)
   if (mixed && !fixed && (rc = prepare_mixed(m, st))) return rc;
+  // FP32 adjoint (and FP32 pair gradients and force sums) in the mixed
+  // path (dE/dB2 written in FP32 by the mapped gradient), unless the fold
+  // guard asked for FP64-level forces or the power has no folded form
+  // (FP64 kernel stage); its A is written in FP32 by the forward
+  const bool adj32 = mixed && !m->force_f64 &&
+                     (m->power == 2.0 || m->power == 1.0);
+  if (!adj32 &&
+      (rc = m->ws.A.ensure(sizeof(double) * ((size_t)N * p.n_A + 1))))
+    return rc;
   {
     StageTimer _pt(kStB2Forward, st);
     // mixed precision: the descriptor in double-float (about 46 bits)
-    if ((rc = launch_b2_forward(p, &m->nl, d_species, m->ws.A.as<double>(),
+    if ((rc = launch_b2_forward(p, &m->nl, d_species,
+                                adj32 ? nullptr : m->ws.A.as<double>(),
                                 m->ws.B2.as<double>(), m->ws.norms.as<double>(),
                                 st, mixed && !m->force_f64,
-                                mixed ? m->ws.rowmax.as<double>() : nullptr)))
+                                mixed ? m->ws.rowmax.as<double>() : nullptr,
+                                adj32 ? m->ws.A.as<float>() : nullptr)))
       return rc;
   }
   std::vector<int> counts;
@@ -745,16 +756,12 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
       return rc;
   }
   if (want_grad) {
-    // FP32 adjoint (and FP32 pair gradients and force sums) in the mixed
-    // path (dE/dB2 written in FP32 by the mapped gradient), unless the fold
-    // guard asked for FP64-level forces or the power has no folded form
-    // (FP64 kernel stage)
-    const bool adj32 = mixed && !m->force_f64 &&
-                       (m->power == 2.0 || m->power == 1.0);
     {
       StageTimer _pt(kStB2Adjoint, st);
-      if ((rc = launch_b2_adjoint(p, &m->nl, d_species, m->ws.A.as<double>(),
-                                  m->ws.gB2.p, m->ws.pair_grad.p, st, adj32)))
+      if ((rc = launch_b2_adjoint(p, &m->nl, d_species,
+                                  adj32 ? nullptr : m->ws.A.as<double>(),
+                                  m->ws.gB2.p, m->ws.pair_grad.p, st, adj32,
+                                  adj32 ? m->ws.A.as<float>() : nullptr)))
         return rc;
     }
     {
