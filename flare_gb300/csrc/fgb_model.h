@@ -7,7 +7,23 @@
 #include "fgb_internal.h"
 #include "fgb_ozaki.h"
 
+// Page-locked species counts (and range flag) of the species permutation
+// and the event recorded after their copy, so that the host can wait for
+// them after queueing more work.
+struct fgb_pinned_counts {
+  int *h = nullptr;
+  cudaEvent_t ev = nullptr;
+  fgb_pinned_counts() = default;
+  fgb_pinned_counts(const fgb_pinned_counts &) = delete;
+  fgb_pinned_counts &operator=(const fgb_pinned_counts &) = delete;
+  ~fgb_pinned_counts() {
+    if (h) cudaFreeHost(h);
+    if (ev) cudaEventDestroy(ev);
+  }
+};
+
 struct fgb_workspace {
+  fgb_pinned_counts counts;
   fgb::DevBuf perm, flags, pos, scal, scan_tmp, flag;
   fgb::DevBuf A, B2, norms, e_atom, var, volume, atom_off;
   fgb::DevBuf rowmax;   // largest |B2| per row (tensor-core row scales)
@@ -157,6 +173,15 @@ int species_permutation(fgb_model_s *m, const int *d_species, int N,
 int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st,
                         const int *h_species = nullptr);
+// The same in two halves: start queues the kernels and the counts' copy
+// to page-locked memory (pending = true when finish must wait for it);
+// finish waits for that copy alone, so work queued in between keeps the
+// GPU busy meanwhile, and checks the species range.
+int species_permutation_start(int S, fgb_workspace &ws, const int *d_species,
+                              int N, std::vector<int> &counts, cudaStream_t st,
+                              const int *h_species, bool &pending);
+int species_permutation_finish(int S, fgb_workspace &ws,
+                               std::vector<int> &counts);
 int envs_struc_impl(const B2Params &p, double sigma, double power,
                     const int *h_counts, const double *d_sparse,
                     fgb_nlist_s *nl, const int *d_species, double *d_kern,

@@ -269,6 +269,7 @@ __device__ __forceinline__ void cursor_seek(LaneCursor &c, const StrucGeom &g,
 }
 
 constexpr int kFillWarps = 4;   // warps (atoms) per block of k_fill
+constexpr int kFillBlocks = 8;  // resident blocks per SM (64 registers)
 constexpr int kQueue = 64;      // per-warp candidate queue
 
 // Warp per atom: write the pairs (key = local j, packed shift; FP64
@@ -282,7 +283,7 @@ constexpr int kQueue = 64;      // per-warp candidate queue
 // queue and evaluated in FP64 32 at a time, so the FP64 work runs on full
 // warps.  flag[1] is set when the FP64 decisions disagree with the count
 // pass or with a certain-inside class.
-__global__ void __launch_bounds__(32 * kFillWarps)
+__global__ void __launch_bounds__(32 * kFillWarps, kFillBlocks)
 k_fill(int n, const int *__restrict__ atom_struct,
        const StrucGeom *__restrict__ geom, const double *__restrict__ wrapped,
        const float4 *__restrict__ w32, const int *__restrict__ raw,

@@ -353,6 +353,17 @@ int species_permutation(fgb_model_s *m, const int *d_species, int N,
 int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st,
                         const int *h_species) {
+  bool pending = false;
+  int rc = species_permutation_start(S, ws, d_species, N, counts, st,
+                                     h_species, pending);
+  if (rc || !pending) return rc;
+  return species_permutation_finish(S, ws, counts);
+}
+
+int species_permutation_start(int S, fgb_workspace &ws, const int *d_species,
+                              int N, std::vector<int> &counts, cudaStream_t st,
+                              const int *h_species, bool &pending) {
+  pending = false;
   counts.assign(S, 0);
   if (S < 1 || S > kMaxSpecies) {
     set_error("species permutation: %d species (at most %d)", S, kMaxSpecies);
@@ -386,15 +397,28 @@ int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
                                                ws.perm.as<int>());
   FGB_LAUNCH_CHECK("k_species_scatter");
   if (h_species) return FGB_OK;   // counted and checked above
-  std::vector<int> h(S + 1);
-  FGB_CUDA(cudaMemcpyAsync(h.data(), tot, sizeof(int) * (S + 1),
+  fgb_pinned_counts &pc = ws.counts;
+  if (!pc.h)
+    FGB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&pc.h),
+                           sizeof(int) * (kMaxSpecies + 1),
+                           cudaHostAllocDefault));
+  if (!pc.ev) FGB_CUDA(cudaEventCreateWithFlags(&pc.ev, cudaEventDisableTiming));
+  FGB_CUDA(cudaMemcpyAsync(pc.h, tot, sizeof(int) * (S + 1),
                            cudaMemcpyDeviceToHost, st));
-  FGB_CUDA(cudaStreamSynchronize(st));
-  if (h[S]) {
+  FGB_CUDA(cudaEventRecord(pc.ev, st));
+  pending = true;
+  return FGB_OK;
+}
+
+int species_permutation_finish(int S, fgb_workspace &ws,
+                               std::vector<int> &counts) {
+  const fgb_pinned_counts &pc = ws.counts;
+  FGB_CUDA(cudaEventSynchronize(pc.ev));
+  if (pc.h[S]) {
     set_error("species must lie in [0, %d)", S);
     return FGB_EINVAL;
   }
-  counts.assign(h.begin(), h.begin() + S);
+  counts.assign(pc.h, pc.h + S);
   return FGB_OK;
 }
 
@@ -671,6 +695,9 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   const bool want_e = want & FGB_WANT_ENERGY, want_f = want & FGB_WANT_FORCES,
              want_s = want & FGB_WANT_STRESS, want_v = want & FGB_WANT_LOCAL_VAR;
   const bool want_grad = want_f || want_s;
+  // forces and local variances go straight to the caller's buffers when
+  // given (no device-to-device copy at the end)
+  const bool f_direct = want_f && d_forces, v_direct = want_v && d_local_var;
   if ((rc = m->ws.A.ensure(sizeof(float) * ((size_t)N * p.n_A + 2))) ||
       (rc = m->ws.B2.ensure(sizeof(double) * ((size_t)N * p.n_d + 1))) ||
       (rc = m->ws.norms.ensure(sizeof(double) * (N + 1))) ||
@@ -696,7 +723,8 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   }
   if (N > 0) {
     FGB_CUDA(cudaMemsetAsync(m->ws.e_atom.p, 0, sizeof(double) * N, st));
-    FGB_CUDA(cudaMemsetAsync(m->ws.var.p, 0, sizeof(double) * N, st));
+    FGB_CUDA(cudaMemsetAsync(v_direct ? d_local_var : m->ws.var.as<double>(),
+                             0, sizeof(double) * N, st));
   }
   // the fold guard is known before the descriptor: models with large folded
   // coefficients take the descriptor, force product and adjoint at FP64
@@ -711,6 +739,20 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (!adj32 &&
       (rc = m->ws.A.ensure(sizeof(double) * ((size_t)N * p.n_A + 1))))
     return rc;
+  // species counts: queued before the descriptor and waited for after it,
+  // so the GPU runs the descriptor while the host waits (on device species)
+  std::vector<int> counts;
+  bool counts_pending = false;
+  if (fixed) {
+    counts = fixed->counts;
+  } else {
+    StageTimer _pt(kStSpeciesPerm, st, 3);
+    if ((rc = species_permutation_start(p.n_species, m->ws, d_species, N,
+                                        counts, st,
+                                        hio ? hio->species : nullptr,
+                                        counts_pending)))
+      return rc;
+  }
   {
     StageTimer _pt(kStB2Forward, st);
     // mixed precision: the descriptor in double-float (about 46 bits)
@@ -722,16 +764,10 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
                                 adj32 ? m->ws.A.as<float>() : nullptr)))
       return rc;
   }
-  std::vector<int> counts;
-  if (fixed) {
-    counts = fixed->counts;
-  } else {
-    StageTimer _pt(kStSpeciesPerm, st, 3);
-    if ((rc = species_permutation(m, d_species, N, counts, st,
-                                  hio ? hio->species : nullptr)))
-      return rc;
-    m->last_species_counts = counts;
-  }
+  if (counts_pending &&
+      (rc = species_permutation_finish(p.n_species, m->ws, counts)))
+    return rc;
+  if (!fixed) m->last_species_counts = counts;
   // dE/dB2 rows: the kernel stages write every row of a species with sparse
   // environments; rows of species without any stay zero
   if (want_grad && N > 0) {
@@ -745,13 +781,15 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
   if (precision == FGB_PREC_MIXED) {
     if ((rc = kernel_stage_mixed(m, N, counts, want_grad, want_v,
                                  m->ws.e_atom.as<double>(),
-                                 m->ws.gB2.as<double>(), m->ws.var.as<double>(),
+                                 m->ws.gB2.as<double>(),
+                                 v_direct ? d_local_var : m->ws.var.as<double>(),
                                  st, fixed != nullptr)))
       return rc;
   } else {
     if ((rc = kernel_stage_fp64(m, N, counts, want_grad, want_v,
                                 m->ws.e_atom.as<double>(),
-                                m->ws.gB2.as<double>(), m->ws.var.as<double>(),
+                                m->ws.gB2.as<double>(),
+                                v_direct ? d_local_var : m->ws.var.as<double>(),
                                 st)))
       return rc;
   }
@@ -767,26 +805,20 @@ int predict_impl(fgb_model_s *m, int n_struc, const int *h_atom_offsets,
     {
       StageTimer _pt(kStForces, st);
       if ((rc = launch_forces(&m->nl, m->ws.pair_grad.p, adj32,
-                              m->ws.forces.as<double>(),
+                              f_direct ? d_forces : m->ws.forces.as<double>(),
                               m->ws.virial.as<double>(), st)))
         return rc;
     }
-    if (d_forces && want_f && N > 0)
-      FGB_CUDA(cudaMemcpyAsync(d_forces, m->ws.forces.p,
-                               sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice,
-                               st));
   }
-  StageTimer _ptr(kStStructReduce, st);
-  if ((want_e && d_energy) || (want_s && d_stress))
+  if ((want_e && d_energy) || (want_s && d_stress)) {
+    StageTimer _ptr(kStStructReduce, st);
     if ((rc = launch_struct_reduce(
              n_struc, m->ws.atom_off.as<int>(), m->ws.volume.as<double>(),
              m->ws.e_atom.as<double>(),
              want_grad ? m->ws.virial.as<double>() : nullptr,
              want_e ? d_energy : nullptr, want_s ? d_stress : nullptr, st)))
       return rc;
-  if (want_v && d_local_var && N > 0)
-    FGB_CUDA(cudaMemcpyAsync(d_local_var, m->ws.var.p, sizeof(double) * N,
-                             cudaMemcpyDeviceToDevice, st));
+  }
   if (fixed) return FGB_OK;
   if (hio) {   // results to the host ahead of the one synchronisation below
     if (hio->energy && want_e)

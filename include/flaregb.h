@@ -226,8 +226,9 @@ int fgb_predict(fgb_model_t m, int n_struc, const int *h_atom_offsets,
 /* Same with HOST input/output buffers: copies in, predicts, copies out on
  * `stream` and synchronises it once (the species are counted and range-
  * checked on the host; results are queued for copy-back before that
- * synchronisation).  fgb_predict synchronises twice (the species counts,
- * then the deferred checks). */
+ * synchronisation).  fgb_predict waits twice: for the species counts
+ * (queued before the descriptor, waited for while it runs), then for the
+ * deferred checks. */
 int fgb_predict_host(fgb_model_t m, int n_struc, const int *h_atom_offsets,
                      const double *h_cells, const double *h_positions,
                      const int *h_species, double cutoff, int want,
