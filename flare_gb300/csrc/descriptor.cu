@@ -386,7 +386,7 @@ constexpr int kAdjThreads = 128;
 // per SM, which measured 0.36 ms against 0.51 ms at 4 blocks (128
 // registers) on the alloy workload, despite a few spilled values.
 template <typename T, int NC, int LC>
-__global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 8 : 2)
+__global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 10 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
              const int *__restrict__ nbr_j, const double4_16a *__restrict__ rel,
              const int *__restrict__ species, const double *__restrict__ A_in,
