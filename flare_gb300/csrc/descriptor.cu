@@ -381,10 +381,11 @@ __host__ __device__ constexpr int adj_atom_values(int nA, int nd_in_smem) {
 constexpr int kAdjThreads = 128;
 
 // Shared memory, per atom of the block: u[nA] | A[nA] | w[nd] (the atom's
-// dE/dB2 row, when it fits).  The pair loop is latency-bound (recurrence
-// chains): the FP32 kernel is held to 64 registers for 8 blocks (32 warps)
-// per SM, which measured 0.36 ms against 0.51 ms at 4 blocks (128
-// registers) on the alloy workload, despite a few spilled values.
+// dE/dB2 row, when it fits).  The pair loop is latency-bound (per-pair
+// loads, recurrence chains): the FP32 kernel is held to 48 registers for
+// 10 blocks (40 warps) per SM.  On the alloy workload that measured 0.212
+// ms per 32k atoms, against 0.244 ms at 8 blocks (64 registers) and 0.232
+// ms at 12 (40 registers, more spilled values).
 template <typename T, int NC, int LC>
 __global__ void __launch_bounds__(kAdjThreads, sizeof(T) == 4 ? 10 : 2)
 k_b2_adjoint(B2Params p, int n_atoms, const long long *__restrict__ offsets,
