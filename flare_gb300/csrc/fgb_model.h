@@ -175,8 +175,9 @@ int species_permutation(int S, fgb_workspace &ws, const int *d_species, int N,
                         const int *h_species = nullptr);
 // The same in two halves: start queues the kernels and the counts' copy
 // to page-locked memory (pending = true when finish must wait for it);
-// finish waits for that copy alone, so work queued in between keeps the
-// GPU busy meanwhile, and checks the species range.
+// finish waits for the stream up to that copy, not for what was queued
+// after it (so work queued in between keeps the GPU busy meanwhile), and
+// checks the species range.
 int species_permutation_start(int S, fgb_workspace &ws, const int *d_species,
                               int N, std::vector<int> &counts, cudaStream_t st,
                               const int *h_species, bool &pending);

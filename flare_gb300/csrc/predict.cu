@@ -342,7 +342,7 @@ int check_species(const int *d_species, int n, int n_species, DevBuf &flag,
 
 // Species permutation: perm = atoms of species 0 (ascending), then 1, ...
 // The species range check and every species count come back to the host in
-// one read (a single synchronisation).
+// one read (a single wait).
 int species_permutation(fgb_model_s *m, const int *d_species, int N,
                         std::vector<int> &counts, cudaStream_t st,
                         const int *h_species) {
