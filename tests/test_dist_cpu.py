@@ -59,3 +59,32 @@ def test_two_rank_gloo_replicas(tmp_path):
     assert res["max"] == 2.5          # the slower rank's time
     s0, s1 = res["seeds"]
     assert len(s0) == len(s1) == 4 and not set(s0) & set(s1)
+
+
+def test_reference_arm_two_ranks():
+    """bench.py --impl reference under two gloo ranks: rank 0 alone times
+    the CPU oracle and prints one JSON line; rank 1 exits 0 without work."""
+    pytest.importorskip("torch.distributed")
+    port = _free_port()
+    procs = []
+    for r in range(2):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE="2", LOCAL_RANK=str(r),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
+                   CUDA_VISIBLE_DEVICES="")
+        procs.append(subprocess.Popen(
+            [sys.executable, os.path.join(ROOT, "bench.py"), "--impl",
+             "reference", "--gpus", "2", "--steps", "1", "--warmup", "0"],
+            env=env, cwd=ROOT, stdout=subprocess.PIPE,
+            stderr=subprocess.PIPE))
+    outs = []
+    for p in procs:
+        o, e = p.communicate(timeout=600)
+        assert p.returncode == 0, e.decode()[-2000:]
+        outs.append([l for l in o.decode().splitlines() if l.startswith("{")])
+    assert outs[1] == [] and len(outs[0]) == 1
+    line = json.loads(outs[0][0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+    assert line["value"] > 0 and line["unit"] == "atoms/s"
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"] == {"value": line["value"], "unit": "atoms/s",
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
